@@ -1,0 +1,371 @@
+"""Benchmark: bit-ops/s of the bcc Gram pass (bcc_lf_YnWt) on one GB300.
+
+Workload (the case/control configuration): cases 4096 x 16384 SNPs and
+controls 4096 x 16384, MAF U[0.05,0.5], 256 x 512 planted bicluster with 5%
+flips, rows split uniformly over 2 covariate bins.  One step = the full Gram
+pass over all bin pairs (AnZt for every pair, AnAt for nb1 <= nb2): seven
+launches of the +/-1 centred D-weighted Gram with FP64 scores.
+
+  value  bit-ops/s with every operand already in HBM (lakgb_gram_device),
+         timed with CUDA events on the launching stream; L2 (129 MB) is flushed
+         before each step because the packed inputs (~18 MB) would fit in it.
+  e2e    the same pass through the reference-facing C entry points
+         (wrap_AnZt_vv__run / wrap_AnAt_vv__run) on host buffers, with the
+         bit-matrix upload and the FP64 result download inside the timed region.
+
+`--impl reference` times the reference's CPU implementation of the pass on
+this host's cores instead: the reference compiled from its sources when it is
+available here (x86-64 with the reference tree), otherwise the plain-C port of
+the same kernels (oracle/liblakoracle.so), OpenMP over all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "bit-ops/s of Gram pass (bcc_lf_YnWt, case/control 2x(2048+2048) x 16384, B_MLT=32)"
+UNIT = "bitop/s"
+WORKLOAD = "case_control_4096x4096x16384_2bins_gram_pass"
+
+
+def _rank_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU: the reference's own kernels (x86 with sources) or the C port
+
+
+def _cpu_backend():
+    ref = os.path.join(ROOT, "oracle", "_ref", "liblakref.so")
+    if os.path.exists(ref) and os.uname().machine == "x86_64":
+        return "ref", "reference"
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
+    return "oracle", "port"
+
+
+def cpu_gram_pass(inst, backend: str, threads: int):
+    """Time the Gram pass on the host; returns (seconds, bit-ops)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from lakcluster_c_gb300 import abi
+    from lakcluster_c_gb300.abi import MHandle
+    from lakcluster_c_gb300.gram_pass import block_allele_freq, products
+    import kernel_cases as kc
+
+    lib = kc.load_backend(backend)
+    if backend == "oracle":
+        lib.lako_set_threads(threads)
+    else:
+        C.c_int.in_dll(lib, "GLOBAL_omp_type").value = 1
+        C.c_int.in_dll(lib, "GLOBAL_thread_count").value = threads
+    MA = [MHandle(a) for a in inst.A_bins]
+    MZ = [MHandle(z) if z.shape[0] else None for z in inst.Z_bins]
+    A_ajdk = abi.calc_A_ajdk(block_allele_freq(inst))
+    lf = {}
+    for b in range(inst.nbins):
+        lf[("A", b)] = kc.lhandle_from(kc.call_an_ajdk(backend, abi.TYPE_pm, abi.SPACING_b, MA[b], A_ajdk),
+                                       MA[b].rpop_b, abi.AJDK_TOT, abi.SPACING_b)
+        if MZ[b] is not None:
+            lf[("Z", b)] = kc.lhandle_from(kc.call_an_ajdk(backend, abi.TYPE_pm, abi.SPACING_b, MZ[b], A_ajdk),
+                                           MZ[b].rpop_b, abi.AJDK_TOT, abi.SPACING_b)
+    work = 0.0
+    t0 = time.perf_counter()
+    for kind, nb1, nb2, sym in products(inst.nbins):
+        if kind == "AnZt":
+            Mz, lz = MZ[nb2], lf.get(("Z", nb2))
+        else:
+            Mz, lz = MA[nb2], lf[("A", nb2)]
+        if Mz is None:
+            continue
+        kc.call_gram(backend, sym, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_b, MA[nb1], Mz, A_ajdk,
+                     lf[("A", nb1)], lz)
+        work += float(MA[nb1].rpop_j) * float(Mz.rpop_j) * float(inst.ncols)
+    return time.perf_counter() - t0, work
+
+
+CPU_SAMPLE = "full Gram pass of the workload (cases 4096 + controls 4096 x 16384 SNPs, 2 bins)"
+
+
+def cpu_sample_instance():
+    """The CPU sample is the whole workload: one full pass takes a few seconds
+    on the host cores, so no subsampling is needed."""
+    from lakcluster_c_gb300 import synth
+    return synth.case_control(seed=2)
+
+
+def run_reference(args):
+    rank, world, _ = _rank_env()
+    if rank != 0:
+        return 0
+    backend, kind = _cpu_backend()
+    threads = os.cpu_count() or 1
+    inst = cpu_sample_instance()
+    for _ in range(args.warmup):
+        cpu_gram_pass(inst, backend, threads)
+    secs, work = 0.0, 0.0
+    for _ in range(args.steps):
+        s, w = cpu_gram_pass(inst, backend, threads)
+        secs += s
+        work += w
+    value = work / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64-popcount+f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": CPU_SAMPLE},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": CPU_SAMPLE},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = _rank_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from lakcluster_c_gb300 import build, synth
+    if rank == 0 or world == 1:
+        build.build_lib()
+    if world > 1:
+        dist.barrier()
+    from lakcluster_c_gb300._lib import load
+    from lakcluster_c_gb300.gram_pass import GramPassDevice, GramPassHost, gram_pass_host
+
+    lib = load()
+    # Replicas: each rank runs its own independent instance (weak scaling).
+    inst = synth.case_control(seed=2 + rank)
+    gp = GramPassHost(inst)
+    dev = GramPassDevice(gp)
+    work = gp.work_bitops()
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        dev.run(sh)
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kstart = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kend = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = lib.lakgb_kernel_launches()
+    with ClockSampler(local) as clk:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            dev.run(sh)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    launches = lib.lakgb_kernel_launches() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * work / (ms / 1000.0)
+
+    # dominant kernel alone: the largest AnZt launch, timed on its stream
+    big = dev.args[0]
+    for _ in range(3):
+        lib.lakgb_gram_device(C.byref(big))
+    torch.cuda.synchronize()
+    kt = []
+    for i in range(args.steps):
+        flush.zero_()
+        kstart[i].record(stream)
+        big.stream = sh
+        lib.lakgb_gram_device(C.byref(big))
+        kend[i].record(stream)
+    torch.cuda.synchronize()
+    kt = [s.elapsed_time(e) for s, e in zip(kstart, kend)]
+    k_ms = sum(kt) / len(kt)
+    k_work = float(big.nA) * float(big.nZ) * float(inst.ncols)
+
+    # e2e through the reference-facing C entry points, host buffers, no residency
+    lib.lakgb_set_residency(0)
+    outputs = {}
+    gram_pass_host(gp, outputs)
+    e2e_t = []
+    d2h = 0
+    for _ in range(max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d2h = gram_pass_host(gp, outputs)
+        e2e_t.append(time.perf_counter() - t0)
+    lib.lakgb_set_residency(1)
+    h2d = 0
+    for kind, nb1, nb2, sym in _products(inst.nbins):
+        MA = gp.MA[nb1]
+        MZ = gp.MZ[nb2] if kind == "AnZt" else gp.MA[nb2]
+        if MZ is None:
+            continue
+        h2d += MA.wX.nbytes + (0 if sym else MZ.wX.nbytes) + MA.mc_length
+    e2e_s = statistics.median(e2e_t)
+
+    # CPU baseline on a bounded sample (rank 0, N=1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        backend, kind = _cpu_backend()
+        threads = os.cpu_count() or 1
+        sample = cpu_sample_instance()
+        cpu_gram_pass(sample, backend, threads)  # warm
+        secs, w = 0.0, 0.0
+        for _ in range(3):
+            s1, w1 = cpu_gram_pass(sample, backend, threads)
+            secs += s1
+            w += w1
+        cpu = {"value": w / secs, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": CPU_SAMPLE + ", 3 passes, %.1f s" % secs}
+
+    peaks, src = _peaks()
+    tflops = 2.0 * k_work / (k_ms / 1000.0) / 1e12
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    clocks = clk.summary()
+    mhz = clocks.get("sm_mhz") or 1920.0
+    popc_peak = 16 * 32 * sm_count * mhz * 1e6  # POPC issue rate: 16 lanes/clk/SM x 32 bits
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32-popcount+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "bins": inst.nbins, "cases": 4096, "controls": 4096,
+                       "snps": inst.ncols, "launches_per_step": len(dev.args),
+                       "l2": "flushed before each step (256 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "gpu_launches": int(launches),
+            "roofline": {
+                "bound": "tensor", "achieved": tflops, "peak": peak_tf, "unit": "TFLOP/s",
+                "frac": tflops / peak_tf, "traffic": None,
+                "kernel": "gram_popc_kernel (largest AnZt launch, %dx%d rows)" % (big.nA, big.nZ),
+                "note": "bit-pair products counted as 2 ops (one MAC) against the %s dense bf16 tensor peak" % src,
+                "int_pipe": {"achieved_bitops": k_work / (k_ms / 1000.0), "peak_bitops": popc_peak,
+                             "frac": (k_work / (k_ms / 1000.0)) / popc_peak,
+                             "note": "POPC issue-rate bound, 16 lanes/clk/SM x 32 bits at the sampled SM clock"},
+                "kernel_ms": k_ms,
+            },
+            "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s},
+            "clocks": clocks,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def _products(nbins):
+    from lakcluster_c_gb300.gram_pass import products
+    return products(nbins)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,162 @@
+/* lakcluster_gb300.h -- C ABI of the GB300 (sm_103a) implementation of
+ * lakcluster's binary case/control loop-counting pass (bcc).
+ *
+ * The data model is the reference's, byte for byte, so a caller built against
+ * the reference headers can link this library in place of the CPU kernels:
+ *   struct M_handle  -- dir_h/M_handle.h:1-27   (packed +/-1 bit matrix + masks)
+ *   struct L_handle  -- dir_h/L_handle.h:1-11   (FP64 output, lf[r + c*row_stride])
+ *
+ * Every wrap_* entry point keeps the reference's signature and semantics:
+ * *output_p == NULL  -> the callee allocates the L_handle (malloc here, the
+ * reference uses its bump arena); otherwise the callee checks its length and
+ * zero-fills it; the return value is the output length.  The thread arguments
+ * (tidx, vpra, thread_in) are accepted for source compatibility: the work is
+ * enqueued on the library's CUDA stream and the call returns after the result
+ * is back in host memory (the reference's later pthread join becomes a no-op).
+ *
+ * Errors: no reference entry point returns a status, so device and argument
+ * errors are recorded in a library-global status read by lakgb_last_error();
+ * fatal conditions abort the way the reference does (exit with RET_* codes).
+ */
+#ifndef LAKCLUSTER_GB300_H
+#define LAKCLUSTER_GB300_H
+
+#include <stdio.h>
+#include <pthread.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LAKGB_FNAMESIZE (4096 + 256)
+
+/* dir_h/M_handle.h:1-27 -- identical field order and types. */
+struct M_handle {
+  unsigned char *mark;
+  int header_length;
+  char A_name[LAKGB_FNAMESIZE];
+  FILE *A_fp; unsigned char *Ara;
+  int bitj;
+  int nrows; int ncols;
+  int nrows_extend; int ncols_extend;
+  long long int rpop_b; long long int rpop_j;
+  long long int cpop_b; long long int cpop_j;
+  unsigned char *wX;
+  unsigned char *mr_b; unsigned char *mr_j;
+  unsigned char *mc_b; unsigned char *mc_j;
+  double *rsum;
+  unsigned int *m_a_;
+  unsigned int *m_b_;
+  unsigned int *n_a_;
+  unsigned int *n_b_;
+  unsigned long mr_length; unsigned long mc_length;
+  unsigned long cc_length;
+  unsigned long wt_length;
+  unsigned char *wt;
+  unsigned long long int length_total;
+  int ncols_per_z;
+  double max_d; double min_d; double mlt_d;
+};
+
+/* dir_h/L_handle.h:1-11 -- identical field order and types. */
+struct L_handle {
+  unsigned long long int length;
+  double *lf;
+  int spacing_row; unsigned long long int row_stride;
+  int spacing_col; unsigned long long int col_stride;
+  int spacing_lyr; unsigned long long int lyr_stride;
+};
+
+/* Constants with the reference's values (dir_h/lakcluster_header.h). */
+#define LAKGB_TYPE_p0 0
+#define LAKGB_TYPE_pm 1
+#define LAKGB_TYPE_00 2
+#define LAKGB_SPACING_b 0
+#define LAKGB_SPACING_j 1
+#define LAKGB_SPACING_a 2
+#define LAKGB_AJDK_TOT 15
+#define LAKGB_POPLENGTH 1920
+
+/* ---------------------------------------------------------------------------
+ * Kernel entry points (drop-in replacements).
+ * ------------------------------------------------------------------------- */
+
+/* Centred, D-weighted +/-1 Gram (An - e*alpha) diag(D) (Zt - alpha*e) over the
+ * current columns mc_j of M_An; TYPE_00 gives the masked AND count instead.
+ * Replaces wrap_AnZt_vv__run, dir_c/AnZt_vv.c:185 (kernel get_AnZt_vv__run,
+ * AnZt_vv.c:5-183). */
+int wrap_AnZt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                      int output_spacing_r, int output_spacing_c,
+                      struct M_handle *M_An, struct M_handle *M_Zn, double *A_ajdk,
+                      struct L_handle *lf_An_ajdk, struct L_handle *lf_Zn_ajdk,
+                      struct L_handle **output_AnZt_p);
+
+/* Symmetric variant with Zn == An.  Replaces wrap_AnAt_vv__run,
+ * dir_c/AnAt_vv.c:157 (kernel AnAt_vv.c:5-155). */
+int wrap_AnAt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                      int output_spacing_r, int output_spacing_c,
+                      struct M_handle *M_An, struct M_handle *M_Zn, double *A_ajdk,
+                      struct L_handle *lf_An_ajdk, struct L_handle *lf_Zn_ajdk,
+                      struct L_handle **output_AnAt_p);
+
+/* Masked row sums An*1 (TYPE_pm: +/-1, TYPE_00: 0/1).  Replaces
+ * wrap_An_v__run, dir_c/An_v.c:59 (kernel An_v.c:5-57). */
+int wrap_An_v__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                   int output_spacing_r, struct M_handle *M_An,
+                   struct L_handle **output_An_v_p);
+
+/* Row products An*diag(alpha^j D^k) for the 15 (j,k) pairs.  Replaces
+ * wrap_An_ajdk_v, dir_c/An_ajdk_v.c:365 (kernel An_ajdk_v.c:272-363). */
+int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                   int output_spacing_r, struct M_handle *M_An, double *A_ajdk,
+                   struct L_handle **output_An_ajdk_p);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident entry points (no reference counterpart: the reference has
+ * no device memory).  All pointers are device pointers; `stream` is a
+ * cudaStream_t (NULL = the library's stream).  The call enqueues and returns.
+ * ------------------------------------------------------------------------- */
+
+/* One Gram launch on device-resident packed rows: the same arithmetic as
+ * wrap_AnZt_vv__run (symmetric = 0) or wrap_AnAt_vv__run (symmetric = 1),
+ * with the host-side argument preparation already done by the caller.
+ * out[out_r[i] + out_c[k]*out_stride] = a0d1 - 2*S_ik - ((lfA[i]+lfZ[k]) - a2d1)
+ * for TYPE_pm (S_ik = sum over 1920-bit blocks b of D[b]*popcount((A_i^Z_k)&mask)),
+ * S_ik alone for TYPE_00; lfA/lfZ may be NULL, D may be NULL (unweighted). */
+struct lakgb_gram_args {
+  const unsigned char *wA; const unsigned int *a_rowb; int nA; long long a_row_bytes;
+  const unsigned char *wZ; const unsigned int *z_rowb; int nZ; long long z_row_bytes;
+  const unsigned char *mask; int P;
+  const double *D; int type_flag;
+  double a0d1; double a2d1;
+  const double *lfA; const double *lfZ;
+  const unsigned int *out_r; const unsigned int *out_c;
+  const unsigned int *out_r2; const unsigned int *out_c2;
+  long long out_stride; double *out;
+  int symmetric;
+  void *stream;
+};
+int lakgb_gram_device(const struct lakgb_gram_args *args);
+
+/* ---------------------------------------------------------------------------
+ * Library control (no reference counterpart).
+ * ------------------------------------------------------------------------- */
+
+/* Last error recorded by any entry point (0 = none) and its message; reading
+ * it clears it. */
+int lakgb_last_error(char *msg, int msg_len);
+/* Keep uploaded wX bit matrices resident on the device between calls, keyed
+ * by their host address (1, default) or re-upload on every call (0).  A caller
+ * that rewrites a wX buffer in place must call lakgb_forget_host_buffer. */
+void lakgb_set_residency(int on);
+void lakgb_forget_host_buffer(const void *host_ptr);
+/* Number of CUDA kernels this library has launched since load. */
+unsigned long long lakgb_kernel_launches(void);
+/* Device time (ms) of the most recent Gram kernel launch, timed with CUDA
+ * events on the launching stream. */
+double lakgb_last_gram_ms(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LAKCLUSTER_GB300_H */

@@ -1,0 +1,252 @@
+// Reference-compatible C entry points for the bcc kernels.  Each takes the
+// reference's host-side M_handle / L_handle structs, moves what the kernel
+// needs to the device (bit matrices stay resident between calls), launches the
+// sm_103a kernel and writes the result into the caller's L_handle exactly where
+// the reference kernel would.
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "gram.cuh"
+#include "lakgb_runtime.cuh"
+#include "rowvec.cuh"
+
+using namespace lakgb;
+
+namespace {
+
+constexpr int kAjdk_0_1 = 5;
+constexpr int kAjdk_1_1 = 6;
+constexpr int kAjdk_2_1 = 7;
+
+unsigned long long spacing_length(int spacing, const M_handle *M) {
+  switch (spacing) {
+    case LAKGB_SPACING_j: return (unsigned long long)M->rpop_j;
+    case LAKGB_SPACING_b: return (unsigned long long)M->rpop_b;
+    case LAKGB_SPACING_a: return (unsigned long long)M->nrows;
+    default: return 0;
+  }
+}
+
+// Index of the j-th retained row in the given spacing (AnZt_vv.c:71-77).
+std::vector<uint32_t> spacing_index(int spacing, const M_handle *M) {
+  std::vector<uint32_t> v((size_t)M->rpop_j);
+  for (long long j = 0; j < M->rpop_j; ++j) {
+    switch (spacing) {
+      case LAKGB_SPACING_j: v[j] = (uint32_t)j; break;
+      case LAKGB_SPACING_b: v[j] = M->m_b_[j]; break;
+      case LAKGB_SPACING_a: v[j] = M->m_a_[j]; break;
+      default: v[j] = 0; break;
+    }
+  }
+  return v;
+}
+
+// Allocate (malloc, zero-filled) or check-and-zero the output, as the
+// reference wrappers do (AnZt_vv.c:203-204).
+L_handle *ensure_output(L_handle **pp, unsigned long long length, const char *who) {
+  if (*pp == nullptr) {
+    L_handle *L = (L_handle *)calloc(1, sizeof(L_handle));
+    L->length = length;
+    L->lf = (double *)calloc(length ? length : 1, sizeof(double));
+    if (!L->lf) {
+      fprintf(stderr, " %% Warning! out of memory in %s\n", who);
+      exit(1);  // RET_NOMEM
+    }
+    *pp = L;
+  }
+  L_handle *L = *pp;
+  if (L->length < length) {
+    printf(" %% Warning! length %llu<%llu in %s\n", L->length, length, who);
+    set_error(2, "output length %llu < %llu in %s", L->length, length, who);
+    return nullptr;
+  }
+  memset(L->lf, 0, length * sizeof(double));
+  return L;
+}
+
+int popcount_bytes(const unsigned char *p, long n) {
+  int c = 0;
+  for (long i = 0; i < n; ++i) c += __builtin_popcount((unsigned)p[i]);
+  return c;
+}
+
+template <class T>
+DBuf upload_vec(const std::vector<T> &v) {
+  DBuf d(v.size() * sizeof(T));
+  d.upload(v.data(), v.size() * sizeof(T));
+  return d;
+}
+
+void copy_back(double *host, const DBuf &dev, unsigned long long length) {
+  if (length) LAKGB_CUDA(cudaMemcpyAsync(host, dev.p, length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  LAKGB_CUDA(cudaStreamSynchronize(stream()));
+}
+
+int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_handle *M_An,
+               M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk, L_handle *lf_Zn_ajdk,
+               L_handle **out_p, const char *who) {
+  const unsigned long long length_r = spacing_length(spacing_r, M_An);
+  const unsigned long long length_c = spacing_length(spacing_c, M_Zn);
+  const unsigned long long length = length_r * length_c;
+  L_handle *out = ensure_output(out_p, length, who);
+  if (!out) return (int)length;
+  out->spacing_row = spacing_r; out->row_stride = length_r;
+  out->spacing_col = spacing_c; out->col_stride = length_c;
+  if (type_flag == LAKGB_TYPE_p0) {
+    printf(" %% Warning! TYPE_p0 not implemented within %s\n", who);
+    return (int)length;
+  }
+  const int P = (int)(M_An->mc_length / kBlockBytes);
+  const int nA = (int)M_An->rpop_j, nZ = (int)M_Zn->rpop_j;
+  // Column-mask sums (AnZt_vv.c:62-63), host side in block order.
+  double a0d1 = 0.0, a2d1 = 0.0;
+  for (int nc = 0; nc < P; ++nc) {
+    const double c = (double)popcount_bytes(M_An->mc_j + (long)nc * kBlockBytes, kBlockBytes);
+    a0d1 += (A_ajdk ? A_ajdk[nc + kAjdk_0_1 * P] : 1.0) * c;
+    a2d1 += (A_ajdk ? A_ajdk[nc + kAjdk_2_1 * P] : 0.0) * c;
+  }
+  if (nA == 0 || nZ == 0 || P == 0) return (int)length;
+
+  const void *wA = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
+  const void *wZ = resident(M_Zn->wX, (size_t)M_Zn->rpop_b * M_Zn->mc_length);
+  DBuf mask(M_An->mc_length);
+  mask.upload(M_An->mc_j, M_An->mc_length);
+  std::vector<uint32_t> arow(M_An->m_b_, M_An->m_b_ + nA), zrow(M_Zn->m_b_, M_Zn->m_b_ + nZ);
+  DBuf d_arow = upload_vec(arow), d_zrow = upload_vec(zrow);
+  DBuf d_outr = upload_vec(spacing_index(spacing_r, M_An));
+  DBuf d_outc = upload_vec(spacing_index(spacing_c, M_Zn));
+  DBuf d_outr2, d_outc2;
+  if (symmetric) {
+    d_outr2 = upload_vec(spacing_index(spacing_r, M_Zn));
+    d_outc2 = upload_vec(spacing_index(spacing_c, M_An));
+  }
+  DBuf d_D;
+  if (A_ajdk) {
+    d_D = DBuf((size_t)P * sizeof(double));
+    d_D.upload(A_ajdk + (size_t)kAjdk_0_1 * P, (size_t)P * sizeof(double));
+  }
+  DBuf d_lfA, d_lfZ;
+  if (lf_An_ajdk && lf_Zn_ajdk) {
+    std::vector<double> a((size_t)nA), z((size_t)nZ);
+    std::vector<uint32_t> ia = spacing_index(lf_An_ajdk->spacing_row, M_An);
+    std::vector<uint32_t> iz = spacing_index(lf_Zn_ajdk->spacing_row, M_Zn);
+    for (int i = 0; i < nA; ++i) a[i] = lf_An_ajdk->lf[ia[i] + kAjdk_1_1 * lf_An_ajdk->row_stride];
+    for (int k = 0; k < nZ; ++k) z[k] = lf_Zn_ajdk->lf[iz[k] + kAjdk_1_1 * lf_Zn_ajdk->row_stride];
+    d_lfA = upload_vec(a);
+    d_lfZ = upload_vec(z);
+  }
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+
+  GramParams p{};
+  p.wA = (const uint8_t *)wA; p.a_rowb = d_arow.as<uint32_t>(); p.nA = nA; p.a_row_bytes = (long long)M_An->mc_length;
+  p.wZ = (const uint8_t *)wZ; p.z_rowb = d_zrow.as<uint32_t>(); p.nZ = nZ; p.z_row_bytes = (long long)M_Zn->mc_length;
+  p.mask = mask.as<uint8_t>(); p.P = P; p.D = d_D.as<double>();
+  p.type = (type_flag == LAKGB_TYPE_pm) ? 1 : 2;
+  p.a0d1 = a0d1; p.a2d1 = a2d1;
+  p.lfA = d_lfA.as<double>(); p.lfZ = d_lfZ.as<double>();
+  p.out_r = d_outr.as<uint32_t>(); p.out_c = d_outc.as<uint32_t>();
+  p.out_r2 = d_outr2.as<uint32_t>(); p.out_c2 = d_outc2.as<uint32_t>();
+  p.out_stride = (long long)length_r; p.out = d_out.as<double>();
+  p.symmetric = symmetric ? 1 : 0;
+  launch_gram(p);
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}
+
+}  // namespace
+
+extern "C" int wrap_AnZt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                                 int output_spacing_r, int output_spacing_c, M_handle *M_An,
+                                 M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk,
+                                 L_handle *lf_Zn_ajdk, L_handle **output_AnZt_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  return gram_entry(false, type_flag, output_spacing_r, output_spacing_c, M_An, M_Zn, A_ajdk,
+                    lf_An_ajdk, lf_Zn_ajdk, output_AnZt_p, "wrap_AnZt_vv__run");
+}
+
+extern "C" int wrap_AnAt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                                 int output_spacing_r, int output_spacing_c, M_handle *M_An,
+                                 M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk,
+                                 L_handle *lf_Zn_ajdk, L_handle **output_AnAt_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  return gram_entry(true, type_flag, output_spacing_r, output_spacing_c, M_An, M_Zn, A_ajdk,
+                    lf_An_ajdk, lf_Zn_ajdk, output_AnAt_p, "wrap_AnAt_vv__run");
+}
+
+extern "C" int wrap_An_v__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                              int output_spacing_r, M_handle *M_An, L_handle **output_An_v_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  const unsigned long long length = spacing_length(output_spacing_r, M_An);
+  L_handle *out = ensure_output(output_An_v_p, length, "wrap_An_v__run");
+  if (!out) return (int)length;
+  out->spacing_row = output_spacing_r; out->row_stride = length;
+  if (type_flag == LAKGB_TYPE_p0) {
+    printf(" %% Warning! TYPE_p0 not implemented within get_An_v__run\n");
+    return (int)length;
+  }
+  const int n = (int)M_An->rpop_j;
+  if (n == 0) return (int)length;
+  const int P = (int)(M_An->mc_length / kBlockBytes);
+  const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
+  DBuf mask(M_An->mc_length);
+  mask.upload(M_An->mc_j, M_An->mc_length);
+  std::vector<uint32_t> rows(M_An->m_b_, M_An->m_b_ + n);
+  DBuf d_rows = upload_vec(rows), d_outr = upload_vec(spacing_index(output_spacing_r, M_An));
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+  RowvecParams p{};
+  p.w = (const uint8_t *)w; p.rowb = d_rows.as<uint32_t>(); p.n = n; p.row_bytes = (long long)M_An->mc_length;
+  p.mask = mask.as<uint8_t>(); p.P = P; p.type = (type_flag == LAKGB_TYPE_pm) ? 1 : 2;
+  p.cpop_j = M_An->cpop_j; p.out_r = d_outr.as<uint32_t>(); p.out = d_out.as<double>();
+  launch_an_v(p);
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}
+
+extern "C" int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
+                              int output_spacing_r, M_handle *M_An, double *A_ajdk,
+                              L_handle **output_An_ajdk_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  const unsigned long long length_r = spacing_length(output_spacing_r, M_An);
+  const unsigned long long length = length_r * LAKGB_AJDK_TOT;
+  L_handle *out = ensure_output(output_An_ajdk_p, length, "wrap_An_ajdk_v");
+  if (!out) return (int)length;
+  out->spacing_row = output_spacing_r; out->row_stride = length_r;
+  out->spacing_col = LAKGB_SPACING_a; out->col_stride = LAKGB_AJDK_TOT;
+  if (type_flag == LAKGB_TYPE_p0) {
+    printf(" %% Warning! TYPE_p0 not implemented within get_An_ajdk_v\n");
+    return (int)length;
+  }
+  const int P = (int)(M_An->mc_length / kBlockBytes);
+  double base[LAKGB_AJDK_TOT];
+  for (int k = 0; k < LAKGB_AJDK_TOT; ++k) {
+    double s = 0.0;
+    for (int nc = 0; nc < P; ++nc)
+      s += A_ajdk[nc + k * P] * (double)popcount_bytes(M_An->mc_j + (long)nc * kBlockBytes, kBlockBytes);
+    base[k] = s;
+  }
+  const int n = (int)M_An->rpop_j;
+  if (n == 0) return (int)length;
+  const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
+  DBuf mask(M_An->mc_length);
+  mask.upload(M_An->mc_j, M_An->mc_length);
+  std::vector<uint32_t> rows(M_An->m_b_, M_An->m_b_ + n);
+  DBuf d_rows = upload_vec(rows), d_outr = upload_vec(spacing_index(output_spacing_r, M_An));
+  DBuf d_ajdk((size_t)P * LAKGB_AJDK_TOT * sizeof(double));
+  d_ajdk.upload(A_ajdk, (size_t)P * LAKGB_AJDK_TOT * sizeof(double));
+  DBuf d_base(sizeof(base));
+  d_base.upload(base, sizeof(base));
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+  RowvecParams p{};
+  p.w = (const uint8_t *)w; p.rowb = d_rows.as<uint32_t>(); p.n = n; p.row_bytes = (long long)M_An->mc_length;
+  p.mask = mask.as<uint8_t>(); p.P = P; p.type = (type_flag == LAKGB_TYPE_pm) ? 1 : 2;
+  p.ajdk = d_ajdk.as<double>(); p.base = d_base.as<double>();
+  p.out_r = d_outr.as<uint32_t>(); p.out_stride = (long long)length_r; p.out = d_out.as<double>();
+  launch_an_ajdk(p);
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}

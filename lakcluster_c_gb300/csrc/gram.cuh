@@ -1,0 +1,41 @@
+// Device entry for the +/-1 Gram (AnZt_vv / AnAt_vv) on device-resident data.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lakgb {
+
+struct GramParams {
+  const uint8_t *wA;       // packed rows of A (row r at wA + a_rowb[i]*a_row_bytes)
+  const uint32_t *a_rowb;  // wX row of the i-th retained A row (M_An->m_b_)
+  int nA;
+  long long a_row_bytes;   // M_An->mc_length
+  const uint8_t *wZ;
+  const uint32_t *z_rowb;
+  int nZ;
+  long long z_row_bytes;
+  const uint8_t *mask;     // M_An->mc_j, P*240 bytes
+  int P;                   // number of 1920-bit blocks
+  const double *D;         // A_ajdk + AJDK_0_1*P, or null (unweighted counts)
+  int type;                // 1: XOR (TYPE_pm), 2: AND (TYPE_00)
+  double a0d1, a2d1;       // sum_blocks D*popcnt(mask) and sum_blocks alpha^2 D*popcnt(mask)
+  const double *lfA;       // AJDK_1_1 row term per retained A row, or null
+  const double *lfZ;       // AJDK_1_1 row term per retained Z row, or null
+  const uint32_t *out_r;   // output row index of the i-th A row
+  const uint32_t *out_c;   // output column index of the k-th Z row
+  const uint32_t *out_r2;  // symmetric only: output row index of the k-th Z row
+  const uint32_t *out_c2;  // symmetric only: output column index of the i-th A row
+  long long out_stride;    // row_stride of the output
+  double *out;
+  int symmetric;           // AnAt: compute pairs i<=k only and mirror them
+  cudaStream_t stream;     // launch stream (null: the library stream)
+};
+
+// Enqueue the Gram kernel on the library stream.
+void launch_gram(const GramParams &p);
+
+// Algorithmic bit-ops of one Gram launch: rows_A * rows_Z * retained columns
+// (the full square for the symmetric variant, as the reference counts it).
+double gram_bitops(const GramParams &p, long long retained_cols);
+
+}  // namespace lakgb

@@ -1,0 +1,155 @@
+// Library runtime: stream, errors, allocation, residency cache.
+#include "lakgb_runtime.cuh"
+
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
+
+namespace lakgb {
+
+namespace {
+std::mutex g_mu;
+int g_err = 0;
+char g_msg[512] = {0};
+std::atomic<unsigned long long> g_launches{0};
+cudaStream_t g_stream = nullptr;
+bool g_residency = true;
+struct ResEntry { void *d; size_t n; };
+std::map<std::pair<const void *, size_t>, ResEntry> g_res;
+cudaEvent_t g_ev0 = nullptr, g_ev1 = nullptr;
+bool g_ev_pending = false;
+}  // namespace
+
+void set_error(int code, const char *fmt, ...) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_err) return;
+  g_err = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+  va_end(ap);
+}
+
+void check_cuda(cudaError_t e, const char *what, const char *file, int line) {
+  if (e == cudaSuccess) return;
+  set_error(1000 + (int)e, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  fprintf(stderr, " %% Error! %s failed: %s (%s:%d)\n", what, cudaGetErrorString(e), file, line);
+  exit(1);  // RET_NOMEM-style hard stop, as the reference does on fatal errors
+}
+
+cudaStream_t stream() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      fprintf(stderr, " %% Error! no CUDA device usable by liblakgb300: %s\n", cudaGetErrorString(e));
+      exit(1);
+    }
+  }
+  return g_stream;
+}
+
+void count_launch(unsigned long long n) { g_launches += n; }
+
+void *dalloc(size_t bytes) {
+  void *p = nullptr;
+  LAKGB_CUDA(cudaMallocAsync(&p, bytes, stream()));
+  return p;
+}
+
+void dfree(void *p) {
+  if (p) LAKGB_CUDA(cudaFreeAsync(p, stream()));
+}
+
+void DBuf::upload(const void *h, size_t bytes) {
+  if (bytes) LAKGB_CUDA(cudaMemcpyAsync(p, h, bytes, cudaMemcpyHostToDevice, stream()));
+}
+
+void DBuf::zero() {
+  if (n) LAKGB_CUDA(cudaMemsetAsync(p, 0, n, stream()));
+}
+
+const void *resident(const void *host, size_t bytes) {
+  if (bytes == 0) return nullptr;
+  stream();  // create the stream before taking the lock
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto key = std::make_pair(host, bytes);
+  auto it = g_res.find(key);
+  if (g_residency && it != g_res.end()) return it->second.d;
+  if (it != g_res.end()) {
+    cudaFreeAsync(it->second.d, g_stream);
+    g_res.erase(it);
+  }
+  void *d = nullptr;
+  LAKGB_CUDA(cudaMallocAsync(&d, bytes, g_stream));
+  LAKGB_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, g_stream));
+  g_res[key] = ResEntry{d, bytes};
+  return d;
+}
+
+void gram_timer_begin(cudaStream_t s) {
+  if (!g_ev0) {
+    LAKGB_CUDA(cudaEventCreate(&g_ev0));
+    LAKGB_CUDA(cudaEventCreate(&g_ev1));
+  }
+  LAKGB_CUDA(cudaEventRecord(g_ev0, s));
+}
+
+void gram_timer_end(cudaStream_t s) {
+  LAKGB_CUDA(cudaEventRecord(g_ev1, s));
+  g_ev_pending = true;
+}
+
+}  // namespace lakgb
+
+using namespace lakgb;
+
+extern "C" int lakgb_last_error(char *msg, int msg_len) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int e = g_err;
+  if (msg && msg_len > 0) {
+    strncpy(msg, g_msg, (size_t)msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  g_err = 0;
+  g_msg[0] = 0;
+  return e;
+}
+
+extern "C" void lakgb_set_residency(int on) {
+  stream();
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_residency = (on != 0);
+  if (!g_residency) {
+    for (auto &kv : g_res) cudaFreeAsync(kv.second.d, g_stream);
+    g_res.clear();
+  }
+}
+
+extern "C" void lakgb_forget_host_buffer(const void *host_ptr) {
+  stream();
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto it = g_res.begin(); it != g_res.end();) {
+    if (it->first.first == host_ptr) {
+      cudaFreeAsync(it->second.d, g_stream);
+      it = g_res.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
+extern "C" unsigned long long lakgb_kernel_launches(void) { return g_launches.load(); }
+
+extern "C" double lakgb_last_gram_ms(void) {
+  if (!g_ev_pending) return 0.0;
+  float ms = 0.f;
+  LAKGB_CUDA(cudaEventSynchronize(g_ev1));
+  LAKGB_CUDA(cudaEventElapsedTime(&ms, g_ev0, g_ev1));
+  return (double)ms;
+}

@@ -1,0 +1,65 @@
+// Runtime shared by every translation unit of liblakgb300.so: the library's
+// CUDA stream, error recording, launch accounting and a small residency cache
+// that keeps uploaded bit matrices on the device between calls.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+
+#include "../../include/lakcluster_gb300.h"
+
+namespace lakgb {
+
+// 1920-bit column block (POPLENGTH, dir_h/lakcluster_header.h:268): the unit
+// over which the reference's column weights are constant.
+constexpr int kBlockBits = 1920;
+constexpr int kBlockBytes = 240;
+constexpr int kBlockWords = 60;  // 32-bit words per block
+
+// Record an error (first one wins until lakgb_last_error() reads it).
+void set_error(int code, const char *fmt, ...);
+// Abort on a CUDA error the way the reference aborts on fatal conditions.
+void check_cuda(cudaError_t e, const char *what, const char *file, int line);
+#define LAKGB_CUDA(x) ::lakgb::check_cuda((x), #x, __FILE__, __LINE__)
+
+cudaStream_t stream();
+void count_launch(unsigned long long n = 1);
+
+// Device allocation on the library stream (stream-ordered allocator).
+void *dalloc(size_t bytes);
+void dfree(void *p);
+
+// Device copy of a host buffer.  With residency on, buffers are cached by
+// (host pointer, size) and reused without re-upload.
+const void *resident(const void *host, size_t bytes);
+
+// A device buffer freed when the object goes out of scope (after the stream
+// has drained the work that uses it).
+struct DBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t bytes) : p(bytes ? dalloc(bytes) : nullptr), n(bytes) {}
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      if (p) dfree(p);
+      p = o.p; n = o.n;
+      o.p = nullptr; o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { if (p) dfree(p); }
+  template <class T> T *as() const { return static_cast<T *>(p); }
+  void upload(const void *h, size_t bytes);
+  void zero();
+};
+
+// Events bracketing the most recent Gram launch.
+void gram_timer_begin(cudaStream_t s);
+void gram_timer_end(cudaStream_t s);
+
+}  // namespace lakgb

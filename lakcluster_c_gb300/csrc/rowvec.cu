@@ -1,0 +1,82 @@
+// Row-vector products over packed bit rows (HBM-bound scans).
+//
+//  An_v    (dir_c/An_v.c:5-57):       out_r = -cpop_j + 2*popcount(row & mc_j)   (TYPE_pm)
+//                                      out_r =          popcount(row & mc_j)    (TYPE_00)
+//  An_ajdk (dir_c/An_ajdk_v.c:272-363): for each of the 15 weight vectors w_k,
+//          out_rk = -sum_b w_kb*popcount(mc_j block b) + 2*sum_b w_kb*c_rb  (TYPE_pm)
+//          with the block sums accumulated in ascending block order, one multiply
+//          and one add per block and no FMA, as popcount_lf (popcount.c:252-308).
+//
+// One warp per row: lanes 0..29 read the 240-byte block as 8-byte words, the
+// warp reduces the block count with shuffles, and lanes 0..14 each carry one
+// of the 15 FP64 accumulators.
+#include "lakgb_runtime.cuh"
+#include "rowvec.cuh"
+
+namespace lakgb {
+
+namespace {
+
+__device__ __forceinline__ int block_count(const uint8_t *row, const uint8_t *mask, int lane) {
+  int c = 0;
+  if (lane < 30) {
+    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(row) + lane);
+    const uint2 m = __ldg(reinterpret_cast<const uint2 *>(mask) + lane);
+    c = __popc(x.x & m.x) + __popc(x.y & m.y);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  return c;
+}
+
+__global__ void an_v_kernel(RowvecParams p) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= p.n) return;
+  const uint8_t *row = p.w + (long long)p.rowb[warp] * p.row_bytes;
+  long long tot = 0;
+  for (int b = 0; b < p.P; ++b)
+    tot += block_count(row + (long long)b * kBlockBytes, p.mask + (long long)b * kBlockBytes, lane);
+  if (lane == 0) {
+    double o = (p.type == 1) ? __dadd_rn(-(double)p.cpop_j, __dmul_rn(2.0, (double)tot)) : (double)tot;
+    p.out[p.out_r[warp]] = o;
+  }
+}
+
+__global__ void an_ajdk_kernel(RowvecParams p) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= p.n) return;
+  const uint8_t *row = p.w + (long long)p.rowb[warp] * p.row_bytes;
+  double s = 0.0;
+  for (int b = 0; b < p.P; ++b) {
+    const int c = block_count(row + (long long)b * kBlockBytes, p.mask + (long long)b * kBlockBytes, lane);
+    if (lane < 15) s = __dadd_rn(s, __dmul_rn(p.ajdk[b + (long long)lane * p.P], (double)c));
+  }
+  if (lane < 15) {
+    double o = (p.type == 1) ? __dadd_rn(-p.base[lane], __dmul_rn(2.0, s)) : s;
+    p.out[(long long)p.out_r[warp] + (long long)lane * p.out_stride] = o;
+  }
+}
+
+}  // namespace
+
+void launch_an_v(const RowvecParams &p) {
+  if (p.n <= 0) return;
+  const int threads = 256;
+  const int blocks = (int)(((long long)p.n * 32 + threads - 1) / threads);
+  an_v_kernel<<<blocks, threads, 0, stream()>>>(p);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+void launch_an_ajdk(const RowvecParams &p) {
+  if (p.n <= 0) return;
+  const int threads = 256;
+  const int blocks = (int)(((long long)p.n * 32 + threads - 1) / threads);
+  an_ajdk_kernel<<<blocks, threads, 0, stream()>>>(p);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+}  // namespace lakgb

@@ -222,7 +222,11 @@ def run_gpu(args):
     gp = GramPassHost(inst)
     dev = GramPassDevice(gp)
     work = gp.work_bitops()
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: its handle is non-zero, so the library launches on it
+    # (a zero handle would select the library's own stream) and the CUDA
+    # events below bracket exactly the launched kernels.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -280,7 +284,7 @@ def run_gpu(args):
     gram_pass_host(gp, outputs)
     e2e_t = []
     d2h = 0
-    for _ in range(max(1, min(args.steps, 5))):
+    for _ in range(max(1, min(args.steps, 10))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         d2h = gram_pass_host(gp, outputs)
@@ -357,8 +361,8 @@ def _products(nbins):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

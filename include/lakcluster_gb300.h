@@ -111,6 +111,65 @@ int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
                    int output_spacing_r, struct M_handle *M_An, double *A_ajdk,
                    struct L_handle **output_An_ajdk_p);
 
+/* Quantise an FP64 matrix YnWt (rows mr_*, columns mc_*) into 1+b_mlt bit
+ * planes over the Yn rows: plane 0 marks the retained rows, planes
+ * 1..b_mlt hold the bits of floor(mlt*(x-min)) cropped to [1, D_MLT-1]
+ * (D_MLT = 2^b_mlt unless set with lakgb_set_d_mlt).  trm_flag = 1 reads
+ * YnWt transposed.  *M_X_p must be pre-allocated (the reference allocates it
+ * when NULL; this library requires it).  Replaces wrap_xcalc,
+ * dir_c/xcalc.c:248 (kernel get_xcalc, xcalc.c:41-246). */
+void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigned char *mr_j,
+                unsigned char *mr_b, unsigned char *mc_j, unsigned char *mc_b,
+                struct L_handle *lf_YnWt, double *YnWt, int *Yn_nrows_p, int *Wn_nrows_p,
+                struct M_handle **M_X_p, int *b_mlt_p, int trm_flag);
+
+/* out[na, t] = sum_w sum_z (At_na - alpha) diag(T_t) (YnWt)_w diag(S_t) (Zt - alpha)
+ * evaluated through the bit planes M_YnWt made by wrap_xcalc (the loop product
+ * behind the column scores).  Replaces wrap_At_T_YnWt_S_Zn_ww__run,
+ * dir_c/At_T_YnWt_S_Zn_ww.c:435 (kernel At_T_YnWt_S_Zn_ww.c:5-433). */
+int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a,
+                                int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                                struct M_handle *M_Yn, struct M_handle *M_Wn,
+                                struct M_handle *M_St, struct M_handle *M_Zt, double *A_ajdk,
+                                struct M_handle *M_YnWt,
+                                struct L_handle **output_At_T_YnWt_S_Zn_ww_p);
+
+/* out[na, s] = sum_z AnZt[na,z] * S[s,z] * YnWt[na,z] (the loop product behind
+ * the row scores).  Replaces wrap_AnZt_S_WnYt_vv__run,
+ * dir_c/AnZt_S_WnYt_vv.c:103 (kernel AnZt_S_WnYt_vv.c:5-101). */
+int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                             int output_spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                             struct M_handle *M_Zn, struct L_handle *lf_AnZt,
+                             struct L_handle *lf_YnWt, struct L_handle **output_p);
+
+/* out[na, s] = An_na . ZtSn[:, s] evaluated through the bit planes M_ZtSn made
+ * by wrap_xcalc.  Replaces wrap_An_ZtSn_ww__run, dir_c/An_ZtSn_ww.c:110
+ * (kernel An_ZtSn_ww.c:5-108). */
+int wrap_An_ZtSn_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a,
+                         int spacing_s, struct M_handle *M_An, struct L_handle *lf_ZtSn,
+                         struct M_handle *M_ZtSn, struct M_handle *M_St,
+                         struct L_handle **output_An_ZtSn_ww_p);
+
+/* out[na, ny, t] = (At_na - alpha) diag(T_t) (Yt_ny - alpha)^T over the rows
+ * (a SNP x SNP x covariate product).  Replaces wrap_AtTYn_vv__run,
+ * dir_c/AtTYn_vv.c:204 (kernel AtTYn_vv.c:5-202). */
+int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                       int output_spacing_y, int output_spacing_t, struct M_handle *M_At,
+                       struct M_handle *M_Tt, struct M_handle *M_Yt, double *A_ajdk,
+                       double *Y_ajdk, struct L_handle *lf_AtTn, struct L_handle *lf_YtTn,
+                       struct L_handle **output_AtTYn_p);
+
+/* out[na, s] = sum_{ny,nw} AtTYn[na,ny,s] * D[ny] * ZtSWn[nw..,s] (contraction of
+ * two AtTYn products).  Replaces wrap_AtTYn____WtSZn_vv__run,
+ * dir_c/AtTYn____WtSZn_vv.c:117 (kernel AtTYn____WtSZn_vv.c:5-115). */
+int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *thread_in,
+                                int output_spacing_a, int output_spacing_s,
+                                struct M_handle *M_At, struct M_handle *M_Tt,
+                                struct M_handle *M_Yt, struct M_handle *M_Wt,
+                                struct M_handle *M_St, struct M_handle *M_Zt, double *Y_ajdk,
+                                struct L_handle *lf_AtTYn, struct L_handle *lf_ZtSWn,
+                                struct L_handle **output_p);
+
 /* ---------------------------------------------------------------------------
  * Device-resident entry points (no reference counterpart: the reference has
  * no device memory).  All pointers are device pointers; `stream` is a

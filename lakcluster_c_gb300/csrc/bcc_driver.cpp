@@ -1,0 +1,1572 @@
+// bcc solve for the YnWt row/column strategies (lakcluster_driver,
+// dir_c/lakcluster_driver.c:14-251), restated over the reference data model.
+//
+// Every heavy product goes through the reference-compatible kernel entry
+// points (wrap_AnZt_vv__run, wrap_xcalc, wrap_At_T_YnWt_S_Zn_ww__run, ...),
+// which this library implements on the GPU.  The remaining per-row and
+// per-column FP64 bookkeeping (corrections for collapsed loops, score
+// normalisation, the tie-ordered sort and the elimination schedule) is
+// evaluated here in exactly the reference's operation order so that the
+// elimination trace is bit-identical.  Host code must be compiled without
+// FP contraction.
+//
+// Scope of this restatement: no extra column blocks (Y/W absent), one
+// covariate column of ones per bin (T = S = 1), GLOBAL_Ireq <= 0 -- the
+// configurations of the bcc case/control benchmark.  Other settings are
+// rejected with an error rather than computed differently.
+#include "bcc_driver.h"
+
+#include <math.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <memory>
+
+namespace lakbcc {
+
+namespace {
+
+int g_tidx = 0;
+void *g_vpra[128];
+pthread_t g_thread;
+#define TARGS &g_tidx, g_vpra, &g_thread
+
+// ---------------------------------------------------------------------------
+// State (the subset of bcc_ajdk / bcc_single / bcc_double used on this path)
+
+struct Single {
+  int nb = 0;
+  int A_nrows = 0, A_rbother = 0;
+  long A_mr_length = 0;
+  std::vector<unsigned char> A_bmr_b, A_bmr_j, A_bmr_j_rmv, A_bmr_j_rtn;
+  std::vector<unsigned char> A_umr_j, A_umr_j_rmv, A_umr_j_rtn;
+  unsigned A_rpop_b = 0, A_rpop_j = 0, A_rpop_j_rmv = 0, A_rpop_j_rtn = 0;
+  int Z_nrows = 0, Z_rbother = 0;
+  long Z_mr_length = 0;
+  std::vector<unsigned char> Z_bmr_b, Z_bmr_j;
+  unsigned Z_rpop_b = 0, Z_rpop_j = 0;
+  // packed data
+  std::vector<unsigned char> An_w, At_w, Zn_w, Zt_w, Tn_w, Tt_w, Sn_w, St_w;
+  MH *M_An = nullptr, *M_At = nullptr, *M_Zn = nullptr, *M_Zt = nullptr;
+  MH *M_Tn = nullptr, *M_Tt = nullptr, *M_Sn = nullptr, *M_St = nullptr;
+  MH *M_an = nullptr, *M_at = nullptr, *M_jn = nullptr, *M_jt = nullptr, *M_kn = nullptr, *M_kt = nullptr;
+  MH *M_hn = nullptr, *M_ht = nullptr, *M_zn = nullptr, *M_zt = nullptr, *M_vn = nullptr, *M_vt = nullptr;
+  MH *M_tt = nullptr, *M_rt = nullptr, *M_1 = nullptr;
+  MH *M_An_a1d1 = nullptr, *M_a2d2_ZtSn = nullptr, *M_a2d2_AtTn = nullptr;
+  L_handle *lf_At_rsum = nullptr, *lf_Zt_rsum = nullptr;
+  L_handle *lf_An_ajdk = nullptr, *lf_Zn_ajdk = nullptr, *lf_AtTn = nullptr, *lf_ZtSn = nullptr;
+  L_handle *lf_jn_ajdk = nullptr, *lf_vn_ajdk = nullptr, *lf_kn_ajdk = nullptr, *lf_zn_ajdk = nullptr;
+  L_handle *lf_hn_ajdk = nullptr, *lf_an_ajdk = nullptr;
+  L_handle *lf_attn = nullptr, *lf_jttn = nullptr, *lf_ktrn = nullptr, *lf_htrn = nullptr;
+  L_handle *lf_ztsn = nullptr, *lf_vtsn = nullptr, *lf_ztsvn = nullptr, *lf_attjn = nullptr, *lf_ktrhn = nullptr;
+  L_handle *lf_a1d2_Zt_Sn, *lf_a2d2_Zt_Sn, *lf_a3d2_Zt_Sn, *lf_a1d2_At_Tn, *lf_a2d2_At_Tn, *lf_a3d2_At_Tn;
+  L_handle *lf_et_Tn, *lf_et_Sn, *lf_et_An, *lf_a1d1_At_en, *lf_a1d2_At_en, *lf_a3d2_At_en;
+  L_handle *lf_et_An_a1d1, *lf_Tt_An_a1d1, *lf_T_AnAt_AnAt;
+  L_handle *lf_An_a1d1 = nullptr, *lf_At_An_a1d1 = nullptr, *lf_a2d2_ZtSn = nullptr, *lf_a2d2_AtTn = nullptr;
+  std::vector<double> QR_AnZtSZnAt_nrm, QR_AnAtTAnAt_nrm;
+  std::vector<int> QR_index_global_mr_a, QR_index_global_mr_b, QR_index_global_mr_j;
+};
+
+struct Double {
+  int nb1 = 0, nb2 = 0;
+  L_handle *lf_AnZt = nullptr, *lf_AnAt = nullptr;
+  MH *M_AnZt = nullptr, *M_AnAt = nullptr;
+  int M_AnZt_trm = 0, M_AnAt_trm = 0;
+  L_handle *lf_jnvt = nullptr, *lf_jnjt = nullptr;
+  L_handle *lf_knzt = nullptr, *lf_hnvt = nullptr, *lf_ankt = nullptr, *lf_knat = nullptr, *lf_knkt = nullptr;
+  MH *M_knzt = nullptr, *M_hnvt = nullptr, *M_ankt = nullptr, *M_knkt = nullptr;
+  int M_knzt_trm = 0, M_hnvt_trm = 0, M_ankt_trm = 0, M_knkt_trm = 0;
+  L_handle *lf_kt_r_knzt_s_zn, *lf_kt_r_hnvt_s_zn, *lf_at_t_ankt_r_kn, *lf_kt_r_knat_t_an, *lf_kt_r_knkt_r_kn;
+  L_handle *lf_attjn____vtszn, *lf_attjn____jttan, *lf_attjn____htrkn, *lf_ktrhn____jttan, *lf_ktrhn____htrkn;
+  L_handle *lf_AnZt_S_ZnAt, *lf_AnAt_T_AnAt;
+  L_handle *lf_At_T_AnZt_S_Zn, *lf_At_T_AnAt_T_An;
+  L_handle *lf_An_a2d2_Zt_Sn, *lf_An_a2d2_At_Tn;
+  L_handle *QR_AnZtSZnAt, *QR_AnAtTAnAt, *QC_AtTAnZtSZn, *QC_AtTAnAtTAn;
+};
+
+struct State {
+  Params P;
+  int nbins = 0;
+  int A_ncols = 0, A_cbother = 0, A_pcols = 0;
+  long A_mc_length = 0;
+  std::vector<unsigned char> A_bmc_b, A_bmc_j, A_bmc_j_rmv, A_bmc_j_rtn;
+  std::vector<unsigned char> A_umc_j, A_umc_j_rmv, A_umc_j_rtn;
+  unsigned A_cpop_b = 0, A_cpop_j = 0, A_cpop_j_rmv = 0, A_cpop_j_rtn = 0;
+  int T_ncols = 1;
+  long T_mc_length = 0;
+  std::vector<unsigned char> T_bmc_b, T_bmc_j;
+  unsigned T_cpop_b = 0, T_cpop_j = 0;
+  int A_nrows_total = 0; unsigned A_rpop_b_total = 0, A_rpop_j_total = 0;
+  int Z_nrows_total = 0; unsigned Z_rpop_b_total = 0, Z_rpop_j_total = 0;
+  std::vector<double> AZ_rsum, A_p, A_ajdk;
+  std::vector<double> QC_AtTAnZtSZn_nrm, QC_AtTAnAtTAn_nrm;
+  std::vector<double> QC_svalue, QR_svalue;
+  std::vector<int> QC_index_local_mc_a, QC_index_local_mc_b, QC_index_local_mc_j;
+  std::vector<int> QR_index_local_mr_a, QR_index_local_mr_b, QR_index_local_mr_j, QR_index_local_nb;
+  std::vector<int> QR_index_global_mr_a, QR_index_global_mr_b, QR_index_global_mr_j;
+  int Irem = 0, Ireq = 0;
+  std::vector<std::unique_ptr<Single>> E;
+  std::vector<std::unique_ptr<Double>> F;  // F[nb1 + nb2*nbins]
+  std::vector<MH *> all_mh;
+  std::vector<L_handle *> all_lh;
+  Output *out = nullptr;
+
+  const Hooks *hooks = nullptr;
+
+  Double *f(int nb1, int nb2) { return F[nb1 + nb2 * nbins].get(); }
+  L_handle *L(unsigned long long n) { L_handle *h = lh_make(n); all_lh.push_back(h); return h; }
+  MH *keep(MH *m) { all_mh.push_back(m); return m; }
+  void release(L_handle *L) {
+    if (L && hooks && hooks->release_L) hooks->release_L(L);
+  }
+  void forget(const std::vector<unsigned char> &v) {
+    if (!v.empty() && hooks && hooks->forget_host) hooks->forget_host(v.data());
+  }
+  ~State() {
+    // Outputs the kernel entry points allocated on first use.
+    for (auto &E : this->E) {
+      for (L_handle *L : {E->lf_An_ajdk, E->lf_Zn_ajdk, E->lf_AtTn, E->lf_ZtSn, E->lf_jn_ajdk, E->lf_vn_ajdk,
+                          E->lf_kn_ajdk, E->lf_zn_ajdk, E->lf_hn_ajdk, E->lf_an_ajdk, E->lf_attn, E->lf_jttn,
+                          E->lf_ktrn, E->lf_htrn, E->lf_ztsn, E->lf_vtsn, E->lf_ztsvn, E->lf_attjn, E->lf_ktrhn,
+                          E->lf_At_An_a1d1})
+        release(L);
+      for (auto *v : {&E->An_w, &E->At_w, &E->Zn_w, &E->Zt_w, &E->Tn_w, &E->Tt_w, &E->Sn_w, &E->St_w}) forget(*v);
+    }
+    for (auto *m : all_mh) { forget(m->own_rows); delete m; }
+    for (auto *h : all_lh) lh_free(h);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// small reference helpers restated
+
+void ura_from_bits(std::vector<unsigned char> &u, const std::vector<unsigned char> &b, int n) {
+  for (int i = 0; i < n; ++i) u[i] = (unsigned char)bget_on(b.data(), i);
+}
+void bits_from_ura(std::vector<unsigned char> &b, const std::vector<unsigned char> &u, int n) {
+  std::fill(b.begin(), b.end(), 0);
+  for (int i = 0; i < n; ++i)
+    if (u[i] > 0) bset_on(b.data(), i);
+}
+
+// get_xdrop, dir_c/xdrop.c:5-64
+void get_xdrop(const Params &P, double lrij, double lcij, int *rdrop_p, int *cdrop_p) {
+  if (lrij > lcij) { get_xdrop(P, lcij, lrij, cdrop_p, rdrop_p); return; }
+  const double dbl1 = 1.000000 - 0.000001;
+  const double gamma = P.gamma;
+  double gamma_tmp_row = 0, ammag_tmp_row = 0, gamma_tmp_col = 0, ammag_tmp_col = 0;
+  int rdrop = 0, cdrop = 0;
+  if (lrij <= 2) {
+    rdrop = (int)lrij; cdrop = (int)lcij;
+  } else {
+    if (gamma > 0) {
+      gamma_tmp_row = std::max(gamma, dbl1 / std::max(1.0, lrij));
+      ammag_tmp_row = std::min(1 - gamma, (lrij - 1) / std::max(1.0, lrij));
+    } else {
+      gamma_tmp_row = dbl1 / std::max(1.0, lrij);
+      ammag_tmp_row = (lrij - 1) / std::max(1.0, lrij);
+    }
+    switch (P.gamma_type) {
+      case 0: ammag_tmp_col = exp(log(ammag_tmp_row) * log(lcij) / std::max(1.0, log(std::max(1.0, lrij)))); break;
+      case 1: ammag_tmp_col = sqrt(ammag_tmp_row * lrij) * sqrt(lcij) / std::max(1.0, sqrt(std::max(1.0, lrij))) /
+                              ((double)std::max(1.0, lcij)); break;
+      case 2: ammag_tmp_col = ammag_tmp_row; break;
+      case 3: ammag_tmp_col = 0; break;
+      default: break;
+    }
+    gamma_tmp_col = dbl1 - ammag_tmp_col;
+    rdrop = (int)ceil(gamma_tmp_row * lrij);
+    cdrop = (int)ceil(gamma_tmp_col * lcij);
+    if (P.gamma_type == 3) cdrop = 0;
+  }
+  rdrop = (int)std::min((double)rdrop, lrij);
+  cdrop = (int)std::min((double)cdrop, lcij);
+  if (rdrop_p) *rdrop_p = rdrop;
+  if (cdrop_p) *cdrop_p = cdrop;
+}
+
+// dQuickSort_xij, dir_c/Quicksort.c:83-141 (first-element pivot, recursion
+// limit), written with an explicit stack.
+int partition_xij(double *d, int *i_, int *ib, int *ij, int *nb, int *ga, int *gb, int l, int r) {
+  const double pivot = d[l];
+  int i = l, j = r + 1;
+  auto sw = [&](int a, int b) {
+    std::swap(d[a], d[b]);
+    if (i_) std::swap(i_[a], i_[b]);
+    if (ib) std::swap(ib[a], ib[b]);
+    if (ij) std::swap(ij[a], ij[b]);
+    if (nb) std::swap(nb[a], nb[b]);
+    if (ga) std::swap(ga[a], ga[b]);
+    if (gb) std::swap(gb[a], gb[b]);
+  };
+  while (true) {
+    do { i++; } while (i <= r && d[i] <= pivot);
+    do { j--; } while (d[j] > pivot);
+    if (i >= j) break;
+    sw(i, j);
+  }
+  sw(l, j);
+  return j;
+}
+
+void quicksort_xij(unsigned limit, double *d, int *i_, int *ib, int *ij, int *nb, int *ga, int *gb, int l, int r) {
+  struct Node { int l, r; unsigned nn; };
+  std::vector<Node> st;
+  st.push_back({l, r, 0});
+  while (!st.empty()) {
+    Node n = st.back();
+    st.pop_back();
+    if (n.l < n.r) {
+      int j = partition_xij(d, i_, ib, ij, nb, ga, gb, n.l, n.r);
+      if (n.nn < limit) {
+        st.push_back({j + 1, n.r, n.nn + 1});
+        st.push_back({n.l, j - 1, n.nn + 1});
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// load (bcc_load, dir_c/bcc.c:1482-1540 and the functions it calls)
+
+// rows: a-space rows of a (nrows x ncols) matrix, bsize(ncols) bytes each.
+// Returns the compacted-by-mask rows (M_handle_v_make / M_load semantics).
+std::vector<unsigned char> compact_rows(const std::vector<unsigned char> &rows, int nrows, long row_bytes,
+                                        const std::vector<unsigned char> &mr_b) {
+  std::vector<unsigned char> out;
+  out.reserve(rows.size());
+  for (int r = 0; r < nrows; ++r)
+    if (bget_on(mr_b.data(), r)) out.insert(out.end(), rows.begin() + (long)r * row_bytes, rows.begin() + (long)(r + 1) * row_bytes);
+  out.resize(out.size() + POPLENGTH / BIT8, 0);  // one block of slack (see mh_init)
+  return out;
+}
+
+// Transpose a-space rows (nrows x ncols) into a-space rows of the transpose.
+std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows, int nrows, int ncols) {
+  const long rb = bsize(ncols), tb = bsize(nrows);
+  std::vector<unsigned char> t((size_t)std::max(1, ncols) * (size_t)tb, 0);
+  for (int r = 0; r < nrows; ++r) {
+    const unsigned char *row = rows.data() + (long)r * rb;
+    for (int c = 0; c < ncols; ++c)
+      if (bget_on(row, c)) bset_on(t.data() + (long)c * tb, r);
+  }
+  return t;
+}
+
+MH *xcalc_out(State &S, int n1a, int n1b, int n2a, int n2b, int *trm) {
+  // bcc_double_init_lf_excerpt / M_handle_w_make (bcc.c:992-1003, M_init.c:418-430)
+  int nrows_bZ, ncols_tmp;
+  if (n2b <= n1b) { *trm = 0; nrows_bZ = n1a; ncols_tmp = n2b; }
+  else { *trm = 1; nrows_bZ = n2a; ncols_tmp = n1b; }
+  const int ncols_bZ = (1 + S.P.B_MLT) * ncols_tmp;
+  return S.keep(mh_make_owned(ncols_bZ, nrows_bZ));
+}
+
+int load(State &S, const Input &I, std::string &err) {
+  const Params &P = S.P;
+  S.nbins = (int)I.bins.size();
+  if (S.nbins <= 0) { err = "NBINS must be positive"; return 2; }
+  // bcc_ajdk_load (bcc.c:54-115)
+  S.A_ncols = I.ncols;
+  S.A_cbother = S.A_ncols > 0;
+  S.A_mc_length = bsize(S.A_ncols);
+  S.A_bmc_b.assign(S.A_mc_length, 0);
+  if (!I.mc_b.empty()) memcpy(S.A_bmc_b.data(), I.mc_b.data(), std::min<size_t>(I.mc_b.size(), S.A_mc_length));
+  else for (int c = 0; c < S.A_ncols; ++c) bset_on(S.A_bmc_b.data(), c);
+  S.A_bmc_j = S.A_bmc_b;
+  S.A_bmc_j_rmv.assign(S.A_mc_length, 0);
+  S.A_bmc_j_rtn.assign(S.A_mc_length, 0);
+  S.A_cpop_b = popcount_bytes(S.A_bmc_b.data(), S.A_mc_length);
+  S.A_cpop_j = popcount_bytes(S.A_bmc_j.data(), S.A_mc_length);
+  S.A_umc_j.assign(std::max(1, S.A_ncols), 0);
+  S.A_umc_j_rmv.assign(std::max(1, S.A_ncols), 0);
+  S.A_umc_j_rtn.assign(std::max(1, S.A_ncols), 0);
+  ura_from_bits(S.A_umc_j, S.A_bmc_j, S.A_ncols);
+  S.T_ncols = 1;
+  S.T_mc_length = bsize(S.T_ncols);
+  S.T_bmc_b.assign(S.T_mc_length, 0);
+  for (int c = 0; c < S.T_ncols; ++c) bset_on(S.T_bmc_b.data(), c);
+  S.T_bmc_j = S.T_bmc_b;
+  S.T_cpop_b = popcount_bytes(S.T_bmc_b.data(), S.T_mc_length);
+  S.T_cpop_j = S.T_cpop_b;
+  const long row_bytes = bsize(S.A_ncols);
+
+  // bcc_single_load_M_An (bcc.c:270-413), per bin
+  for (int nb = 0; nb < S.nbins; ++nb) {
+    const BinInput &B = I.bins[nb];
+    auto E = std::make_unique<Single>();
+    E->nb = nb;
+    E->A_nrows = B.A_nrows;
+    E->A_rbother = E->A_nrows > 0;
+    E->A_mr_length = bsize(E->A_nrows);
+    E->A_bmr_b.assign(E->A_mr_length, 0);
+    if (!B.A_mr_b.empty()) memcpy(E->A_bmr_b.data(), B.A_mr_b.data(), std::min<size_t>(B.A_mr_b.size(), E->A_mr_length));
+    else for (int r = 0; r < E->A_nrows; ++r) bset_on(E->A_bmr_b.data(), r);
+    E->A_bmr_j = E->A_bmr_b;
+    E->A_bmr_j_rmv.assign(E->A_mr_length, 0);
+    E->A_bmr_j_rtn.assign(E->A_mr_length, 0);
+    E->A_rpop_b = popcount_bytes(E->A_bmr_b.data(), E->A_mr_length);
+    E->A_rpop_j = popcount_bytes(E->A_bmr_j.data(), E->A_mr_length);
+    E->A_umr_j.assign(std::max(1, E->A_nrows), 0);
+    E->A_umr_j_rmv.assign(std::max(1, E->A_nrows), 0);
+    E->A_umr_j_rtn.assign(std::max(1, E->A_nrows), 0);
+    ura_from_bits(E->A_umr_j, E->A_bmr_j, E->A_nrows);
+    E->Z_nrows = B.Z_nrows;
+    E->Z_rbother = E->Z_nrows > 0;
+    E->Z_mr_length = bsize(E->Z_nrows);
+    E->Z_bmr_b.assign(E->Z_mr_length, 0);
+    if (!B.Z_mr_b.empty()) memcpy(E->Z_bmr_b.data(), B.Z_mr_b.data(), std::min<size_t>(B.Z_mr_b.size(), E->Z_mr_length));
+    else for (int r = 0; r < E->Z_nrows; ++r) bset_on(E->Z_bmr_b.data(), r);
+    E->Z_bmr_j = E->Z_bmr_b;
+    E->Z_rpop_b = popcount_bytes(E->Z_bmr_b.data(), E->Z_mr_length);
+    E->Z_rpop_j = popcount_bytes(E->Z_bmr_j.data(), E->Z_mr_length);
+    // packed data: An rows compacted by A_bmr_b; At rows (SNPs) compacted by A_bmc_b
+    E->An_w = compact_rows(B.A_rows, E->A_nrows, row_bytes, E->A_bmr_b);
+    E->At_w = compact_rows(transpose_rows(B.A_rows, E->A_nrows, S.A_ncols), S.A_ncols, bsize(E->A_nrows), S.A_bmc_b);
+    E->M_An = S.keep(mh_make(E->A_nrows, S.A_ncols, E->An_w.data(), E->A_bmr_b.data(), S.A_bmc_b.data()));
+    E->M_At = S.keep(mh_make(S.A_ncols, E->A_nrows, E->At_w.data(), S.A_bmc_b.data(), E->A_bmr_b.data()));
+    if (E->Z_nrows > 0) {
+      E->Zn_w = compact_rows(B.Z_rows, E->Z_nrows, row_bytes, E->Z_bmr_b);
+      E->Zt_w = compact_rows(transpose_rows(B.Z_rows, E->Z_nrows, S.A_ncols), S.A_ncols, bsize(E->Z_nrows), S.A_bmc_b);
+    } else {
+      E->Zn_w.assign(POPLENGTH / BIT8, 0);
+      E->Zt_w.assign(POPLENGTH / BIT8, 0);
+    }
+    E->M_Zn = S.keep(mh_make(E->Z_nrows, S.A_ncols, E->Zn_w.data(), E->Z_bmr_b.data(), S.A_bmc_b.data()));
+    E->M_Zt = S.keep(mh_make(S.A_ncols, E->Z_nrows, E->Zt_w.data(), S.A_bmc_b.data(), E->Z_bmr_b.data()));
+    // T and S: one covariate column of ones (bcc.c:374-399)
+    E->Tn_w.assign((size_t)std::max(1, E->A_nrows) * (size_t)bsize(1), 0);
+    for (int r = 0; r < E->A_nrows; ++r) E->Tn_w[(size_t)r * bsize(1)] |= (1 << 7);
+    E->Tt_w.assign((size_t)bsize(E->A_nrows) + POPLENGTH / BIT8, 0);
+    for (int r = 0; r < E->A_nrows; ++r) bset_on(E->Tt_w.data(), r);
+    E->M_Tn = S.keep(mh_make(E->A_nrows, S.T_ncols, E->Tn_w.data(), E->A_bmr_b.data(), S.T_bmc_b.data()));
+    E->M_Tt = S.keep(mh_make(S.T_ncols, E->A_nrows, E->Tt_w.data(), S.T_bmc_b.data(), E->A_bmr_b.data()));
+    E->Sn_w.assign((size_t)std::max(1, E->Z_nrows) * (size_t)bsize(1), 0);
+    for (int r = 0; r < E->Z_nrows; ++r) E->Sn_w[(size_t)r * bsize(1)] |= (1 << 7);
+    E->St_w.assign((size_t)bsize(E->Z_nrows) + POPLENGTH / BIT8, 0);
+    for (int r = 0; r < E->Z_nrows; ++r) bset_on(E->St_w.data(), r);
+    E->M_Sn = S.keep(mh_make(E->Z_nrows, S.T_ncols, E->Sn_w.data(), E->Z_bmr_b.data(), S.T_bmc_b.data()));
+    E->M_St = S.keep(mh_make(S.T_ncols, E->Z_nrows, E->St_w.data(), S.T_bmc_b.data(), E->Z_bmr_b.data()));
+    // low-rank-update views share the packed data with their base handles
+    M_handle &An = E->M_An->h, &At = E->M_At->h, &Zn = E->M_Zn->h, &Zt = E->M_Zt->h, &Tt = E->M_Tt->h;
+    auto view = [&](M_handle &base) {
+      return S.keep(mh_make(base.nrows, base.ncols, base.wX, base.mr_b, base.mc_b));
+    };
+    E->M_an = view(An); E->M_jn = view(An); E->M_kn = view(An); E->M_hn = view(An);
+    E->M_at = view(At); E->M_jt = view(At); E->M_kt = view(At); E->M_ht = view(At);
+    E->M_zn = view(Zn); E->M_vn = view(Zn);
+    E->M_zt = view(Zt); E->M_vt = view(Zt);
+    E->M_tt = view(Tt); E->M_rt = view(Tt);
+    S.E.push_back(std::move(E));
+  }
+  // bcc_X_nrows_total (bcc.c:1179-1192)
+  for (auto &E : S.E) {
+    S.A_nrows_total += E->A_nrows; S.A_rpop_b_total += E->A_rpop_b; S.A_rpop_j_total += E->A_rpop_j;
+    S.Z_nrows_total += E->Z_nrows; S.Z_rpop_b_total += E->Z_rpop_b; S.Z_rpop_j_total += E->Z_rpop_j;
+  }
+  // bcc_single_init_lf (bcc.c:652-990): buffers used on this path
+  for (auto &Ep : S.E) {
+    Single *E = Ep.get();
+    E->lf_At_rsum = S.L(S.A_ncols);
+    E->lf_Zt_rsum = S.L(S.A_ncols);
+    const int T = S.T_ncols;
+    E->lf_a1d2_Zt_Sn = S.L(T); E->lf_a2d2_Zt_Sn = S.L(T); E->lf_a3d2_Zt_Sn = S.L(T);
+    E->lf_a1d2_At_Tn = S.L(T); E->lf_a2d2_At_Tn = S.L(T); E->lf_a3d2_At_Tn = S.L(T);
+    E->lf_et_Tn = S.L(T); E->lf_et_Sn = S.L(T);
+    E->lf_et_An = S.L(S.A_ncols); E->lf_a1d1_At_en = S.L(S.A_ncols);
+    E->lf_a1d2_At_en = S.L(S.A_ncols); E->lf_a3d2_At_en = S.L(S.A_ncols);
+    E->lf_et_An_a1d1 = S.L(1); E->lf_Tt_An_a1d1 = S.L(T);
+    E->lf_T_AnAt_AnAt = S.L((unsigned long long)T * E->A_nrows);
+    E->M_1 = S.keep(mh_make_owned(1, 1));
+    E->lf_An_a1d1 = S.L((unsigned long long)E->A_rpop_b * 1);
+    E->M_An_a1d1 = S.keep(mh_make_owned((1 + P.B_MLT) * 1, E->A_nrows));
+    E->lf_a2d2_ZtSn = S.L((unsigned long long)S.A_cpop_b * S.T_cpop_b);
+    E->M_a2d2_ZtSn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_ncols));
+    E->lf_a2d2_AtTn = S.L((unsigned long long)S.A_cpop_b * S.T_cpop_b);
+    E->M_a2d2_AtTn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_ncols));
+  }
+  // bcc_double_init_lf (bcc.c:1005-1150)
+  int rdrop = 0;
+  get_xdrop(P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, &rdrop, nullptr);
+  const int rdrop2 = std::max(2, rdrop);
+  S.F.resize((size_t)S.nbins * S.nbins);
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1) {
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      auto F = std::make_unique<Double>();
+      F->nb1 = nb1; F->nb2 = nb2;
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      const int A1a = E1->M_An->h.nrows, A1b = (int)E1->M_An->h.rpop_b;
+      const int A2a = E2->M_An->h.nrows, A2b = (int)E2->M_An->h.rpop_b;
+      const int Z2a = E2->M_Zn->h.nrows, Z2b = (int)E2->M_Zn->h.rpop_b;
+      F->lf_AnZt = S.L((unsigned long long)A1b * Z2b);
+      F->M_AnZt = xcalc_out(S, A1a, A1b, Z2a, Z2b, &F->M_AnZt_trm);
+      F->lf_AnAt = S.L((unsigned long long)A1b * A2b);
+      F->M_AnAt = xcalc_out(S, A1a, A1b, A2a, A2b, &F->M_AnAt_trm);
+      F->lf_jnvt = S.L((unsigned long long)A1b * Z2b);
+      F->lf_jnjt = S.L((unsigned long long)A1b * A2b);
+      const int c = S.A_cbother;
+      int n1b = c * std::min(rdrop2, A1b);
+      F->lf_knzt = S.L((unsigned long long)n1b * (c * Z2b));
+      F->M_knzt = xcalc_out(S, c * A1a, n1b, c * Z2a, c * Z2b, &F->M_knzt_trm);
+      F->lf_hnvt = S.L((unsigned long long)n1b * (c * Z2b));
+      F->M_hnvt = xcalc_out(S, c * A1a, n1b, c * Z2a, c * Z2b, &F->M_hnvt_trm);
+      F->lf_ankt = S.L((unsigned long long)(c * A1b) * (c * std::min(rdrop2, A2b)));
+      F->M_ankt = xcalc_out(S, c * A1a, c * A1b, c * A2a, c * std::min(rdrop2, A2b), &F->M_ankt_trm);
+      F->lf_knat = S.L((unsigned long long)n1b * (c * A2b));
+      F->lf_knkt = S.L((unsigned long long)n1b * (c * std::min(rdrop2, A2b)));
+      F->M_knkt = xcalc_out(S, c * A1a, n1b, c * A2a, c * std::min(rdrop2, A2b), &F->M_knkt_trm);
+      const unsigned long long AT = (unsigned long long)S.A_ncols * S.T_ncols;
+      F->lf_kt_r_knzt_s_zn = S.L(AT); F->lf_kt_r_hnvt_s_zn = S.L(AT); F->lf_at_t_ankt_r_kn = S.L(AT);
+      F->lf_kt_r_knat_t_an = S.L(AT); F->lf_kt_r_knkt_r_kn = S.L(AT);
+      F->lf_attjn____vtszn = S.L(AT); F->lf_attjn____jttan = S.L(AT); F->lf_attjn____htrkn = S.L(AT);
+      F->lf_ktrhn____jttan = S.L(AT); F->lf_ktrhn____htrkn = S.L(AT);
+      const unsigned long long NT = (unsigned long long)E1->M_An->h.nrows * S.T_ncols;
+      F->lf_AnZt_S_ZnAt = S.L(NT); F->lf_AnAt_T_AnAt = S.L(NT);
+      F->lf_At_T_AnZt_S_Zn = S.L(AT); F->lf_At_T_AnAt_T_An = S.L(AT);
+      F->lf_An_a2d2_Zt_Sn = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
+      F->lf_An_a2d2_At_Tn = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
+      F->QR_AnZtSZnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
+      F->QR_AnAtTAnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
+      F->QC_AtTAnZtSZn = S.L(AT); F->QC_AtTAnAtTAn = S.L(AT);
+      S.F[nb1 + nb2 * S.nbins] = std::move(F);
+    }
+  }
+  // bcc_load_A_p (bcc.c:1197-1313)
+  S.A_pcols = (int)psize(S.A_ncols);
+  S.AZ_rsum.assign(std::max(1, S.A_ncols), 0.0);
+  S.A_p.assign(std::max(1, S.A_pcols), 0.0);
+  for (auto &E : S.E) {
+    memset(E->lf_At_rsum->lf, 0, sizeof(double) * S.A_ncols);
+    wrap_An_v__run(TARGS, LAKGB_TYPE_00, SP_a, E->M_At->p(), &E->lf_At_rsum);
+    memset(E->lf_Zt_rsum->lf, 0, sizeof(double) * S.A_ncols);
+    wrap_An_v__run(TARGS, LAKGB_TYPE_00, SP_a, E->M_Zt->p(), &E->lf_Zt_rsum);
+  }
+  for (auto &E : S.E) {
+    for (int c = 0; c < S.A_ncols; ++c) S.AZ_rsum[c] += E->lf_At_rsum->lf[c];
+    for (int c = 0; c < S.A_ncols; ++c) S.AZ_rsum[c] += E->lf_Zt_rsum->lf[c];
+  }
+  for (int p = 0; p < S.A_pcols; ++p) {
+    S.A_p[p] = 0.5;
+    if (!P.test_sparse) continue;
+    const int nc_start = std::min(S.A_ncols - 1, std::max(0, p * POPLENGTH));
+    const int nc_final = std::min(S.A_ncols - 1, std::max(0, (p + 1) * POPLENGTH - 1));
+    double tmp_sum = 0, tmp_num = 0;
+    for (int nc = nc_start; nc <= nc_final; ++nc)
+      if (bget_on(S.A_bmc_b.data(), nc)) { tmp_sum += S.AZ_rsum[nc]; tmp_num += 1; }
+    if (tmp_num == 0) S.A_p[p] = 0.5;
+    else {
+      double v = tmp_sum / (tmp_num * (double)(S.A_rpop_b_total + S.Z_rpop_b_total));
+      S.A_p[p] = v < 0.01 ? 0.01 : (v > 0.99 ? 0.99 : v);
+    }
+  }
+  // calc_A_ajdk (An_ajdk_v.c:5-30)
+  S.A_ajdk.assign((size_t)AJDK_TOT * std::max(1, S.A_pcols), 0.0);
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 5; ++j)
+      for (int nc = 0; nc < S.A_pcols; ++nc) {
+        const double p = S.A_p[nc];
+        S.A_ajdk[nc + (j + 5 * k) * S.A_pcols] =
+            pow(p - (1 - p), j) * pow(1.0 / std::max(0.01, (4.0 * p * (1 - p))), k);
+      }
+  // bcc_init_QX (bcc.c:1369-1412)
+  const size_t QC = (size_t)S.A_ncols * S.T_ncols * S.nbins * S.nbins;
+  S.QC_AtTAnZtSZn_nrm.assign(std::max<size_t>(1, QC), 0.0);
+  S.QC_AtTAnAtTAn_nrm.assign(std::max<size_t>(1, QC), 0.0);
+  S.QC_svalue.assign(std::max(1, S.A_ncols), 0.0);
+  S.QC_index_local_mc_a.assign(std::max(1, S.A_ncols), 0);
+  S.QC_index_local_mc_b.assign(std::max(1, S.A_ncols), 0);
+  S.QC_index_local_mc_j.assign(std::max(1, S.A_ncols), 0);
+  const int NR = std::max(1, S.A_nrows_total);
+  S.QR_svalue.assign(NR, 0.0);
+  S.QR_index_global_mr_a.assign(NR, 0); S.QR_index_global_mr_b.assign(NR, 0); S.QR_index_global_mr_j.assign(NR, 0);
+  S.QR_index_local_mr_a.assign(NR, 0); S.QR_index_local_mr_b.assign(NR, 0);
+  S.QR_index_local_mr_j.assign(NR, 0); S.QR_index_local_nb.assign(NR, 0);
+  int mx_a = 0, mx_b = 0, mx_j = 0;
+  for (auto &E : S.E) {
+    E->QR_index_global_mr_a.assign(std::max(1, E->A_nrows), 0);
+    E->QR_index_global_mr_b.assign(std::max(1, E->A_nrows), 0);
+    E->QR_index_global_mr_j.assign(std::max(1, E->A_nrows), 0);
+    for (int mr_a = 0; mr_a < E->A_nrows; ++mr_a) {
+      E->QR_index_global_mr_a[mr_a] = mx_a;
+      if (bget_on(E->A_bmr_b.data(), mr_a)) {
+        E->QR_index_global_mr_b[mr_a] = mx_b;
+        if (bget_on(E->A_bmr_j.data(), mr_a)) { E->QR_index_global_mr_j[mr_a] = mx_j; mx_j++; }
+        mx_b++;
+      }
+      mx_a++;
+    }
+    const size_t n = (size_t)E->A_nrows * S.T_ncols * S.nbins;
+    E->QR_AnZtSZnAt_nrm.assign(std::max<size_t>(1, n), 0.0);
+    E->QR_AnAtTAnAt_nrm.assign(std::max<size_t>(1, n), 0.0);
+  }
+  return 0;
+}
+
+// bcc_M_mxset (bcc.c:1414-1438)
+void M_mxset_all(State &S) {
+  S.A_cpop_j = popcount_bytes(S.A_bmc_j.data(), S.A_mc_length);
+  S.T_cpop_j = popcount_bytes(S.T_bmc_j.data(), S.T_mc_length);
+  S.A_rpop_j_total = 0; S.Z_rpop_j_total = 0;
+  for (auto &E : S.E) {
+    E->A_rpop_j = popcount_bytes(E->A_bmr_j.data(), E->A_mr_length); S.A_rpop_j_total += E->A_rpop_j;
+    E->Z_rpop_j = popcount_bytes(E->Z_bmr_j.data(), E->Z_mr_length); S.Z_rpop_j_total += E->Z_rpop_j;
+    mh_mxset(E->M_An, E->A_bmr_j.data(), S.A_bmc_j.data()); mh_mxset(E->M_At, S.A_bmc_j.data(), E->A_bmr_j.data());
+    mh_mxset(E->M_Zn, E->Z_bmr_j.data(), S.A_bmc_j.data()); mh_mxset(E->M_Zt, S.A_bmc_j.data(), E->Z_bmr_j.data());
+    mh_mxset(E->M_Tn, E->A_bmr_j.data(), S.T_bmc_j.data()); mh_mxset(E->M_Tt, S.T_bmc_j.data(), E->A_bmr_j.data());
+    mh_mxset(E->M_Sn, E->Z_bmr_j.data(), S.T_bmc_j.data()); mh_mxset(E->M_St, S.T_bmc_j.data(), E->Z_bmr_j.data());
+  }
+}
+
+// bcc_lrup_mxset (bcc_lrup.c:1101-1126)
+void lrup_mxset(State &S) {
+  for (auto &E : S.E) {
+    unsigned char *rtn = E->A_bmr_j_rtn.data(), *rmv = E->A_bmr_j_rmv.data();
+    unsigned char *crtn = S.A_bmc_j_rtn.data(), *crmv = S.A_bmc_j_rmv.data();
+    mh_mxset(E->M_an, rtn, crtn); mh_mxset(E->M_at, crtn, rtn);
+    mh_mxset(E->M_jn, rtn, crmv); mh_mxset(E->M_jt, crmv, rtn);
+    mh_mxset(E->M_kn, rmv, crtn); mh_mxset(E->M_kt, crtn, rmv);
+    mh_mxset(E->M_hn, rmv, crmv); mh_mxset(E->M_ht, crmv, rmv);
+    mh_mxset(E->M_zn, E->Z_bmr_j.data(), crtn); mh_mxset(E->M_zt, crtn, E->Z_bmr_j.data());
+    mh_mxset(E->M_vn, E->Z_bmr_j.data(), crmv); mh_mxset(E->M_vt, crmv, E->Z_bmr_j.data());
+    mh_mxset(E->M_tt, S.T_bmc_j.data(), rtn);
+    mh_mxset(E->M_rt, S.T_bmc_j.data(), rmv);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stages
+
+void An_ajdk_all(State &S) {  // bcc_An_ajdk (bcc_lf.c:7-51)
+  for (auto &E : S.E) {
+    if (E->A_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_An->p(), S.A_ajdk.data(), &E->lf_An_ajdk);
+    if (E->Z_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_Zn->p(), S.A_ajdk.data(), &E->lf_Zn_ajdk);
+  }
+}
+
+void lf_ZtSn_all(State &S) {  // bcc_lf_ZtSn (bcc_lf.c:53-100)
+  for (auto &E : S.E) {
+    if (E->A_rbother && S.A_cbother)
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_At->p(), E->M_Tt->p(), nullptr, nullptr, nullptr, &E->lf_AtTn);
+    if (E->Z_rbother && S.A_cbother)
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_Zt->p(), E->M_St->p(), nullptr, nullptr, nullptr, &E->lf_ZtSn);
+  }
+}
+
+void lf_YnWt_all(State &S) {  // bcc_lf_YnWt (bcc_lf.c:223-290)
+  double *aj = S.A_ajdk.data();
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        wrap_AnZt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_An->p(), E2->M_Zn->p(), aj, E1->lf_An_ajdk, E2->lf_Zn_ajdk, &F->lf_AnZt);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        if (nb1 == nb2)
+          wrap_AnAt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_An->p(), E2->M_An->p(), aj, E1->lf_An_ajdk, E2->lf_An_ajdk, &F->lf_AnAt);
+        if (nb1 < nb2)
+          wrap_AnZt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_An->p(), E2->M_An->p(), aj, E1->lf_An_ajdk, E2->lf_An_ajdk, &F->lf_AnAt);
+      }
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
+        lh_transpose(S.f(nb1, nb2)->lf_AnAt, S.f(nb2, nb1)->lf_AnAt);
+    }
+}
+
+// bcc_M_YnWt_excerpt (bcc_lf.c:300-316)
+void xcalc_excerpt(State &S, int trm, MH *M_in1, MH *M_in2, L_handle *L_in, MH *M_out) {
+  M_handle *out = M_out->p();
+  int b_mlt = S.P.B_MLT;
+  if (trm == 0)
+    wrap_xcalc(TARGS, M_in1->h.mr_j, M_in1->h.mr_b, M_in2->h.mr_j, M_in2->h.mr_b, L_in, L_in->lf,
+               &M_in1->h.nrows, &M_in2->h.nrows, &out, &b_mlt, 0);
+  else
+    wrap_xcalc(TARGS, M_in2->h.mr_j, M_in2->h.mr_b, M_in1->h.mr_j, M_in1->h.mr_b, L_in, L_in->lf,
+               &M_in2->h.nrows, &M_in1->h.nrows, &out, &b_mlt, 1);
+}
+
+void M_YnWt_all(State &S) {  // bcc_M_YnWt (bcc_lf.c:318-356)
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) xcalc_excerpt(S, F->M_AnZt_trm, E1->M_An, E2->M_Zn, F->lf_AnZt, F->M_AnZt);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) xcalc_excerpt(S, F->M_AnAt_trm, E1->M_An, E2->M_An, F->lf_AnAt, F->M_AnAt);
+    }
+}
+
+// bcc_lf_At_T_YnWt_S_Zn_excerpt (bcc_lf.c:636-647)
+void bitplane_excerpt(State &S, int trm, MH *At, MH *Tt, MH *Yn, MH *Wn, MH *St, MH *Zt, MH *YnWt, L_handle **out) {
+  if (trm == 0)
+    wrap_At_T_YnWt_S_Zn_ww__run(TARGS, SP_a, SP_a, At->p(), Tt->p(), Yn->p(), Wn->p(), St->p(), Zt->p(), S.A_ajdk.data(), YnWt->p(), out);
+  else
+    wrap_At_T_YnWt_S_Zn_ww__run(TARGS, SP_a, SP_a, Zt->p(), St->p(), Wn->p(), Yn->p(), Tt->p(), At->p(), S.A_ajdk.data(), YnWt->p(), out);
+}
+
+void lf_At_T_YnWt_S_Zn_all(State &S) {  // bcc_lf_At_T_YnWt_S_Zn (bcc_lf.c:649-709)
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        bitplane_excerpt(S, F->M_AnZt_trm, E1->M_At, E1->M_Tt, E1->M_An, E2->M_Zn, E2->M_St, E2->M_Zt, F->M_AnZt, &F->lf_At_T_AnZt_S_Zn);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 <= nb2)
+        bitplane_excerpt(S, F->M_AnAt_trm, E1->M_At, E1->M_Tt, E1->M_An, E2->M_An, E2->M_Tt, E2->M_At, F->M_AnAt, &F->lf_At_T_AnAt_T_An);
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
+        lh_duplicate(S.f(nb1, nb2)->lf_At_T_AnAt_T_An, S.f(nb2, nb1)->lf_At_T_AnAt_T_An);
+    }
+}
+
+void lf_AnZt_S_WnYt_all(State &S) {  // bcc_lf_AnZt_S_WnYt (bcc_lf.c:360-410)
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        wrap_AnZt_S_WnYt_vv__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->M_St->p(), E2->M_Zn->p(), F->lf_AnZt, F->lf_AnZt, &F->lf_AnZt_S_ZnAt);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother)
+        wrap_AnZt_S_WnYt_vv__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->M_Tt->p(), E2->M_An->p(), F->lf_AnAt, F->lf_AnAt, &F->lf_AnAt_T_AnAt);
+    }
+}
+
+void set_l1(L_handle *L, unsigned long long length) {
+  L->row_stride = length; L->spacing_row = SP_a; lh_zero(L);
+}
+
+unsigned popcount_masked_row(const unsigned char *row, const unsigned char *mask, long nbytes) {
+  unsigned c = 0;
+  for (long i = 0; i < nbytes; ++i) c += (unsigned)__builtin_popcount((unsigned)(row[i] & mask[i]));
+  return c;
+}
+
+// get_singlestudy_vv (bcc_flattenloop.c:359-731) for one bin, without the Y terms.
+void singlestudy_vv(State &S, Single *E) {
+  M_handle *An = E->M_An->p(), *At = E->M_At->p(), *Tt = E->M_Tt->p(), *St = E->M_St->p(), *Zt = E->M_Zt->p();
+  L_handle *lfA = E->lf_An_ajdk, *lfZ = E->lf_Zn_ajdk;
+  double *aj = S.A_ajdk.data();
+  const int P = (int)psize(At->nrows);
+  const int T = Tt->nrows, A_ncols = At->nrows, A_nrows = At->ncols;
+  set_l1(E->lf_a1d2_Zt_Sn, T); set_l1(E->lf_a2d2_Zt_Sn, T); set_l1(E->lf_a3d2_Zt_Sn, T);
+  set_l1(E->lf_a1d2_At_Tn, T); set_l1(E->lf_a2d2_At_Tn, T); set_l1(E->lf_a3d2_At_Tn, T);
+  set_l1(E->lf_et_Tn, T); set_l1(E->lf_et_Sn, T);
+  set_l1(E->lf_et_An, A_ncols); set_l1(E->lf_a1d1_At_en, A_ncols);
+  set_l1(E->lf_a1d2_At_en, A_ncols); set_l1(E->lf_a3d2_At_en, A_ncols);
+  set_l1(E->lf_et_An_a1d1, 1); set_l1(E->lf_Tt_An_a1d1, T);
+  L_handle *TAA = E->lf_T_AnAt_AnAt;
+  TAA->row_stride = T; TAA->spacing_row = SP_a; TAA->col_stride = A_nrows; TAA->spacing_col = SP_a; lh_zero(TAA);
+  const int QR_AnZtSZnAt = E->A_rbother && S.A_cbother && E->Z_rbother;
+  const int QR_AnAtTAnAt = E->A_rbother && S.A_cbother;
+  const int QC_AtTAnZtSZn = QR_AnZtSZnAt;
+  const int QC_AtTAnAtTAn = QR_AnAtTAnAt;
+  unsigned *ma_a_ = An->m_a_, *ma_b_ = An->m_b_;
+  unsigned *na_a_ = An->n_a_, *na_b_ = An->n_b_;
+  unsigned *mz_a_ = Zt->n_a_, *mz_b_ = Zt->n_b_;
+  unsigned *ns_a_ = St->m_a_, *ns_b_ = St->m_b_;
+  if (QC_AtTAnAtTAn) {
+    for (int ns_j = 0; ns_j < Tt->rpop_j; ++ns_j) {
+      const unsigned ns_a = ns_a_[ns_j], ns_b = ns_b_[ns_j];
+      const unsigned char *Tt_tag = Tt->wX + (long)ns_b * Tt->mc_length;
+      for (int ma_j = 0; ma_j < At->cpop_j; ++ma_j) {
+        const unsigned ma_a = ma_a_[ma_j], ma_b = ma_b_[ma_j];
+        const int vT = bget_pm(Tt_tag, ma_a);
+        *L1_get(E->lf_Tt_An_a1d1, ns_j, ns_b, ns_a) += vT * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1));
+      }
+    }
+  }
+  if (QR_AnZtSZnAt || QR_AnAtTAnAt) {
+    for (int ns_j = 0; ns_j < Tt->rpop_j; ++ns_j) {
+      const unsigned ns_a = ns_a_[ns_j], ns_b = ns_b_[ns_j];
+      const unsigned char *Tt_tag = Tt->wX + (long)ns_b * Tt->mc_length;
+      if (QR_AnAtTAnAt) {
+        for (int ma_j = 0; ma_j < At->cpop_j; ++ma_j) {
+          const unsigned ma_a = ma_a_[ma_j], ma_b = ma_b_[ma_j];
+          const int vT = bget_pm(Tt_tag, ma_a);
+          *L1_get(E->lf_a1d2_At_Tn, ns_j, ns_b, ns_a) += vT * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_2));
+          *L1_get(E->lf_a2d2_At_Tn, ns_j, ns_b, ns_a) += vT * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_2_2));
+          *L1_get(E->lf_a3d2_At_Tn, ns_j, ns_b, ns_a) += vT * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_3_2));
+        }
+      }
+      const unsigned char *St_tag = St->wX + (long)ns_b * St->mc_length;
+      if (QR_AnZtSZnAt) {
+        for (int mz_j = 0; mz_j < Zt->cpop_j; ++mz_j) {
+          const unsigned mz_a = mz_a_[mz_j], mz_b = mz_b_[mz_j];
+          const int vS = bget_pm(St_tag, mz_a);
+          *L1_get(E->lf_a1d2_Zt_Sn, ns_j, ns_b, ns_a) += vS * (*L2_get(lfZ, mz_j, mz_b, mz_a, 0, 0, AJDK_1_2));
+          *L1_get(E->lf_a2d2_Zt_Sn, ns_j, ns_b, ns_a) += vS * (*L2_get(lfZ, mz_j, mz_b, mz_a, 0, 0, AJDK_2_2));
+          *L1_get(E->lf_a3d2_Zt_Sn, ns_j, ns_b, ns_a) += vS * (*L2_get(lfZ, mz_j, mz_b, mz_a, 0, 0, AJDK_3_2));
+        }
+      }
+    }
+  }
+  if (QC_AtTAnAtTAn || QR_AnAtTAnAt) {
+    for (int na_j = 0; na_j < At->rpop_j; ++na_j) {
+      const unsigned na_a = na_a_[na_j], na_b = na_b_[na_j];
+      const unsigned char *row = At->wX + (long)na_b * At->mc_length;
+      if (QC_AtTAnAtTAn)
+        *L1_get(E->lf_et_An, na_j, na_b, na_a) += (double)(-At->cpop_j + 2 * (long long)popcount_masked_row(row, At->mc_j, (long)At->mc_length));
+      if (QR_AnAtTAnAt) {
+        *L1_get(E->lf_a1d1_At_en, na_j, na_b, na_a) += aj[na_a / POPLENGTH + AJDK_1_1 * P] * (*L1_get(E->lf_et_An, na_j, na_b, na_a));
+        *L1_get(E->lf_a1d2_At_en, na_j, na_b, na_a) += aj[na_a / POPLENGTH + AJDK_1_2 * P] * (*L1_get(E->lf_et_An, na_j, na_b, na_a));
+        *L1_get(E->lf_a3d2_At_en, na_j, na_b, na_a) += aj[na_a / POPLENGTH + AJDK_3_2 * P] * (*L1_get(E->lf_et_An, na_j, na_b, na_a));
+      }
+    }
+  }
+  if (QC_AtTAnZtSZn || QC_AtTAnAtTAn || QR_AnZtSZnAt || QR_AnAtTAnAt) {
+    for (int ns_j = 0; ns_j < Tt->rpop_j; ++ns_j) {
+      const unsigned ns_a = ns_a_[ns_j], ns_b = ns_b_[ns_j];
+      if (QC_AtTAnZtSZn || QC_AtTAnAtTAn || QR_AnAtTAnAt) {
+        const unsigned char *row = Tt->wX + (long)ns_b * Tt->mc_length;
+        *L1_get(E->lf_et_Tn, ns_j, ns_b, ns_a) = (double)(-Tt->cpop_j + 2 * (long long)popcount_masked_row(row, Tt->mc_j, (long)Tt->mc_length));
+      }
+      if (QC_AtTAnZtSZn || QR_AnZtSZnAt) {
+        const unsigned char *row = St->wX + (long)ns_b * St->mc_length;
+        *L1_get(E->lf_et_Sn, ns_j, ns_b, ns_a) = (double)(-St->cpop_j + 2 * (long long)popcount_masked_row(row, St->mc_j, (long)St->mc_length));
+      }
+    }
+  }
+  if (QC_AtTAnAtTAn) {
+    for (int ma_j = 0; ma_j < At->cpop_j; ++ma_j) {
+      const unsigned ma_a = ma_a_[ma_j], ma_b = ma_b_[ma_j];
+      *L1_get(E->lf_et_An_a1d1, 0, 0, 0) += (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1));
+    }
+  }
+  if (QR_AnAtTAnAt) {
+    double A_dtmp_a0d1 = 0, A_dtmp_a2d1 = 0;
+    const int AP = (int)psize(An->ncols);
+    for (int nc = 0; nc < AP; ++nc)
+      A_dtmp_a0d1 += (double)aj[nc + AJDK_0_1 * AP] * (double)popcount_bytes(An->mc_j + (long)nc * (POPLENGTH / BIT8), POPLENGTH / BIT8);
+    for (int nc = 0; nc < AP; ++nc)
+      A_dtmp_a2d1 += (double)aj[nc + AJDK_2_1 * AP] * (double)popcount_bytes(An->mc_j + (long)nc * (POPLENGTH / BIT8), POPLENGTH / BIT8);
+    for (int ma_j = 0; ma_j < At->cpop_j; ++ma_j) {
+      const unsigned ma_a = ma_a_[ma_j], ma_b = ma_b_[ma_j];
+      double A_dtmp = A_dtmp_a0d1;
+      // The reference subtracts 2*popcount_xor_lf(row, row), a weighted
+      // popcount of a row XORed with itself, which is exactly zero.
+      A_dtmp -= (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1)) + (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1)) - A_dtmp_a2d1;
+      for (int ns_j = 0; ns_j < Tt->rpop_j; ++ns_j) {
+        const unsigned ns_a = ns_a_[ns_j], ns_b = ns_b_[ns_j];
+        const unsigned char *Tt_tag = Tt->wX + (long)ns_b * Tt->mc_length;
+        const int vT = bget_pm(Tt_tag, ma_a);
+        *L2_get(TAA, ns_j, ns_b, ns_a, ma_j, ma_b, ma_a) = vT * A_dtmp * A_dtmp;
+      }
+    }
+  }
+}
+
+void singlestudy_ww(State &S) {  // bcc_singlestudy_ww (bcc_flattenloop.c:773-831)
+  for (auto &Ep : S.E) {
+    Single *E = Ep.get();
+    if (E->A_rbother && S.A_cbother) {  // At_Yn_a1d1_excerpt (:753-771)
+      L_handle *L = E->lf_An_a1d1;
+      L->spacing_row = SP_b; L->spacing_col = SP_b; L->row_stride = E->M_An->h.rpop_b; L->col_stride = 1;
+      lh_zero(L);
+      M_handle *An = E->M_An->p();
+      for (int my_j = 0; my_j < An->rpop_j; ++my_j) {
+        const unsigned my_a = An->m_a_[my_j], my_b = An->m_b_[my_j];
+        *L1_get(L, my_j, my_b, my_a) = *L2_get(E->lf_An_ajdk, my_j, my_b, my_a, 0, 0, AJDK_1_1);
+      }
+    }
+  }
+  for (auto &Ep : S.E) {
+    Single *E = Ep.get();
+    if (E->A_rbother && S.A_cbother) {
+      M_handle *out = E->M_An_a1d1->p();
+      int one = 1, b_mlt = S.P.B_MLT;
+      wrap_xcalc(TARGS, E->M_An->h.mr_j, E->M_An->h.mr_b, E->M_1->h.mr_j, E->M_1->h.mr_b, E->lf_An_a1d1,
+                 E->lf_An_a1d1->lf, &E->M_An->h.nrows, &one, &out, &b_mlt, 0);
+    }
+  }
+  for (auto &Ep : S.E) {
+    Single *E = Ep.get();
+    if (E->A_rbother && S.A_cbother)
+      wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E->M_At->p(), E->lf_An_a1d1, E->M_An_a1d1->p(), E->M_1->p(), &E->lf_At_An_a1d1);
+  }
+  for (auto &Ep : S.E) singlestudy_vv(S, Ep.get());
+}
+
+// An_a2d2_ZtSn_excerpt (An_ZtSn_ww.c:267-289)
+void a2d2_excerpt(State &S, M_handle *Zt, M_handle *St, L_handle *lf_ZtSn, L_handle *out) {
+  out->spacing_row = SP_b; out->spacing_col = SP_b;
+  out->row_stride = Zt->rpop_b; out->col_stride = St->rpop_b;
+  lh_zero(out);
+  const int P = (int)psize(Zt->nrows);
+  for (int nz_j = 0; nz_j < Zt->rpop_j; ++nz_j) {
+    const unsigned nz_a = Zt->m_a_[nz_j], nz_b = Zt->m_b_[nz_j];
+    for (int ns_j = 0; ns_j < St->rpop_j; ++ns_j) {
+      const unsigned ns_a = St->m_a_[ns_j], ns_b = St->m_b_[ns_j];
+      *L2_get(out, nz_j, nz_b, nz_a, ns_j, ns_b, ns_a) =
+          S.A_ajdk[nz_a / POPLENGTH + AJDK_2_2 * P] * (*L2_get(lf_ZtSn, nz_j, nz_b, nz_a, ns_j, ns_b, ns_a));
+    }
+  }
+}
+
+void doublestudy_ww(State &S) {  // bcc_doublestudy_ww (bcc_flattenloop.c:977-1029)
+  for (auto &E : S.E) {
+    if (E->Z_rbother && S.A_cbother) a2d2_excerpt(S, E->M_Zt->p(), E->M_St->p(), E->lf_ZtSn, E->lf_a2d2_ZtSn);
+    if (E->A_rbother && S.A_cbother) a2d2_excerpt(S, E->M_At->p(), E->M_Tt->p(), E->lf_AtTn, E->lf_a2d2_AtTn);
+  }
+  int b_mlt = S.P.B_MLT;
+  for (auto &E : S.E) {
+    if (E->Z_rbother && S.A_cbother) {
+      M_handle *out = E->M_a2d2_ZtSn->p();
+      wrap_xcalc(TARGS, E->M_Zt->h.mr_j, E->M_Zt->h.mr_b, E->M_St->h.mr_j, E->M_St->h.mr_b, E->lf_a2d2_ZtSn,
+                 E->lf_a2d2_ZtSn->lf, &E->M_Zt->h.nrows, &E->M_St->h.nrows, &out, &b_mlt, 0);
+    }
+    if (E->A_rbother && S.A_cbother) {
+      M_handle *out = E->M_a2d2_AtTn->p();
+      wrap_xcalc(TARGS, E->M_At->h.mr_j, E->M_At->h.mr_b, E->M_Tt->h.mr_j, E->M_Tt->h.mr_b, E->lf_a2d2_AtTn,
+                 E->lf_a2d2_AtTn->lf, &E->M_At->h.nrows, &E->M_Tt->h.nrows, &out, &b_mlt, 0);
+    }
+  }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      for (L_handle *L : {F->lf_An_a2d2_Zt_Sn, F->lf_An_a2d2_At_Tn}) {
+        L->row_stride = E1->A_nrows; L->spacing_row = SP_a; L->col_stride = S.T_ncols; L->spacing_col = SP_a; lh_zero(L);
+      }
+      if (E1->A_rbother && S.A_cbother && E2->Z_rbother)
+        wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->lf_a2d2_ZtSn, E2->M_a2d2_ZtSn->p(), E2->M_St->p(), &F->lf_An_a2d2_Zt_Sn);
+      if (E1->A_rbother && S.A_cbother && E2->A_rbother)
+        wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->lf_a2d2_AtTn, E2->M_a2d2_AtTn->p(), E2->M_Tt->p(), &F->lf_An_a2d2_At_Tn);
+    }
+}
+
+double mask_sum(State &S, M_handle *An, int k) {
+  const int P = (int)psize(An->ncols);
+  double s = 0;
+  for (int nc = 0; nc < P; ++nc)
+    s += (double)S.A_ajdk[nc + k * P] * (double)popcount_bytes(An->mc_j + (long)nc * (POPLENGTH / BIT8), POPLENGTH / BIT8);
+  return s;
+}
+
+// get_flattenloop (bcc_flattenloop.c:1431-1889) for one bin pair, without Y terms.
+void flattenloop_pair(State &S, Double *F) {
+  Single *E1 = S.E[F->nb1].get(), *E2 = S.E[F->nb2].get();
+  M_handle *An1 = E1->M_An->p(), *At1 = E1->M_At->p(), *Tt2 = E2->M_Tt->p();
+  double *aj = S.A_ajdk.data();
+  const int P = (int)psize(At1->nrows);
+  const int A_ncols = At1->nrows, T = E1->M_Tt->h.nrows, A_nrows1 = At1->ncols;
+  const int QR_AnZtSZnAt = E1->A_rbother && S.A_cbother && E2->Z_rbother;
+  const int QR_AnAtTAnAt = E1->A_rbother && S.A_cbother && E2->A_rbother;
+  const int QC_AtTAnZtSZn = QR_AnZtSZnAt, QC_AtTAnAtTAn = QR_AnAtTAnAt;
+  for (L_handle *L : {F->QR_AnZtSZnAt, F->QR_AnAtTAnAt}) {
+    L->row_stride = A_nrows1; L->spacing_row = SP_a; L->col_stride = T; L->spacing_col = SP_b; lh_zero(L);
+  }
+  for (L_handle *L : {F->QC_AtTAnZtSZn, F->QC_AtTAnAtTAn}) {
+    L->row_stride = A_ncols; L->spacing_row = SP_a; L->col_stride = T; L->spacing_col = SP_b; lh_zero(L);
+  }
+  double lf_A_a0d2 = 0, lf_A_a2d2 = 0, lf_A_a4d2 = 0, lf_A_a0d1 = 0, lf_A_a2d1 = 0;
+  if (QR_AnZtSZnAt || QR_AnAtTAnAt) {
+    lf_A_a0d2 = mask_sum(S, An1, AJDK_0_2);
+    lf_A_a2d2 = mask_sum(S, An1, AJDK_2_2);
+    lf_A_a4d2 = mask_sum(S, An1, AJDK_4_2);
+    lf_A_a0d1 = mask_sum(S, An1, AJDK_0_1);
+    lf_A_a2d1 = mask_sum(S, An1, AJDK_2_1);
+  }
+  if (QR_AnZtSZnAt || QR_AnAtTAnAt) {
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int ma_j = 0; ma_j < An1->rpop_j; ++ma_j) {
+        const unsigned ma_a = An1->m_a_[ma_j], ma_b = An1->m_b_[ma_j];
+        if (QR_AnZtSZnAt) *L2_get(F->QR_AnZtSZnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) = *L2_get(F->lf_AnZt_S_ZnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a);
+        if (QR_AnAtTAnAt) *L2_get(F->QR_AnAtTAnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) = *L2_get(F->lf_AnAt_T_AnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a);
+      }
+    }
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int ma_j = 0; ma_j < An1->rpop_j; ++ma_j) {
+        const unsigned ma_a = An1->m_a_[ma_j], ma_b = An1->m_b_[ma_j];
+        L_handle *lfA = E1->lf_An_ajdk;
+        if (QR_AnZtSZnAt) {
+          const double et = *L1_get(E2->lf_et_Sn, ns_j, ns_b, ns_a);
+          const double dtmp =
+              +1 * lf_A_a0d2 * et
+              - 2 * (*L1_get(E2->lf_a1d2_Zt_Sn, ns_j, ns_b, ns_a))
+              + 1 * lf_A_a2d2 * et
+              - 2 * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_2)) * et
+              + 4 * (*L2_get(F->lf_An_a2d2_Zt_Sn, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a))
+              - 2 * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_3_2)) * et
+              + 1 * lf_A_a2d2 * et
+              - 2 * (*L1_get(E2->lf_a3d2_Zt_Sn, ns_j, ns_b, ns_a))
+              + 1 * lf_A_a4d2 * et;
+          *L2_get(F->QR_AnZtSZnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += -dtmp;
+        }
+        if (QR_AnAtTAnAt) {
+          const double et = *L1_get(E2->lf_et_Tn, ns_j, ns_b, ns_a);
+          const double dtmp =
+              +1 * lf_A_a0d2 * et
+              - 2 * (*L1_get(E2->lf_a1d2_At_Tn, ns_j, ns_b, ns_a))
+              + 1 * lf_A_a2d2 * et
+              - 2 * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_2)) * et
+              + 4 * (*L2_get(F->lf_An_a2d2_At_Tn, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a))
+              - 2 * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_3_2)) * et
+              + 1 * lf_A_a2d2 * et
+              - 2 * (*L1_get(E2->lf_a3d2_At_Tn, ns_j, ns_b, ns_a))
+              + 1 * lf_A_a4d2 * et;
+          *L2_get(F->QR_AnAtTAnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += -dtmp;
+        }
+      }
+    }
+  }
+  if (QR_AnAtTAnAt && F->nb1 == F->nb2) {
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int ma_j = 0; ma_j < An1->rpop_j; ++ma_j) {
+        const unsigned ma_a = An1->m_a_[ma_j], ma_b = An1->m_b_[ma_j];
+        const double dtmp = *L2_get(E1->lf_T_AnAt_AnAt, ns_j, ns_b, ns_a, ma_j, ma_b, ma_a);
+        *L2_get(F->QR_AnAtTAnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += -dtmp;
+      }
+    }
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      const unsigned char *Tt_tag = Tt2->wX + (long)ns_b * Tt2->mc_length;
+      for (int ma_j = 0; ma_j < An1->rpop_j; ++ma_j) {
+        const unsigned ma_a = An1->m_a_[ma_j], ma_b = An1->m_b_[ma_j];
+        const int vT = bget_pm(Tt_tag, ma_a);
+        L_handle *lfA = E1->lf_An_ajdk;
+        const double dtmp = vT * (+1 * lf_A_a0d2
+                                  - 4 * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_1_2))
+                                  + 6 * lf_A_a2d2
+                                  - 4 * (*L2_get(lfA, ma_j, ma_b, ma_a, 0, 0, AJDK_3_2))
+                                  + 1 * lf_A_a4d2);
+        *L2_get(F->QR_AnAtTAnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += +dtmp;
+      }
+    }
+  }
+  if (QC_AtTAnZtSZn || QC_AtTAnAtTAn) {
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int na_j = 0; na_j < At1->rpop_j; ++na_j) {
+        const unsigned na_a = At1->m_a_[na_j], na_b = At1->m_b_[na_j];
+        const double D = aj[na_a / POPLENGTH + AJDK_0_1 * P];
+        if (QC_AtTAnZtSZn) *L2_get(F->QC_AtTAnZtSZn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = D * (*L2_get(F->lf_At_T_AnZt_S_Zn, na_j, na_b, na_a, ns_j, ns_b, ns_a));
+        if (QC_AtTAnAtTAn) *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = D * (*L2_get(F->lf_At_T_AnAt_T_An, na_j, na_b, na_a, ns_j, ns_b, ns_a));
+      }
+    }
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int na_j = 0; na_j < At1->rpop_j; ++na_j) {
+        const unsigned na_a = At1->m_a_[na_j], na_b = At1->m_b_[na_j];
+        const double D01 = aj[na_a / POPLENGTH + AJDK_0_1 * P];
+        const double A10 = aj[na_a / POPLENGTH + AJDK_1_0 * P];
+        const double A20 = aj[na_a / POPLENGTH + AJDK_2_0 * P];
+        const double etT1 = *L1_get(E1->lf_et_Tn, ns_j, ns_b, ns_a);
+        const double AtTn1 = *L2_get(E1->lf_AtTn, na_j, na_b, na_a, ns_j, ns_b, ns_a);
+        if (QC_AtTAnZtSZn) {
+          const double etS2 = *L1_get(E2->lf_et_Sn, ns_j, ns_b, ns_a);
+          const double ZtSn2 = *L2_get(E2->lf_ZtSn, na_j, na_b, na_a, ns_j, ns_b, ns_a);
+          const double dtmp = D01 * (+(1 * etT1) - (2 * A10 * AtTn1) + (A20 * etT1)) * D01 *
+                              (+(1 * etS2) - (2 * A10 * ZtSn2) + (A20 * etS2));
+          *L2_get(F->QC_AtTAnZtSZn, na_j, na_b, na_a, ns_j, ns_b, ns_a) += -dtmp;
+        }
+        if (QC_AtTAnAtTAn) {
+          const double etT2 = *L1_get(E2->lf_et_Tn, ns_j, ns_b, ns_a);
+          const double AtTn2 = *L2_get(E2->lf_AtTn, na_j, na_b, na_a, ns_j, ns_b, ns_a);
+          const double dtmp = D01 * (+(1 * etT1) - (2 * A10 * AtTn1) + (A20 * etT1)) * D01 *
+                              (+(1 * etT2) - (2 * A10 * AtTn2) + (A20 * etT2));
+          *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) += -dtmp;
+        }
+      }
+    }
+  }
+  if (QC_AtTAnAtTAn && F->nb1 == F->nb2) {
+    const double rpop = (double)An1->rpop_j;
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int na_j = 0; na_j < At1->rpop_j; ++na_j) {
+        const unsigned na_a = At1->m_a_[na_j], na_b = At1->m_b_[na_j];
+        const double A01 = aj[na_a / POPLENGTH + AJDK_0_1 * P], A11 = aj[na_a / POPLENGTH + AJDK_1_1 * P];
+        const double A21 = aj[na_a / POPLENGTH + AJDK_2_1 * P];
+        const double etAn = *L1_get(E1->lf_et_An, na_j, na_b, na_a);
+        const double etAa = *L1_get(E1->lf_et_An_a1d1, 0, 0, 0);
+        const double AtAa = *L1_get(E1->lf_At_An_a1d1, na_j, na_b, na_a);
+        const double dtmp = (+(1 * A01 * rpop * lf_A_a0d1)
+                             - (2 * A11 * etAn * lf_A_a0d1)
+                             + (1 * A21 * rpop * lf_A_a0d1)
+                             - (2 * A01 * etAa)
+                             + (4 * A11 * AtAa)
+                             - (2 * A21 * etAa)
+                             + (1 * A01 * rpop * lf_A_a2d1)
+                             - (2 * A11 * etAn * lf_A_a2d1)
+                             + (1 * A21 * rpop * lf_A_a2d1));
+        *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) += -dtmp;
+      }
+    }
+    for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
+      const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+      for (int na_j = 0; na_j < At1->rpop_j; ++na_j) {
+        const unsigned na_a = At1->m_a_[na_j], na_b = At1->m_b_[na_j];
+        const double etAn = *L1_get(E1->lf_et_An, na_j, na_b, na_a);
+        const double dtmp = (+(1 * aj[na_a / POPLENGTH + AJDK_0_2 * P] * rpop)
+                             - (4 * aj[na_a / POPLENGTH + AJDK_1_2 * P] * etAn)
+                             + (6 * aj[na_a / POPLENGTH + AJDK_2_2 * P] * rpop)
+                             - (4 * aj[na_a / POPLENGTH + AJDK_3_2 * P] * etAn)
+                             + (1 * aj[na_a / POPLENGTH + AJDK_4_2 * P] * rpop));
+        *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) += +dtmp;
+      }
+    }
+  }
+}
+
+void flattenloop(State &S) {
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) flattenloop_pair(S, S.f(nb1, nb2));
+}
+
+// dra_plusdivequals_s___m_m (ra_stats.c:69-76)
+void plusdiv(const State &S, double *d1, unsigned long long nrows, unsigned long long ncols, const double *d2,
+             double denominator, const unsigned char *bmr, const unsigned char *bmc) {
+  double d_use = denominator;
+  if (fabs(d_use) < S.P.tolerance) d_use = 1;
+  for (unsigned long long c = 0; c < ncols; ++c)
+    if (bget_on(bmc, (long)c))
+      for (unsigned long long r = 0; r < nrows; ++r)
+        if (bget_on(bmr, (long)r)) d1[r + c * nrows] += d2[r + c * nrows] / d_use;
+}
+
+// dra_plustimesequals_s___m_m (ra_stats.c:63-68)
+void plustimes(double *d1, unsigned long long nrows, unsigned long long ncols, const double *d2, double m,
+               const unsigned char *bmr, const unsigned char *bmc) {
+  for (unsigned long long c = 0; c < ncols; ++c)
+    if (bget_on(bmc, (long)c))
+      for (unsigned long long r = 0; r < nrows; ++r)
+        if (bget_on(bmr, (long)r)) d1[r + c * nrows] += m * d2[r + c * nrows];
+}
+
+void dra_sumx0(double *d, unsigned long long stride, unsigned long long length) {
+  for (unsigned long long r = 1; r < length; ++r) d[0] += d[r * stride];
+}
+
+void sumscores_nrm(State &S) {  // bcc_sumscores_nrm (bcc_sumscores.c:550-779), GLOBAL_Ireq <= 0
+  const int nb = S.nbins, T = S.T_ncols;
+  for (int nb1 = 0; nb1 < nb; ++nb1)
+    for (int nb2 = 0; nb2 < nb; ++nb2) {
+      const int nbx = nb1 + nb2 * nb;
+      Single *E = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      Double *F = S.f(nb1, nb2);
+      const unsigned long long AN = (unsigned long long)E->A_nrows;
+      if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
+        double *d = &E->QR_AnZtSZnAt_nrm[nb2 * AN * T];
+        memset(d, 0, AN * T * sizeof(double));
+        const long long lld = (long long)(S.Z_rpop_j_total - 0) * (long long)(E2->M_Zn->h.cpop_j) * (long long)(E2->M_Zn->h.cpop_j - 1);
+        plusdiv(S, d, AN, T, F->QR_AnZtSZnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
+      }
+      if (E->A_rbother && S.A_cbother && E2->A_rbother) {
+        double *d = &E->QR_AnAtTAnAt_nrm[nb2 * AN * T];
+        memset(d, 0, AN * T * sizeof(double));
+        const long long lld = (long long)(S.A_rpop_j_total - 1) * (long long)(E2->M_An->h.cpop_j) * (long long)(E2->M_An->h.cpop_j - 1);
+        plusdiv(S, d, AN, T, F->QR_AnAtTAnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
+      }
+      const unsigned long long AC = (unsigned long long)S.A_ncols;
+      if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
+        double *d = &S.QC_AtTAnZtSZn_nrm[nbx * AC * T];
+        memset(d, 0, AC * T * sizeof(double));
+        const long long lld = (long long)(S.A_rpop_j_total) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(S.Z_rpop_j_total);
+        plusdiv(S, d, AC, T, F->QC_AtTAnZtSZn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
+      }
+      if (E->A_rbother && S.A_cbother && E2->A_rbother) {
+        double *d = &S.QC_AtTAnAtTAn_nrm[nbx * AC * T];
+        memset(d, 0, AC * T * sizeof(double));
+        const long long lld = (long long)(S.A_rpop_j_total) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(S.A_rpop_j_total - 1);
+        plusdiv(S, d, AC, T, F->QC_AtTAnAtTAn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
+      }
+    }
+  for (int ns_a = 0; ns_a < T; ++ns_a) {
+    if (!bget_on(S.T_bmc_j.data(), ns_a)) continue;
+    for (int nb1 = 0; nb1 < nb; ++nb1) {
+      Single *E = S.E[nb1].get();
+      const unsigned long long AN = (unsigned long long)E->A_nrows;
+      if (E->A_rbother && S.A_cbother && E->Z_rbother)
+        for (int ma = 0; ma < E->A_nrows; ++ma)
+          if (bget_on(E->A_bmr_b.data(), ma) && bget_on(E->A_bmr_j.data(), ma))
+            dra_sumx0(&E->QR_AnZtSZnAt_nrm[ma + ns_a * AN], AN * T, nb);
+      if (E->A_rbother && S.A_cbother)
+        for (int ma = 0; ma < E->A_nrows; ++ma)
+          if (bget_on(E->A_bmr_b.data(), ma) && bget_on(E->A_bmr_j.data(), ma))
+            dra_sumx0(&E->QR_AnAtTAnAt_nrm[ma + ns_a * AN], AN * T, nb);
+    }
+    const unsigned long long AC = (unsigned long long)S.A_ncols;
+    if (S.A_rpop_b_total && S.A_cbother && S.Z_rpop_b_total)
+      for (int na = 0; na < S.A_ncols; ++na)
+        if (bget_on(S.A_bmc_b.data(), na) && bget_on(S.A_bmc_j.data(), na))
+          dra_sumx0(&S.QC_AtTAnZtSZn_nrm[na + ns_a * AC], AC * T, (unsigned long long)nb * nb);
+    if (S.A_cbother && S.A_rpop_b_total)
+      for (int na = 0; na < S.A_ncols; ++na)
+        if (bget_on(S.A_bmc_b.data(), na) && bget_on(S.A_bmc_j.data(), na))
+          dra_sumx0(&S.QC_AtTAnAtTAn_nrm[na + ns_a * AC], AC * T, (unsigned long long)nb * nb);
+  }
+}
+
+void sumscores_cmb(State &S) {  // bcc_sumscores_cmb (bcc_sumscores.c:324-356)
+  const unsigned char bmc1 = 255;
+  if (S.A_cbother && S.A_rpop_b_total) {
+    if (S.A_rpop_b_total && S.A_cbother && S.Z_rpop_b_total)
+      for (int nbx = 0; nbx < S.nbins * S.nbins; ++nbx) {
+        const size_t o = (size_t)nbx * S.A_ncols * S.T_ncols;
+        plustimes(&S.QC_AtTAnAtTAn_nrm[o], S.A_ncols, 1, &S.QC_AtTAnZtSZn_nrm[o], -1.0, S.A_bmc_j.data(), &bmc1);
+      }
+  }
+  for (auto &E : S.E) {
+    if (E->A_rbother && S.A_cbother && E->Z_rbother)
+      for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+        const size_t o = (size_t)nb2 * E->A_nrows * S.T_ncols;
+        plustimes(&E->QR_AnAtTAnAt_nrm[o], E->A_nrows, 1, &E->QR_AnZtSZnAt_nrm[o], -1.0, E->A_bmr_j.data(), &bmc1);
+      }
+  }
+}
+
+void sumscores_xij(State &S) {  // bcc_sumscores_xij (bcc_sumscores.c:225-322)
+  S.Irem = 0;
+  for (auto &E : S.E) S.Irem += (E->A_rpop_j > 0 ? 1 : 0);
+  S.Ireq = 0;  // xcc_get_Ireq("empty low") with GLOBAL_Ireq <= 0
+  const int Irow = 0, Icol = 0;
+  if (S.A_cbother && S.A_rpop_b_total) {
+    int na_b = 0, na_j = 0;
+    for (int na_a = 0; na_a < S.A_ncols; ++na_a) {
+      if (bget_on(S.A_bmc_b.data(), na_a)) {
+        if (bget_on(S.A_bmc_j.data(), na_a)) {
+          S.QC_svalue[na_j] = S.QC_AtTAnAtTAn_nrm[na_a + 0 * S.A_ncols + (size_t)Icol * S.A_ncols * S.T_ncols];
+          S.QC_index_local_mc_a[na_j] = na_a; S.QC_index_local_mc_b[na_j] = na_b; S.QC_index_local_mc_j[na_j] = na_j;
+          na_j++;
+        }
+        na_b++;
+      }
+    }
+    quicksort_xij(S.P.recursion_limit, S.QC_svalue.data(), S.QC_index_local_mc_a.data(), S.QC_index_local_mc_b.data(),
+                  S.QC_index_local_mc_j.data(), nullptr, nullptr, nullptr, 0, (int)S.A_cpop_j - 1);
+  }
+  if (S.A_rpop_b_total && S.A_cbother) {
+    S.A_nrows_total = 0; S.A_rpop_b_total = 0; S.A_rpop_j_total = 0;
+    for (int nb1 = 0; nb1 < S.nbins; ++nb1) {
+      Single *E = S.E[nb1].get();
+      int ma_b = 0, ma_j = 0;
+      for (int ma_a = 0; ma_a < E->A_nrows; ++ma_a) {
+        if (bget_on(E->A_bmr_b.data(), ma_a)) {
+          if (bget_on(E->A_bmr_j.data(), ma_a)) {
+            const unsigned t = S.A_rpop_j_total;
+            S.QR_svalue[t] = E->QR_AnAtTAnAt_nrm[ma_a + 0 * E->A_nrows + (size_t)Irow * E->A_nrows * S.T_ncols];
+            S.QR_index_local_mr_a[t] = ma_a; S.QR_index_local_mr_b[t] = ma_b; S.QR_index_local_mr_j[t] = ma_j;
+            S.QR_index_local_nb[t] = nb1;
+            S.QR_index_global_mr_a[t] = E->QR_index_global_mr_a[ma_a];
+            S.QR_index_global_mr_b[t] = E->QR_index_global_mr_b[ma_a];
+            ma_j++; S.A_rpop_j_total++;
+          }
+          ma_b++; S.A_rpop_b_total++;
+        }
+        S.A_nrows_total++;
+      }
+    }
+    quicksort_xij(S.P.recursion_limit, S.QR_svalue.data(), S.QR_index_local_mr_a.data(), S.QR_index_local_mr_b.data(),
+                  S.QR_index_local_mr_j.data(), S.QR_index_local_nb.data(), S.QR_index_global_mr_a.data(),
+                  S.QR_index_global_mr_b.data(), 0, (int)S.A_rpop_j_total - 1);
+  }
+}
+
+double ra_mean(const double *v, unsigned long long n) {  // ra_stats "double" mean (ra_stats.c:24-25)
+  double mean = 0;
+  for (unsigned long long i = 0; i < n; ++i) mean += v[i];
+  mean /= (double)n;
+  return mean;
+}
+
+void sumscores_mxA(State &S) {  // bcc_sumscores_mxA / mxB / mxC (bcc_sumscores.c:37-205)
+  int rdrop = 0, cdrop = 0;
+  get_xdrop(S.P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, &rdrop, &cdrop);
+  for (int nc = 0; nc < S.A_ncols; ++nc) S.A_umc_j[nc] = (unsigned char)bget_on(S.A_bmc_j.data(), nc);
+  for (int nc = 0; nc < S.A_ncols; ++nc) { S.A_umc_j_rtn[nc] = S.A_umc_j[nc]; S.A_umc_j_rmv[nc] = 0; }
+  for (int nc = 0; nc < std::min(cdrop, (int)S.A_cpop_j); ++nc) {
+    S.A_umc_j_rmv[S.QC_index_local_mc_a[nc]] = 1; S.A_umc_j_rtn[S.QC_index_local_mc_a[nc]] = 0;
+  }
+  for (auto &E : S.E) {
+    for (int nr = 0; nr < E->A_nrows; ++nr) E->A_umr_j[nr] = (unsigned char)bget_on(E->A_bmr_j.data(), nr);
+    for (int nr = 0; nr < E->A_nrows; ++nr) { E->A_umr_j_rtn[nr] = E->A_umr_j[nr]; E->A_umr_j_rmv[nr] = 0; }
+  }
+  for (int nr = 0; nr < std::min(rdrop, (int)S.A_rpop_j_total); ++nr) {
+    Single *E = S.E[S.QR_index_local_nb[nr]].get();
+    E->A_umr_j_rmv[S.QR_index_local_mr_a[nr]] = 1; E->A_umr_j_rtn[S.QR_index_local_mr_a[nr]] = 0;
+  }
+  // mxB
+  bits_from_ura(S.A_bmc_j, S.A_umc_j, S.A_ncols);
+  bits_from_ura(S.A_bmc_j_rmv, S.A_umc_j_rmv, S.A_ncols);
+  bits_from_ura(S.A_bmc_j_rtn, S.A_umc_j_rtn, S.A_ncols);
+  for (auto &E : S.E) {
+    bits_from_ura(E->A_bmr_j, E->A_umr_j, E->A_nrows);
+    bits_from_ura(E->A_bmr_j_rmv, E->A_umr_j_rmv, E->A_nrows);
+    bits_from_ura(E->A_bmr_j_rtn, E->A_umr_j_rtn, E->A_nrows);
+  }
+  S.A_cpop_j = popcount_bytes(S.A_bmc_j.data(), S.A_mc_length);
+  S.A_cpop_j_rmv = popcount_bytes(S.A_bmc_j_rmv.data(), S.A_mc_length);
+  S.A_cpop_j_rtn = popcount_bytes(S.A_bmc_j_rtn.data(), S.A_mc_length);
+  for (auto &E : S.E) {
+    E->A_rpop_j = popcount_bytes(E->A_bmr_j.data(), E->A_mr_length);
+    E->A_rpop_j_rmv = popcount_bytes(E->A_bmr_j_rmv.data(), E->A_mr_length);
+    E->A_rpop_j_rtn = popcount_bytes(E->A_bmr_j_rtn.data(), E->A_mr_length);
+  }
+  lrup_mxset(S);
+  // mxC: trace
+  Output &O = *S.out;
+  double m = ra_mean(S.QR_svalue.data(), S.A_rpop_j_total);
+  const double trace_QR = std::isfinite(m) ? m : 1.0;
+  m = ra_mean(S.QC_svalue.data(), S.A_cpop_j);
+  const double trace_QC = std::isfinite(m) ? m : 1.0;
+  O.trace.push_back((double)O.iterations);
+  O.trace.push_back((double)S.A_rpop_j_total);
+  O.trace.push_back((double)S.A_cpop_j);
+  O.trace.push_back(trace_QR);
+  O.trace.push_back(trace_QC);
+  O.trace.push_back((double)S.Irem);
+  O.iterations++;
+  for (int nr = 0; nr < std::min(rdrop, (int)S.A_rpop_j_total); ++nr) {
+    O.xdrop_a.push_back(S.QR_index_global_mr_a[nr]); O.xdrop_a.push_back(-1);
+    O.xdrop_b.push_back(S.QR_index_global_mr_b[nr]); O.xdrop_b.push_back(-1);
+  }
+  for (int nc = 0; nc < std::min(cdrop, (int)S.A_cpop_j); ++nc) {
+    O.xdrop_a.push_back(-1); O.xdrop_a.push_back(S.QC_index_local_mc_a[nc]);
+    O.xdrop_b.push_back(-1); O.xdrop_b.push_back(S.QC_index_local_mc_b[nc]);
+  }
+}
+
+// --- low-rank update ------------------------------------------------------------
+
+void lrup_QR(State &S) {  // bcc_lrup_QR_YnWt_stage_0/1/3 (bcc_lrup.c:659-892)
+  double *aj = S.A_ajdk.data();
+  for (auto &E : S.E) {
+    if (E->A_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_jn->p(), aj, &E->lf_jn_ajdk);
+    if (E->Z_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_vn->p(), aj, &E->lf_vn_ajdk);
+  }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        wrap_AnZt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_jn->p(), E2->M_vn->p(), aj, E1->lf_jn_ajdk, E2->lf_vn_ajdk, &F->lf_jnvt);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        if (nb1 == nb2)
+          wrap_AnAt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_jn->p(), E2->M_jn->p(), aj, E1->lf_jn_ajdk, E2->lf_jn_ajdk, &F->lf_jnjt);
+        if (nb1 < nb2)
+          wrap_AnZt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_jn->p(), E2->M_jn->p(), aj, E1->lf_jn_ajdk, E2->lf_jn_ajdk, &F->lf_jnjt);
+      }
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
+        lh_transpose(S.f(nb1, nb2)->lf_jnjt, S.f(nb2, nb1)->lf_jnjt);
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        for (unsigned long long i = 0; i < F->lf_AnZt->length; ++i) F->lf_AnZt->lf[i] -= F->lf_jnvt->lf[i];
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother)
+        for (unsigned long long i = 0; i < F->lf_AnAt->length; ++i) F->lf_AnAt->lf[i] -= F->lf_jnjt->lf[i];
+    }
+}
+
+void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5-481)
+  double *aj = S.A_ajdk.data();
+  // a0
+  for (auto &E : S.E) {
+    if (E->A_rbother && S.A_cbother) {
+      wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_kn->p(), aj, &E->lf_kn_ajdk);
+      wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_hn->p(), aj, &E->lf_hn_ajdk);
+      wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_an->p(), aj, &E->lf_an_ajdk);
+    }
+    if (E->Z_rbother && S.A_cbother) {
+      wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_zn->p(), aj, &E->lf_zn_ajdk);
+      wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_vn->p(), aj, &E->lf_vn_ajdk);
+    }
+  }
+  // a1
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) {
+        wrap_AnZt_vv__run(TARGS, T_pm, SP_j, SP_j, E1->M_kn->p(), E2->M_zn->p(), aj, E1->lf_kn_ajdk, E2->lf_zn_ajdk, &F->lf_knzt);
+        wrap_AnZt_vv__run(TARGS, T_pm, SP_j, SP_j, E1->M_hn->p(), E2->M_vn->p(), aj, E1->lf_hn_ajdk, E2->lf_vn_ajdk, &F->lf_hnvt);
+      }
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        wrap_AnZt_vv__run(TARGS, T_pm, SP_j, SP_j, E1->M_an->p(), E2->M_kn->p(), aj, E1->lf_an_ajdk, E2->lf_kn_ajdk, &F->lf_ankt);
+        if (nb1 == nb2)
+          wrap_AnAt_vv__run(TARGS, T_pm, SP_j, SP_j, E1->M_kn->p(), E2->M_kn->p(), aj, E1->lf_kn_ajdk, E2->lf_kn_ajdk, &F->lf_knkt);
+        if (nb1 < nb2)
+          wrap_AnZt_vv__run(TARGS, T_pm, SP_j, SP_j, E1->M_kn->p(), E2->M_kn->p(), aj, E1->lf_kn_ajdk, E2->lf_kn_ajdk, &F->lf_knkt);
+      }
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2), *Ft = S.f(nb2, nb1);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        lh_transpose(F->lf_knat, Ft->lf_ankt);
+        if (nb1 > nb2) lh_transpose(F->lf_knkt, Ft->lf_knkt);
+      }
+    }
+  // a2
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) {
+        xcalc_excerpt(S, F->M_knzt_trm, E1->M_kn, E2->M_zn, F->lf_knzt, F->M_knzt);
+        xcalc_excerpt(S, F->M_hnvt_trm, E1->M_hn, E2->M_vn, F->lf_hnvt, F->M_hnvt);
+      }
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        xcalc_excerpt(S, F->M_ankt_trm, E1->M_an, E2->M_kn, F->lf_ankt, F->M_ankt);
+        if (nb1 <= nb2) xcalc_excerpt(S, F->M_knkt_trm, E1->M_kn, E2->M_kn, F->lf_knkt, F->M_knkt);
+      }
+    }
+  // a3
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) {
+        bitplane_excerpt(S, F->M_knzt_trm, E1->M_kt, E1->M_rt, E1->M_kn, E2->M_zn, E2->M_St, E2->M_zt, F->M_knzt, &F->lf_kt_r_knzt_s_zn);
+        bitplane_excerpt(S, F->M_hnvt_trm, E1->M_kt, E1->M_rt, E1->M_hn, E2->M_vn, E2->M_St, E2->M_zt, F->M_hnvt, &F->lf_kt_r_hnvt_s_zn);
+      }
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        bitplane_excerpt(S, F->M_ankt_trm, E1->M_at, E1->M_tt, E1->M_an, E2->M_kn, E2->M_rt, E2->M_kt, F->M_ankt, &F->lf_at_t_ankt_r_kn);
+        if (nb1 <= nb2)
+          bitplane_excerpt(S, F->M_knkt_trm, E1->M_kt, E1->M_rt, E1->M_kn, E2->M_kn, E2->M_rt, E2->M_kt, F->M_knkt, &F->lf_kt_r_knkt_r_kn);
+      }
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2), *Ft = S.f(nb2, nb1);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        lh_duplicate(F->lf_kt_r_knat_t_an, Ft->lf_at_t_ankt_r_kn);
+        if (nb1 > nb2) lh_duplicate(F->lf_kt_r_knkt_r_kn, Ft->lf_kt_r_knkt_r_kn);
+      }
+    }
+  // b0
+  for (auto &E : S.E) {
+    if (E->A_rbother && S.A_cbother) {
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_at->p(), E->M_tt->p(), nullptr, nullptr, nullptr, &E->lf_attn);
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_jt->p(), E->M_tt->p(), nullptr, nullptr, nullptr, &E->lf_jttn);
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_kt->p(), E->M_rt->p(), nullptr, nullptr, nullptr, &E->lf_ktrn);
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_ht->p(), E->M_rt->p(), nullptr, nullptr, nullptr, &E->lf_htrn);
+    }
+    if (E->Z_rbother && S.A_cbother) {
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_zt->p(), E->M_St->p(), nullptr, nullptr, nullptr, &E->lf_ztsn);
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_vt->p(), E->M_St->p(), nullptr, nullptr, nullptr, &E->lf_vtsn);
+    }
+  }
+  // b1
+  for (auto &E : S.E) {
+    if (E->Z_rbother && S.A_cbother)
+      wrap_AtTYn_vv__run(TARGS, SP_j, SP_j, SP_j, E->M_zt->p(), E->M_St->p(), E->M_vt->p(), aj, aj, E->lf_ztsn, E->lf_vtsn, &E->lf_ztsvn);
+    if (E->A_rbother && S.A_cbother) {
+      wrap_AtTYn_vv__run(TARGS, SP_j, SP_j, SP_j, E->M_at->p(), E->M_tt->p(), E->M_jt->p(), aj, aj, E->lf_attn, E->lf_jttn, &E->lf_attjn);
+      wrap_AtTYn_vv__run(TARGS, SP_j, SP_j, SP_j, E->M_kt->p(), E->M_rt->p(), E->M_ht->p(), aj, aj, E->lf_ktrn, E->lf_htrn, &E->lf_ktrhn);
+    }
+  }
+  // b2
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_at->p(), E1->M_tt->p(), E1->M_jt->p(), E2->M_vt->p(), E2->M_St->p(), E2->M_zt->p(), aj, E1->lf_attjn, E2->lf_ztsvn, &F->lf_attjn____vtszn);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        if (nb1 <= nb2)
+          wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_at->p(), E1->M_tt->p(), E1->M_jt->p(), E2->M_jt->p(), E2->M_tt->p(), E2->M_at->p(), aj, E1->lf_attjn, E2->lf_attjn, &F->lf_attjn____jttan);
+        wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_at->p(), E1->M_tt->p(), E1->M_jt->p(), E2->M_ht->p(), E2->M_rt->p(), E2->M_kt->p(), aj, E1->lf_attjn, E2->lf_ktrhn, &F->lf_attjn____htrkn);
+        if (nb1 <= nb2)
+          wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_kt->p(), E1->M_rt->p(), E1->M_ht->p(), E2->M_ht->p(), E2->M_rt->p(), E2->M_kt->p(), aj, E1->lf_ktrhn, E2->lf_ktrhn, &F->lf_ktrhn____htrkn);
+      }
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2), *Ft = S.f(nb2, nb1);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        if (nb1 > nb2) lh_duplicate(F->lf_attjn____jttan, Ft->lf_attjn____jttan);
+        lh_duplicate(F->lf_ktrhn____jttan, Ft->lf_attjn____htrkn);
+        if (nb1 > nb2) lh_duplicate(F->lf_ktrhn____htrkn, Ft->lf_ktrhn____htrkn);
+      }
+    }
+}
+
+void lrup_mxdup(State &S) {  // bcc_lrup_mxdup (bcc_lrup.c:1128-1138)
+  S.A_bmc_j = S.A_bmc_j_rtn;
+  for (int i = 0; i < S.A_ncols; ++i) S.A_umc_j[i] = S.A_umc_j_rtn[i];
+  for (auto &E : S.E) {
+    E->A_bmr_j = E->A_bmr_j_rtn;
+    for (int i = 0; i < E->A_nrows; ++i) E->A_umr_j[i] = E->A_umr_j_rtn[i];
+  }
+}
+
+// L2_clean (L_init.c:287-326)
+void L2_clean(L_handle *L, unsigned long long nrows, const unsigned char *mr_b, const unsigned char *mr_j,
+              unsigned long long ncols, const unsigned char *mc_b, const unsigned char *mc_j) {
+  unsigned long long nc_j = 0, nc_b = 0;
+  for (unsigned long long nc_a = 0; nc_a < ncols; ++nc_a) {
+    if (bget_on(mc_b, (long)nc_a)) {
+      if (bget_on(mc_j, (long)nc_a)) {
+        const unsigned long long tab_c = pick(L->spacing_col, nc_j, nc_b, nc_a);
+        unsigned long long nr_j = 0, nr_b = 0;
+        for (unsigned long long nr_a = 0; nr_a < nrows; ++nr_a) {
+          if (bget_on(mr_b, (long)nr_a)) {
+            if (bget_on(mr_j, (long)nr_a)) {
+              nr_j++;
+            } else {
+              const unsigned long long tab_r = pick(L->spacing_row, nr_j, nr_b, nr_a);
+              if (L->spacing_row == SP_b || L->spacing_row == SP_a) L->lf[tab_r + tab_c * L->row_stride] = 0;
+            }
+            nr_b++;
+          } else {
+            const unsigned long long tab_r = pick(L->spacing_row, nr_j, nr_b, nr_a);
+            if (L->spacing_row == SP_a) L->lf[tab_r + tab_c * L->row_stride] = 0;
+          }
+        }
+        nc_j++;
+      } else {
+        const unsigned long long tab_c = pick(L->spacing_col, nc_j, nc_b, nc_a);
+        if (L->spacing_col == SP_b || L->spacing_col == SP_a)
+          for (unsigned long long r = 0; r < L->row_stride; ++r) L->lf[r + tab_c * L->row_stride] = 0;
+      }
+      nc_b++;
+    } else {
+      const unsigned long long tab_c = pick(L->spacing_col, nc_j, nc_b, nc_a);
+      if (L->spacing_col == SP_a)
+        for (unsigned long long r = 0; r < L->row_stride; ++r) L->lf[r + tab_c * L->row_stride] = 0;
+    }
+  }
+}
+
+// LL2_plustimesequals (L_init.c:328-358)
+void LL2_plustimes(L_handle *LA, L_handle *LB, double dtmp, unsigned long long nrows, const unsigned char *mr_b,
+                   const unsigned char *mr_j, unsigned long long ncols, const unsigned char *mc_b,
+                   const unsigned char *mc_j) {
+  unsigned long long nc_j = 0, nc_b = 0;
+  for (unsigned long long nc_a = 0; nc_a < ncols; ++nc_a) {
+    if (bget_on(mc_b, (long)nc_a)) {
+      if (bget_on(mc_j, (long)nc_a)) {
+        unsigned long long nr_j = 0, nr_b = 0;
+        for (unsigned long long nr_a = 0; nr_a < nrows; ++nr_a) {
+          if (bget_on(mr_b, (long)nr_a)) {
+            if (bget_on(mr_j, (long)nr_a)) {
+              *L2_get(LA, nr_j, nr_b, nr_a, nc_j, nc_b, nc_a) += dtmp * (*L2_get(LB, nr_j, nr_b, nr_a, nc_j, nc_b, nc_a));
+              nr_j++;
+            }
+            nr_b++;
+          }
+        }
+        nc_j++;
+      }
+      nc_b++;
+    }
+  }
+}
+
+void lrup_QC_stage_c(State &S) {  // bcc_lrup_QC_YnWt_stage_c (bcc_lrup.c:592-655)
+  const unsigned char *Ab = S.A_bmc_b.data(), *Ar = S.A_bmc_j_rtn.data(), *Tb = S.T_bmc_b.data(), *Tj = S.T_bmc_j.data();
+  const unsigned long long AC = S.A_ncols, T = S.T_ncols;
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) {
+        L2_clean(F->lf_At_T_AnZt_S_Zn, AC, Ab, Ar, T, Tb, Tj);
+        for (L_handle *LB : {F->lf_attjn____vtszn, F->lf_kt_r_knzt_s_zn, F->lf_kt_r_hnvt_s_zn})
+          LL2_plustimes(F->lf_At_T_AnZt_S_Zn, LB, -1.0, AC, Ab, Ar, T, Tb, Tj);
+      }
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
+        L2_clean(F->lf_At_T_AnAt_T_An, AC, Ab, Ar, T, Tb, Tj);
+        for (L_handle *LB : {F->lf_attjn____jttan, F->lf_attjn____htrkn, F->lf_ktrhn____jttan, F->lf_ktrhn____htrkn,
+                             F->lf_at_t_ankt_r_kn, F->lf_kt_r_knat_t_an, F->lf_kt_r_knkt_r_kn})
+          LL2_plustimes(F->lf_At_T_AnAt_T_An, LB, -1.0, AC, Ab, Ar, T, Tb, Tj);
+      }
+    }
+}
+
+void initial_subscores(State &S) {
+  An_ajdk_all(S);
+  lf_ZtSn_all(S);
+  lf_YnWt_all(S);
+  M_YnWt_all(S);
+  lf_At_T_YnWt_S_Zn_all(S);
+  lf_AnZt_S_WnYt_all(S);
+  singlestudy_ww(S);
+  doublestudy_ww(S);
+  flattenloop(S);
+}
+
+}  // namespace
+
+int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks) {
+  if (P.Ireq > 0) { err = "GLOBAL_Ireq > 0 is not supported by this build"; return 4; }
+  if (P.QR_strategy.find("YnWt") == std::string::npos || P.QC_strategy.find("YnWt") == std::string::npos ||
+      P.QR_strategy.find("condense") != std::string::npos || P.QC_strategy.find("store one") != std::string::npos ||
+      P.QR_strategy.find("ZtSWn") != std::string::npos || P.QC_strategy.find("ZtSWn") != std::string::npos) {
+    err = "only the YnWt row and column strategies are supported by this build";
+    return 4;
+  }
+  if (P.B_MLT < 1 || P.B_MLT > 62) { err = "B_MLT out of range"; return 4; }
+  State S;
+  S.P = P;
+  S.hooks = hooks;
+  S.out = &O;
+  O = Output();
+  int rc = load(S, I, err);
+  if (rc) return rc;
+  M_mxset_all(S);
+  initial_subscores(S);
+  while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
+    sumscores_nrm(S);
+    // bcc_sumscores_ifT: no MDS correction with a single covariate column;
+    // bcc_sumscores_srt: no per-bin sort with GLOBAL_Ireq <= 0.
+    sumscores_cmb(S);
+    sumscores_xij(S);
+    sumscores_mxA(S);
+    lrup_QR(S);
+    lrup_QC(S);
+    lrup_mxdup(S);
+    M_mxset_all(S);
+    // bcc_M_YnWt here requantises the updated Grams, but nothing on the
+    // YnWt path reads those planes before they are rebuilt, so it is skipped.
+    lrup_QC_stage_c(S);
+    lf_AnZt_S_WnYt_all(S);
+    An_ajdk_all(S);
+    lf_ZtSn_all(S);
+    singlestudy_ww(S);
+    doublestudy_ww(S);
+    flattenloop(S);
+    if (O.iterations > 10000000) { err = "iteration limit"; return 5; }
+  }
+  return 0;
+}
+
+int write_outputs(const std::string &dir, const Output &O) {
+  std::string p = dir + "/out_trace.txt";
+  FILE *fp = fopen(p.c_str(), "w");
+  if (!fp) return 2;
+  for (int nl = 0; nl < O.iterations; ++nl) {
+    const double *t = &O.trace[(size_t)nl * 6];
+    fprintf(fp, "%d %d %d %0.16f %0.16f %d\n", (int)t[0], (int)t[1], (int)t[2], t[3], t[4], (int)t[5]);
+  }
+  fclose(fp);
+  FILE *fa = fopen((dir + "/out_xdrop_a.txt").c_str(), "w");
+  FILE *fb = fopen((dir + "/out_xdrop_b.txt").c_str(), "w");
+  if (!fa || !fb) { if (fa) fclose(fa); if (fb) fclose(fb); return 2; }
+  for (size_t i = 0; i + 1 < O.xdrop_a.size(); i += 2) {
+    fprintf(fa, "%d %d\n", O.xdrop_a[i], O.xdrop_a[i + 1]);
+    fprintf(fb, "%d %d\n", O.xdrop_b[i], O.xdrop_b[i + 1]);
+  }
+  fclose(fa);
+  fclose(fb);
+  return 0;
+}
+
+}  // namespace lakbcc

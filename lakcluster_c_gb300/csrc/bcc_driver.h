@@ -1,0 +1,67 @@
+// The bcc solve (lakcluster_driver, dir_c/lakcluster_driver.c:14-251) for the
+// YnWt row/column strategies, driving the reference-compatible kernel entry
+// points.  Internal header shared by the driver translation units.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "bcc_model.h"
+
+namespace lakbcc {
+
+// Solve parameters (the reference's GLOBAL_* settings used on this path).
+struct Params {
+  int nbins = 1;
+  int B_MLT = 32;
+  long long D_MLT = 4294967296LL;
+  double gamma = 0.125;
+  int gamma_type = 0;          // GLOBAL_gamma__log
+  int Ireq = 0;
+  int test_sparse = 1;         // GLOBAL_TEST_sparse: 0 fixes every allele frequency at 0.5
+  double kappa_squared = 0.0;
+  double tolerance = 0.000000000001;
+  unsigned recursion_limit = 1024 * 32;
+  std::string QR_strategy = "YnWt", QC_strategy = "YnWt";
+  std::string dir_name;        // output directory (GLOBAL_DIR_NAME); empty: no files
+};
+
+// One bin's inputs: packed rows of A (patients x SNPs, bsize(ncols) bytes per
+// row, all rows in a-space), the row mask (null: all rows), same for Z.
+struct BinInput {
+  int A_nrows = 0, Z_nrows = 0;
+  std::vector<unsigned char> A_rows, Z_rows;   // a-space rows, bsize(ncols) bytes each
+  std::vector<unsigned char> A_mr_b, Z_mr_b;   // bsize(nrows) bytes; empty = all on
+};
+
+struct Input {
+  int ncols = 0;
+  std::vector<unsigned char> mc_b;             // bsize(ncols) bytes; empty = all on
+  std::vector<BinInput> bins;
+};
+
+struct Output {
+  std::vector<int> xdrop_a, xdrop_b;          // pairs (row, col)
+  std::vector<double> trace;                  // 6 values per iteration
+  int iterations = 0;
+};
+
+// Callbacks into the kernel library that owns the entry points the solve
+// calls: release an output L_handle the library allocated, and drop any
+// device copy cached for a host buffer that is about to be freed.  Either may
+// be null (nothing to release).
+struct Hooks {
+  void (*release_L)(L_handle *L) = nullptr;
+  void (*forget_host)(const void *p) = nullptr;
+};
+
+// Parse a reference .in file (updateglobals.c syntax) and load its .b16 files.
+int read_in_file(const char *path, Params &P, Input &I, std::string &err);
+// Create the output directory when it does not exist (set_globals,
+// lakcluster_ver18.c:231).
+int make_output_dir(const std::string &dir);
+// Run the solve.  Returns 0 on success.
+int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks = nullptr);
+// Write out_trace.txt / out_xdrop_a.txt / out_xdrop_b.txt as the reference does.
+int write_outputs(const std::string &dir, const Output &O);
+
+}  // namespace lakbcc

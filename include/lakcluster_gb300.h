@@ -171,6 +171,49 @@ int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *thread_in,
                                 struct L_handle **output_p);
 
 /* ---------------------------------------------------------------------------
+ * Whole solves.
+ * ------------------------------------------------------------------------- */
+
+/* Run the bcc solve described by a reference .in file (YnWt row and column
+ * strategies, no Y/W/T/S matrices) and write out_trace.txt, out_xdrop_a.txt
+ * and out_xdrop_b.txt into its GLOBAL_DIR_NAME, exactly as the reference
+ * program does.  Replaces the reference's main -> read_input ->
+ * lakcluster_driver path (dir_c/lakcluster_ver18.c:238-330,
+ * dir_c/updateglobals.c:188-198, dir_c/lakcluster_driver.c:14-251).
+ * Returns 0 on success; lakgb_bcc_last_error() describes a failure. */
+int lakgb_bcc_run_in_file(const char *in_path);
+
+/* In-memory form of the same solve (no reference counterpart: the reference
+ * only reads files).  Rows are packed MSB-first, bit 1 = minor allele (+1);
+ * each row occupies row_bytes bytes, of which the first rup(ncols,16)/8 are
+ * used.  Masks are rup(n,16)/8 bytes, NULL = all rows / columns. */
+struct lakgb_bcc_bin {
+  int A_nrows; const unsigned char *A_rows; const unsigned char *A_mr_b;
+  int Z_nrows; const unsigned char *Z_rows; const unsigned char *Z_mr_b;
+};
+struct lakgb_bcc_problem {
+  int ncols; long long row_bytes; const unsigned char *mc_b;
+  int nbins; const struct lakgb_bcc_bin *bins;
+  int B_MLT;         /* bits per quantised score (GLOBAL_B_MLT), 1..62 */
+  double gamma;      /* elimination fraction (GLOBAL_gamma) */
+  int gamma_type;    /* GLOBAL_gamma_type (0 = log) */
+  int test_sparse;   /* GLOBAL_TEST_sparse (1 = estimate allele frequencies) */
+};
+/* trace: 6 values per iteration (iteration, rows left, columns left, mean row
+ * score, mean column score, bins with rows); xdrop_a / xdrop_b: 2 ints per
+ * eliminated row or column, (row, -1) or (-1, column), in elimination order,
+ * with a-space and b-space indices -- the contents of the reference's
+ * out_trace.txt / out_xdrop_a.txt / out_xdrop_b.txt. */
+struct lakgb_bcc_result {
+  int iterations; double *trace;
+  int n_xdrop; int *xdrop_a; int *xdrop_b;
+};
+void lakgb_bcc_problem_init(struct lakgb_bcc_problem *p);  /* reference defaults */
+int lakgb_bcc_solve(const struct lakgb_bcc_problem *p, struct lakgb_bcc_result *r);
+void lakgb_bcc_result_free(struct lakgb_bcc_result *r);
+int lakgb_bcc_last_error(char *msg, int msg_len);
+
+/* ---------------------------------------------------------------------------
  * Device-resident entry points (no reference counterpart: the reference has
  * no device memory).  All pointers are device pointers; `stream` is a
  * cudaStream_t (NULL = the library's stream).  The call enqueues and returns.
@@ -209,6 +252,8 @@ int lakgb_last_error(char *msg, int msg_len);
  * that rewrites a wX buffer in place must call lakgb_forget_host_buffer. */
 void lakgb_set_residency(int on);
 void lakgb_forget_host_buffer(const void *host_ptr);
+/* D_MLT used by wrap_xcalc (the reference's GLOBAL_D_MLT, default 2^32). */
+void lakgb_set_d_mlt(long long d_mlt);
 /* Number of CUDA kernels this library has launched since load. */
 unsigned long long lakgb_kernel_launches(void);
 /* Device time (ms) of the most recent Gram kernel launch, timed with CUDA

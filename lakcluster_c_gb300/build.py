@@ -20,7 +20,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblakgb300.so")
 
-CU_SOURCES = ["lakgb_runtime.cu", "gram.cu", "rowvec.cu", "abi_kernels.cu"]
+CU_SOURCES = ["lakgb_runtime.cu", "gram.cu", "rowvec.cu", "abi_kernels.cu", "xcalc.cu", "bitplane.cu",
+              "loopsum.cu"]
+# Host-only translation units (the solve driver and its input reader).
+CPP_SOURCES = ["bcc_model.cpp", "bcc_driver.cpp", "bcc_io.cpp", "bcc_abi.cpp"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(ROOT, "include")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
@@ -63,6 +67,13 @@ def build_lib(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or not _newer(o, [s] + headers):
             jobs.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
+    cxx = shutil.which("g++") or "g++"
+    for src in CPP_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cpp", ".o"))
+        objs.append(o)
+        if force or not _newer(o, [s] + headers):
+            jobs.append([cxx] + CXX_FLAGS + ["-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             list(ex.map(_run, jobs))

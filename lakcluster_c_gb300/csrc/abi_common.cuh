@@ -1,0 +1,85 @@
+// Host-side helpers shared by the reference-compatible entry points:
+// output allocation with the reference's semantics, spacing arithmetic and
+// small upload / download wrappers.
+#pragma once
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "lakgb_runtime.cuh"
+
+namespace lakgb {
+
+inline unsigned long long spacing_length(int spacing, const M_handle *M) {
+  switch (spacing) {
+    case LAKGB_SPACING_j: return (unsigned long long)M->rpop_j;
+    case LAKGB_SPACING_b: return (unsigned long long)M->rpop_b;
+    case LAKGB_SPACING_a: return (unsigned long long)M->nrows;
+    default: return 0;
+  }
+}
+
+// Index of the j-th retained row in the given spacing (AnZt_vv.c:71-77).
+inline std::vector<uint32_t> spacing_index(int spacing, const M_handle *M) {
+  std::vector<uint32_t> v((size_t)M->rpop_j);
+  for (long long j = 0; j < M->rpop_j; ++j) {
+    switch (spacing) {
+      case LAKGB_SPACING_j: v[j] = (uint32_t)j; break;
+      case LAKGB_SPACING_b: v[j] = M->m_b_[j]; break;
+      case LAKGB_SPACING_a: v[j] = M->m_a_[j]; break;
+      default: v[j] = 0; break;
+    }
+  }
+  return v;
+}
+
+// Allocate (malloc, zero-filled) or check-and-zero the output, as the
+// reference wrappers do (AnZt_vv.c:203-204).
+inline L_handle *ensure_output(L_handle **pp, unsigned long long length, const char *who) {
+  if (*pp == nullptr) {
+    L_handle *L = (L_handle *)calloc(1, sizeof(L_handle));
+    L->length = length;
+    L->lf = (double *)calloc(length ? length : 1, sizeof(double));
+    if (!L->lf) {
+      fprintf(stderr, " %% Warning! out of memory in %s\n", who);
+      exit(1);  // RET_NOMEM
+    }
+    *pp = L;
+  }
+  L_handle *L = *pp;
+  if (L->length < length) {
+    printf(" %% Warning! length %llu<%llu in %s\n", L->length, length, who);
+    set_error(2, "output length %llu < %llu in %s", L->length, length, who);
+    return nullptr;
+  }
+  memset(L->lf, 0, length * sizeof(double));
+  return L;
+}
+
+inline int popcount_bytes(const unsigned char *p, long n) {
+  int c = 0;
+  for (long i = 0; i < n; ++i) c += __builtin_popcount((unsigned)p[i]);
+  return c;
+}
+
+inline long long popcount_bytes_masked(const unsigned char *p, const unsigned char *m, long n) {
+  long long c = 0;
+  for (long i = 0; i < n; ++i) c += __builtin_popcount((unsigned)(p[i] & m[i]));
+  return c;
+}
+
+template <class T>
+inline DBuf upload_vec(const std::vector<T> &v) {
+  DBuf d(v.size() * sizeof(T));
+  d.upload(v.data(), v.size() * sizeof(T));
+  return d;
+}
+
+inline void copy_back(double *host, const DBuf &dev, unsigned long long length) {
+  if (length) LAKGB_CUDA(cudaMemcpyAsync(host, dev.p, length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  LAKGB_CUDA(cudaStreamSynchronize(stream()));
+}
+
+}  // namespace lakgb

@@ -11,6 +11,7 @@
 #include "gram.cuh"
 #include "lakgb_runtime.cuh"
 #include "rowvec.cuh"
+#include "abi_common.cuh"
 
 using namespace lakgb;
 
@@ -19,70 +20,6 @@ namespace {
 constexpr int kAjdk_0_1 = 5;
 constexpr int kAjdk_1_1 = 6;
 constexpr int kAjdk_2_1 = 7;
-
-unsigned long long spacing_length(int spacing, const M_handle *M) {
-  switch (spacing) {
-    case LAKGB_SPACING_j: return (unsigned long long)M->rpop_j;
-    case LAKGB_SPACING_b: return (unsigned long long)M->rpop_b;
-    case LAKGB_SPACING_a: return (unsigned long long)M->nrows;
-    default: return 0;
-  }
-}
-
-// Index of the j-th retained row in the given spacing (AnZt_vv.c:71-77).
-std::vector<uint32_t> spacing_index(int spacing, const M_handle *M) {
-  std::vector<uint32_t> v((size_t)M->rpop_j);
-  for (long long j = 0; j < M->rpop_j; ++j) {
-    switch (spacing) {
-      case LAKGB_SPACING_j: v[j] = (uint32_t)j; break;
-      case LAKGB_SPACING_b: v[j] = M->m_b_[j]; break;
-      case LAKGB_SPACING_a: v[j] = M->m_a_[j]; break;
-      default: v[j] = 0; break;
-    }
-  }
-  return v;
-}
-
-// Allocate (malloc, zero-filled) or check-and-zero the output, as the
-// reference wrappers do (AnZt_vv.c:203-204).
-L_handle *ensure_output(L_handle **pp, unsigned long long length, const char *who) {
-  if (*pp == nullptr) {
-    L_handle *L = (L_handle *)calloc(1, sizeof(L_handle));
-    L->length = length;
-    L->lf = (double *)calloc(length ? length : 1, sizeof(double));
-    if (!L->lf) {
-      fprintf(stderr, " %% Warning! out of memory in %s\n", who);
-      exit(1);  // RET_NOMEM
-    }
-    *pp = L;
-  }
-  L_handle *L = *pp;
-  if (L->length < length) {
-    printf(" %% Warning! length %llu<%llu in %s\n", L->length, length, who);
-    set_error(2, "output length %llu < %llu in %s", L->length, length, who);
-    return nullptr;
-  }
-  memset(L->lf, 0, length * sizeof(double));
-  return L;
-}
-
-int popcount_bytes(const unsigned char *p, long n) {
-  int c = 0;
-  for (long i = 0; i < n; ++i) c += __builtin_popcount((unsigned)p[i]);
-  return c;
-}
-
-template <class T>
-DBuf upload_vec(const std::vector<T> &v) {
-  DBuf d(v.size() * sizeof(T));
-  d.upload(v.data(), v.size() * sizeof(T));
-  return d;
-}
-
-void copy_back(double *host, const DBuf &dev, unsigned long long length) {
-  if (length) LAKGB_CUDA(cudaMemcpyAsync(host, dev.p, length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
-  LAKGB_CUDA(cudaStreamSynchronize(stream()));
-}
 
 int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_handle *M_An,
                M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk, L_handle *lf_Zn_ajdk,

@@ -1,0 +1,128 @@
+// C entry points for a whole bcc solve on the GPU library: the .in-file
+// program (the reference's main -> read_input -> lakcluster_driver,
+// dir_c/lakcluster_ver18.c:238-330 and dir_c/lakcluster_driver.c:14-251) and
+// an in-memory variant for callers that hold the packed matrices already.
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+
+#include "bcc_driver.h"
+
+extern "C" void lakgb_set_d_mlt(long long d_mlt);
+extern "C" void lakgb_forget_host_buffer(const void *host_ptr);
+
+namespace {
+
+thread_local std::string g_err;
+
+void release_L(L_handle *L) {
+  if (!L) return;
+  free(L->lf);
+  free(L);
+}
+
+const lakbcc::Hooks kHooks = {release_L, lakgb_forget_host_buffer};
+
+long row_bytes_min(int ncols) { return (long)(ncols + (16 - ncols % 16) % 16) / 8; }
+
+}  // namespace
+
+extern "C" void lakgb_bcc_problem_init(struct lakgb_bcc_problem *p) {
+  memset(p, 0, sizeof(*p));
+  p->B_MLT = 32;
+  p->gamma = 0.125;
+  p->gamma_type = 0;
+  p->test_sparse = 1;
+}
+
+extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakgb_bcc_result *res) {
+  g_err.clear();
+  if (!prob || !res) { g_err = "null argument"; return 2; }
+  memset(res, 0, sizeof(*res));
+  if (prob->nbins <= 0 || !prob->bins || prob->ncols < 0) { g_err = "bad problem description"; return 2; }
+  if (prob->row_bytes < row_bytes_min(prob->ncols)) { g_err = "row_bytes smaller than one packed row"; return 2; }
+  lakbcc::Params P;
+  P.nbins = prob->nbins;
+  P.B_MLT = prob->B_MLT;
+  P.D_MLT = 1LL << prob->B_MLT;
+  P.gamma = prob->gamma;
+  P.gamma_type = prob->gamma_type;
+  P.test_sparse = prob->test_sparse;
+  lakbcc::Input I;
+  I.ncols = prob->ncols;
+  const long rb = lakbcc::bsize(prob->ncols), ch = row_bytes_min(prob->ncols);
+  if (prob->mc_b) I.mc_b.assign(prob->mc_b, prob->mc_b + ch), I.mc_b.resize(rb, 0);
+  I.bins.resize(prob->nbins);
+  for (int nb = 0; nb < prob->nbins; ++nb) {
+    const struct lakgb_bcc_bin &b = prob->bins[nb];
+    lakbcc::BinInput &B = I.bins[nb];
+    if (b.A_nrows < 0 || b.Z_nrows < 0 || (b.A_nrows > 0 && !b.A_rows) || (b.Z_nrows > 0 && !b.Z_rows)) {
+      g_err = "bad bin description";
+      return 2;
+    }
+    B.A_nrows = b.A_nrows;
+    B.Z_nrows = b.Z_nrows;
+    B.A_rows.assign((size_t)(b.A_nrows > 0 ? b.A_nrows : 1) * rb, 0);
+    for (int r = 0; r < b.A_nrows; ++r) memcpy(&B.A_rows[(size_t)r * rb], b.A_rows + (size_t)r * prob->row_bytes, ch);
+    if (b.Z_nrows > 0) {
+      B.Z_rows.assign((size_t)b.Z_nrows * rb, 0);
+      for (int r = 0; r < b.Z_nrows; ++r) memcpy(&B.Z_rows[(size_t)r * rb], b.Z_rows + (size_t)r * prob->row_bytes, ch);
+    }
+    if (b.A_mr_b) {
+      B.A_mr_b.assign(b.A_mr_b, b.A_mr_b + row_bytes_min(b.A_nrows));
+      B.A_mr_b.resize(lakbcc::bsize(b.A_nrows), 0);
+    }
+    if (b.Z_mr_b) {
+      B.Z_mr_b.assign(b.Z_mr_b, b.Z_mr_b + row_bytes_min(b.Z_nrows));
+      B.Z_mr_b.resize(lakbcc::bsize(b.Z_nrows), 0);
+    }
+  }
+  lakgb_set_d_mlt(P.D_MLT);
+  lakbcc::Output O;
+  int rc = lakbcc::solve(P, I, O, g_err, &kHooks);
+  if (rc) return rc;
+  res->iterations = O.iterations;
+  res->trace = (double *)malloc(sizeof(double) * (O.trace.size() ? O.trace.size() : 1));
+  res->n_xdrop = (int)(O.xdrop_a.size() / 2);
+  res->xdrop_a = (int *)malloc(sizeof(int) * (O.xdrop_a.size() ? O.xdrop_a.size() : 1));
+  res->xdrop_b = (int *)malloc(sizeof(int) * (O.xdrop_b.size() ? O.xdrop_b.size() : 1));
+  if (!res->trace || !res->xdrop_a || !res->xdrop_b) { g_err = "out of host memory"; return 2; }
+  if (!O.trace.empty()) memcpy(res->trace, O.trace.data(), sizeof(double) * O.trace.size());
+  if (!O.xdrop_a.empty()) memcpy(res->xdrop_a, O.xdrop_a.data(), sizeof(int) * O.xdrop_a.size());
+  if (!O.xdrop_b.empty()) memcpy(res->xdrop_b, O.xdrop_b.data(), sizeof(int) * O.xdrop_b.size());
+  return 0;
+}
+
+extern "C" void lakgb_bcc_result_free(struct lakgb_bcc_result *res) {
+  if (!res) return;
+  free(res->trace);
+  free(res->xdrop_a);
+  free(res->xdrop_b);
+  memset(res, 0, sizeof(*res));
+}
+
+extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
+  g_err.clear();
+  lakbcc::Params P;
+  lakbcc::Input I;
+  int rc = lakbcc::read_in_file(in_path, P, I, g_err);
+  if (rc) return rc;
+  lakgb_set_d_mlt(P.D_MLT);
+  lakbcc::Output O;
+  rc = lakbcc::solve(P, I, O, g_err, &kHooks);
+  if (rc) return rc;
+  if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_outputs(P.dir_name, O)) {
+    g_err = "cannot write outputs into " + P.dir_name;
+    return 2;
+  }
+  return 0;
+}
+
+extern "C" int lakgb_bcc_last_error(char *msg, int msg_len) {
+  if (msg && msg_len > 0) {
+    strncpy(msg, g_err.c_str(), (size_t)msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  return g_err.empty() ? 0 : 1;
+}

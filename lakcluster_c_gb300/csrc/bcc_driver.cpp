@@ -1491,16 +1491,90 @@ void lrup_QC_stage_c(State &S) {  // bcc_lrup_QC_YnWt_stage_c (bcc_lrup.c:592-65
     }
 }
 
+// Optional stage trace (LAKBCC_TRACE=<file>): after every stage, one line
+// per live intermediate with an FNV-1a hash of its values.  Two builds whose
+// kernels agree bit for bit write identical traces, so the first differing
+// line names the stage and the product that diverged.
+unsigned long long fnv(const void *p, size_t n, unsigned long long h = 1469598103934665603ull) {
+  const unsigned char *b = (const unsigned char *)p;
+  for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ull; }
+  return h;
+}
+
+void trace_L(FILE *f, const char *stage, int it, const char *name, int a, int b, const L_handle *L) {
+  if (!L) return;
+  unsigned long long n = L->row_stride * L->col_stride * (L->lyr_stride ? L->lyr_stride : 1);
+  if (n > L->length) n = L->length;
+  fprintf(f, "%s %d %s %d %d n=%llu h=%016llx\n", stage, it, name, a, b, n, fnv(L->lf, n * sizeof(double)));
+}
+
+void trace_M(FILE *f, const char *stage, int it, const char *name, int a, int b, const MH *M) {
+  const M_handle &h = M->h;
+  unsigned long long x = fnv(h.wX, (size_t)h.nrows * h.mc_length);
+  x = fnv(&h.min_d, sizeof(double), x);
+  x = fnv(&h.mlt_d, sizeof(double), x);
+  fprintf(f, "%s %d %s %d %d rows=%d h=%016llx\n", stage, it, name, a, b, h.nrows, x);
+}
+
+void trace_stage(State &S, const char *stage) {
+  static FILE *f = nullptr;
+  static bool checked = false;
+  if (!checked) {
+    checked = true;
+    const char *path = getenv("LAKBCC_TRACE");
+    if (path && *path) f = fopen(path, "w");
+  }
+  if (!f) return;
+  const int it = S.out ? S.out->iterations : -1;
+#define TL(name, a, b, L) trace_L(f, stage, it, name, a, b, L)
+  for (auto &E : S.E) {
+    const int nb = E->nb;
+    TL("An_ajdk", nb, 0, E->lf_An_ajdk); TL("Zn_ajdk", nb, 0, E->lf_Zn_ajdk);
+    TL("AtTn", nb, 0, E->lf_AtTn); TL("ZtSn", nb, 0, E->lf_ZtSn); TL("At_An_a1d1", nb, 0, E->lf_At_An_a1d1);
+    TL("jn_ajdk", nb, 0, E->lf_jn_ajdk); TL("vn_ajdk", nb, 0, E->lf_vn_ajdk); TL("kn_ajdk", nb, 0, E->lf_kn_ajdk);
+    TL("zn_ajdk", nb, 0, E->lf_zn_ajdk); TL("hn_ajdk", nb, 0, E->lf_hn_ajdk); TL("an_ajdk", nb, 0, E->lf_an_ajdk);
+    TL("attn", nb, 0, E->lf_attn); TL("jttn", nb, 0, E->lf_jttn); TL("ktrn", nb, 0, E->lf_ktrn);
+    TL("htrn", nb, 0, E->lf_htrn); TL("ztsn", nb, 0, E->lf_ztsn); TL("vtsn", nb, 0, E->lf_vtsn);
+    TL("ztsvn", nb, 0, E->lf_ztsvn); TL("attjn", nb, 0, E->lf_attjn); TL("ktrhn", nb, 0, E->lf_ktrhn);
+    TL("At_rsum", nb, 0, E->lf_At_rsum); TL("Zt_rsum", nb, 0, E->lf_Zt_rsum);
+    trace_M(f, stage, it, "M_An_a1d1", nb, 0, E->M_An_a1d1);
+    trace_M(f, stage, it, "M_a2d2_ZtSn", nb, 0, E->M_a2d2_ZtSn);
+    trace_M(f, stage, it, "M_a2d2_AtTn", nb, 0, E->M_a2d2_AtTn);
+  }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      TL("AnZt", nb1, nb2, F->lf_AnZt); TL("AnAt", nb1, nb2, F->lf_AnAt);
+      TL("jnvt", nb1, nb2, F->lf_jnvt); TL("jnjt", nb1, nb2, F->lf_jnjt);
+      TL("knzt", nb1, nb2, F->lf_knzt); TL("hnvt", nb1, nb2, F->lf_hnvt); TL("ankt", nb1, nb2, F->lf_ankt);
+      TL("knat", nb1, nb2, F->lf_knat); TL("knkt", nb1, nb2, F->lf_knkt);
+      TL("kt_r_knzt_s_zn", nb1, nb2, F->lf_kt_r_knzt_s_zn); TL("kt_r_hnvt_s_zn", nb1, nb2, F->lf_kt_r_hnvt_s_zn);
+      TL("at_t_ankt_r_kn", nb1, nb2, F->lf_at_t_ankt_r_kn); TL("kt_r_knkt_r_kn", nb1, nb2, F->lf_kt_r_knkt_r_kn);
+      TL("attjn____vtszn", nb1, nb2, F->lf_attjn____vtszn); TL("attjn____jttan", nb1, nb2, F->lf_attjn____jttan);
+      TL("attjn____htrkn", nb1, nb2, F->lf_attjn____htrkn); TL("ktrhn____htrkn", nb1, nb2, F->lf_ktrhn____htrkn);
+      TL("AnZt_S_ZnAt", nb1, nb2, F->lf_AnZt_S_ZnAt); TL("AnAt_T_AnAt", nb1, nb2, F->lf_AnAt_T_AnAt);
+      TL("At_T_AnZt_S_Zn", nb1, nb2, F->lf_At_T_AnZt_S_Zn); TL("At_T_AnAt_T_An", nb1, nb2, F->lf_At_T_AnAt_T_An);
+      TL("An_a2d2_Zt_Sn", nb1, nb2, F->lf_An_a2d2_Zt_Sn); TL("An_a2d2_At_Tn", nb1, nb2, F->lf_An_a2d2_At_Tn);
+      TL("QR_AnZtSZnAt", nb1, nb2, F->QR_AnZtSZnAt); TL("QR_AnAtTAnAt", nb1, nb2, F->QR_AnAtTAnAt);
+      TL("QC_AtTAnZtSZn", nb1, nb2, F->QC_AtTAnZtSZn); TL("QC_AtTAnAtTAn", nb1, nb2, F->QC_AtTAnAtTAn);
+      trace_M(f, stage, it, "M_AnZt", nb1, nb2, F->M_AnZt); trace_M(f, stage, it, "M_AnAt", nb1, nb2, F->M_AnAt);
+      trace_M(f, stage, it, "M_knzt", nb1, nb2, F->M_knzt); trace_M(f, stage, it, "M_hnvt", nb1, nb2, F->M_hnvt);
+      trace_M(f, stage, it, "M_ankt", nb1, nb2, F->M_ankt); trace_M(f, stage, it, "M_knkt", nb1, nb2, F->M_knkt);
+    }
+#undef TL
+  fflush(f);
+}
+
 void initial_subscores(State &S) {
-  An_ajdk_all(S);
-  lf_ZtSn_all(S);
-  lf_YnWt_all(S);
-  M_YnWt_all(S);
-  lf_At_T_YnWt_S_Zn_all(S);
-  lf_AnZt_S_WnYt_all(S);
-  singlestudy_ww(S);
-  doublestudy_ww(S);
-  flattenloop(S);
+  An_ajdk_all(S); trace_stage(S, "An_ajdk");
+  lf_ZtSn_all(S); trace_stage(S, "lf_ZtSn");
+  lf_YnWt_all(S); trace_stage(S, "lf_YnWt");
+  M_YnWt_all(S); trace_stage(S, "M_YnWt");
+  lf_At_T_YnWt_S_Zn_all(S); trace_stage(S, "lf_At_T_YnWt_S_Zn");
+  lf_AnZt_S_WnYt_all(S); trace_stage(S, "lf_AnZt_S_WnYt");
+  singlestudy_ww(S); trace_stage(S, "singlestudy");
+  doublestudy_ww(S); trace_stage(S, "doublestudy");
+  flattenloop(S); trace_stage(S, "flattenloop");
 }
 
 }  // namespace
@@ -1530,19 +1604,19 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     sumscores_cmb(S);
     sumscores_xij(S);
     sumscores_mxA(S);
-    lrup_QR(S);
-    lrup_QC(S);
+    lrup_QR(S); trace_stage(S, "lrup_QR");
+    lrup_QC(S); trace_stage(S, "lrup_QC");
     lrup_mxdup(S);
     M_mxset_all(S);
     // bcc_M_YnWt here requantises the updated Grams, but nothing on the
     // YnWt path reads those planes before they are rebuilt, so it is skipped.
-    lrup_QC_stage_c(S);
-    lf_AnZt_S_WnYt_all(S);
-    An_ajdk_all(S);
-    lf_ZtSn_all(S);
-    singlestudy_ww(S);
-    doublestudy_ww(S);
-    flattenloop(S);
+    lrup_QC_stage_c(S); trace_stage(S, "lrup_QC_stage_c");
+    lf_AnZt_S_WnYt_all(S); trace_stage(S, "lf_AnZt_S_WnYt");
+    An_ajdk_all(S); trace_stage(S, "An_ajdk");
+    lf_ZtSn_all(S); trace_stage(S, "lf_ZtSn");
+    singlestudy_ww(S); trace_stage(S, "singlestudy");
+    doublestudy_ww(S); trace_stage(S, "doublestudy");
+    flattenloop(S); trace_stage(S, "flattenloop");
     if (O.iterations > 10000000) { err = "iteration limit"; return 5; }
   }
   return 0;

@@ -77,11 +77,12 @@ static void mxget_excerpt(int n, const unsigned char *mb, const unsigned char *m
   }
 }
 
-void mh_mxget(MH *M) {
-  M_handle &h = M->h;
-  mxget_excerpt(h.nrows, h.mr_b, h.mr_j, &h.rpop_b, &h.rpop_j, h.m_a_, h.m_b_, (long)h.mr_length);
-  mxget_excerpt(h.ncols, h.mc_b, h.mc_j, &h.cpop_b, &h.cpop_j, h.n_a_, h.n_b_, (long)h.mc_length);
+void mhandle_mxget(M_handle *h) {
+  mxget_excerpt(h->nrows, h->mr_b, h->mr_j, &h->rpop_b, &h->rpop_j, h->m_a_, h->m_b_, (long)h->mr_length);
+  mxget_excerpt(h->ncols, h->mc_b, h->mc_j, &h->cpop_b, &h->cpop_j, h->n_a_, h->n_b_, (long)h->mc_length);
 }
+
+void mh_mxget(MH *M) { mhandle_mxget(&M->h); }
 
 void mh_mxset(MH *M, const unsigned char *mr_j, const unsigned char *mc_j) {
   M_handle &h = M->h;

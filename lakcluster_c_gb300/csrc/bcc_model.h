@@ -60,6 +60,8 @@ MH *mh_make(int nrows, int ncols, unsigned char *rows, const unsigned char *mr_b
 MH *mh_make_owned(int nrows, int ncols);
 // M_mxget (M_init.c:268-295): pops and index lists from the masks.
 void mh_mxget(MH *M);
+// The same on a bare M_handle whose mask and index arrays are already sized.
+void mhandle_mxget(M_handle *h);
 // M_mxset (M_init.c:359-374): current masks = given & base, then mxget.
 void mh_mxset(MH *M, const unsigned char *mr_j, const unsigned char *mc_j);
 

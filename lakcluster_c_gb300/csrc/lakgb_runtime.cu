@@ -92,6 +92,23 @@ const void *resident(const void *host, size_t bytes) {
   return d;
 }
 
+void resident_put(const void *host, size_t bytes, DBuf &&d) {
+  stream();
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto it = g_res.begin(); it != g_res.end();) {
+    if (it->first.first == host) {
+      cudaFreeAsync(it->second.d, g_stream);
+      it = g_res.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  if (!g_residency || bytes == 0 || !d.p) return;  // d frees itself
+  g_res[std::make_pair(host, bytes)] = ResEntry{d.p, bytes};
+  d.p = nullptr;
+  d.n = 0;
+}
+
 void gram_timer_begin(cudaStream_t s) {
   if (!g_ev0) {
     LAKGB_CUDA(cudaEventCreate(&g_ev0));

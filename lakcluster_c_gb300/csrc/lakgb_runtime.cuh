@@ -58,6 +58,12 @@ struct DBuf {
   void zero();
 };
 
+// Make the device buffer `d`, which holds the current contents of the host
+// buffer `host` (`bytes` bytes), its resident copy, replacing any earlier copy
+// of that host buffer.  The cache takes ownership of the device memory.  With
+// residency off the buffer is simply released.
+void resident_put(const void *host, size_t bytes, DBuf &&d);
+
 // Events bracketing the most recent Gram launch.
 void gram_timer_begin(cudaStream_t s);
 void gram_timer_end(cudaStream_t s);

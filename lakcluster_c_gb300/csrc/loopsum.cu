@@ -1,0 +1,370 @@
+// Loop-sum products over FP64 score matrices, and the SNP x SNP product AtTYn.
+//
+// AnZt_S_WnYt_vv (dir_c/AnZt_S_WnYt_vv.c:5-101, wrapper :103-145):
+//   out[ma, s] = sum over Zn rows mz, in order, of (AnZt[ma,mz] * vS(s,mz)) * YnWt[ma,mz]
+// AtTYn____WtSZn_vv (dir_c/AtTYn____WtSZn_vv.c:5-115, wrapper :117-159): over
+// paired rows (na with nz) and paired inner rows (ny with nw), in order,
+//   out[na, s] = sum (AtTYn[na,ny,s] * D_Yn[ny]) * ZtSWn[nz,nw,s]
+// Both are sequential FP64 sums; one thread per output element runs the
+// reference's recurrence (left-to-right, no FMA), with adjacent threads on
+// adjacent rows so the column-major loads coalesce.
+//
+// AtTYn_vv (dir_c/AtTYn_vv.c:5-202, wrapper :204-235):
+//   out[na, ny, t] = ((hhAY - hhAy*aY) - aA*hhaY) + (aA*hhay)*aY
+//   hhAY = cpop_j(At) - 2*popcount(~(At_na ^ Tt_t ^ Yt_ny) & mc_j(At))
+//        = 2*popcount((At_na ^ Tt_t ^ Yt_ny) & mc_j) - cpop_j
+//   hhAy = AtTn[na,t], hhaY = YtTn[ny,t] (integers read from FP64),
+//   hhay = -cpop_j(Tt) + 2*popcount(Tt_t & mc_j(Tt)), aA / aY the column
+//   means of the At / Yt rows' 1920-bit blocks.
+// The popcount is a tiled XOR Gram: per 1920-bit block the CTA stages
+// (At ^ Tt) & mask for 64 At rows and Yt & mask for 64 Yt rows, and each
+// thread accumulates a 4 x 4 tile of integer counts over all blocks.
+#include "abi_common.cuh"
+#include "bcc_model.h"
+
+namespace lakgb {
+
+namespace {
+
+inline unsigned long long pick_u(int s, unsigned long long j, unsigned long long b, unsigned long long a) {
+  return s == LAKGB_SPACING_j ? j : (s == LAKGB_SPACING_b ? b : a);
+}
+
+// Number of values in the populated part of an L_handle (2-D or 3-D).
+unsigned long long populated(const L_handle *L, bool three_d) {
+  unsigned long long n = L->row_stride * L->col_stride * (three_d ? L->lyr_stride : 1);
+  return n > L->length ? L->length : n;
+}
+
+unsigned long long max_index(const std::vector<unsigned long long> &v) {
+  unsigned long long m = 0;
+  for (unsigned long long x : v) m = x > m ? x : m;
+  return m;
+}
+
+// Upload the populated part of an L_handle's values.
+DBuf upload_L(const L_handle *L, bool three_d) {
+  const unsigned long long n = populated(L, three_d);
+  DBuf d((size_t)(n ? n : 1) * sizeof(double));
+  if (n) d.upload(L->lf, (size_t)n * sizeof(double));
+  return d;
+}
+
+__global__ void anzt_s_wnyt_kernel(const double *A, const unsigned long long *a_r, const unsigned long long *a_c,
+                                   const double *Y, const unsigned long long *y_r, const unsigned long long *y_c,
+                                   const int8_t *vS, int nA, int nZ, int nS, const unsigned long long *out_r,
+                                   const unsigned long long *s_off, double *out) {
+  const int ma = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (ma >= nA || s >= nS) return;
+  const unsigned long long ar = a_r[ma], yr = y_r[ma];
+  const int8_t *vs = vS + (long long)s * nZ;
+  double acc = 0.0;
+  for (int mz = 0; mz < nZ; ++mz) {
+    const double a = A[ar + a_c[mz]], y = Y[yr + y_c[mz]];
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(a, (double)vs[mz]), y));
+  }
+  out[out_r[ma] + s_off[s]] = acc;
+}
+
+__global__ void attyn_wtszn_kernel(const double *AY, const unsigned long long *ay_a, const unsigned long long *ay_y,
+                                   const unsigned long long *ay_s, const double *ZW, const unsigned long long *zw_z,
+                                   const unsigned long long *zw_w, const unsigned long long *zw_s, const double *Dy,
+                                   int npairs, int ninner, int nS, const unsigned long long *out_r,
+                                   const unsigned long long *s_off, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (i >= npairs || s >= nS) return;
+  const unsigned long long a0 = ay_a[i] + ay_s[s], z0 = zw_z[i] + zw_s[s];
+  double acc = 0.0;
+  for (int k = 0; k < ninner; ++k)
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(AY[a0 + ay_y[k]], Dy[k]), ZW[z0 + zw_w[k]]));
+  out[out_r[i] + s_off[s]] = acc;
+}
+
+constexpr int kLd = kBlockWords + 1;
+constexpr int kTY_M = 64, kTY_N = 64, kTY_TM = 4, kTY_TN = 4, kTY_T = 256;
+
+struct AtTYnParams {
+  const uint8_t *At; const uint32_t *a_rowb; int nA; long long a_row_bytes;
+  const uint8_t *Yt; const uint32_t *y_rowb; int nY; long long y_row_bytes;
+  const uint8_t *Tt; const uint32_t *t_rowb; long long t_row_bytes;
+  const uint8_t *mask; int P; long long cpop;
+  const double *hhAy;   // [t][na]
+  const double *hhaY;   // [t][ny]
+  const double *hhay;   // [t]
+  const double *aA; const double *aY;
+  const unsigned long long *out_a; const unsigned long long *out_y; const unsigned long long *out_t;
+  double *out;
+};
+
+__global__ void __launch_bounds__(kTY_T, 2) attyn_kernel(AtTYnParams p) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t *As = smem, *Ys = smem + kTY_M * kLd;
+  __shared__ long long a_off[kTY_M], y_off[kTY_N];
+  const int t = blockIdx.z;
+  const int n0 = blockIdx.x * kTY_N, m0 = blockIdx.y * kTY_M;
+  const int tid = threadIdx.x, tx = tid % (kTY_N / kTY_TN), ty = tid / (kTY_N / kTY_TN);
+  for (int i = tid; i < kTY_M; i += kTY_T) a_off[i] = m0 + i < p.nA ? (long long)p.a_rowb[m0 + i] * p.a_row_bytes : -1;
+  for (int i = tid; i < kTY_N; i += kTY_T) y_off[i] = n0 + i < p.nY ? (long long)p.y_rowb[n0 + i] * p.y_row_bytes : -1;
+  const uint8_t *trow = p.Tt + (long long)p.t_rowb[t] * p.t_row_bytes;
+  int c[kTY_TM][kTY_TN];
+#pragma unroll
+  for (int i = 0; i < kTY_TM; ++i)
+#pragma unroll
+    for (int j = 0; j < kTY_TN; ++j) c[i][j] = 0;
+  for (int blk = 0; blk < p.P; ++blk) {
+    __syncthreads();
+    const long long boff = (long long)blk * kBlockBytes;
+    const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + boff);
+    const uint4 *tk = reinterpret_cast<const uint4 *>(trow + boff);
+    for (int idx = tid; idx < kTY_M * 15; idx += kTY_T) {
+      const int r = idx / 15, v = idx - r * 15;
+      uint4 x = make_uint4(0u, 0u, 0u, 0u);
+      if (a_off[r] >= 0) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(p.At + a_off[r] + boff) + v);
+        const uint4 tt = __ldg(tk + v), m = __ldg(mk + v);
+        x.x = (a.x ^ tt.x) & m.x; x.y = (a.y ^ tt.y) & m.y; x.z = (a.z ^ tt.z) & m.z; x.w = (a.w ^ tt.w) & m.w;
+      }
+      uint32_t *d = As + r * kLd + 4 * v;
+      d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
+    }
+    for (int idx = tid; idx < kTY_N * 15; idx += kTY_T) {
+      const int r = idx / 15, v = idx - r * 15;
+      uint4 x = make_uint4(0u, 0u, 0u, 0u);
+      if (y_off[r] >= 0) {
+        const uint4 y = __ldg(reinterpret_cast<const uint4 *>(p.Yt + y_off[r] + boff) + v);
+        const uint4 m = __ldg(mk + v);
+        x.x = y.x & m.x; x.y = y.y & m.y; x.z = y.z & m.z; x.w = y.w & m.w;
+      }
+      uint32_t *d = Ys + r * kLd + 4 * v;
+      d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int w = 0; w < kBlockWords; ++w) {
+      uint32_t a[kTY_TM], y[kTY_TN];
+#pragma unroll
+      for (int i = 0; i < kTY_TM; ++i) a[i] = As[(ty + 16 * i) * kLd + w];
+#pragma unroll
+      for (int j = 0; j < kTY_TN; ++j) y[j] = Ys[(tx + 16 * j) * kLd + w];
+#pragma unroll
+      for (int i = 0; i < kTY_TM; ++i)
+#pragma unroll
+        for (int j = 0; j < kTY_TN; ++j) c[i][j] += __popc(a[i] ^ y[j]);
+    }
+  }
+  const double hhay = p.hhay[t];
+#pragma unroll
+  for (int i = 0; i < kTY_TM; ++i) {
+    const int na = m0 + ty + 16 * i;
+    if (na >= p.nA) continue;
+    const double hhAy = p.hhAy[(long long)t * p.nA + na], aA = p.aA[na];
+#pragma unroll
+    for (int j = 0; j < kTY_TN; ++j) {
+      const int ny = n0 + tx + 16 * j;
+      if (ny >= p.nY) continue;
+      const double hhaY = p.hhaY[(long long)t * p.nY + ny], aY = p.aY[ny];
+      const double hhAY = (double)(2ll * c[i][j] - p.cpop);
+      const double v = __dadd_rn(__dsub_rn(__dsub_rn(hhAY, __dmul_rn(hhAy, aY)), __dmul_rn(aA, hhaY)),
+                                 __dmul_rn(__dmul_rn(aA, hhay), aY));
+      p.out[p.out_a[na] + p.out_y[ny] + p.out_t[t]] = v;
+    }
+  }
+}
+
+}  // namespace
+
+}  // namespace lakgb
+
+using namespace lakgb;
+
+extern "C" int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                                        int output_spacing_s, M_handle *M_An, M_handle *M_St, M_handle *M_Zn,
+                                        L_handle *lf_AnZt, L_handle *lf_YnWt, L_handle **output_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  const unsigned long long length_a = spacing_length(output_spacing_a, M_An);
+  const unsigned long long length_s = spacing_length(output_spacing_s, M_St);
+  const unsigned long long length = length_a * length_s;
+  L_handle *out = ensure_output(output_p, length, "wrap_AnZt_S_WnYt_vv__run");
+  if (!out) return (int)length;
+  out->spacing_row = output_spacing_a; out->row_stride = length_a;
+  out->spacing_col = output_spacing_s; out->col_stride = length_s;
+  const int nA = (int)M_An->rpop_j, nZ = (int)M_Zn->rpop_j, nS = (int)M_St->rpop_j;
+  if (!lf_AnZt || !lf_YnWt || nA == 0 || nS == 0) return (int)length;
+  std::vector<unsigned long long> a_r(nA), y_r(nA), out_r(nA), a_c(nZ), y_c(nZ), s_off(nS);
+  for (int i = 0; i < nA; ++i) {
+    a_r[i] = pick_u(lf_AnZt->spacing_row, i, M_An->m_b_[i], M_An->m_a_[i]);
+    y_r[i] = pick_u(lf_YnWt->spacing_row, i, M_An->m_b_[i], M_An->m_a_[i]);
+    out_r[i] = pick_u(output_spacing_a, i, M_An->m_b_[i], M_An->m_a_[i]);
+  }
+  for (int k = 0; k < nZ; ++k) {
+    a_c[k] = pick_u(lf_AnZt->spacing_col, k, M_Zn->m_b_[k], M_Zn->m_a_[k]) * lf_AnZt->row_stride;
+    y_c[k] = pick_u(lf_YnWt->spacing_col, k, M_Zn->m_b_[k], M_Zn->m_a_[k]) * lf_YnWt->row_stride;
+  }
+  std::vector<int8_t> vS((size_t)nS * (nZ > 0 ? nZ : 1));
+  for (int s = 0; s < nS; ++s) {
+    s_off[s] = pick_u(output_spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * length_a;
+    const unsigned char *st = M_St->wX + (size_t)M_St->m_b_[s] * M_St->mc_length;
+    for (int k = 0; k < nZ; ++k) {
+      vS[(size_t)s * nZ + k] = (int8_t)lakbcc::bget_pm(st, M_Zn->m_a_[k]);
+      if (!lakbcc::bget_on(M_St->mc_j, M_Zn->m_a_[k]))
+        printf(" %% Warning! bit %d,%d,%d off in M_St->mc_j\n", k, (int)M_Zn->m_b_[k], (int)M_Zn->m_a_[k]);
+    }
+  }
+  if (max_index(a_r) + max_index(a_c) >= populated(lf_AnZt, false) ||
+      max_index(y_r) + max_index(y_c) >= populated(lf_YnWt, false)) {
+    set_error(4, "wrap_AnZt_S_WnYt_vv__run: L_handle smaller than the rows and columns it is indexed by");
+    return (int)length;
+  }
+  DBuf dA = upload_L(lf_AnZt, false);
+  DBuf dY = (lf_YnWt == lf_AnZt) ? DBuf() : upload_L(lf_YnWt, false);
+  const double *pY = (lf_YnWt == lf_AnZt) ? dA.as<double>() : dY.as<double>();
+  DBuf d_ar = upload_vec(a_r), d_yr = upload_vec(y_r), d_ac = upload_vec(a_c), d_yc = upload_vec(y_c);
+  DBuf d_vS = upload_vec(vS), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+  dim3 grid((nA + 127) / 128, nS);
+  anzt_s_wnyt_kernel<<<grid, 128, 0, stream()>>>(dA.as<double>(), d_ar.as<unsigned long long>(), d_ac.as<unsigned long long>(),
+                                                 pY, d_yr.as<unsigned long long>(), d_yc.as<unsigned long long>(),
+                                                 d_vS.as<int8_t>(), nA, nZ, nS, d_or.as<unsigned long long>(),
+                                                 d_so.as<unsigned long long>(), d_out.as<double>());
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}
+
+extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                                           int output_spacing_s, M_handle *M_At, M_handle *M_Tt, M_handle *M_Yt,
+                                           M_handle *M_Wt, M_handle *M_St, M_handle *M_Zt, double *Y_ajdk,
+                                           L_handle *lf_AtTYn, L_handle *lf_ZtSWn, L_handle **output_p) {
+  (void)tidx; (void)vpra; (void)thread_in; (void)M_Tt;
+  const unsigned long long length_a = spacing_length(output_spacing_a, M_At);
+  const unsigned long long length_s = spacing_length(output_spacing_s, M_St);
+  const unsigned long long length = length_a * length_s;
+  L_handle *out = ensure_output(output_p, length, "wrap_AtTYn____WtSZn_vv__run");
+  if (!out) return (int)length;
+  out->spacing_row = output_spacing_a; out->row_stride = length_a;
+  out->spacing_col = output_spacing_s; out->col_stride = length_s;
+  const int npairs = (int)std::min(M_At->rpop_j, M_Zt->rpop_j);
+  const int ninner = (int)std::min(M_Yt->rpop_j, M_Wt->rpop_j);
+  const int nS = (int)M_St->rpop_j;
+  if (npairs == 0 || nS == 0) return (int)length;
+  const int Y_pcols = (int)lakbcc::psize(M_Yt->nrows);
+  const double *D_Yn = Y_ajdk + (size_t)lakbcc::AJDK_0_1 * Y_pcols;
+  const L_handle *LA = lf_AtTYn, *LZ = lf_ZtSWn;
+  std::vector<unsigned long long> ay_a(npairs), zw_z(npairs), out_r(npairs), ay_y(ninner > 0 ? ninner : 1),
+      zw_w(ninner > 0 ? ninner : 1), ay_s(nS), zw_s(nS), s_off(nS);
+  std::vector<double> Dy(ninner > 0 ? ninner : 1);
+  for (int i = 0; i < npairs; ++i) {
+    ay_a[i] = pick_u(LA->spacing_row, i, M_At->m_b_[i], M_At->m_a_[i]);
+    zw_z[i] = pick_u(LZ->spacing_row, i, M_Zt->m_b_[i], M_Zt->m_a_[i]);
+    out_r[i] = pick_u(output_spacing_a, i, M_At->m_b_[i], M_At->m_a_[i]);
+  }
+  for (int k = 0; k < ninner; ++k) {
+    ay_y[k] = pick_u(LA->spacing_col, k, M_Yt->m_b_[k], M_Yt->m_a_[k]) * LA->row_stride;
+    zw_w[k] = pick_u(LZ->spacing_col, k, M_Wt->m_b_[k], M_Wt->m_a_[k]) * LZ->row_stride;
+    Dy[k] = D_Yn[M_Yt->m_a_[k] / lakbcc::POPLENGTH];
+  }
+  for (int s = 0; s < nS; ++s) {
+    ay_s[s] = pick_u(LA->spacing_lyr, s, M_St->m_b_[s], M_St->m_a_[s]) * LA->row_stride * LA->col_stride;
+    zw_s[s] = pick_u(LZ->spacing_lyr, s, M_St->m_b_[s], M_St->m_a_[s]) * LZ->row_stride * LZ->col_stride;
+    s_off[s] = pick_u(output_spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * length_a;
+  }
+  if (max_index(ay_a) + (ninner ? max_index(ay_y) : 0) + max_index(ay_s) >= populated(LA, true) ||
+      max_index(zw_z) + (ninner ? max_index(zw_w) : 0) + max_index(zw_s) >= populated(LZ, true)) {
+    set_error(4, "wrap_AtTYn____WtSZn_vv__run: L_handle smaller than the rows and columns it is indexed by");
+    return (int)length;
+  }
+  DBuf dA = upload_L(LA, true);
+  DBuf dZ = (LZ == LA) ? DBuf() : upload_L(LZ, true);
+  const double *pZ = (LZ == LA) ? dA.as<double>() : dZ.as<double>();
+  DBuf d_aa = upload_vec(ay_a), d_ay = upload_vec(ay_y), d_as = upload_vec(ay_s);
+  DBuf d_zz = upload_vec(zw_z), d_zw = upload_vec(zw_w), d_zs = upload_vec(zw_s);
+  DBuf d_D = upload_vec(Dy), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+  dim3 grid((npairs + 127) / 128, nS);
+  attyn_wtszn_kernel<<<grid, 128, 0, stream()>>>(dA.as<double>(), d_aa.as<unsigned long long>(), d_ay.as<unsigned long long>(),
+                                                 d_as.as<unsigned long long>(), pZ, d_zz.as<unsigned long long>(),
+                                                 d_zw.as<unsigned long long>(), d_zs.as<unsigned long long>(),
+                                                 d_D.as<double>(), npairs, ninner, nS, d_or.as<unsigned long long>(),
+                                                 d_so.as<unsigned long long>(), d_out.as<double>());
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}
+
+extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                                  int output_spacing_y, int output_spacing_t, M_handle *M_At, M_handle *M_Tt,
+                                  M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, L_handle *lf_AtTn,
+                                  L_handle *lf_YtTn, L_handle **output_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  const unsigned long long la = spacing_length(output_spacing_a, M_At);
+  const unsigned long long ly = spacing_length(output_spacing_y, M_Yt);
+  const unsigned long long lt = spacing_length(output_spacing_t, M_Tt);
+  const unsigned long long length = la * ly * lt;
+  L_handle *out = ensure_output(output_p, length, "wrap_AtTYn_vv__run");
+  if (!out) return (int)length;
+  out->spacing_row = output_spacing_a; out->row_stride = la;
+  out->spacing_col = output_spacing_y; out->col_stride = ly;
+  out->spacing_lyr = output_spacing_t; out->lyr_stride = lt;
+  const int nA = (int)M_At->rpop_j, nY = (int)M_Yt->rpop_j, nT = (int)M_Tt->rpop_j;
+  if (nA == 0 || nY == 0 || nT == 0) return (int)length;
+  if (M_Yt->mc_length != M_At->mc_length || M_Tt->mc_length != M_At->mc_length) {
+    set_error(4, "wrap_AtTYn_vv__run: rows of unequal length");
+    return (int)length;
+  }
+  const int A_pcols = (int)lakbcc::psize(M_At->nrows), Y_pcols = (int)lakbcc::psize(M_Yt->nrows);
+  const double *a_An = A_ajdk + (size_t)lakbcc::AJDK_1_0 * A_pcols;
+  const double *a_Yn = Y_ajdk + (size_t)lakbcc::AJDK_1_0 * Y_pcols;
+  std::vector<uint32_t> a_rowb(M_At->m_b_, M_At->m_b_ + nA), y_rowb(M_Yt->m_b_, M_Yt->m_b_ + nY), t_rowb(nT);
+  std::vector<double> hhAy((size_t)nT * nA), hhaY((size_t)nT * nY), hhay(nT), aA(nA), aY(nY);
+  std::vector<unsigned long long> out_a(nA), out_y(nY), out_t(nT);
+  for (int i = 0; i < nA; ++i) {
+    aA[i] = a_An[M_At->m_a_[i] / lakbcc::POPLENGTH];
+    out_a[i] = pick_u(output_spacing_a, i, M_At->m_b_[i], M_At->m_a_[i]);
+  }
+  for (int k = 0; k < nY; ++k) {
+    aY[k] = a_Yn[M_Yt->m_a_[k] / lakbcc::POPLENGTH];
+    out_y[k] = pick_u(output_spacing_y, k, M_Yt->m_b_[k], M_Yt->m_a_[k]) * la;
+  }
+  for (int t = 0; t < nT; ++t) {
+    const unsigned tb = M_Tt->m_b_[t], ta = M_Tt->m_a_[t];
+    t_rowb[t] = tb;
+    out_t[t] = pick_u(output_spacing_t, t, tb, ta) * la * ly;
+    hhay[t] = (double)(-M_Tt->cpop_j + 2ll * popcount_bytes_masked(M_Tt->wX + (size_t)tb * M_Tt->mc_length, M_Tt->mc_j, (long)M_Tt->mc_length));
+    for (int i = 0; i < nA; ++i)
+      hhAy[(size_t)t * nA + i] = (double)(long long)(*lakbcc::L2_get(lf_AtTn, i, M_At->m_b_[i], M_At->m_a_[i], t, tb, ta));
+    for (int k = 0; k < nY; ++k)
+      hhaY[(size_t)t * nY + k] = (double)(long long)(*lakbcc::L2_get(lf_YtTn, k, M_Yt->m_b_[k], M_Yt->m_a_[k], t, tb, ta));
+  }
+  AtTYnParams p{};
+  p.At = (const uint8_t *)resident(M_At->wX, (size_t)M_At->rpop_b * M_At->mc_length);
+  p.Yt = (const uint8_t *)resident(M_Yt->wX, (size_t)M_Yt->rpop_b * M_Yt->mc_length);
+  p.Tt = (const uint8_t *)resident(M_Tt->wX, (size_t)M_Tt->rpop_b * M_Tt->mc_length);
+  p.a_row_bytes = p.y_row_bytes = p.t_row_bytes = (long long)M_At->mc_length;
+  DBuf d_ar = upload_vec(a_rowb), d_yr = upload_vec(y_rowb), d_tr = upload_vec(t_rowb);
+  p.a_rowb = d_ar.as<uint32_t>(); p.y_rowb = d_yr.as<uint32_t>(); p.t_rowb = d_tr.as<uint32_t>();
+  p.nA = nA; p.nY = nY;
+  DBuf mask(M_At->mc_length);
+  mask.upload(M_At->mc_j, M_At->mc_length);
+  p.mask = mask.as<uint8_t>(); p.P = (int)(M_At->mc_length / kBlockBytes); p.cpop = M_At->cpop_j;
+  DBuf d_hAy = upload_vec(hhAy), d_haY = upload_vec(hhaY), d_hay = upload_vec(hhay), d_aA = upload_vec(aA), d_aY = upload_vec(aY);
+  DBuf d_oa = upload_vec(out_a), d_oy = upload_vec(out_y), d_ot = upload_vec(out_t);
+  p.hhAy = d_hAy.as<double>(); p.hhaY = d_haY.as<double>(); p.hhay = d_hay.as<double>();
+  p.aA = d_aA.as<double>(); p.aY = d_aY.as<double>();
+  p.out_a = d_oa.as<unsigned long long>(); p.out_y = d_oy.as<unsigned long long>(); p.out_t = d_ot.as<unsigned long long>();
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+  p.out = d_out.as<double>();
+  const size_t smem = (size_t)(kTY_M + kTY_N) * kLd * sizeof(uint32_t);
+  dim3 grid((nY + kTY_N - 1) / kTY_N, (nA + kTY_M - 1) / kTY_M, nT);
+  attyn_kernel<<<grid, kTY_T, smem, stream()>>>(p);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}

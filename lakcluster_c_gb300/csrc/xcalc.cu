@@ -1,0 +1,265 @@
+// Quantisation of an FP64 matrix into bit planes: get_xcalc / wrap_xcalc
+// (dir_c/xcalc.c:5-263).
+//
+// Given YnWt (rows: the Yn rows selected by mr_b & mr_j; columns: the Wn rows
+// selected by mc_b & mc_j), the planes M_X hold, for each retained column
+// nc_j, ncols_per = b_mlt + 1 rows of bits over the Yn rows (a-space):
+//   plane ncols_per*nc_j + ncols_per-1-nb = bit nb of
+//       cz = crop((unsigned long long)(mlt*(x - min)), 1, D_MLT-1)
+// and plane 0 additionally marks the rows set in mr_j.  min, max and mlt come
+// from the masked extremes (xcalc_setmaxmin, xcalc.c:5-39):
+//   min = min_x - (max_x-min_x)/16,  max = max_x + (max_x-min_x)/16,
+//   mlt = D_MLT / (max - min).
+// The products that read the planes (At_T_YnWt_S_Zn_ww, An_ZtSn_ww) undo the
+// scaling exactly as the reference does, so the planes must match bit for bit:
+// the conversion is one IEEE subtract, one multiply and a truncation, computed
+// here with the same rounding.
+//
+// Device side: the masked min / max is a grid reduction (exact, order-free);
+// the planes are built one warp per (column, 32-row word): every lane
+// quantises one row and each plane word is one __ballot_sync, bit-reversed
+// into the reference's MSB-first byte order.  The planes stay resident on the
+// device for the products that follow, and are copied into M_X->wX for
+// callers that read them on the host.
+#include <math.h>
+
+#include "abi_common.cuh"
+#include "bcc_model.h"
+
+namespace lakgb {
+
+namespace {
+
+long long g_d_mlt = 4294967296LL;  // GLOBAL_D_MLT default (lakcluster_ver18.c:83)
+
+struct XcalcParams {
+  const double *lf;
+  const long long *row_off;  // per a-row of Yn (nrows_a): element offset, -1 = not retained
+  int nrows_a;
+  const long long *col_off;  // per retained column nc_j
+  int ncols_j;
+  double min, mlt;
+  unsigned long long dmax;   // D_MLT - 1
+  int ncols_per;
+  long long brows;           // bytes per plane row
+  uint8_t *planes;
+};
+
+__global__ void xcalc_minmax_kernel(const double *lf, const long long *rows_j, int nr,
+                                    const long long *cols_j, int nc, double *pmin, double *pmax,
+                                    int *pany) {
+  double mn = 0.0, mx = 0.0;
+  int any = 0;
+  const long long total = (long long)nr * nc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e % nr), c = (int)(e / nr);
+    const double x = lf[rows_j[r] + cols_j[c]];
+    if (!any) { mn = x; mx = x; any = 1; }
+    else { mn = x < mn ? x : mn; mx = x > mx ? x : mx; }
+  }
+  __shared__ double smn[32], smx[32];
+  __shared__ int sany[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const double omn = __shfl_xor_sync(0xffffffffu, mn, o);
+    const double omx = __shfl_xor_sync(0xffffffffu, mx, o);
+    const int oany = __shfl_xor_sync(0xffffffffu, any, o);
+    if (oany) {
+      if (!any) { mn = omn; mx = omx; any = 1; }
+      else { mn = omn < mn ? omn : mn; mx = omx > mx ? omx : mx; }
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { smn[warp] = mn; smx[warp] = mx; sany[warp] = any; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int a = 0;
+    double bmn = 0.0, bmx = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      if (!sany[w]) continue;
+      if (!a) { bmn = smn[w]; bmx = smx[w]; a = 1; }
+      else { bmn = smn[w] < bmn ? smn[w] : bmn; bmx = smx[w] > bmx ? smx[w] : bmx; }
+    }
+    pmin[blockIdx.x] = bmn; pmax[blockIdx.x] = bmx; pany[blockIdx.x] = a;
+  }
+}
+
+__global__ void xcalc_planes_kernel(XcalcParams p) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwords = (p.nrows_a + 31) >> 5;
+  if (warp >= nwords * p.ncols_j) return;
+  const int w = warp % nwords, c = warp / nwords;
+  const int r = (w << 5) + lane;
+  unsigned long long cz = 0ull;
+  if (r < p.nrows_a) {
+    const long long ro = p.row_off[r];
+    if (ro >= 0) {
+      const double x = p.lf[ro + p.col_off[c]];
+      cz = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
+      if (cz < 1ull) cz = 1ull;
+      if (cz > p.dmax) cz = p.dmax;
+    }
+  }
+  const int nbits = p.ncols_per - 1;
+  for (int nb = 0; nb < nbits; ++nb) {
+    const unsigned bal = __ballot_sync(0xffffffffu, (unsigned)((cz >> nb) & 1ull));
+    if (lane == 0 && bal) {
+      // ballot bit i = row 32w+i; memory wants row 8k+j at byte k, bit 7-j.
+      const unsigned word = __byte_perm(__brev(bal), 0u, 0x0123);
+      const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - nb;
+      *reinterpret_cast<unsigned *>(p.planes + plane * p.brows + 4ll * w) = word;
+    }
+  }
+}
+
+inline bool bit_on(const unsigned char *b, long n) { return (b[n / 8] >> (7 - n % 8)) & 1; }
+inline unsigned long long pick(int s, unsigned long long j, unsigned long long b, unsigned long long a) {
+  return s == LAKGB_SPACING_j ? j : (s == LAKGB_SPACING_b ? b : a);
+}
+
+}  // namespace
+
+}  // namespace lakgb
+
+using namespace lakgb;
+
+extern "C" void lakgb_set_d_mlt(long long d_mlt) { g_d_mlt = d_mlt; }
+
+extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigned char *mr_j,
+                           unsigned char *mr_b, unsigned char *mc_j, unsigned char *mc_b,
+                           L_handle *lf_YnWt, double *YnWt, int *Yn_nrows_p, int *Wn_nrows_p,
+                           M_handle **M_X_p, int *b_mlt_p, int trm_flag) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  const int Yn_nrows = *Yn_nrows_p, Wn_nrows = *Wn_nrows_p, b_mlt = *b_mlt_p;
+  if (!M_X_p || !*M_X_p) {
+    set_error(3, "wrap_xcalc: *M_X_p must be pre-allocated");
+    return;
+  }
+  if (!mr_j || !mr_b || !mc_j || !mc_b) printf(" %% Warning! null mask in get_xcalc\n");
+  M_handle *M_X = *M_X_p;
+  const long ylen = lakbcc::bsize(Yn_nrows), wlen = lakbcc::bsize(Wn_nrows);
+  const int rpop_j = popcount_bytes(mr_j, ylen), rpop_b = popcount_bytes(mr_b, ylen);
+  const int cpop_j = popcount_bytes(mc_j, wlen);
+  const long long length = (long long)Yn_nrows * Wn_nrows;
+  const int ncols_per = b_mlt + 1;
+  if (ncols_per > 63) printf(" %% Warning! overflow in get_xcalc!\n");
+
+  // Retained rows / columns and their element offsets (L2_lf_get, L_init.c:188-200).
+  const int sr = lf_YnWt ? lf_YnWt->spacing_row : 0, sc = lf_YnWt ? lf_YnWt->spacing_col : 0;
+  const unsigned long long rs = lf_YnWt ? lf_YnWt->row_stride : 0;
+  std::vector<long long> row_off_a((size_t)(Yn_nrows > 0 ? Yn_nrows : 1), -1), rows_j, cols_j;
+  {
+    unsigned long long j = 0, b = 0;
+    for (int a = 0; a < Yn_nrows; ++a) {
+      if (!bit_on(mr_b, a)) continue;
+      if (bit_on(mr_j, a)) {
+        const long long o = trm_flag ? (long long)(pick(sc, j, b, a) * rs) : (long long)pick(sr, j, b, a);
+        row_off_a[a] = o;
+        rows_j.push_back(o);
+        ++j;
+      }
+      ++b;
+    }
+    j = 0; b = 0;
+    for (int a = 0; a < Wn_nrows; ++a) {
+      if (!bit_on(mc_b, a)) continue;
+      if (bit_on(mc_j, a)) {
+        cols_j.push_back(trm_flag ? (long long)pick(sr, j, b, a) : (long long)(pick(sc, j, b, a) * rs));
+        ++j;
+      }
+      ++b;
+    }
+  }
+  long long max_off = 0;
+  for (long long o : rows_j) max_off = o > max_off ? o : max_off;
+  long long max_coff = 0;
+  for (long long o : cols_j) max_coff = o > max_coff ? o : max_coff;
+  const size_t lf_elems = (size_t)(max_off + max_coff + 1);
+
+  DBuf d_lf, d_rows, d_cols;
+  double min_data = 0.0, max_data = 0.0;
+  const int nr = (int)rows_j.size(), nc = (int)cols_j.size();
+  if (nr > 0 && nc > 0 && YnWt) {
+    d_lf = DBuf(lf_elems * sizeof(double));
+    d_lf.upload(YnWt, lf_elems * sizeof(double));
+    d_rows = upload_vec(rows_j);
+    d_cols = upload_vec(cols_j);
+    const long long total = (long long)nr * nc;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 1024) blocks = 1024;
+    DBuf d_min(blocks * sizeof(double)), d_max(blocks * sizeof(double)), d_any(blocks * sizeof(int));
+    xcalc_minmax_kernel<<<blocks, 256, 0, stream()>>>(d_lf.as<double>(), d_rows.as<long long>(), nr,
+                                                       d_cols.as<long long>(), nc, d_min.as<double>(),
+                                                       d_max.as<double>(), d_any.as<int>());
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch();
+    std::vector<double> hmin(blocks), hmax(blocks);
+    std::vector<int> hany(blocks);
+    LAKGB_CUDA(cudaMemcpyAsync(hmin.data(), d_min.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    LAKGB_CUDA(cudaMemcpyAsync(hmax.data(), d_max.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    LAKGB_CUDA(cudaMemcpyAsync(hany.data(), d_any.p, blocks * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    bool set = false;
+    for (int i = 0; i < blocks; ++i) {
+      if (!hany[i]) continue;
+      if (!set) { min_data = hmin[i]; max_data = hmax[i]; set = true; }
+      else { min_data = hmin[i] < min_data ? hmin[i] : min_data; max_data = hmax[i] > max_data ? hmax[i] : max_data; }
+    }
+  }
+  if (min_data >= max_data) max_data = min_data + 1;
+  const double min = min_data - 0.0625 * (max_data - min_data);
+  const double max = max_data + 0.0625 * (max_data - min_data);
+  const double mlt = (double)g_d_mlt / (max - min);
+
+  int ncols_bZ = 0, nrows_bZ = 0;
+  long long brows = 0;
+  if (length > 0 && lf_YnWt != nullptr) {
+    ncols_bZ = ncols_per * cpop_j;
+    nrows_bZ = Yn_nrows;
+    brows = lakbcc::bsize(nrows_bZ);
+    const size_t nbytes = (size_t)ncols_bZ * (size_t)brows;
+    if (!M_X->Ara) {
+      M_X->Ara = (unsigned char *)calloc(nbytes + kBlockBytes, 1);
+      if (!M_X->Ara) { set_error(2, "wrap_xcalc: out of host memory"); return; }
+    }
+    DBuf planes(nbytes);
+    planes.zero();
+    // Plane 0: the rows set in mr_j (xcalc.c:141).
+    std::vector<unsigned char> row0((size_t)brows, 0);
+    for (int a = 0; a < Yn_nrows; ++a)
+      if (bit_on(mr_j, a)) row0[a / 8] |= (unsigned char)(1 << (7 - a % 8));
+    if (nbytes) planes.upload(row0.data(), (size_t)brows);
+    if (nr > 0 && nc > 0 && YnWt) {
+      XcalcParams p{};
+      p.lf = d_lf.as<double>();
+      DBuf d_roff = upload_vec(row_off_a);
+      p.row_off = d_roff.as<long long>(); p.nrows_a = Yn_nrows;
+      p.col_off = d_cols.as<long long>(); p.ncols_j = nc;
+      p.min = min; p.mlt = mlt; p.dmax = (unsigned long long)(g_d_mlt - 1);
+      p.ncols_per = ncols_per; p.brows = brows; p.planes = planes.as<uint8_t>();
+      const long long warps = (long long)((Yn_nrows + 31) / 32) * nc;
+      const int blocks = (int)((warps * 32 + 255) / 256);
+      xcalc_planes_kernel<<<blocks, 256, 0, stream()>>>(p);
+      LAKGB_CUDA(cudaGetLastError());
+      count_launch();
+    }
+    if (nbytes) LAKGB_CUDA(cudaMemcpyAsync(M_X->Ara, planes.p, nbytes, cudaMemcpyDeviceToHost, stream()));
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    resident_put(M_X->Ara, nbytes, std::move(planes));
+  }
+  // M_X fields (xcalc.c:231-241).
+  M_X->nrows = ncols_bZ; M_X->ncols = nrows_bZ;
+  M_X->nrows_extend = (lakbcc::BITJ - (M_X->nrows % lakbcc::BITJ)) % lakbcc::BITJ;
+  M_X->mr_length = lakbcc::bsize(M_X->nrows);
+  M_X->ncols_extend = (lakbcc::BITJ - (M_X->ncols % lakbcc::BITJ)) % lakbcc::BITJ;
+  M_X->mc_length = lakbcc::bsize(M_X->ncols);
+  for (int j = 0; j < ncols_bZ; ++j) { lakbcc::bset_on(M_X->mr_b, j); lakbcc::bset_on(M_X->mr_j, j); }
+  M_X->rpop_b = ncols_bZ; M_X->rpop_j = ncols_bZ;
+  for (unsigned long i = 0; i < M_X->mc_length; ++i) { M_X->mc_b[i] = mr_b[i]; M_X->mc_j[i] = mr_j[i]; }
+  M_X->cpop_b = rpop_b; M_X->cpop_j = rpop_j;
+  M_X->wX = M_X->Ara;
+  M_X->ncols_per_z = ncols_per; M_X->max_d = max; M_X->min_d = min; M_X->mlt_d = mlt;
+  if (!isfinite(M_X->mlt_d) || M_X->mlt_d <= 0) M_X->mlt_d = 1;
+  lakbcc::mhandle_mxget(M_X);
+}

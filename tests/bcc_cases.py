@@ -1,0 +1,212 @@
+"""Whole-solve parity cases: seeded inputs, how to write them, how to run them.
+
+Each case is a bcc problem small enough for the reference to solve in seconds
+on one core.  Inputs come from lakcluster_c_gb300.synth (numpy PCG64 streams,
+identical on x86-64 and aarch64), so the committed golden traces
+(tests/golden/bcc_traces.npz, made by tests/golden/make_bcc_golden.py) can be
+checked on a machine without the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from lakcluster_c_gb300 import infiles, synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
+REF_PROGRAM = os.path.join(REF_DIR, "lakcluster_ref")
+REF_KERNELS_DRIVER = os.path.join(REF_DIR, "lakbcc_refkernels")
+GOLDEN = os.path.join(ROOT, "tests", "golden", "bcc_traces.npz")
+
+
+def _masked_case_control():
+    inst = synth.case_control(260, 230, 2000, 25, 50, 0.05, nbins=2, seed=5)
+    rng = np.random.default_rng(7)
+    Am = [(rng.random(a.shape[0]) < 0.85).astype(np.uint8) for a in inst.A_bins]
+    Zm = [(rng.random(z.shape[0]) < 0.8).astype(np.uint8) for z in inst.Z_bins]
+    cm = (rng.random(inst.ncols) < 0.9).astype(np.uint8)
+    return dict(A=inst.A_bins, Z=inst.Z_bins, A_masks=Am, Z_masks=Zm, col_mask=cm, gamma=0.05)
+
+
+def _case_only(n, m, k, seed):
+    inst = synth.case_only(n, m, k=k, flip=0.1, seed=seed)
+    return dict(A=inst.A_bins, Z=None, gamma=0.05)
+
+
+def _case_control(nA, nZ, m, kr, kc, nbins, seed, gamma=0.05, gamma_type=None):
+    inst = synth.case_control(nA, nZ, m, kr, kc, 0.05, nbins=nbins, seed=seed)
+    d = dict(A=inst.A_bins, Z=inst.Z_bins, gamma=gamma)
+    if gamma_type is not None:
+        d["gamma_type"] = gamma_type
+    return d
+
+
+# name -> (builder, has controls in every bin)
+CASES = {
+    "case_only_200x300": (lambda: _case_only(200, 300, 20, 1), False),
+    "case_only_1024x1024": (lambda: _case_only(1024, 1024, 45, 1), False),
+    "case_control_2bin_300x250x2100": (lambda: _case_control(300, 250, 2100, 30, 60, 2, 3), True),
+    "case_control_2bin_masked": (_masked_case_control, True),
+    "case_control_1bin_gamma_lin": (lambda: _case_control(180, 160, 1500, 20, 40, 1, 11, 0.1, 2), True),
+    "case_control_3bin_ragged": (lambda: _case_control(333, 271, 1931, 21, 33, 3, 13), True),
+}
+SMALL = ["case_only_200x300", "case_control_2bin_300x250x2100", "case_control_2bin_masked",
+         "case_control_1bin_gamma_lin", "case_control_3bin_ragged"]
+
+
+def build(name):
+    return CASES[name][0]()
+
+
+def write_case(name, in_dir, out_dir, fname="bcc.in"):
+    d = build(name)
+    return infiles.write_bcc_inputs(in_dir, out_dir, d["A"], d.get("Z"), gamma=d["gamma"], B_MLT=32,
+                                    A_row_masks=d.get("A_masks"), Z_row_masks=d.get("Z_masks"),
+                                    col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), name=fname)
+
+
+def read_outputs(out_dir):
+    """The three output files as lists of text lines."""
+    res = {}
+    for key, fn in (("trace", "out_trace.txt"), ("xdrop_a", "out_xdrop_a.txt"), ("xdrop_b", "out_xdrop_b.txt")):
+        with open(os.path.join(out_dir, fn)) as f:
+            res[key] = [ln.rstrip("\n") for ln in f if ln.strip()]
+    return res
+
+
+def run_reference(in_path, env=None):
+    with open(in_path) as f:
+        r = subprocess.run([REF_PROGRAM], stdin=f, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                           env=env, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference program failed:\n" + r.stdout[-2000:])
+
+
+def run_refkernels(in_path, env=None):
+    r = subprocess.run([REF_KERNELS_DRIVER, in_path], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       env=env, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver on reference kernels failed:\n" + r.stdout[-2000:])
+
+
+def trace_digest(path):
+    """Per (stage, iteration) digest of a LAKBCC_TRACE file: one line each."""
+    import hashlib
+    out, cur, h = [], None, None
+    with open(path) as f:
+        for ln in f:
+            parts = ln.split(" ", 2)
+            key = parts[0] + " " + parts[1]
+            if key != cur:
+                if cur is not None:
+                    out.append(cur + " " + h.hexdigest()[:16])
+                cur, h = key, hashlib.sha1()
+            h.update(ln.encode())
+    if cur is not None:
+        out.append(cur + " " + h.hexdigest()[:16])
+    return out
+
+
+def load_golden():
+    z = np.load(GOLDEN, allow_pickle=False)
+    out = {}
+    for name in CASES:
+        if name + "/trace" in z:
+            out[name] = {k: [str(s) for s in z[name + "/" + k]] for k in ("trace", "xdrop_a", "xdrop_b")}
+            if name + "/stages" in z:
+                out[name]["stages"] = [str(s) for s in z[name + "/stages"]]
+    return out
+
+
+# --- the GPU library's whole-solve entry points --------------------------------
+
+class BccBin(C.Structure):
+    _fields_ = [("A_nrows", C.c_int), ("A_rows", C.c_void_p), ("A_mr_b", C.c_void_p),
+                ("Z_nrows", C.c_int), ("Z_rows", C.c_void_p), ("Z_mr_b", C.c_void_p)]
+
+
+class BccProblem(C.Structure):
+    _fields_ = [("ncols", C.c_int), ("row_bytes", C.c_longlong), ("mc_b", C.c_void_p),
+                ("nbins", C.c_int), ("bins", C.POINTER(BccBin)),
+                ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int)]
+
+
+class BccResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("trace", C.POINTER(C.c_double)),
+                ("n_xdrop", C.c_int), ("xdrop_a", C.POINTER(C.c_int)), ("xdrop_b", C.POINTER(C.c_int))]
+
+
+def bind_solve(lib):
+    lib.lakgb_bcc_problem_init.argtypes = [C.POINTER(BccProblem)]
+    lib.lakgb_bcc_solve.argtypes = [C.POINTER(BccProblem), C.POINTER(BccResult)]
+    lib.lakgb_bcc_solve.restype = C.c_int
+    lib.lakgb_bcc_result_free.argtypes = [C.POINTER(BccResult)]
+    lib.lakgb_bcc_run_in_file.argtypes = [C.c_char_p]
+    lib.lakgb_bcc_run_in_file.restype = C.c_int
+    lib.lakgb_bcc_last_error.argtypes = [C.c_char_p, C.c_int]
+    return lib
+
+
+def _pack(bits):
+    bits = np.asarray(bits, np.uint8)
+    n = bits.shape[-1]
+    pad = (16 - n % 16) % 16
+    if pad:
+        bits = np.concatenate([bits, np.zeros(bits.shape[:-1] + (pad,), np.uint8)], axis=-1)
+    return np.ascontiguousarray(np.packbits(bits, axis=-1, bitorder="big"))
+
+
+def solve_in_memory(lib, name):
+    """Run a case through lakgb_bcc_solve; returns the outputs as text lines."""
+    return solve_arrays(lib, build(name))
+
+
+def solve_arrays(lib, d):
+    """lakgb_bcc_solve on a problem given as 0/1 arrays (see the CASES builders)."""
+    keep = []
+    A, Z = d["A"], d.get("Z") or [None] * len(d["A"])
+    ncols = A[0].shape[1]
+    bins = (BccBin * len(A))()
+    for nb, a in enumerate(A):
+        pa = _pack(a); keep.append(pa)
+        bins[nb].A_nrows = a.shape[0]; bins[nb].A_rows = pa.ctypes.data
+        if d.get("A_masks") is not None:
+            m = _pack(d["A_masks"][nb]); keep.append(m); bins[nb].A_mr_b = m.ctypes.data
+        z = Z[nb]
+        if z is not None and z.shape[0] > 0:
+            pz = _pack(z); keep.append(pz)
+            bins[nb].Z_nrows = z.shape[0]; bins[nb].Z_rows = pz.ctypes.data
+            if d.get("Z_masks") is not None:
+                m = _pack(d["Z_masks"][nb]); keep.append(m); bins[nb].Z_mr_b = m.ctypes.data
+    prob = BccProblem()
+    lib.lakgb_bcc_problem_init(C.byref(prob))
+    prob.ncols = ncols
+    prob.row_bytes = (ncols + (16 - ncols % 16) % 16) // 8
+    if d.get("col_mask") is not None:
+        m = _pack(d["col_mask"]); keep.append(m); prob.mc_b = m.ctypes.data
+    prob.nbins = len(A); prob.bins = bins
+    prob.gamma = d["gamma"]
+    if d.get("gamma_type") is not None:
+        prob.gamma_type = d["gamma_type"]
+    res = BccResult()
+    rc = lib.lakgb_bcc_solve(C.byref(prob), C.byref(res))
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        lib.lakgb_bcc_last_error(buf, 512)
+        raise RuntimeError("lakgb_bcc_solve failed (%d): %s" % (rc, buf.value.decode()))
+    try:
+        tr = [res.trace[i] for i in range(6 * res.iterations)]
+        xa = [res.xdrop_a[i] for i in range(2 * res.n_xdrop)]
+        xb = [res.xdrop_b[i] for i in range(2 * res.n_xdrop)]
+    finally:
+        lib.lakgb_bcc_result_free(C.byref(res))
+    trace = ["%d %d %d %0.16f %0.16f %d" % (int(tr[6 * i]), int(tr[6 * i + 1]), int(tr[6 * i + 2]),
+                                             tr[6 * i + 3], tr[6 * i + 4], int(tr[6 * i + 5]))
+             for i in range(len(tr) // 6)]
+    return {"trace": trace,
+            "xdrop_a": ["%d %d" % (xa[2 * i], xa[2 * i + 1]) for i in range(len(xa) // 2)],
+            "xdrop_b": ["%d %d" % (xb[2 * i], xb[2 * i + 1]) for i in range(len(xb) // 2)]}

@@ -20,6 +20,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <chrono>
 #include <memory>
 
 namespace lakbcc {
@@ -1516,7 +1517,26 @@ void trace_M(FILE *f, const char *stage, int it, const char *name, int a, int b,
   fprintf(f, "%s %d %s %d %d rows=%d h=%016llx\n", stage, it, name, a, b, h.nrows, x);
 }
 
+// Optional wall-clock profile per stage (LAKBCC_PROFILE=1): printed to
+// stderr when the solve ends.
+struct StageClock {
+  bool on = false;
+  std::chrono::steady_clock::time_point last;
+  std::vector<std::pair<std::string, double>> acc;
+  void tick(const char *stage) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    const double dt = std::chrono::duration<double>(now - last).count();
+    last = now;
+    for (auto &kv : acc)
+      if (kv.first == stage) { kv.second += dt; return; }
+    acc.emplace_back(stage, dt);
+  }
+};
+StageClock g_clock;
+
 void trace_stage(State &S, const char *stage) {
+  g_clock.tick(stage);
   static FILE *f = nullptr;
   static bool checked = false;
   if (!checked) {
@@ -1592,10 +1612,15 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   S.P = P;
   S.hooks = hooks;
   S.out = &O;
+  const char *prof = getenv("LAKBCC_PROFILE");
+  g_clock = StageClock();
+  g_clock.on = prof && *prof && *prof != '0';
+  g_clock.last = std::chrono::steady_clock::now();
   O = Output();
   int rc = load(S, I, err);
   if (rc) return rc;
   M_mxset_all(S);
+  trace_stage(S, "load");
   initial_subscores(S);
   while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
     sumscores_nrm(S);
@@ -1604,6 +1629,7 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     sumscores_cmb(S);
     sumscores_xij(S);
     sumscores_mxA(S);
+    trace_stage(S, "sumscores");
     lrup_QR(S); trace_stage(S, "lrup_QR");
     lrup_QC(S); trace_stage(S, "lrup_QC");
     lrup_mxdup(S);
@@ -1618,6 +1644,12 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     doublestudy_ww(S); trace_stage(S, "doublestudy");
     flattenloop(S); trace_stage(S, "flattenloop");
     if (O.iterations > 10000000) { err = "iteration limit"; return 5; }
+  }
+  if (g_clock.on) {
+    double tot = 0;
+    for (auto &kv : g_clock.acc) tot += kv.second;
+    fprintf(stderr, " %% stage profile (%d iterations, %.3f s):\n", O.iterations, tot);
+    for (auto &kv : g_clock.acc) fprintf(stderr, " %%   %-20s %9.3f s\n", kv.first.c_str(), kv.second);
   }
   return 0;
 }

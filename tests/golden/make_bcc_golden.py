@@ -22,6 +22,7 @@ reference program's files byte for byte.
 usage: python tests/golden/make_bcc_golden.py [case ...]
 """
 import os
+import subprocess
 import sys
 import tempfile
 
@@ -54,6 +55,9 @@ def infiles_read_mda(path):
 
 
 def make(names):
+    # The driver on reference kernels must be built from the current sources.
+    subprocess.run(["make", "-s", "-C", os.path.join(os.path.dirname(bc.GOLDEN), "..", "..", "oracle"), "ref"],
+                   check=True)
     out = {}
     if os.path.exists(bc.GOLDEN):
         z = np.load(bc.GOLDEN, allow_pickle=False)

@@ -200,3 +200,364 @@ void lako_calc_A_ajdk(const double *A_p, int A_pcols, double *A_ajdk)
             pow(A_p[nc] - (1 - A_p[nc]), j) *
             pow(1.0 / fmax(0.01, (4.0 * A_p[nc] * (1 - A_p[nc]))), k);
 }
+
+/* ------------------------------------------------------------------------
+ * Loop-product kernels of the YnWt solve path.
+ * ------------------------------------------------------------------------ */
+
+static inline int bit_on(const unsigned char *b, long n) { return (b[n / 8] >> (7 - n % 8)) & 1; }
+static inline int bit_pm(const unsigned char *b, long n) { return 2 * bit_on(b, n) - 1; }
+static inline void bit_set(unsigned char *b, long n) { b[n / 8] |= (unsigned char)(1 << (7 - n % 8)); }
+static long bsize_c(long n) { long m = n + (16 - n % 16) % 16; return (m + (1920 - m % 1920) % 1920) / 8; }
+static long psize_c(long n) { long m = n + (16 - n % 16) % 16; return (m + (1920 - m % 1920) % 1920) / 1920; }
+static unsigned long long pick(int s, unsigned long long j, unsigned long long b, unsigned long long a)
+{
+  return s == LAKGB_SPACING_j ? j : (s == LAKGB_SPACING_b ? b : a);
+}
+static double *L2(struct L_handle *L, unsigned long long rj, unsigned long long rb, unsigned long long ra,
+                  unsigned long long cj, unsigned long long cb, unsigned long long ca)
+{
+  return &L->lf[pick(L->spacing_row, rj, rb, ra) + pick(L->spacing_col, cj, cb, ca) * L->row_stride];
+}
+static double *L3(struct L_handle *L, unsigned long long rj, unsigned long long rb, unsigned long long ra,
+                  unsigned long long cj, unsigned long long cb, unsigned long long ca, unsigned long long lj,
+                  unsigned long long lb, unsigned long long la)
+{
+  return &L->lf[pick(L->spacing_row, rj, rb, ra) + pick(L->spacing_col, cj, cb, ca) * L->row_stride +
+                pick(L->spacing_lyr, lj, lb, la) * L->row_stride * L->col_stride];
+}
+
+/* masked signed popcounts over whole rows (popcount.c:425-540):
+ *   pm0(a,y)     = #(a=1,y=1) - #(a=0,y=1)
+ *   pmpm0(a,t,y) = #(a==t,y=1) - #(a!=t,y=1)
+ *   notxorxor    = #(~(a^t^y)) ; all under mask m, nbytes a multiple of 240 */
+static long long row_pm0(const unsigned char *a, const unsigned char *y, const unsigned char *m, long nbytes)
+{
+  long long c = 0;
+  for (long w = 0; w < nbytes / 8; w++) {
+    uint64_t ym = ld64(y + 8 * w) & ld64(m + 8 * w), aa = ld64(a + 8 * w);
+    c += __builtin_popcountll(aa & ym) - __builtin_popcountll(~aa & ym);
+  }
+  return c;
+}
+static long long row_pmpm0(const unsigned char *a, const unsigned char *t, const unsigned char *y,
+                           const unsigned char *m, long nbytes)
+{
+  long long c = 0;
+  for (long w = 0; w < nbytes / 8; w++) {
+    uint64_t ym = ld64(y + 8 * w) & ld64(m + 8 * w), x = ld64(a + 8 * w) ^ ld64(t + 8 * w);
+    c += __builtin_popcountll(~x & ym) - __builtin_popcountll(x & ym);
+  }
+  return c;
+}
+static long long row_notxorxor(const unsigned char *a, const unsigned char *t, const unsigned char *y,
+                               const unsigned char *m, long nbytes)
+{
+  long long c = 0;
+  for (long w = 0; w < nbytes / 8; w++)
+    c += __builtin_popcountll(~(ld64(a + 8 * w) ^ ld64(t + 8 * w) ^ ld64(y + 8 * w)) & ld64(m + 8 * w));
+  return c;
+}
+static long long row_and(const unsigned char *a, const unsigned char *m, long nbytes)
+{
+  long long c = 0;
+  for (long w = 0; w < nbytes / 8; w++) c += __builtin_popcountll(ld64(a + 8 * w) & ld64(m + 8 * w));
+  return c;
+}
+
+/* M_mxget (M_init.c:268-295) */
+static void mxget_part(int n, const unsigned char *mb, const unsigned char *mj, long long *pb, long long *pj,
+                       unsigned int *a_, unsigned int *b_, long length)
+{
+  *pb = popc_bytes(mb, (int)length);
+  *pj = popc_bytes(mj, (int)length);
+  int a = 0, b = 0, j = 0;
+  while (a < n) {
+    while (a < n && !bit_on(mb, a)) a++;
+    if (a < n && bit_on(mb, a) && bit_on(mj, a)) { b_[j] = b; a_[j] = a; j++; b++; a++; }
+    else if (a < n && bit_on(mb, a)) { b++; a++; }
+  }
+}
+static void mxget(struct M_handle *M)
+{
+  mxget_part(M->nrows, M->mr_b, M->mr_j, &M->rpop_b, &M->rpop_j, M->m_a_, M->m_b_, (long)M->mr_length);
+  mxget_part(M->ncols, M->mc_b, M->mc_j, &M->cpop_b, &M->cpop_j, M->n_a_, M->n_b_, (long)M->mc_length);
+}
+
+static long long g_d_mlt = 4294967296LL;
+void lako_set_d_mlt(long long d) { g_d_mlt = d; }
+
+/* dir_c/xcalc.c:5-246 (xcalc_setmaxmin + get_xcalc), into a pre-allocated M_X */
+void lako_xcalc(unsigned char *mr_j, unsigned char *mr_b, unsigned char *mc_j, unsigned char *mc_b,
+                struct L_handle *lf, double *YnWt, int Yn_nrows, int Wn_nrows, struct M_handle *M_X,
+                int b_mlt, int trm_flag)
+{
+  const int rpop_j = popc_bytes(mr_j, (int)bsize_c(Yn_nrows)), rpop_b = popc_bytes(mr_b, (int)bsize_c(Yn_nrows));
+  const int cpop_j = popc_bytes(mc_j, (int)bsize_c(Wn_nrows));
+  double min_d = 0, max_d = 0;
+  int set = 0;
+#define XGET(nrj, nrb, nra, ncj, ncb, nca) \
+  (trm_flag ? YnWt[pick(lf->spacing_row, ncj, ncb, nca) + pick(lf->spacing_col, nrj, nrb, nra) * lf->row_stride] \
+            : YnWt[pick(lf->spacing_row, nrj, nrb, nra) + pick(lf->spacing_col, ncj, ncb, nca) * lf->row_stride])
+  {
+    long nc_j = 0, nc_b = 0;
+    for (long nc_a = 0; nc_a < Wn_nrows; nc_a++) {
+      if (!bit_on(mc_b, nc_a)) continue;
+      if (bit_on(mc_j, nc_a)) {
+        long nr_j = 0, nr_b = 0;
+        for (long nr_a = 0; nr_a < Yn_nrows; nr_a++) {
+          if (!bit_on(mr_b, nr_a)) continue;
+          if (bit_on(mr_j, nr_a)) {
+            double x = XGET(nr_j, nr_b, nr_a, nc_j, nc_b, nc_a);
+            if (!set) { min_d = x; max_d = x; set = 1; }
+            else { min_d = x < min_d ? x : min_d; max_d = x > max_d ? x : max_d; }
+            nr_j++;
+          }
+          nr_b++;
+        }
+        nc_j++;
+      }
+      nc_b++;
+    }
+  }
+  if (min_d >= max_d) max_d = min_d + 1;
+  const double mn = min_d - 0.0625 * (max_d - min_d), mx = max_d + 0.0625 * (max_d - min_d);
+  const double mlt = (double)g_d_mlt / (mx - mn);
+  const int ncols_per = b_mlt + 1;
+  int ncols_bZ = 0, nrows_bZ = 0;
+  if ((long long)Yn_nrows * Wn_nrows > 0 && lf) {
+    ncols_bZ = ncols_per * cpop_j;
+    nrows_bZ = Yn_nrows;
+    const long brows = bsize_c(nrows_bZ);
+    if (!M_X->Ara) M_X->Ara = (unsigned char *)calloc((size_t)ncols_bZ * brows + 240, 1);
+    unsigned char *bZ = M_X->Ara;
+    memset(bZ, 0, (size_t)ncols_bZ * brows);
+    for (long nr_a = 0; nr_a < Yn_nrows; nr_a++)
+      if (bit_on(mr_j, nr_a)) bit_set(bZ, nr_a);
+    long nc_j = 0, nc_b = 0;
+    for (long nc_a = 0; nc_a < Wn_nrows; nc_a++) {
+      if (!bit_on(mc_b, nc_a)) continue;
+      if (bit_on(mc_j, nc_a)) {
+        long nr_j = 0, nr_b = 0;
+        for (long nr_a = 0; nr_a < Yn_nrows; nr_a++) {
+          if (!bit_on(mr_b, nr_a)) continue;
+          if (bit_on(mr_j, nr_a)) {
+            double x = XGET(nr_j, nr_b, nr_a, nc_j, nc_b, nc_a);
+            unsigned long long cz = (unsigned long long)(mlt * (double)(x - mn));
+            if (cz < 1) cz = 1;
+            if (cz > (unsigned long long)(g_d_mlt - 1)) cz = (unsigned long long)(g_d_mlt - 1);
+            for (int nb = 0; nb < ncols_per - 1; nb++)
+              if ((cz >> nb) & 1) bit_set(bZ + (long)(ncols_per * nc_j + ncols_per - 1 - nb) * brows, nr_a);
+            nr_j++;
+          }
+          nr_b++;
+        }
+        nc_j++;
+      }
+      nc_b++;
+    }
+  }
+#undef XGET
+  M_X->nrows = ncols_bZ; M_X->ncols = nrows_bZ;
+  M_X->nrows_extend = (16 - M_X->nrows % 16) % 16; M_X->mr_length = bsize_c(M_X->nrows);
+  M_X->ncols_extend = (16 - M_X->ncols % 16) % 16; M_X->mc_length = bsize_c(M_X->ncols);
+  for (int j = 0; j < ncols_bZ; j++) { bit_set(M_X->mr_b, j); bit_set(M_X->mr_j, j); }
+  M_X->rpop_b = ncols_bZ; M_X->rpop_j = ncols_bZ;
+  for (unsigned long i = 0; i < M_X->mc_length; i++) { M_X->mc_b[i] = mr_b[i]; M_X->mc_j[i] = mr_j[i]; }
+  M_X->cpop_b = rpop_b; M_X->cpop_j = rpop_j;
+  M_X->wX = M_X->Ara;
+  M_X->ncols_per_z = ncols_per; M_X->max_d = mx; M_X->min_d = mn; M_X->mlt_d = mlt;
+  if (!isfinite(M_X->mlt_d) || M_X->mlt_d <= 0) M_X->mlt_d = 1;
+  mxget(M_X);
+}
+
+/* dir_c/At_T_YnWt_S_Zn_ww.c:5-190 (serial branch, :44-111) */
+int lako_At_T_YnWt_S_Zn_ww(int spacing_a, int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                           struct M_handle *M_Yn, struct M_handle *M_Wn, struct M_handle *M_St,
+                           struct M_handle *M_Zt, double *A_ajdk, struct M_handle *M_YnWt,
+                           struct L_handle **out_p)
+{
+  (void)M_Yn;
+  unsigned long long la = spacing_len(spacing_a, M_At), lt = spacing_len(spacing_t, M_Tt);
+  struct L_handle *out = ensure(out_p, la * lt);
+  if (!out) return (int)(la * lt);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_t; out->col_stride = lt;
+  const int A_pcols = (int)psize_c(M_At->nrows);
+  const double *a_An = A_ajdk + 1 * A_pcols; /* AJDK_1_0 */
+  const long nb = (long)M_At->mc_length;
+  const int ncp = M_YnWt->ncols_per_z;
+  const long long nT = M_Tt->rpop_j < M_St->rpop_j ? M_Tt->rpop_j : M_St->rpop_j;
+  const long long nP = M_At->rpop_j < M_Zt->rpop_j ? M_At->rpop_j : M_Zt->rpop_j;
+  const long long nW = M_Wn->rpop_j;
+  double *ttmp = (double *)calloc((size_t)(nW ? nW : 1), sizeof(double));
+  for (long long t = 0; t < nT; t++) {
+    const unsigned char *St = M_St->wX + (long long)M_St->m_b_[t] * M_St->mc_length;
+    const unsigned char *Tt = M_Tt->wX + (long long)M_Tt->m_b_[t] * M_Tt->mc_length;
+    const unsigned char *p0 = M_YnWt->wX;
+    const unsigned long long tab_t = pick(spacing_t, t, M_Tt->m_b_[t], M_Tt->m_a_[t]);
+    const double tbase = (double)row_pmpm0(p0, Tt, p0, M_At->mc_j, nb) * M_YnWt->min_d * M_YnWt->mlt_d;
+    for (long long mw = 0; mw < nW; mw++) {
+      double s = 0;
+      long long n2 = 1;
+      for (int mx = ncp - 1; mx > 0; mx--) {
+        double d = (double)row_pmpm0(p0, Tt, M_YnWt->wX + (long long)(ncp * mw + mx) * M_YnWt->mc_length, M_At->mc_j, nb);
+        s += n2 * d;
+        n2 *= 2;
+      }
+      ttmp[mw] = s;
+    }
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+    for (long long i = 0; i < nP; i++) {
+      const unsigned na_a = M_At->m_a_[i], nz_a = M_Zt->m_a_[i];
+      const unsigned char *At = M_At->wX + (long long)M_At->m_b_[i] * M_At->mc_length;
+      const unsigned char *Zt = M_Zt->wX + (long long)M_Zt->m_b_[i] * M_Zt->mc_length;
+      const double Abase = (double)row_pmpm0(At, Tt, M_YnWt->wX, M_At->mc_j, nb) * M_YnWt->min_d * M_YnWt->mlt_d;
+      double acc = 0;
+      for (long long mw = 0; mw < nW; mw++) {
+        const unsigned mw_a = M_Wn->m_a_[mw];
+        const int vS = bit_pm(St, mw_a), vZ = bit_pm(Zt, mw_a);
+        double Atmp = 0;
+        long long n2 = 1;
+        for (int mx = ncp - 1; mx > 0; mx--) {
+          Atmp += n2 * row_pmpm0(At, Tt, M_YnWt->wX + (long long)(ncp * mw + mx) * M_YnWt->mc_length, M_At->mc_j, nb);
+          n2 *= 2;
+        }
+        const double abase = tbase * a_An[na_a / 1920], atmp = ttmp[mw] * a_An[na_a / 1920];
+        const double X = (double)(Abase + Atmp) / M_YnWt->mlt_d - (double)(abase + atmp) / M_YnWt->mlt_d;
+        acc += X * vS * (vZ - a_An[nz_a / 1920]);
+      }
+      out->lf[pick(spacing_a, i, M_At->m_b_[i], na_a) + tab_t * la] = acc;
+    }
+  }
+  free(ttmp);
+  return (int)(la * lt);
+}
+
+/* dir_c/An_ZtSn_ww.c:5-136 */
+int lako_An_ZtSn_ww(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_ZtSn,
+                    struct M_handle *M_St, struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_An), ls = spacing_len(spacing_s, M_St);
+  struct L_handle *out = ensure(out_p, la * ls);
+  if (!out) return (int)(la * ls);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_s; out->col_stride = ls;
+  const long nb = (long)M_An->mc_length;
+  const int ncp = M_ZtSn->ncols_per_z;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (long long i = 0; i < M_An->rpop_j; i++) {
+    const unsigned char *a = M_An->wX + (long long)M_An->m_b_[i] * M_An->mc_length;
+    const double base = (double)row_pm0(a, M_ZtSn->wX, M_An->mc_j, nb) * M_ZtSn->min_d * M_ZtSn->mlt_d;
+    for (long long s = 0; s < M_St->rpop_j; s++) {
+      double tmp = 0;
+      long long n2 = 1;
+      for (int mx = ncp - 1; mx > 0; mx--) {
+        double d = (double)row_pm0(a, M_ZtSn->wX + (long long)(ncp * s + mx) * M_ZtSn->mc_length, M_An->mc_j, nb);
+        tmp += n2 * d;
+        n2 *= 2;
+      }
+      out->lf[pick(spacing_a, i, M_An->m_b_[i], M_An->m_a_[i]) +
+              pick(spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * la] = (double)(base + tmp) / M_ZtSn->mlt_d;
+    }
+  }
+  return (int)(la * ls);
+}
+
+/* dir_c/AnZt_S_WnYt_vv.c:5-101 */
+int lako_AnZt_S_WnYt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                        struct M_handle *M_Zn, struct L_handle *lf_AnZt, struct L_handle *lf_YnWt,
+                        struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_An), ls = spacing_len(spacing_s, M_St);
+  struct L_handle *out = ensure(out_p, la * ls);
+  if (!out) return (int)(la * ls);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_s; out->col_stride = ls;
+  if (!lf_AnZt || !lf_YnWt) return (int)(la * ls);
+  for (long long s = 0; s < M_St->rpop_j; s++) {
+    const unsigned char *St = M_St->wX + (long long)M_St->m_b_[s] * M_St->mc_length;
+    const unsigned long long ts = pick(spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads())
+    for (long long ma = 0; ma < M_An->rpop_j; ma++) {
+      const unsigned ma_a = M_An->m_a_[ma], ma_b = M_An->m_b_[ma];
+      double acc = 0;
+      for (long long mz = 0; mz < M_Zn->rpop_j; mz++) {
+        const unsigned mz_a = M_Zn->m_a_[mz], mz_b = M_Zn->m_b_[mz];
+        const int vS = bit_pm(St, mz_a);
+        acc += (*L2(lf_AnZt, ma, ma_b, ma_a, mz, mz_b, mz_a)) * vS * (*L2(lf_YnWt, ma, ma_b, ma_a, mz, mz_b, mz_a));
+      }
+      out->lf[pick(spacing_a, ma, ma_b, ma_a) + ts * la] = acc;
+    }
+  }
+  return (int)(la * ls);
+}
+
+/* dir_c/AtTYn_vv.c:5-202 */
+int lako_AtTYn_vv(int spacing_a, int spacing_y, int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                  struct M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_AtTn,
+                  struct L_handle *lf_YtTn, struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_At), ly = spacing_len(spacing_y, M_Yt),
+                     lt = spacing_len(spacing_t, M_Tt);
+  struct L_handle *out = ensure(out_p, la * ly * lt);
+  if (!out) return (int)(la * ly * lt);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_y; out->col_stride = ly;
+  out->spacing_lyr = spacing_t; out->lyr_stride = lt;
+  const double *a_An = A_ajdk + 1 * psize_c(M_At->nrows), *a_Yn = Y_ajdk + 1 * psize_c(M_Yt->nrows);
+  const long nb = (long)M_At->mc_length;
+  for (long long t = 0; t < M_Tt->rpop_j; t++) {
+    const unsigned t_a = M_Tt->m_a_[t], t_b = M_Tt->m_b_[t];
+    const unsigned char *Tt = M_Tt->wX + (long long)t_b * M_Tt->mc_length;
+    const long long hhay = -M_Tt->cpop_j + 2 * row_and(Tt, M_Tt->mc_j, (long)M_Tt->mc_length);
+    const unsigned long long tab_t = pick(spacing_t, t, t_b, t_a);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+    for (long long na = 0; na < M_At->rpop_j; na++) {
+      const unsigned na_a = M_At->m_a_[na], na_b = M_At->m_b_[na];
+      const unsigned char *At = M_At->wX + (long long)na_b * M_At->mc_length;
+      const long long hhAy = (long long)*L2(lf_AtTn, na, na_b, na_a, t, t_b, t_a);
+      for (long long ny = 0; ny < M_Yt->rpop_j; ny++) {
+        const unsigned ny_a = M_Yt->m_a_[ny], ny_b = M_Yt->m_b_[ny];
+        const long long hhaY = (long long)*L2(lf_YtTn, ny, ny_b, ny_a, t, t_b, t_a);
+        long long hhAY = M_At->cpop_j;
+        hhAY -= 2 * row_notxorxor(At, Tt, M_Yt->wX + (long long)ny_b * M_Yt->mc_length, M_At->mc_j, nb);
+        out->lf[pick(spacing_a, na, na_b, na_a) + pick(spacing_y, ny, ny_b, ny_a) * la + tab_t * la * ly] =
+            (hhAY - hhAy * a_Yn[ny_a / 1920] - a_An[na_a / 1920] * hhaY + a_An[na_a / 1920] * hhay * a_Yn[ny_a / 1920]);
+      }
+    }
+  }
+  return (int)(la * ly * lt);
+}
+
+/* dir_c/AtTYn____WtSZn_vv.c:5-115 */
+int lako_AtTYn____WtSZn_vv(int spacing_a, int spacing_s, struct M_handle *M_At, struct M_handle *M_Tt,
+                           struct M_handle *M_Yt, struct M_handle *M_Wt, struct M_handle *M_St,
+                           struct M_handle *M_Zt, double *Y_ajdk, struct L_handle *lf_AtTYn,
+                           struct L_handle *lf_ZtSWn, struct L_handle **out_p)
+{
+  (void)M_Tt;
+  unsigned long long la = spacing_len(spacing_a, M_At), ls = spacing_len(spacing_s, M_St);
+  struct L_handle *out = ensure(out_p, la * ls);
+  if (!out) return (int)(la * ls);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_s; out->col_stride = ls;
+  const double *D_Yn = Y_ajdk + 5 * psize_c(M_Yt->nrows); /* AJDK_0_1 */
+  const long long nP = M_At->rpop_j < M_Zt->rpop_j ? M_At->rpop_j : M_Zt->rpop_j;
+  const long long nI = M_Yt->rpop_j < M_Wt->rpop_j ? M_Yt->rpop_j : M_Wt->rpop_j;
+  for (long long s = 0; s < M_St->rpop_j; s++) {
+    const unsigned s_a = M_St->m_a_[s], s_b = M_St->m_b_[s];
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads())
+    for (long long i = 0; i < nP; i++) {
+      const unsigned na_a = M_At->m_a_[i], na_b = M_At->m_b_[i], nz_a = M_Zt->m_a_[i], nz_b = M_Zt->m_b_[i];
+      double acc = 0;
+      for (long long k = 0; k < nI; k++) {
+        const unsigned ny_a = M_Yt->m_a_[k], ny_b = M_Yt->m_b_[k], nw_a = M_Wt->m_a_[k], nw_b = M_Wt->m_b_[k];
+        acc += (*L3(lf_AtTYn, i, na_b, na_a, k, ny_b, ny_a, s, s_b, s_a)) * D_Yn[ny_a / 1920] *
+               (*L3(lf_ZtSWn, i, nz_b, nz_a, k, nw_b, nw_a, s, s_b, s_a));
+      }
+      out->lf[pick(spacing_a, i, na_b, na_a) + pick(spacing_s, s, s_b, s_a) * la] = acc;
+    }
+  }
+  return (int)(la * ls);
+}

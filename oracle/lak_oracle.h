@@ -35,6 +35,33 @@ int lako_An_ajdk_v(int type_flag, int spacing_r, struct M_handle *M_An, double *
 /* dir_c/An_ajdk_v.c:5-30 */
 void lako_calc_A_ajdk(const double *A_p, int A_pcols, double *A_ajdk);
 
+/* dir_c/xcalc.c:5-246 (into a pre-allocated M_X; D_MLT from lako_set_d_mlt) */
+void lako_xcalc(unsigned char *mr_j, unsigned char *mr_b, unsigned char *mc_j, unsigned char *mc_b,
+                struct L_handle *lf_YnWt, double *YnWt, int Yn_nrows, int Wn_nrows, struct M_handle *M_X,
+                int b_mlt, int trm_flag);
+void lako_set_d_mlt(long long d_mlt);
+/* dir_c/At_T_YnWt_S_Zn_ww.c:5-190 */
+int lako_At_T_YnWt_S_Zn_ww(int spacing_a, int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                           struct M_handle *M_Yn, struct M_handle *M_Wn, struct M_handle *M_St,
+                           struct M_handle *M_Zt, double *A_ajdk, struct M_handle *M_YnWt,
+                           struct L_handle **out_p);
+/* dir_c/An_ZtSn_ww.c:5-136 */
+int lako_An_ZtSn_ww(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_ZtSn,
+                    struct M_handle *M_St, struct L_handle **out_p);
+/* dir_c/AnZt_S_WnYt_vv.c:5-101 */
+int lako_AnZt_S_WnYt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                        struct M_handle *M_Zn, struct L_handle *lf_AnZt, struct L_handle *lf_YnWt,
+                        struct L_handle **out_p);
+/* dir_c/AtTYn_vv.c:5-202 */
+int lako_AtTYn_vv(int spacing_a, int spacing_y, int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                  struct M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_AtTn,
+                  struct L_handle *lf_YtTn, struct L_handle **out_p);
+/* dir_c/AtTYn____WtSZn_vv.c:5-115 */
+int lako_AtTYn____WtSZn_vv(int spacing_a, int spacing_s, struct M_handle *M_At, struct M_handle *M_Tt,
+                           struct M_handle *M_Yt, struct M_handle *M_Wt, struct M_handle *M_St,
+                           struct M_handle *M_Zt, double *Y_ajdk, struct L_handle *lf_AtTYn,
+                           struct L_handle *lf_ZtSWn, struct L_handle **out_p);
+
 /* Threads used by the OpenMP loops (default: all). */
 void lako_set_threads(int n);
 

@@ -90,3 +90,23 @@ def test_b16_round_trip(tmp_path):
         assert np.array_equal(infiles.read_b16(p), x)
         hdr = np.fromfile(p, dtype=np.int32, count=3)
         assert list(hdr) == [16, shape[1], shape[0]]
+
+
+@pytest.fixture(scope="module")
+def port_driver():
+    import subprocess
+    subprocess.run(["make", "-s", "-C", os.path.join(bc.ROOT, "oracle"), "port"], check=True)
+    return os.path.join(bc.ROOT, "oracle", "lakbcc_port")
+
+
+@pytest.mark.parametrize("name", list(bc.CASES))
+def test_oracle_port_solve_matches_golden(tmp_path, golden, port_driver, name):
+    """The driver on the plain-C oracle kernels: a whole solve that builds on
+    every machine, pinned to the reference's outputs."""
+    import subprocess
+    p = bc.write_case(name, str(tmp_path / "in"), str(tmp_path / "out"))
+    r = subprocess.run([port_driver, p], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout[-2000:]
+    got = bc.read_outputs(str(tmp_path / "out"))
+    for key in ("trace", "xdrop_a", "xdrop_b"):
+        assert got[key] == golden[name][key], key

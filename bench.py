@@ -13,6 +13,11 @@ launches of the +/-1 centred D-weighted Gram with FP64 scores.
          (wrap_AnZt_vv__run / wrap_AnAt_vv__run) on host buffers, with the
          bit-matrix upload and the FP64 result download inside the timed region.
 
+Whole solves ("solves" in the JSON line): config 1 (case-only 1024 x 1024,
+the reference's CPU-runnable case) timed over repeated lakgb_bcc_solve calls
+and checked against the reference's golden trace, and one solve of the
+case/control workload; the config-1 solve is also timed on the host cores.
+
 `--impl reference` times the reference's CPU implementation of the pass on
 this host's cores instead: the reference compiled from its sources when it is
 available here (x86-64 with the reference tree), otherwise the plain-C port of
@@ -184,6 +189,7 @@ def run_reference(args):
         secs += s
         work += w
     value = work / secs
+    solves = {"case_only_1024x1024": {"cpu": cpu_solve_c1()}} if not args.no_solves else None
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
@@ -192,6 +198,8 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": CPU_SAMPLE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if solves is not None:
+        line["solves"] = solves
     print(json.dumps(line), flush=True)
     return 0
 
@@ -314,6 +322,10 @@ def run_gpu(args):
         cpu = {"value": w / secs, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": CPU_SAMPLE + ", 3 passes, %.1f s" % secs}
 
+    solves = None
+    if rank == 0 and not args.no_solves:
+        solves = solve_measurements(args, with_cpu=(world == 1 and not args.no_cpu_baseline))
+
     peaks, src = _peaks()
     tflops = 2.0 * k_work / (k_ms / 1000.0) / 1e12
     peak_tf = float(peaks.get("bf16_tflops", 1900.0))
@@ -347,10 +359,79 @@ def run_gpu(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if solves is not None:
+            line["solves"] = solves
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def solve_measurements(args, with_cpu: bool):
+    """Whole-solve timings: config 1 (case-only 1024 x 1024, the reference's
+    CPU-runnable case) and the case/control workload above, through
+    lakgb_bcc_solve from host arrays (uploads and downloads included), and the
+    same config-1 solve on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import bcc_cases as bc
+    from lakcluster_c_gb300 import solve as sv, synth
+
+    golden = bc.load_golden()
+    out = {}
+    d1 = bc.build("case_only_1024x1024")
+    p1 = sv.Problem(d1["A"], None, gamma=d1["gamma"])
+    r = p1.solve()
+    same1 = all(r[k] == golden["case_only_1024x1024"][k] for k in ("trace", "xdrop_a", "xdrop_b"))
+    t = []
+    for _ in range(max(3, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        p1.solve()
+        t.append(time.perf_counter() - t0)
+    s1 = statistics.median(t)
+    out["case_only_1024x1024"] = {"seconds": s1, "solves_per_s": 1.0 / s1, "iterations": len(r["trace"]),
+                                  "matches_reference": same1, "reps": len(t)}
+    inst = synth.case_control(seed=2)
+    p2 = sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05)
+    t0 = time.perf_counter()
+    r2 = p2.solve()
+    s2 = time.perf_counter() - t0
+    c2 = {"seconds": s2, "solves_per_s": 1.0 / s2, "iterations": len(r2["trace"]), "reps": 1}
+    if "case_control_4096x4096x16384" in golden:
+        g = golden["case_control_4096x4096x16384"]
+        c2["matches_oracle_port"] = all(r2[k] == g[k] for k in ("trace", "xdrop_a", "xdrop_b"))
+    out["case_control_4096x4096x16384"] = c2
+    if with_cpu:
+        out["case_only_1024x1024"]["cpu"] = cpu_solve_c1()
+    return out
+
+
+def cpu_solve_c1():
+    """Config-1 solve on the host cores: the reference program where it
+    builds (x86-64 with its sources), else the solve driver on the C oracle."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import bcc_cases as bc
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as td:
+        p = bc.write_case("case_only_1024x1024", os.path.join(td, "in"), os.path.join(td, "out"))
+        txt = open(p).read().replace("GLOBAL_thread_count= 1;", "GLOBAL_thread_count= %d;" % threads)
+        txt = txt.replace("GLOBAL_omp_type= 0;", "GLOBAL_omp_type= 1;")
+        open(p, "w").write(txt)
+        if os.path.exists(bc.REF_PROGRAM) and os.uname().machine == "x86_64":
+            cmd, kind = None, "reference"
+        else:
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+            cmd, kind = [os.path.join(ROOT, "oracle", "lakbcc_port"), p, str(threads)], "port"
+        t = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            if cmd is None:
+                bc.run_reference(p)
+            else:
+                subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+            t.append(time.perf_counter() - t0)
+    s = min(t)
+    return {"seconds": s, "solves_per_s": 1.0 / s, "cores": threads, "kind": kind, "reps": len(t)}
 
 
 def _products(nbins):
@@ -365,6 +446,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solves", action="store_true", help="skip the whole-solve timings")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

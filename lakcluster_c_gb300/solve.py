@@ -1,0 +1,135 @@
+"""Whole bcc solves on the GPU library (lakgb_bcc_solve / lakgb_bcc_run_in_file).
+
+`solve(A_bins, Z_bins, ...)` takes per-bin 0/1 matrices (rows x SNPs, 1 = the
+minor allele), packs them MSB-first the way the reference's .b16 files are,
+and returns the solve's outputs: the per-iteration trace and the elimination
+order, both as the text lines the reference writes to out_trace.txt and
+out_xdrop_{a,b}.txt (dir_c/bcc_sumscores.c:143-153).  `run_in_file(path)`
+runs a reference .in file and writes those files itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import load
+
+
+class BccBin(C.Structure):
+    _fields_ = [("A_nrows", C.c_int), ("A_rows", C.c_void_p), ("A_mr_b", C.c_void_p),
+                ("Z_nrows", C.c_int), ("Z_rows", C.c_void_p), ("Z_mr_b", C.c_void_p)]
+
+
+class BccProblem(C.Structure):
+    _fields_ = [("ncols", C.c_int), ("row_bytes", C.c_longlong), ("mc_b", C.c_void_p),
+                ("nbins", C.c_int), ("bins", C.POINTER(BccBin)),
+                ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int)]
+
+
+class BccResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("trace", C.POINTER(C.c_double)),
+                ("n_xdrop", C.c_int), ("xdrop_a", C.POINTER(C.c_int)), ("xdrop_b", C.POINTER(C.c_int))]
+
+
+def bind(lib):
+    lib.lakgb_bcc_problem_init.argtypes = [C.POINTER(BccProblem)]
+    lib.lakgb_bcc_solve.argtypes = [C.POINTER(BccProblem), C.POINTER(BccResult)]
+    lib.lakgb_bcc_solve.restype = C.c_int
+    lib.lakgb_bcc_result_free.argtypes = [C.POINTER(BccResult)]
+    lib.lakgb_bcc_run_in_file.argtypes = [C.c_char_p]
+    lib.lakgb_bcc_run_in_file.restype = C.c_int
+    lib.lakgb_bcc_last_error.argtypes = [C.c_char_p, C.c_int]
+    return lib
+
+
+def pack_rows(bits) -> np.ndarray:
+    """0/1 array (..., n) -> packed rows of rup(n,16)/8 bytes, MSB first."""
+    bits = np.asarray(bits, np.uint8)
+    n = bits.shape[-1]
+    pad = (16 - n % 16) % 16
+    if pad:
+        bits = np.concatenate([bits, np.zeros(bits.shape[:-1] + (pad,), np.uint8)], axis=-1)
+    return np.ascontiguousarray(np.packbits(bits, axis=-1, bitorder="big"))
+
+
+class Problem:
+    """A packed bcc problem kept alive for repeated solves."""
+
+    def __init__(self, A_bins, Z_bins=None, *, gamma=0.125, B_MLT=32, gamma_type=0, A_masks=None,
+                 Z_masks=None, col_mask=None, test_sparse=1, lib=None):
+        self.lib = bind(lib or load())
+        self._keep = []
+        nb = len(A_bins)
+        Z_bins = Z_bins if Z_bins is not None else [None] * nb
+        ncols = np.asarray(A_bins[0]).shape[1]
+        self.bins = (BccBin * nb)()
+        for b in range(nb):
+            a = np.asarray(A_bins[b], np.uint8)
+            pa = self._hold(pack_rows(a))
+            self.bins[b].A_nrows = a.shape[0]
+            self.bins[b].A_rows = pa.ctypes.data
+            if A_masks is not None:
+                self.bins[b].A_mr_b = self._hold(pack_rows(A_masks[b])).ctypes.data
+            z = Z_bins[b]
+            if z is not None and np.asarray(z).shape[0] > 0:
+                z = np.asarray(z, np.uint8)
+                self.bins[b].Z_nrows = z.shape[0]
+                self.bins[b].Z_rows = self._hold(pack_rows(z)).ctypes.data
+                if Z_masks is not None:
+                    self.bins[b].Z_mr_b = self._hold(pack_rows(Z_masks[b])).ctypes.data
+        self.prob = BccProblem()
+        self.lib.lakgb_bcc_problem_init(C.byref(self.prob))
+        self.prob.ncols = ncols
+        self.prob.row_bytes = (ncols + (16 - ncols % 16) % 16) // 8
+        if col_mask is not None:
+            self.prob.mc_b = self._hold(pack_rows(col_mask)).ctypes.data
+        self.prob.nbins = nb
+        self.prob.bins = self.bins
+        self.prob.gamma = gamma
+        self.prob.B_MLT = B_MLT
+        self.prob.gamma_type = gamma_type
+        self.prob.test_sparse = test_sparse
+        self.ncols = ncols
+
+    def _hold(self, x):
+        self._keep.append(x)
+        return x
+
+    def solve(self):
+        res = BccResult()
+        rc = self.lib.lakgb_bcc_solve(C.byref(self.prob), C.byref(res))
+        if rc != 0:
+            buf = C.create_string_buffer(512)
+            self.lib.lakgb_bcc_last_error(buf, 512)
+            raise RuntimeError("lakgb_bcc_solve failed (%d): %s" % (rc, buf.value.decode()))
+        try:
+            tr = np.ctypeslib.as_array(res.trace, (6 * res.iterations,)).copy() if res.iterations else np.zeros(0)
+            xa = np.ctypeslib.as_array(res.xdrop_a, (2 * res.n_xdrop,)).copy() if res.n_xdrop else np.zeros(0, int)
+            xb = np.ctypeslib.as_array(res.xdrop_b, (2 * res.n_xdrop,)).copy() if res.n_xdrop else np.zeros(0, int)
+        finally:
+            self.lib.lakgb_bcc_result_free(C.byref(res))
+        return format_outputs(tr, xa, xb)
+
+
+def format_outputs(tr, xa, xb):
+    """The reference's output-file lines from a trace / xdrop array triple."""
+    trace = ["%d %d %d %0.16f %0.16f %d" % (int(tr[6 * i]), int(tr[6 * i + 1]), int(tr[6 * i + 2]),
+                                             tr[6 * i + 3], tr[6 * i + 4], int(tr[6 * i + 5]))
+             for i in range(len(tr) // 6)]
+    return {"trace": trace,
+            "xdrop_a": ["%d %d" % (xa[2 * i], xa[2 * i + 1]) for i in range(len(xa) // 2)],
+            "xdrop_b": ["%d %d" % (xb[2 * i], xb[2 * i + 1]) for i in range(len(xb) // 2)]}
+
+
+def solve(A_bins, Z_bins=None, **kw):
+    return Problem(A_bins, Z_bins, **kw).solve()
+
+
+def run_in_file(path: str) -> None:
+    lib = bind(load())
+    rc = lib.lakgb_bcc_run_in_file(path.encode())
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        lib.lakgb_bcc_last_error(buf, 512)
+        raise RuntimeError("lakgb_bcc_run_in_file failed (%d): %s" % (rc, buf.value.decode()))

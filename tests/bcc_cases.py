@@ -8,7 +8,6 @@ checked on a machine without the reference.
 """
 from __future__ import annotations
 
-import ctypes as C
 import os
 import subprocess
 
@@ -124,40 +123,9 @@ def load_golden():
 
 # --- the GPU library's whole-solve entry points --------------------------------
 
-class BccBin(C.Structure):
-    _fields_ = [("A_nrows", C.c_int), ("A_rows", C.c_void_p), ("A_mr_b", C.c_void_p),
-                ("Z_nrows", C.c_int), ("Z_rows", C.c_void_p), ("Z_mr_b", C.c_void_p)]
-
-
-class BccProblem(C.Structure):
-    _fields_ = [("ncols", C.c_int), ("row_bytes", C.c_longlong), ("mc_b", C.c_void_p),
-                ("nbins", C.c_int), ("bins", C.POINTER(BccBin)),
-                ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int)]
-
-
-class BccResult(C.Structure):
-    _fields_ = [("iterations", C.c_int), ("trace", C.POINTER(C.c_double)),
-                ("n_xdrop", C.c_int), ("xdrop_a", C.POINTER(C.c_int)), ("xdrop_b", C.POINTER(C.c_int))]
-
-
 def bind_solve(lib):
-    lib.lakgb_bcc_problem_init.argtypes = [C.POINTER(BccProblem)]
-    lib.lakgb_bcc_solve.argtypes = [C.POINTER(BccProblem), C.POINTER(BccResult)]
-    lib.lakgb_bcc_solve.restype = C.c_int
-    lib.lakgb_bcc_result_free.argtypes = [C.POINTER(BccResult)]
-    lib.lakgb_bcc_run_in_file.argtypes = [C.c_char_p]
-    lib.lakgb_bcc_run_in_file.restype = C.c_int
-    lib.lakgb_bcc_last_error.argtypes = [C.c_char_p, C.c_int]
-    return lib
-
-
-def _pack(bits):
-    bits = np.asarray(bits, np.uint8)
-    n = bits.shape[-1]
-    pad = (16 - n % 16) % 16
-    if pad:
-        bits = np.concatenate([bits, np.zeros(bits.shape[:-1] + (pad,), np.uint8)], axis=-1)
-    return np.ascontiguousarray(np.packbits(bits, axis=-1, bitorder="big"))
+    from lakcluster_c_gb300 import solve as sv
+    return sv.bind(lib)
 
 
 def solve_in_memory(lib, name):
@@ -167,46 +135,7 @@ def solve_in_memory(lib, name):
 
 def solve_arrays(lib, d):
     """lakgb_bcc_solve on a problem given as 0/1 arrays (see the CASES builders)."""
-    keep = []
-    A, Z = d["A"], d.get("Z") or [None] * len(d["A"])
-    ncols = A[0].shape[1]
-    bins = (BccBin * len(A))()
-    for nb, a in enumerate(A):
-        pa = _pack(a); keep.append(pa)
-        bins[nb].A_nrows = a.shape[0]; bins[nb].A_rows = pa.ctypes.data
-        if d.get("A_masks") is not None:
-            m = _pack(d["A_masks"][nb]); keep.append(m); bins[nb].A_mr_b = m.ctypes.data
-        z = Z[nb]
-        if z is not None and z.shape[0] > 0:
-            pz = _pack(z); keep.append(pz)
-            bins[nb].Z_nrows = z.shape[0]; bins[nb].Z_rows = pz.ctypes.data
-            if d.get("Z_masks") is not None:
-                m = _pack(d["Z_masks"][nb]); keep.append(m); bins[nb].Z_mr_b = m.ctypes.data
-    prob = BccProblem()
-    lib.lakgb_bcc_problem_init(C.byref(prob))
-    prob.ncols = ncols
-    prob.row_bytes = (ncols + (16 - ncols % 16) % 16) // 8
-    if d.get("col_mask") is not None:
-        m = _pack(d["col_mask"]); keep.append(m); prob.mc_b = m.ctypes.data
-    prob.nbins = len(A); prob.bins = bins
-    prob.gamma = d["gamma"]
-    if d.get("gamma_type") is not None:
-        prob.gamma_type = d["gamma_type"]
-    res = BccResult()
-    rc = lib.lakgb_bcc_solve(C.byref(prob), C.byref(res))
-    if rc != 0:
-        buf = C.create_string_buffer(512)
-        lib.lakgb_bcc_last_error(buf, 512)
-        raise RuntimeError("lakgb_bcc_solve failed (%d): %s" % (rc, buf.value.decode()))
-    try:
-        tr = [res.trace[i] for i in range(6 * res.iterations)]
-        xa = [res.xdrop_a[i] for i in range(2 * res.n_xdrop)]
-        xb = [res.xdrop_b[i] for i in range(2 * res.n_xdrop)]
-    finally:
-        lib.lakgb_bcc_result_free(C.byref(res))
-    trace = ["%d %d %d %0.16f %0.16f %d" % (int(tr[6 * i]), int(tr[6 * i + 1]), int(tr[6 * i + 2]),
-                                             tr[6 * i + 3], tr[6 * i + 4], int(tr[6 * i + 5]))
-             for i in range(len(tr) // 6)]
-    return {"trace": trace,
-            "xdrop_a": ["%d %d" % (xa[2 * i], xa[2 * i + 1]) for i in range(len(xa) // 2)],
-            "xdrop_b": ["%d %d" % (xb[2 * i], xb[2 * i + 1]) for i in range(len(xb) // 2)]}
+    from lakcluster_c_gb300 import solve as sv
+    p = sv.Problem(d["A"], d.get("Z"), gamma=d["gamma"], gamma_type=d.get("gamma_type") or 0,
+                   A_masks=d.get("A_masks"), Z_masks=d.get("Z_masks"), col_mask=d.get("col_mask"), lib=lib)
+    return p.solve()

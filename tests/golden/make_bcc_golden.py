@@ -20,6 +20,7 @@ constant injected into that one An_v call, the same driver reproduces the
 reference program's files byte for byte.
 
 usage: python tests/golden/make_bcc_golden.py [case ...]
+       python tests/golden/make_bcc_golden.py --port [case ...]   (PORT_CASES, minutes)
 """
 import os
 import subprocess
@@ -94,5 +95,28 @@ def make(names):
     np.savez_compressed(bc.GOLDEN, **out)
 
 
+def make_port(names, threads):
+    """Golden outputs of the cases in PORT_CASES, from oracle/lakbcc_port."""
+    subprocess.run(["make", "-s", "-C", os.path.join(os.path.dirname(bc.GOLDEN), "..", "..", "oracle"), "port"],
+                   check=True)
+    z = np.load(bc.GOLDEN, allow_pickle=False)
+    out = {k: z[k] for k in z.files}
+    for name in names:
+        with tempfile.TemporaryDirectory() as td:
+            p = bc.write_case(name, os.path.join(td, "in"), os.path.join(td, "out"))
+            subprocess.run([os.path.join(os.path.dirname(bc.GOLDEN), "..", "..", "oracle", "lakbcc_port"), p,
+                            str(threads)], check=True, stdout=subprocess.DEVNULL)
+            golden = bc.read_outputs(os.path.join(td, "out"))
+            for key in ("trace", "xdrop_a", "xdrop_b"):
+                out[name + "/" + key] = np.array(golden[key])
+            out[name + "/source"] = np.array(["solve driver on the C oracle kernels"])
+            print("%-34s %4d iterations  %5d drops  (oracle port)" % (name, len(golden["trace"]), len(golden["xdrop_a"])))
+    np.savez_compressed(bc.GOLDEN, **out)
+
+
 if __name__ == "__main__":
-    make(sys.argv[1:] or list(bc.CASES))
+    args = sys.argv[1:]
+    if args[:1] == ["--port"]:
+        make_port(args[1:] or list(bc.PORT_CASES), os.cpu_count() or 1)
+    else:
+        make(args or list(bc.CASES))

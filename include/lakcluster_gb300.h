@@ -240,6 +240,37 @@ struct lakgb_gram_args {
 };
 int lakgb_gram_device(const struct lakgb_gram_args *args);
 
+/* Allocation-free quantisation (no counterpart in the reference): the
+ * arithmetic of wrap_xcalc on caller-owned device buffers, for callers that
+ * must not allocate device memory -- e.g. a process whose device memory is
+ * fully reserved up front by its own pool (the serving loop admits solves by
+ * HBM footprint), or code on a path where a cudaMalloc would synchronise the
+ * device.  Its scratch is one static device array of
+ * 3 * LAKGB_XCALC_NOALLOC_MAX_COLS + 4 doubles (786,464 bytes), so at most
+ * LAKGB_XCALC_NOALLOC_MAX_COLS retained columns; larger problems are rejected
+ * with an error.  The array is shared by every call on a device: calls whose
+ * kernels overlap on the GPU race.  The first call on a device looks the array
+ * up (cudaGetSymbolAddress) and should come before any stream capture.
+ * Inputs (device): lf, the element offset of each Yn a-row (-1 = not
+ * retained, nrows_a entries), of each retained row (rows_j) and column
+ * (cols_j) in j order, and plane 0 (row0, brows bytes, may be NULL).
+ * Output: planes ((b_mlt+1)*n_cols_j rows of brows bytes, overwritten) and,
+ * in host memory, {min, max, mlt} as wrap_xcalc stores them in M_X.  Returns 0,
+ * or non-zero with lakgb_last_error() set. */
+#define LAKGB_XCALC_NOALLOC_MAX_COLS 32768
+struct lakgb_xcalc_noalloc_args {
+  const double *lf;
+  const long long *row_off_a; int nrows_a;
+  const long long *rows_j; int n_rows_j;
+  const long long *cols_j; int n_cols_j;
+  const unsigned char *row0;
+  int b_mlt; long long d_mlt; long long brows;
+  unsigned char *planes;
+  double *min_max_mlt;
+  void *stream;   /* cudaStream_t; NULL = the legacy default stream */
+};
+int lakgb_xcalc_noalloc(const struct lakgb_xcalc_noalloc_args *args);
+
 /* ---------------------------------------------------------------------------
  * Library control (no reference counterpart).
  * ------------------------------------------------------------------------- */

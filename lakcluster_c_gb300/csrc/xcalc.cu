@@ -23,6 +23,8 @@
 // callers that read them on the host.
 #include <math.h>
 
+#include <mutex>
+
 #include "abi_common.cuh"
 #include "bcc_model.h"
 
@@ -111,6 +113,136 @@ __global__ void xcalc_planes_kernel(XcalcParams p) {
       *reinterpret_cast<unsigned *>(p.planes + plane * p.brows + 4ll * w) = word;
     }
   }
+}
+
+// --- allocation-free variant ---------------------------------------------
+//
+// lakgb_xcalc_noalloc runs the same quantisation on caller-owned device
+// buffers for callers that cannot allocate device memory.  Its only scratch
+// is this file-scope array: per retained column, the column's min, max and a
+// "has values" flag (3 x kNoAllocMaxCols doubles), then min / max / mlt of
+// the whole matrix (4 doubles) -- 786,464 bytes in all.  Every entry a call
+// reads is written earlier in the same call, so nothing needs clearing; the
+// array is shared by every call on a device, so calls whose kernels overlap
+// on the GPU race.
+constexpr int kNoAllocMaxCols = LAKGB_XCALC_NOALLOC_MAX_COLS;
+static __device__ __align__(256) double g_xcalc_noalloc_scratch[3 * kNoAllocMaxCols + 4];
+
+// Column-wise min / max of the retained entries: one block per column.
+__global__ void xcalc_colminmax_kernel(const double *lf, const long long *rows_j, int nr, const long long *cols_j,
+                                       int nc, double *scratch) {
+  const int c = blockIdx.x;
+  if (c >= nc) return;
+  double mn = 0.0, mx = 0.0;
+  int any = 0;
+  for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+    const double x = lf[rows_j[r] + cols_j[c]];
+    if (!any) { mn = x; mx = x; any = 1; }
+    else { mn = x < mn ? x : mn; mx = x > mx ? x : mx; }
+  }
+  __shared__ double smn[32], smx[32];
+  __shared__ int sany[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const double omn = __shfl_xor_sync(0xffffffffu, mn, o);
+    const double omx = __shfl_xor_sync(0xffffffffu, mx, o);
+    const int oany = __shfl_xor_sync(0xffffffffu, any, o);
+    if (oany) {
+      if (!any) { mn = omn; mx = omx; any = 1; }
+      else { mn = omn < mn ? omn : mn; mx = omx > mx ? omx : mx; }
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { smn[warp] = mn; smx[warp] = mx; sany[warp] = any; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int a = 0;
+    double bmn = 0.0, bmx = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      if (!sany[w]) continue;
+      if (!a) { bmn = smn[w]; bmx = smx[w]; a = 1; }
+      else { bmn = smn[w] < bmn ? smn[w] : bmn; bmx = smx[w] > bmx ? smx[w] : bmx; }
+    }
+    scratch[c] = bmn;
+    scratch[kNoAllocMaxCols + c] = bmx;
+    scratch[2 * kNoAllocMaxCols + c] = a ? 1.0 : 0.0;
+  }
+}
+
+// One thread folds the column partials in column order (min / max are exact,
+// so the order does not change the result) and derives min, max and mlt with
+// the host formula's operations (xcalc.c:129-130, 240).
+__global__ void xcalc_scalars_kernel(int nc, double d_mlt, double *scratch) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double mn = 0.0, mx = 0.0;
+  int set = 0;
+  for (int c = 0; c < nc; ++c) {
+    if (scratch[2 * kNoAllocMaxCols + c] == 0.0) continue;
+    const double a = scratch[c], b = scratch[kNoAllocMaxCols + c];
+    if (!set) { mn = a; mx = b; set = 1; }
+    else { mn = a < mn ? a : mn; mx = b > mx ? b : mx; }
+  }
+  if (mn >= mx) mx = __dadd_rn(mn, 1.0);
+  const double range = __dsub_rn(mx, mn);
+  const double lo = __dsub_rn(mn, __dmul_rn(0.0625, range));
+  const double hi = __dadd_rn(mx, __dmul_rn(0.0625, range));
+  double mlt = __ddiv_rn(d_mlt, __dsub_rn(hi, lo));
+  double* out = scratch + 3 * kNoAllocMaxCols;
+  out[0] = lo;
+  out[1] = hi;
+  out[2] = mlt;            // used by the plane kernel
+  if (!isfinite(mlt) || mlt <= 0) mlt = 1.0;
+  out[3] = mlt;            // the value wrap_xcalc stores as M_X->mlt_d
+}
+
+__global__ void xcalc_planes_dev_kernel(XcalcParams p, const double *scalars) {
+  p.min = scalars[0];
+  p.mlt = scalars[2];
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwords = (p.nrows_a + 31) >> 5;
+  if (warp >= nwords * p.ncols_j) return;
+  const int w = warp % nwords, c = warp / nwords;
+  const int r = (w << 5) + lane;
+  unsigned long long cz = 0ull;
+  if (r < p.nrows_a) {
+    const long long ro = p.row_off[r];
+    if (ro >= 0) {
+      const double x = p.lf[ro + p.col_off[c]];
+      cz = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
+      if (cz < 1ull) cz = 1ull;
+      if (cz > p.dmax) cz = p.dmax;
+    }
+  }
+  for (int nb = 0; nb < p.ncols_per - 1; ++nb) {
+    const unsigned bal = __ballot_sync(0xffffffffu, (unsigned)((cz >> nb) & 1ull));
+    if (lane == 0 && bal) {
+      const unsigned word = __byte_perm(__brev(bal), 0u, 0x0123);
+      const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - nb;
+      *reinterpret_cast<unsigned *>(p.planes + plane * p.brows + 4ll * w) = word;
+    }
+  }
+}
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_scratch[64] = {nullptr};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the lookup is a runtime call that must not run inside a stream
+// capture, so callers make their first call before any capture).
+double *noalloc_scratch() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_scratch[dev]) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_xcalc_noalloc_scratch);
+    if (e != cudaSuccess) {
+      set_error(1000 + (int)e, "lakgb_xcalc_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return nullptr;
+    }
+    g_noalloc_scratch[dev] = ptr;
+  }
+  return static_cast<double *>(g_noalloc_scratch[dev]);
 }
 
 inline bool bit_on(const unsigned char *b, long n) { return (b[n / 8] >> (7 - n % 8)) & 1; }
@@ -262,4 +394,54 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
   M_X->ncols_per_z = ncols_per; M_X->max_d = max; M_X->min_d = min; M_X->mlt_d = mlt;
   if (!isfinite(M_X->mlt_d) || M_X->mlt_d <= 0) M_X->mlt_d = 1;
   lakbcc::mhandle_mxget(M_X);
+}
+
+extern "C" int lakgb_xcalc_noalloc(const struct lakgb_xcalc_noalloc_args *a) {
+  if (!a || !a->planes || !a->min_max_mlt || (a->n_rows_j > 0 && a->n_cols_j > 0 && (!a->lf || !a->rows_j ||
+      !a->cols_j || !a->row_off_a))) {
+    set_error(2, "lakgb_xcalc_noalloc: null argument");
+    return 2;
+  }
+  if (a->n_cols_j > kNoAllocMaxCols || a->n_cols_j < 0 || a->n_rows_j < 0 || a->nrows_a < 0) {
+    set_error(2, "lakgb_xcalc_noalloc: %d retained columns exceed the scratch limit of %d", a->n_cols_j,
+              kNoAllocMaxCols);
+    return 2;
+  }
+  if (a->b_mlt < 1 || a->b_mlt > 62 || a->brows < (long long)((a->nrows_a + 31) / 32) * 4) {
+    set_error(2, "lakgb_xcalc_noalloc: b_mlt out of range or plane rows too short");
+    return 2;
+  }
+  double *scratch = noalloc_scratch();
+  if (!scratch) return 3;
+  cudaStream_t s = static_cast<cudaStream_t>(a->stream);
+  const int ncols_per = a->b_mlt + 1;
+  const size_t nbytes = (size_t)ncols_per * (size_t)a->n_cols_j * (size_t)a->brows;
+  if (nbytes) LAKGB_CUDA(cudaMemsetAsync(a->planes, 0, nbytes, s));
+  if (nbytes && a->row0) LAKGB_CUDA(cudaMemcpyAsync(a->planes, a->row0, (size_t)a->brows, cudaMemcpyDeviceToDevice, s));
+  const int nc = (a->n_rows_j > 0) ? a->n_cols_j : 0;
+  if (nc > 0) {
+    xcalc_colminmax_kernel<<<nc, 128, 0, s>>>(a->lf, a->rows_j, a->n_rows_j, a->cols_j, nc, scratch);
+    LAKGB_CUDA(cudaGetLastError());
+  }
+  xcalc_scalars_kernel<<<1, 32, 0, s>>>(nc, (double)a->d_mlt, scratch);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch(nc > 0 ? 2 : 1);
+  if (nc > 0) {
+    XcalcParams p{};
+    p.lf = a->lf; p.row_off = a->row_off_a; p.nrows_a = a->nrows_a;
+    p.col_off = a->cols_j; p.ncols_j = nc;
+    p.dmax = (unsigned long long)(a->d_mlt - 1); p.ncols_per = ncols_per; p.brows = a->brows;
+    p.planes = a->planes;
+    const long long warps = (long long)((a->nrows_a + 31) / 32) * nc;
+    xcalc_planes_dev_kernel<<<(int)((warps * 32 + 255) / 256), 256, 0, s>>>(p, scratch + 3 * kNoAllocMaxCols);
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch();
+  }
+  double sc[4];
+  LAKGB_CUDA(cudaMemcpyAsync(sc, scratch + 3 * kNoAllocMaxCols, sizeof(sc), cudaMemcpyDeviceToHost, s));
+  LAKGB_CUDA(cudaStreamSynchronize(s));
+  a->min_max_mlt[0] = sc[0];
+  a->min_max_mlt[1] = sc[1];
+  a->min_max_mlt[2] = sc[3];
+  return 0;
 }

@@ -325,6 +325,8 @@ def run_gpu(args):
     solves = None
     if rank == 0 and not args.no_solves:
         solves = solve_measurements(args, with_cpu=(world == 1 and not args.no_cpu_baseline))
+        if not args.no_many:
+            solves.update(many_solves_measurements(args))
 
     peaks, src = _peaks()
     tflops = 2.0 * k_work / (k_ms / 1000.0) / 1e12
@@ -405,6 +407,44 @@ def solve_measurements(args, with_cpu: bool):
     return out
 
 
+def many_solves_measurements(args):
+    """Batched label-shuffled nulls and a served Poisson stream, each against
+    the plain one-solve-at-a-time path on the same problems (results must be
+    identical)."""
+    from lakcluster_c_gb300 import serve, solve as sv, synth
+    workers = max(2, min(16, os.cpu_count() or 2))
+    out = {}
+    # Batched nulls: label-shuffled case/control instances of uneven sizes.
+    n_null = 12
+    probs = []
+    for i in range(n_null):
+        inst = synth.null_instance(1000 + i, rows=(1024, 8192), cols=(4096, 16384))
+        probs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05))
+    plain, t_plain = serve.solve_plain(probs)
+    batched, t_batch, peak = serve.solve_batched(probs, workers=workers)
+    out["batched_nulls"] = {
+        "instances": n_null, "rows": "logU[1024,8192]", "cols": "logU[4096,16384]", "workers": workers,
+        "plain_solves_per_s": n_null / t_plain, "batched_solves_per_s": n_null / t_batch,
+        "speedup": t_plain / t_batch, "peak_concurrency": peak, "identical_to_plain": batched == plain}
+    # Served stream: Poisson arrivals at twice the plain path's throughput.
+    n_req = 16
+    reqs = []
+    for i in range(n_req):
+        inst = synth.served_request(5000 + i, rows=(512, 4096), cols=(2048, 16384))
+        reqs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05))
+    solo, t_solo = serve.solve_plain(reqs)
+    rate = 2.0 * n_req / t_solo
+    r1, lat1, wall1, _ = serve.serve_stream(reqs, rate, workers=1, seed=7)
+    rw, latw, wallw, peakw = serve.serve_stream(reqs, rate, workers=workers, seed=7)
+    out["served"] = {
+        "requests": n_req, "rows": "logU[512,4096]", "cols": "logU[2048,16384]", "categories": "U{0..3}",
+        "arrival_rate_per_s": rate, "workers": workers,
+        "plain": dict(serve.latency_stats(lat1), solves_per_s=n_req / wall1),
+        "continuous_batching": dict(serve.latency_stats(latw), solves_per_s=n_req / wallw, peak_concurrency=peakw),
+        "identical_to_solo": (r1 == solo) and (rw == solo)}
+    return out
+
+
 def cpu_solve_c1():
     """Config-1 solve on the host cores: the reference program where it
     builds (x86-64 with its sources), else the solve driver on the C oracle."""
@@ -447,6 +487,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solves", action="store_true", help="skip the whole-solve timings")
+    ap.add_argument("--no-many", action="store_true", help="skip the batched / served timings")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

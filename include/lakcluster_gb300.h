@@ -213,6 +213,27 @@ int lakgb_bcc_solve(const struct lakgb_bcc_problem *p, struct lakgb_bcc_result *
 void lakgb_bcc_result_free(struct lakgb_bcc_result *r);
 int lakgb_bcc_last_error(char *msg, int msg_len);
 
+/* Many solves at once (no reference counterpart).  A server owns `workers`
+ * host threads, each driving whole solves on its own CUDA stream, and admits a
+ * submitted problem as soon as a worker is idle and its estimated device
+ * footprint (lakgb_bcc_footprint) fits hbm_budget_bytes beside the solves
+ * already running (<= 0: no budget); a problem that does not fit yet does not
+ * hold back smaller ones submitted after it.  submit copies the problem's
+ * arrays; wait blocks for one result (ownership passes to the caller; free it
+ * with lakgb_bcc_result_free) and reports {queueing, solving, total} seconds.
+ * Each result equals the same problem solved alone. */
+struct lakgb_server;
+struct lakgb_server *lakgb_server_create(int workers, long long hbm_budget_bytes);
+long long lakgb_server_submit(struct lakgb_server *s, const struct lakgb_bcc_problem *p);
+int lakgb_server_wait(struct lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times3);
+int lakgb_server_peak_concurrency(struct lakgb_server *s);
+void lakgb_server_destroy(struct lakgb_server *s);
+long long lakgb_bcc_footprint(const struct lakgb_bcc_problem *p);
+/* Solve n problems on a server of `workers` threads; returns the number that
+ * failed (per-problem status in rcs, may be NULL). */
+int lakgb_bcc_solve_many(const struct lakgb_bcc_problem *ps, int n, struct lakgb_bcc_result *rs, int *rcs,
+                         int workers, long long hbm_budget_bytes);
+
 /* ---------------------------------------------------------------------------
  * Device-resident entry points (no reference counterpart: the reference has
  * no device memory).  All pointers are device pointers; `stream` is a
@@ -239,6 +260,20 @@ struct lakgb_gram_args {
   void *stream;
 };
 int lakgb_gram_device(const struct lakgb_gram_args *args);
+
+/* Device mirrors of L_handles (no reference counterpart).  After
+ * lakgb_L_mirror(L) the values of L live on the device: the kernel entry
+ * points above write a mirrored output there (not into L->lf) and read a
+ * mirrored input from there; lakgb_L_to_host copies them back into L->lf.
+ * lakgb_L_sub (dst->lf[i] -= src->lf[i] for i < dst->length) and
+ * lakgb_L_transpose (L2_transpose, dir_c/L_init.c:31-38) run on the device
+ * when both handles are mirrored.  The bcc solve mirrors its Gram matrices
+ * (AnZt, AnAt and their low-rank updates) for the whole solve. */
+void lakgb_L_mirror(struct L_handle *L);
+void lakgb_L_release_mirror(struct L_handle *L);
+void lakgb_L_to_host(struct L_handle *L);
+void lakgb_L_sub(struct L_handle *dst, const struct L_handle *src);
+void lakgb_L_transpose(struct L_handle *dst, const struct L_handle *src);
 
 /* Allocation-free quantisation (no counterpart in the reference): the
  * arithmetic of wrap_xcalc on caller-owned device buffers, for callers that

@@ -72,9 +72,7 @@ inline long long popcount_bytes_masked(const unsigned char *p, const unsigned ch
 
 template <class T>
 inline DBuf upload_vec(const std::vector<T> &v) {
-  DBuf d(v.size() * sizeof(T));
-  d.upload(v.data(), v.size() * sizeof(T));
-  return d;
+  return upload_bytes(v.data(), v.size() * sizeof(T));
 }
 
 inline void copy_back(double *host, const DBuf &dev, unsigned long long length) {

@@ -12,6 +12,7 @@
 #include "lakgb_runtime.cuh"
 #include "rowvec.cuh"
 #include "abi_common.cuh"
+#include "lmirror.cuh"
 
 using namespace lakgb;
 
@@ -27,7 +28,20 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   const unsigned long long length_r = spacing_length(spacing_r, M_An);
   const unsigned long long length_c = spacing_length(spacing_c, M_Zn);
   const unsigned long long length = length_r * length_c;
-  L_handle *out = ensure_output(out_p, length, who);
+  // A mirrored output (lmirror.cu) is produced on the device only.
+  Mirror *mo = *out_p ? find_mirror(*out_p) : nullptr;
+  L_handle *out = nullptr;
+  if (mo) {
+    out = *out_p;
+    if (out->length < length || mo->n < length) {
+      set_error(2, "output length %llu < %llu in %s", out->length, length, who);
+      return (int)length;
+    }
+    if (length) LAKGB_CUDA(cudaMemsetAsync(mo->d, 0, length * sizeof(double), stream()));
+    mo->host_stale = true;
+  } else {
+    out = ensure_output(out_p, length, who);
+  }
   if (!out) return (int)length;
   out->spacing_row = spacing_r; out->row_stride = length_r;
   out->spacing_col = spacing_c; out->col_stride = length_c;
@@ -47,9 +61,9 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   if (nA == 0 || nZ == 0 || P == 0) return (int)length;
 
   const void *wA = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
+  Stager st;
   const void *wZ = resident(M_Zn->wX, (size_t)M_Zn->rpop_b * M_Zn->mc_length);
-  DBuf mask(M_An->mc_length);
-  mask.upload(M_An->mc_j, M_An->mc_length);
+  DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> arow(M_An->m_b_, M_An->m_b_ + nA), zrow(M_Zn->m_b_, M_Zn->m_b_ + nZ);
   DBuf d_arow = upload_vec(arow), d_zrow = upload_vec(zrow);
   DBuf d_outr = upload_vec(spacing_index(spacing_r, M_An));
@@ -61,8 +75,7 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   }
   DBuf d_D;
   if (A_ajdk) {
-    d_D = DBuf((size_t)P * sizeof(double));
-    d_D.upload(A_ajdk + (size_t)kAjdk_0_1 * P, (size_t)P * sizeof(double));
+    d_D = upload_bytes(A_ajdk + (size_t)kAjdk_0_1 * P, (size_t)P * sizeof(double));
   }
   DBuf d_lfA, d_lfZ;
   if (lf_An_ajdk && lf_Zn_ajdk) {
@@ -74,8 +87,15 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
     d_lfA = upload_vec(a);
     d_lfZ = upload_vec(z);
   }
-  DBuf d_out(length * sizeof(double));
-  d_out.zero();
+  DBuf d_out;
+  double *dout = nullptr;
+  if (mo) {
+    dout = mo->d;
+  } else {
+    d_out = DBuf(length * sizeof(double));
+    d_out.zero();
+    dout = d_out.as<double>();
+  }
 
   GramParams p{};
   p.wA = (const uint8_t *)wA; p.a_rowb = d_arow.as<uint32_t>(); p.nA = nA; p.a_row_bytes = (long long)M_An->mc_length;
@@ -86,9 +106,11 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   p.lfA = d_lfA.as<double>(); p.lfZ = d_lfZ.as<double>();
   p.out_r = d_outr.as<uint32_t>(); p.out_c = d_outc.as<uint32_t>();
   p.out_r2 = d_outr2.as<uint32_t>(); p.out_c2 = d_outc2.as<uint32_t>();
-  p.out_stride = (long long)length_r; p.out = d_out.as<double>();
+  p.out_stride = (long long)length_r; p.out = dout;
   p.symmetric = symmetric ? 1 : 0;
+  st.flush();
   launch_gram(p);
+  if (mo) return (int)length;
   copy_back(out->lf, d_out, length);
   return (int)length;
 }
@@ -128,10 +150,11 @@ extern "C" int wrap_An_v__run(int *tidx, void **vpra, pthread_t *thread_in, int 
   if (n == 0) return (int)length;
   const int P = (int)(M_An->mc_length / kBlockBytes);
   const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
-  DBuf mask(M_An->mc_length);
-  mask.upload(M_An->mc_j, M_An->mc_length);
+  Stager st;
+  DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> rows(M_An->m_b_, M_An->m_b_ + n);
   DBuf d_rows = upload_vec(rows), d_outr = upload_vec(spacing_index(output_spacing_r, M_An));
+  st.flush();
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   RowvecParams p{};
@@ -168,14 +191,12 @@ extern "C" int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int 
   const int n = (int)M_An->rpop_j;
   if (n == 0) return (int)length;
   const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
-  DBuf mask(M_An->mc_length);
-  mask.upload(M_An->mc_j, M_An->mc_length);
+  Stager st;
+  DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> rows(M_An->m_b_, M_An->m_b_ + n);
   DBuf d_rows = upload_vec(rows), d_outr = upload_vec(spacing_index(output_spacing_r, M_An));
-  DBuf d_ajdk((size_t)P * LAKGB_AJDK_TOT * sizeof(double));
-  d_ajdk.upload(A_ajdk, (size_t)P * LAKGB_AJDK_TOT * sizeof(double));
-  DBuf d_base(sizeof(base));
-  d_base.upload(base, sizeof(base));
+  DBuf d_ajdk = upload_bytes(A_ajdk, (size_t)P * LAKGB_AJDK_TOT * sizeof(double));
+  DBuf d_base = upload_bytes(base, sizeof(base));
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   RowvecParams p{};
@@ -183,6 +204,7 @@ extern "C" int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int 
   p.mask = mask.as<uint8_t>(); p.P = P; p.type = (type_flag == LAKGB_TYPE_pm) ? 1 : 2;
   p.ajdk = d_ajdk.as<double>(); p.base = d_base.as<double>();
   p.out_r = d_outr.as<uint32_t>(); p.out_stride = (long long)length_r; p.out = d_out.as<double>();
+  st.flush();
   launch_an_ajdk(p);
   copy_back(out->lf, d_out, length);
   return (int)length;

@@ -9,8 +9,7 @@
 
 #include "bcc_driver.h"
 
-extern "C" void lakgb_set_d_mlt(long long d_mlt);
-extern "C" void lakgb_forget_host_buffer(const void *host_ptr);
+#include "../../include/lakcluster_gb300.h"
 
 namespace {
 
@@ -22,7 +21,8 @@ void release_L(L_handle *L) {
   free(L);
 }
 
-const lakbcc::Hooks kHooks = {release_L, lakgb_forget_host_buffer};
+const lakbcc::Hooks kHooks = {release_L,     lakgb_forget_host_buffer, lakgb_L_mirror, lakgb_L_release_mirror,
+                               lakgb_L_to_host, lakgb_L_sub,             lakgb_L_transpose};
 
 long row_bytes_min(int ncols) { return (long)(ncols + (16 - ncols % 16) % 16) / 8; }
 

@@ -32,6 +32,24 @@ void *g_vpra[128];
 pthread_t g_thread;
 #define TARGS &g_tidx, g_vpra, &g_thread
 
+// Optional wall-clock profile per stage (LAKBCC_PROFILE=1): printed to
+// stderr when the solve ends.
+struct StageClock {
+  bool on = false;
+  std::chrono::steady_clock::time_point last;
+  std::vector<std::pair<std::string, double>> acc;
+  void tick(const char *stage) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    const double dt = std::chrono::duration<double>(now - last).count();
+    last = now;
+    for (auto &kv : acc)
+      if (kv.first == stage) { kv.second += dt; return; }
+    acc.emplace_back(stage, dt);
+  }
+};
+thread_local StageClock g_clock;
+
 // ---------------------------------------------------------------------------
 // State (the subset of bcc_ajdk / bcc_single / bcc_double used on this path)
 
@@ -123,7 +141,27 @@ struct State {
   void forget(const std::vector<unsigned char> &v) {
     if (!v.empty() && hooks && hooks->forget_host) hooks->forget_host(v.data());
   }
+  std::vector<L_handle *> mirrored;
+  void mirror(L_handle *L) {
+    if (!hooks || !hooks->L_mirror || !L) return;
+    if (std::find(mirrored.begin(), mirrored.end(), L) != mirrored.end()) return;
+    hooks->L_mirror(L);
+    mirrored.push_back(L);
+  }
+  void to_host(L_handle *L) {
+    if (hooks && hooks->L_to_host && L) hooks->L_to_host(L);
+  }
+  void sub(L_handle *dst, const L_handle *src) {
+    if (hooks && hooks->L_sub) { hooks->L_sub(dst, src); return; }
+    for (unsigned long long i = 0; i < dst->length; ++i) dst->lf[i] -= src->lf[i];
+  }
+  void transpose(L_handle *dst, const L_handle *src) {
+    if (hooks && hooks->L_transpose) { hooks->L_transpose(dst, src); return; }
+    lh_transpose(dst, src);
+  }
   ~State() {
+    if (hooks && hooks->L_release_mirror)
+      for (L_handle *L : mirrored) hooks->L_release_mirror(L);
     // Outputs the kernel entry points allocated on first use.
     for (auto &E : this->E) {
       for (L_handle *L : {E->lf_An_ajdk, E->lf_Zn_ajdk, E->lf_AtTn, E->lf_ZtSn, E->lf_jn_ajdk, E->lf_vn_ajdk,
@@ -242,14 +280,38 @@ std::vector<unsigned char> compact_rows(const std::vector<unsigned char> &rows, 
   return out;
 }
 
-// Transpose a-space rows (nrows x ncols) into a-space rows of the transpose.
+// Transpose a-space rows (nrows x ncols) into a-space rows of the transpose,
+// 8 x 8 bit blocks at a time (byte k of row r holds columns 8k..8k+7,
+// most significant bit first).
+inline uint64_t transpose8(uint64_t x) {
+  // Bit-matrix transpose of an 8 x 8 block held one row per byte (row i in
+  // byte i, column j in bit 7-j): three rounds of block swaps.
+  uint64_t t;
+  t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull; x = x ^ t ^ (t << 7);
+  t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull; x = x ^ t ^ (t << 14);
+  t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull; x = x ^ t ^ (t << 28);
+  return x;
+}
+
 std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows, int nrows, int ncols) {
   const long rb = bsize(ncols), tb = bsize(nrows);
   std::vector<unsigned char> t((size_t)std::max(1, ncols) * (size_t)tb, 0);
-  for (int r = 0; r < nrows; ++r) {
-    const unsigned char *row = rows.data() + (long)r * rb;
-    for (int c = 0; c < ncols; ++c)
-      if (bget_on(row, c)) bset_on(t.data() + (long)c * tb, r);
+  const int rblocks = (nrows + 7) / 8, cblocks = (ncols + 7) / 8;
+  for (int i = 0; i < rblocks; ++i) {
+    for (int k = 0; k < cblocks; ++k) {
+      uint64_t x = 0;
+      for (int q = 0; q < 8; ++q) {
+        const int r = 8 * i + q;
+        const uint64_t byte = r < nrows ? rows[(size_t)r * rb + k] : 0;
+        x |= byte << (8 * (7 - q));
+      }
+      if (!x) continue;
+      x = transpose8(x);
+      for (int q = 0; q < 8; ++q) {
+        const int c = 8 * k + q;
+        if (c < ncols) t[(size_t)c * tb + i] = (unsigned char)(x >> (8 * (7 - q)));
+      }
+    }
   }
   return t;
 }
@@ -429,6 +491,8 @@ int load(State &S, const Input &I, std::string &err) {
       F->QR_AnZtSZnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
       F->QR_AnAtTAnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
       F->QC_AtTAnZtSZn = S.L(AT); F->QC_AtTAnAtTAn = S.L(AT);
+      S.mirror(F->lf_AnZt); S.mirror(F->lf_AnAt); S.mirror(F->lf_jnvt); S.mirror(F->lf_jnjt);
+      S.mirror(F->lf_knzt); S.mirror(F->lf_hnvt); S.mirror(F->lf_ankt); S.mirror(F->lf_knat); S.mirror(F->lf_knkt);
       S.F[nb1 + nb2 * S.nbins] = std::move(F);
     }
   }
@@ -572,7 +636,7 @@ void lf_YnWt_all(State &S) {  // bcc_lf_YnWt (bcc_lf.c:223-290)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
       if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
-        lh_transpose(S.f(nb1, nb2)->lf_AnAt, S.f(nb2, nb1)->lf_AnAt);
+        S.transpose(S.f(nb1, nb2)->lf_AnAt, S.f(nb2, nb1)->lf_AnAt);
     }
 }
 
@@ -642,7 +706,14 @@ void set_l1(L_handle *L, unsigned long long length) {
 
 unsigned popcount_masked_row(const unsigned char *row, const unsigned char *mask, long nbytes) {
   unsigned c = 0;
-  for (long i = 0; i < nbytes; ++i) c += (unsigned)__builtin_popcount((unsigned)(row[i] & mask[i]));
+  long i = 0;
+  for (; i + 8 <= nbytes; i += 8) {
+    uint64_t a, m;
+    memcpy(&a, row + i, 8);
+    memcpy(&m, mask + i, 8);
+    c += (unsigned)__builtin_popcountll(a & m);
+  }
+  for (; i < nbytes; ++i) c += (unsigned)__builtin_popcount((unsigned)(row[i] & mask[i]));
   return c;
 }
 
@@ -1259,16 +1330,14 @@ void lrup_QR(State &S) {  // bcc_lrup_QR_YnWt_stage_0/1/3 (bcc_lrup.c:659-892)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
       if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
-        lh_transpose(S.f(nb1, nb2)->lf_jnjt, S.f(nb2, nb1)->lf_jnjt);
+        S.transpose(S.f(nb1, nb2)->lf_jnjt, S.f(nb2, nb1)->lf_jnjt);
     }
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
       Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
-      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
-        for (unsigned long long i = 0; i < F->lf_AnZt->length; ++i) F->lf_AnZt->lf[i] -= F->lf_jnvt->lf[i];
-      if (S.A_cbother && E1->A_rbother && E2->A_rbother)
-        for (unsigned long long i = 0; i < F->lf_AnAt->length; ++i) F->lf_AnAt->lf[i] -= F->lf_jnjt->lf[i];
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) S.sub(F->lf_AnZt, F->lf_jnvt);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother) S.sub(F->lf_AnAt, F->lf_jnjt);
     }
 }
 
@@ -1286,6 +1355,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_vn->p(), aj, &E->lf_vn_ajdk);
     }
   }
+  g_clock.tick("lrup_QC_a0");
   // a1
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
@@ -1308,10 +1378,11 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       Double *F = S.f(nb1, nb2), *Ft = S.f(nb2, nb1);
       Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
       if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
-        lh_transpose(F->lf_knat, Ft->lf_ankt);
-        if (nb1 > nb2) lh_transpose(F->lf_knkt, Ft->lf_knkt);
+        S.transpose(F->lf_knat, Ft->lf_ankt);
+        if (nb1 > nb2) S.transpose(F->lf_knkt, Ft->lf_knkt);
       }
     }
+  g_clock.tick("lrup_QC_a1");
   // a2
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
@@ -1326,6 +1397,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
         if (nb1 <= nb2) xcalc_excerpt(S, F->M_knkt_trm, E1->M_kn, E2->M_kn, F->lf_knkt, F->M_knkt);
       }
     }
+  g_clock.tick("lrup_QC_a2");
   // a3
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
@@ -1350,6 +1422,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
         if (nb1 > nb2) lh_duplicate(F->lf_kt_r_knkt_r_kn, Ft->lf_kt_r_knkt_r_kn);
       }
     }
+  g_clock.tick("lrup_QC_a3");
   // b0
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother) {
@@ -1363,6 +1436,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_vt->p(), E->M_St->p(), nullptr, nullptr, nullptr, &E->lf_vtsn);
     }
   }
+  g_clock.tick("lrup_QC_b0");
   // b1
   for (auto &E : S.E) {
     if (E->Z_rbother && S.A_cbother)
@@ -1371,7 +1445,11 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       wrap_AtTYn_vv__run(TARGS, SP_j, SP_j, SP_j, E->M_at->p(), E->M_tt->p(), E->M_jt->p(), aj, aj, E->lf_attn, E->lf_jttn, &E->lf_attjn);
       wrap_AtTYn_vv__run(TARGS, SP_j, SP_j, SP_j, E->M_kt->p(), E->M_rt->p(), E->M_ht->p(), aj, aj, E->lf_ktrn, E->lf_htrn, &E->lf_ktrhn);
     }
+    // The SNP x SNP products are read only by the next stage's kernels: keep
+    // them on the device from their first (allocating) call on.
+    S.mirror(E->lf_ztsvn); S.mirror(E->lf_attjn); S.mirror(E->lf_ktrhn);
   }
+  g_clock.tick("lrup_QC_b1");
   // b2
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
@@ -1502,8 +1580,11 @@ unsigned long long fnv(const void *p, size_t n, unsigned long long h = 146959810
   return h;
 }
 
+thread_local const Hooks *g_trace_hooks = nullptr;
+
 void trace_L(FILE *f, const char *stage, int it, const char *name, int a, int b, const L_handle *L) {
   if (!L) return;
+  if (g_trace_hooks && g_trace_hooks->L_to_host) g_trace_hooks->L_to_host(const_cast<L_handle *>(L));
   unsigned long long n = L->row_stride * L->col_stride * (L->lyr_stride ? L->lyr_stride : 1);
   if (n > L->length) n = L->length;
   fprintf(f, "%s %d %s %d %d n=%llu h=%016llx\n", stage, it, name, a, b, n, fnv(L->lf, n * sizeof(double)));
@@ -1517,34 +1598,18 @@ void trace_M(FILE *f, const char *stage, int it, const char *name, int a, int b,
   fprintf(f, "%s %d %s %d %d rows=%d h=%016llx\n", stage, it, name, a, b, h.nrows, x);
 }
 
-// Optional wall-clock profile per stage (LAKBCC_PROFILE=1): printed to
-// stderr when the solve ends.
-struct StageClock {
-  bool on = false;
-  std::chrono::steady_clock::time_point last;
-  std::vector<std::pair<std::string, double>> acc;
-  void tick(const char *stage) {
-    if (!on) return;
-    const auto now = std::chrono::steady_clock::now();
-    const double dt = std::chrono::duration<double>(now - last).count();
-    last = now;
-    for (auto &kv : acc)
-      if (kv.first == stage) { kv.second += dt; return; }
-    acc.emplace_back(stage, dt);
-  }
-};
-StageClock g_clock;
 
 void trace_stage(State &S, const char *stage) {
   g_clock.tick(stage);
-  static FILE *f = nullptr;
-  static bool checked = false;
+  thread_local FILE *f = nullptr;
+  thread_local bool checked = false;
   if (!checked) {
     checked = true;
     const char *path = getenv("LAKBCC_TRACE");
     if (path && *path) f = fopen(path, "w");
   }
   if (!f) return;
+  g_trace_hooks = S.hooks;
   const int it = S.out ? S.out->iterations : -1;
 #define TL(name, a, b, L) trace_L(f, stage, it, name, a, b, L)
   for (auto &E : S.E) {

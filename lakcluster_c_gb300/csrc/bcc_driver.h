@@ -52,6 +52,16 @@ struct Output {
 struct Hooks {
   void (*release_L)(L_handle *L) = nullptr;
   void (*forget_host)(const void *p) = nullptr;
+  // Device mirrors for the large score matrices (AnZt, AnAt and their
+  // low-rank updates): keep L's values on the device, drop the mirror, copy
+  // the device values back into L->lf, and the two matrix operations the
+  // driver applies to them (dst -= src elementwise; L2_transpose).  All null:
+  // the matrices stay on the host.
+  void (*L_mirror)(L_handle *L) = nullptr;
+  void (*L_release_mirror)(L_handle *L) = nullptr;
+  void (*L_to_host)(L_handle *L) = nullptr;
+  void (*L_sub)(L_handle *dst, const L_handle *src) = nullptr;
+  void (*L_transpose)(L_handle *dst, const L_handle *src) = nullptr;
 };
 
 // Parse a reference .in file (updateglobals.c syntax) and load its .b16 files.

@@ -1,0 +1,232 @@
+// Many bcc solves at once on one GPU: a batch entry point and a serving loop.
+// (No counterpart in the reference, which runs one solve per process.)
+//
+// Each worker thread drives whole solves through the same driver and kernels
+// as lakgb_bcc_solve.  The library gives every host thread its own CUDA stream
+// and staging arena, so the kernels, copies and host-side stages of different
+// solves overlap: while one solve sorts its scores on the host, another's
+// Gram runs on the device.
+//
+// Serving is continuous batching rather than a queue in front of one solver:
+// a request is admitted as soon as a worker is idle and its estimated device
+// footprint fits the HBM budget beside the solves already running; requests
+// that arrive while others are on the GPU join them as slots free up, in
+// arrival order except that a request which does not fit yet does not hold
+// back smaller ones behind it.  A solve's result does not depend on what runs
+// beside it: solves share no mutable state (each owns its buffers, mirrors,
+// stream and staging arena), so every result is identical to the same solve
+// alone.
+#include <string.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/lakcluster_gb300.h"
+#include "bcc_model.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// A deep copy of a problem, so the caller's buffers may be freed after submit.
+struct OwnedProblem {
+  lakgb_bcc_problem p{};
+  std::vector<lakgb_bcc_bin> bins;
+  std::vector<std::vector<unsigned char>> store;
+
+  explicit OwnedProblem(const lakgb_bcc_problem &src) {
+    p = src;
+    const long rb = (long)src.row_bytes;
+    bins.assign(src.bins, src.bins + src.nbins);
+    auto keep = [&](const unsigned char *ptr, size_t n) -> const unsigned char * {
+      if (!ptr) return nullptr;
+      store.emplace_back(ptr, ptr + n);
+      return store.back().data();
+    };
+    store.reserve((size_t)src.nbins * 4 + 1);
+    for (auto &b : bins) {
+      b.A_rows = keep(b.A_rows, (size_t)b.A_nrows * rb);
+      b.Z_rows = keep(b.Z_rows, (size_t)b.Z_nrows * rb);
+      b.A_mr_b = keep(b.A_mr_b, (size_t)(b.A_nrows + 15) / 16 * 2);
+      b.Z_mr_b = keep(b.Z_mr_b, (size_t)(b.Z_nrows + 15) / 16 * 2);
+    }
+    p.mc_b = keep(src.mc_b, (size_t)(src.ncols + 15) / 16 * 2);
+    p.bins = bins.data();
+  }
+};
+
+// Device bytes a solve holds at its peak (an upper estimate): the packed
+// matrices and their transposes, the FP64 Gram matrices of every bin pair
+// with their low-rank updates (kept on the device for the whole solve), the
+// bit planes of the initial loop product, and the SNP x SNP low-rank blocks.
+long long footprint(const lakgb_bcc_problem &p) {
+  const long long m = lakbcc::bsize(p.ncols) * 8;  // padded columns
+  long long bytes = 0, rows_total = 0;
+  for (int i = 0; i < p.nbins; ++i) rows_total += p.bins[i].A_nrows + p.bins[i].Z_nrows;
+  bytes += 2 * rows_total * m / 8;                              // rows and transposes
+  for (int a = 0; a < p.nbins; ++a)
+    for (int b = 0; b < p.nbins; ++b) {
+      const long long na = p.bins[a].A_nrows, nz = p.bins[b].Z_nrows, nb = p.bins[b].A_nrows;
+      bytes += 8 * 2 * (na * nz + na * nb);                      // AnZt, AnAt and their updates
+      bytes += 8 * 3 * (na * nz + na * nb) / 4;                  // low-rank Gram blocks
+      bytes += (long long)(p.B_MLT + 1) * (nz + nb) * lakbcc::bsize(na);  // planes
+    }
+  const long long cdrop = p.ncols / 8 + 1;
+  bytes += 8 * 3 * (long long)p.ncols * cdrop * p.nbins;        // SNP x SNP blocks
+  return bytes + (64ll << 20);                                  // staging arena, scratch
+}
+
+struct Job {
+  long long id = 0;
+  std::unique_ptr<OwnedProblem> prob;
+  long long bytes = 0;
+  Clock::time_point t_submit, t_start, t_end;
+  int rc = 0;
+  std::string err;
+  lakgb_bcc_result res{};
+  bool done = false;
+};
+
+}  // namespace
+
+struct lakgb_server {
+  int workers = 1;
+  long long budget = 0, in_use = 0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Job *> pending;
+  std::map<long long, std::unique_ptr<Job>> jobs;
+  std::vector<std::thread> threads;
+  long long next_id = 1;
+  int running = 0, peak_running = 0;
+  bool stop = false;
+
+  // Next admissible job: the oldest that fits the budget (continuous
+  // batching with first-fit admission).
+  Job *admit_locked() {
+    for (auto it = pending.begin(); it != pending.end(); ++it) {
+      Job *j = *it;
+      if (running == 0 || in_use + j->bytes <= budget) {
+        pending.erase(it);
+        in_use += j->bytes;
+        ++running;
+        if (running > peak_running) peak_running = running;
+        return j;
+      }
+    }
+    return nullptr;
+  }
+
+  void worker() {
+    for (;;) {
+      Job *j = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_work.wait(lk, [&] { return stop || (j = admit_locked()) != nullptr; });
+        if (!j) return;
+      }
+      j->t_start = Clock::now();
+      j->rc = lakgb_bcc_solve(&j->prob->p, &j->res);
+      if (j->rc) {
+        char msg[512];
+        lakgb_bcc_last_error(msg, sizeof msg);
+        j->err = msg;
+      }
+      j->t_end = Clock::now();
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        j->done = true;
+        in_use -= j->bytes;
+        --running;
+        j->prob.reset();
+      }
+      cv_done.notify_all();
+      cv_work.notify_all();
+    }
+  }
+};
+
+extern "C" lakgb_server *lakgb_server_create(int workers, long long hbm_budget_bytes) {
+  auto *s = new lakgb_server();
+  s->workers = workers > 0 ? workers : 1;
+  s->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : (1ll << 62);
+  for (int i = 0; i < s->workers; ++i) s->threads.emplace_back([s] { s->worker(); });
+  return s;
+}
+
+extern "C" long long lakgb_server_submit(lakgb_server *s, const struct lakgb_bcc_problem *p) {
+  auto j = std::make_unique<Job>();
+  j->prob = std::make_unique<OwnedProblem>(*p);
+  j->bytes = footprint(*p);
+  j->t_submit = Clock::now();
+  long long id;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    id = j->id = s->next_id++;
+    s->pending.push_back(j.get());
+    s->jobs[id] = std::move(j);
+  }
+  s->cv_work.notify_all();
+  return id;
+}
+
+extern "C" int lakgb_server_wait(lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times) {
+  std::unique_ptr<Job> j;
+  {
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) return -1;
+    Job *raw = it->second.get();
+    s->cv_done.wait(lk, [&] { return raw->done; });
+    j = std::move(it->second);
+    s->jobs.erase(it);
+  }
+  if (r) *r = j->res;
+  else lakgb_bcc_result_free(&j->res);
+  if (times) {
+    times[0] = std::chrono::duration<double>(j->t_start - j->t_submit).count();  // queueing
+    times[1] = std::chrono::duration<double>(j->t_end - j->t_start).count();     // solving
+    times[2] = std::chrono::duration<double>(j->t_end - j->t_submit).count();    // latency
+  }
+  return j->rc;
+}
+
+extern "C" int lakgb_server_peak_concurrency(lakgb_server *s) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  return s->peak_running;
+}
+
+extern "C" long long lakgb_bcc_footprint(const struct lakgb_bcc_problem *p) { return footprint(*p); }
+
+extern "C" void lakgb_server_destroy(lakgb_server *s) {
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (auto &t : s->threads) t.join();
+  for (auto &kv : s->jobs) lakgb_bcc_result_free(&kv.second->res);
+  delete s;
+}
+
+extern "C" int lakgb_bcc_solve_many(const struct lakgb_bcc_problem *ps, int n, struct lakgb_bcc_result *rs,
+                                    int *rcs, int workers, long long hbm_budget_bytes) {
+  lakgb_server *s = lakgb_server_create(workers, hbm_budget_bytes);
+  std::vector<long long> ids(n);
+  for (int i = 0; i < n; ++i) ids[i] = lakgb_server_submit(s, &ps[i]);
+  int bad = 0;
+  for (int i = 0; i < n; ++i) {
+    const int rc = lakgb_server_wait(s, ids[i], &rs[i], nullptr);
+    if (rcs) rcs[i] = rc;
+    bad += rc != 0;
+  }
+  lakgb_server_destroy(s);
+  return bad;
+}

@@ -28,6 +28,8 @@
 // popcount(a' & plane).  With pmpm0 = 2*popcount(a' & y) - popcount(y & mask),
 // the chunk's counts fold into exact At_tmp values, and 32 threads (one per
 // SNP) then run the FP64 recurrence over the chunk's Wn rows in order.
+#include <mutex>
+
 #include "abi_common.cuh"
 #include "bcc_model.h"
 
@@ -378,6 +380,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   for (int mw = 0; mw < nW; ++mw) mw_a[mw] = M_Wn->m_a_[mw];
 
   BitplaneParams p{};
+  Stager st;
   p.At = (const uint8_t *)resident(M_At->wX, (size_t)M_At->rpop_b * M_At->mc_length);
   p.at_row_bytes = (long long)M_At->mc_length;
   p.Tt = (const uint8_t *)resident(M_Tt->wX, (size_t)M_Tt->rpop_b * M_Tt->mc_length);
@@ -386,8 +389,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   p.plane_bytes = (long long)M_YnWt->mc_length;
   p.Zt = (const uint8_t *)resident(M_Zt->wX, (size_t)M_Zt->rpop_b * M_Zt->mc_length);
   p.zt_row_bytes = (long long)M_Zt->mc_length;
-  DBuf mask(M_At->mc_length);
-  mask.upload(M_At->mc_j, M_At->mc_length);
+  DBuf mask = upload_bytes(M_At->mc_j, M_At->mc_length);
   p.mask = mask.as<uint8_t>(); p.P = P; p.npairs = npairs;
   DBuf d_at = upload_vec(at_rowb), d_zt = upload_vec(zt_rowb), d_tt = upload_vec(tt_rowb), d_mw = upload_vec(mw_a);
   DBuf d_vS = upload_vec(vS), d_aA = upload_vec(aA), d_aZ = upload_vec(aZ);
@@ -403,6 +405,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   DBuf d_Tb((size_t)nT * sizeof(double)), d_Tt((size_t)nT * nW * sizeof(double));
   {
     const long long warps = (long long)nq * nT;
+    st.flush();
     bitplane_prep_kernel<<<(int)((warps * 32 + 255) / 256), 256, 0, stream()>>>(p, nT, d_pm.as<int>(), d_ycnt.as<int>());
     LAKGB_CUDA(cudaGetLastError());
     const int n = nT * (nW + 1);
@@ -416,11 +419,10 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   p.out = d_out.as<double>();
   const size_t smem = std::max((size_t)(kBP_M + kBP_N) * kLd * sizeof(uint32_t),
                                (size_t)kBP_M * (kBP_N + 1) * sizeof(int) + (size_t)kBP_M * kBP_N * sizeof(double));
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag attr;
+  std::call_once(attr, [&] {
     LAKGB_CUDA(cudaFuncSetAttribute(bitplane_main_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  });
   dim3 grid((npairs + kBP_M - 1) / kBP_M, nT);
   bitplane_main_kernel<<<grid, kBP_T, smem, stream()>>>(p);
   LAKGB_CUDA(cudaGetLastError());
@@ -451,12 +453,12 @@ extern "C" int wrap_An_ZtSn_ww__run(int *tidx, void **vpra, pthread_t *thread_in
   for (int i = 0; i < n; ++i) out_r[i] = pick_u(spacing_a, i, M_An->m_b_[i], M_An->m_a_[i]);
   for (int s = 0; s < nS; ++s) s_off[s] = pick_u(spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * length_a;
   AnZtSnParams p{};
+  Stager st;
   p.An = (const uint8_t *)resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   p.row_bytes = (long long)M_An->mc_length;
   DBuf d_rowb = upload_vec(rowb), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
   p.rowb = d_rowb.as<uint32_t>(); p.n = n;
-  DBuf mask(M_An->mc_length);
-  mask.upload(M_An->mc_j, M_An->mc_length);
+  DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   p.mask = mask.as<uint8_t>(); p.nwords = (int)(M_An->mc_length / 4);
   p.planes = (const uint8_t *)resident(M_ZtSn->wX, (size_t)M_ZtSn->nrows * M_ZtSn->mc_length);
   p.plane_bytes = (long long)M_ZtSn->mc_length;
@@ -466,6 +468,7 @@ extern "C" int wrap_An_ZtSn_ww__run(int *tidx, void **vpra, pthread_t *thread_in
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   p.out = d_out.as<double>();
+  st.flush();
   an_ztsn_kernel<<<(n * 32 + 255) / 256, 256, 0, stream()>>>(p);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();

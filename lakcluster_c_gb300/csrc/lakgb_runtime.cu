@@ -17,7 +17,6 @@ std::mutex g_mu;
 int g_err = 0;
 char g_msg[512] = {0};
 std::atomic<unsigned long long> g_launches{0};
-cudaStream_t g_stream = nullptr;
 bool g_residency = true;
 struct ResEntry { void *d; size_t n; };
 std::map<std::pair<const void *, size_t>, ResEntry> g_res;
@@ -42,16 +41,91 @@ void check_cuda(cudaError_t e, const char *what, const char *file, int line) {
   exit(1);  // RET_NOMEM-style hard stop, as the reference does on fatal errors
 }
 
+// One non-blocking stream per host thread: solves run from different
+// threads overlap on the device, while the calls of one solve stay ordered.
 cudaStream_t stream() {
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_stream) {
-    cudaError_t e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+  thread_local cudaStream_t s = nullptr;
+  if (!s) {
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
       fprintf(stderr, " %% Error! no CUDA device usable by liblakgb300: %s\n", cudaGetErrorString(e));
       exit(1);
     }
   }
-  return g_stream;
+  return s;
+}
+
+// --- per-thread staging arena -----------------------------------------------
+
+namespace {
+struct Arena {
+  unsigned char *host = nullptr;   // pinned
+  unsigned char *dev = nullptr;
+  size_t cap = 0, used = 0;
+  cudaEvent_t done = nullptr;      // the last flush's copy has completed
+  bool pending = false;
+};
+Arena &arena() {
+  thread_local Arena a;
+  return a;
+}
+}  // namespace
+
+namespace {
+thread_local Stager *t_active = nullptr;
+}
+
+Stager *active_stager() { return t_active; }
+
+DBuf upload_bytes(const void *h, size_t n) {
+  if (Stager *s = t_active) {
+    const void *d = s->put_bytes(h, n);
+    return DBuf::view(d, n);
+  }
+  DBuf d(n ? n : 1);
+  d.upload(h, n);
+  return d;
+}
+
+void Stager::begin() {
+  t_active = this;
+  Arena &a = arena();
+  if (!a.host) {
+    a.cap = kStageBytes;
+    LAKGB_CUDA(cudaMallocHost((void **)&a.host, a.cap));
+    LAKGB_CUDA(cudaMalloc((void **)&a.dev, a.cap));
+    LAKGB_CUDA(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+  }
+  if (a.pending) LAKGB_CUDA(cudaEventSynchronize(a.done));  // the host bytes are free again
+  a.pending = false;
+  a.used = 0;
+  active_ = true;
+}
+
+const void *Stager::put_bytes(const void *h, size_t n) {
+  Arena &a = arena();
+  const size_t off = (a.used + 255) & ~(size_t)255;
+  if (!active_ || off + n > a.cap) {
+    // Too large for the arena: a dedicated buffer, uploaded in order.
+    spill_.emplace_back(n ? n : 1);
+    spill_.back().upload(h, n);
+    return spill_.back().p;
+  }
+  if (n) memcpy(a.host + off, h, n);
+  a.used = off + n;
+  return a.dev + off;
+}
+
+void Stager::flush() {
+  Arena &a = arena();
+  if (t_active == this) t_active = nullptr;
+  if (!active_) return;
+  if (a.used) {
+    LAKGB_CUDA(cudaMemcpyAsync(a.dev, a.host, a.used, cudaMemcpyHostToDevice, stream()));
+    LAKGB_CUDA(cudaEventRecord(a.done, stream()));
+    a.pending = true;
+  }
+  active_ = false;
 }
 
 void count_launch(unsigned long long n) { g_launches += n; }
@@ -82,12 +156,14 @@ const void *resident(const void *host, size_t bytes) {
   auto it = g_res.find(key);
   if (g_residency && it != g_res.end()) return it->second.d;
   if (it != g_res.end()) {
-    cudaFreeAsync(it->second.d, g_stream);
+    cudaFreeAsync(it->second.d, stream());
     g_res.erase(it);
   }
   void *d = nullptr;
-  LAKGB_CUDA(cudaMallocAsync(&d, bytes, g_stream));
-  LAKGB_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, g_stream));
+  LAKGB_CUDA(cudaMallocAsync(&d, bytes, stream()));
+  LAKGB_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, stream()));
+  // Complete before other threads' streams may read it.
+  LAKGB_CUDA(cudaStreamSynchronize(stream()));
   g_res[key] = ResEntry{d, bytes};
   return d;
 }
@@ -97,7 +173,7 @@ void resident_put(const void *host, size_t bytes, DBuf &&d) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto it = g_res.begin(); it != g_res.end();) {
     if (it->first.first == host) {
-      cudaFreeAsync(it->second.d, g_stream);
+      cudaFreeAsync(it->second.d, stream());
       it = g_res.erase(it);
     } else {
       ++it;
@@ -143,7 +219,7 @@ extern "C" void lakgb_set_residency(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_residency = (on != 0);
   if (!g_residency) {
-    for (auto &kv : g_res) cudaFreeAsync(kv.second.d, g_stream);
+    for (auto &kv : g_res) cudaFreeAsync(kv.second.d, stream());
     g_res.clear();
   }
 }
@@ -153,7 +229,7 @@ extern "C" void lakgb_forget_host_buffer(const void *host_ptr) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto it = g_res.begin(); it != g_res.end();) {
     if (it->first.first == host_ptr) {
-      cudaFreeAsync(it->second.d, g_stream);
+      cudaFreeAsync(it->second.d, stream());
       it = g_res.erase(it);
     } else {
       ++it;

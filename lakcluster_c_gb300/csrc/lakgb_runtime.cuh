@@ -6,6 +6,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <string>
+#include <vector>
 
 #include "../../include/lakcluster_gb300.h"
 
@@ -39,24 +40,65 @@ const void *resident(const void *host, size_t bytes);
 struct DBuf {
   void *p = nullptr;
   size_t n = 0;
+  bool owned = true;   // false: a view into the staging arena
   DBuf() = default;
   explicit DBuf(size_t bytes) : p(bytes ? dalloc(bytes) : nullptr), n(bytes) {}
+  static DBuf view(const void *p, size_t n) {
+    DBuf d;
+    d.p = const_cast<void *>(p);
+    d.n = n;
+    d.owned = false;
+    return d;
+  }
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
-  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n), owned(o.owned) { o.p = nullptr; o.n = 0; }
   DBuf &operator=(DBuf &&o) noexcept {
     if (this != &o) {
-      if (p) dfree(p);
-      p = o.p; n = o.n;
+      if (p && owned) dfree(p);
+      p = o.p; n = o.n; owned = o.owned;
       o.p = nullptr; o.n = 0;
     }
     return *this;
   }
-  ~DBuf() { if (p) dfree(p); }
+  ~DBuf() { if (p && owned) dfree(p); }
   template <class T> T *as() const { return static_cast<T *>(p); }
   void upload(const void *h, size_t bytes);
   void zero();
 };
+
+// Per-thread staging of a call's small host-to-device inputs: begin(), put()
+// each array (host bytes are copied into a pinned arena, the returned device
+// pointer is valid for kernels enqueued after flush()), flush() issues one
+// copy for all of them.  Arrays that do not fit the arena are uploaded on
+// their own.  One Stager per call; the arena is reused by the next call once
+// its copy has completed.
+constexpr size_t kStageBytes = 32u << 20;
+class Stager {
+ public:
+  Stager() { begin(); }
+  ~Stager() { flush(); }
+  Stager(const Stager &) = delete;
+  Stager &operator=(const Stager &) = delete;
+  void begin();
+  template <class T> const T *put(const T *h, size_t n) {
+    return static_cast<const T *>(put_bytes(h, n * sizeof(T)));
+  }
+  template <class V> const typename V::value_type *put(const V &v) { return put(v.data(), v.size()); }
+  void flush();
+ private:
+  const void *put_bytes(const void *h, size_t n);
+  bool active_ = false;
+  std::vector<DBuf> spill_;
+  friend DBuf upload_bytes(const void *h, size_t n);
+};
+
+// The Stager of the current call on this thread (null outside one).
+Stager *active_stager();
+
+// Upload n host bytes: into the active Stager when there is one (a view into
+// its arena, valid after its flush), else into a new device buffer.
+DBuf upload_bytes(const void *h, size_t n);
 
 // Make the device buffer `d`, which holds the current contents of the host
 // buffer `host` (`bytes` bytes), its resident copy, replacing any earlier copy

@@ -20,6 +20,7 @@
 // (At ^ Tt) & mask for 64 At rows and Yt & mask for 64 Yt rows, and each
 // thread accumulates a 4 x 4 tile of integer counts over all blocks.
 #include "abi_common.cuh"
+#include "lmirror.cuh"
 #include "bcc_model.h"
 
 namespace lakgb {
@@ -50,21 +51,40 @@ DBuf upload_L(const L_handle *L, bool three_d) {
   return d;
 }
 
-__global__ void anzt_s_wnyt_kernel(const double *A, const unsigned long long *a_r, const unsigned long long *a_c,
-                                   const double *Y, const unsigned long long *y_r, const unsigned long long *y_c,
-                                   const int8_t *vS, int nA, int nZ, int nS, const unsigned long long *out_r,
-                                   const unsigned long long *s_off, double *out) {
-  const int ma = blockIdx.x * blockDim.x + threadIdx.x;
+// One CTA per 16 rows: all 256 threads compute the products of a 16 x 128
+// (row, mz) tile into shared memory -- reads of consecutive rows for one mz are
+// contiguous in the column-major matrix -- then 16 threads add their row's
+// products in mz order.  The additions stay sequential per row; the loads
+// and multiplies run 256 wide.
+constexpr int kSW_R = 16, kSW_Z = 128, kSW_T = 256;
+__global__ void __launch_bounds__(kSW_T) anzt_s_wnyt_kernel(
+    const double *A, const unsigned long long *a_r, const unsigned long long *a_c, const double *Y,
+    const unsigned long long *y_r, const unsigned long long *y_c, const int8_t *vS, int nA, int nZ, int nS,
+    const unsigned long long *out_r, const unsigned long long *s_off, double *out) {
+  __shared__ double prod[kSW_Z][kSW_R + 1];
+  const int r0 = blockIdx.x * kSW_R;
   const int s = blockIdx.y;
-  if (ma >= nA || s >= nS) return;
-  const unsigned long long ar = a_r[ma], yr = y_r[ma];
   const int8_t *vs = vS + (long long)s * nZ;
+  const int lr = threadIdx.x % kSW_R, lz = threadIdx.x / kSW_R;   // 16 rows x 16 columns per pass
+  const int ma = r0 + lr;
+  const unsigned long long ar = ma < nA ? a_r[ma] : 0, yr = ma < nA ? y_r[ma] : 0;
   double acc = 0.0;
-  for (int mz = 0; mz < nZ; ++mz) {
-    const double a = A[ar + a_c[mz]], y = Y[yr + y_c[mz]];
-    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(a, (double)vs[mz]), y));
+  for (int z0 = 0; z0 < nZ; z0 += kSW_Z) {
+    const int zn = min(kSW_Z, nZ - z0);
+    __syncthreads();
+    for (int z = lz; z < zn; z += kSW_T / kSW_R) {
+      double v = 0.0;
+      if (ma < nA) {
+        const int mz = z0 + z;
+        v = __dmul_rn(__dmul_rn(A[ar + a_c[mz]], (double)vs[mz]), Y[yr + y_c[mz]]);
+      }
+      prod[z][lr] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kSW_R)
+      for (int z = 0; z < zn; ++z) acc = __dadd_rn(acc, prod[z][threadIdx.x]);
   }
-  out[out_r[ma] + s_off[s]] = acc;
+  if (threadIdx.x < kSW_R && r0 + threadIdx.x < nA) out[out_r[r0 + threadIdx.x] + s_off[s]] = acc;
 }
 
 __global__ void attyn_wtszn_kernel(const double *AY, const unsigned long long *ay_a, const unsigned long long *ay_y,
@@ -217,15 +237,20 @@ extern "C" int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *threa
     set_error(4, "wrap_AnZt_S_WnYt_vv__run: L_handle smaller than the rows and columns it is indexed by");
     return (int)length;
   }
-  DBuf dA = upload_L(lf_AnZt, false);
-  DBuf dY = (lf_YnWt == lf_AnZt) ? DBuf() : upload_L(lf_YnWt, false);
-  const double *pY = (lf_YnWt == lf_AnZt) ? dA.as<double>() : dY.as<double>();
+  // Mirrored matrices (lmirror.cu) are read in place.
+  Mirror *mA = find_mirror(lf_AnZt), *mY = find_mirror(lf_YnWt);
+  Stager st;
+  DBuf dA = mA ? DBuf() : upload_L(lf_AnZt, false);
+  DBuf dY = (mY || lf_YnWt == lf_AnZt) ? DBuf() : upload_L(lf_YnWt, false);
+  const double *pA = mA ? mA->d : dA.as<double>();
+  const double *pY = mY ? mY->d : ((lf_YnWt == lf_AnZt) ? pA : dY.as<double>());
   DBuf d_ar = upload_vec(a_r), d_yr = upload_vec(y_r), d_ac = upload_vec(a_c), d_yc = upload_vec(y_c);
   DBuf d_vS = upload_vec(vS), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
   DBuf d_out(length * sizeof(double));
   d_out.zero();
-  dim3 grid((nA + 127) / 128, nS);
-  anzt_s_wnyt_kernel<<<grid, 128, 0, stream()>>>(dA.as<double>(), d_ar.as<unsigned long long>(), d_ac.as<unsigned long long>(),
+  dim3 grid((nA + kSW_R - 1) / kSW_R, nS);
+  st.flush();
+  anzt_s_wnyt_kernel<<<grid, kSW_T, 0, stream()>>>(pA, d_ar.as<unsigned long long>(), d_ac.as<unsigned long long>(),
                                                  pY, d_yr.as<unsigned long long>(), d_yc.as<unsigned long long>(),
                                                  d_vS.as<int8_t>(), nA, nZ, nS, d_or.as<unsigned long long>(),
                                                  d_so.as<unsigned long long>(), d_out.as<double>());
@@ -277,16 +302,21 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
     set_error(4, "wrap_AtTYn____WtSZn_vv__run: L_handle smaller than the rows and columns it is indexed by");
     return (int)length;
   }
-  DBuf dA = upload_L(LA, true);
-  DBuf dZ = (LZ == LA) ? DBuf() : upload_L(LZ, true);
-  const double *pZ = (LZ == LA) ? dA.as<double>() : dZ.as<double>();
+  // Mirrored inputs (lmirror.cu) are read in place.
+  Mirror *mLA = find_mirror(LA), *mLZ = find_mirror(LZ);
+  Stager st;
+  DBuf dA = mLA ? DBuf() : upload_L(LA, true);
+  DBuf dZ = (mLZ || LZ == LA) ? DBuf() : upload_L(LZ, true);
+  const double *pA = mLA ? mLA->d : dA.as<double>();
+  const double *pZ = mLZ ? mLZ->d : ((LZ == LA) ? pA : dZ.as<double>());
   DBuf d_aa = upload_vec(ay_a), d_ay = upload_vec(ay_y), d_as = upload_vec(ay_s);
   DBuf d_zz = upload_vec(zw_z), d_zw = upload_vec(zw_w), d_zs = upload_vec(zw_s);
   DBuf d_D = upload_vec(Dy), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   dim3 grid((npairs + 127) / 128, nS);
-  attyn_wtszn_kernel<<<grid, 128, 0, stream()>>>(dA.as<double>(), d_aa.as<unsigned long long>(), d_ay.as<unsigned long long>(),
+  st.flush();
+  attyn_wtszn_kernel<<<grid, 128, 0, stream()>>>(pA, d_aa.as<unsigned long long>(), d_ay.as<unsigned long long>(),
                                                  d_as.as<unsigned long long>(), pZ, d_zz.as<unsigned long long>(),
                                                  d_zw.as<unsigned long long>(), d_zs.as<unsigned long long>(),
                                                  d_D.as<double>(), npairs, ninner, nS, d_or.as<unsigned long long>(),
@@ -306,7 +336,20 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   const unsigned long long ly = spacing_length(output_spacing_y, M_Yt);
   const unsigned long long lt = spacing_length(output_spacing_t, M_Tt);
   const unsigned long long length = la * ly * lt;
-  L_handle *out = ensure_output(output_p, length, "wrap_AtTYn_vv__run");
+  // A mirrored output (lmirror.cu) is produced on the device only.
+  Mirror *mo = *output_p ? find_mirror(*output_p) : nullptr;
+  L_handle *out = nullptr;
+  if (mo) {
+    out = *output_p;
+    if (out->length < length || mo->n < length) {
+      set_error(2, "output length %llu < %llu in wrap_AtTYn_vv__run", out->length, length);
+      return (int)length;
+    }
+    if (length) LAKGB_CUDA(cudaMemsetAsync(mo->d, 0, length * sizeof(double), stream()));
+    mo->host_stale = true;
+  } else {
+    out = ensure_output(output_p, length, "wrap_AtTYn_vv__run");
+  }
   if (!out) return (int)length;
   out->spacing_row = output_spacing_a; out->row_stride = la;
   out->spacing_col = output_spacing_y; out->col_stride = ly;
@@ -342,6 +385,7 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
       hhaY[(size_t)t * nY + k] = (double)(long long)(*lakbcc::L2_get(lf_YtTn, k, M_Yt->m_b_[k], M_Yt->m_a_[k], t, tb, ta));
   }
   AtTYnParams p{};
+  Stager st;
   p.At = (const uint8_t *)resident(M_At->wX, (size_t)M_At->rpop_b * M_At->mc_length);
   p.Yt = (const uint8_t *)resident(M_Yt->wX, (size_t)M_Yt->rpop_b * M_Yt->mc_length);
   p.Tt = (const uint8_t *)resident(M_Tt->wX, (size_t)M_Tt->rpop_b * M_Tt->mc_length);
@@ -349,22 +393,28 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   DBuf d_ar = upload_vec(a_rowb), d_yr = upload_vec(y_rowb), d_tr = upload_vec(t_rowb);
   p.a_rowb = d_ar.as<uint32_t>(); p.y_rowb = d_yr.as<uint32_t>(); p.t_rowb = d_tr.as<uint32_t>();
   p.nA = nA; p.nY = nY;
-  DBuf mask(M_At->mc_length);
-  mask.upload(M_At->mc_j, M_At->mc_length);
+  DBuf mask = upload_bytes(M_At->mc_j, M_At->mc_length);
   p.mask = mask.as<uint8_t>(); p.P = (int)(M_At->mc_length / kBlockBytes); p.cpop = M_At->cpop_j;
   DBuf d_hAy = upload_vec(hhAy), d_haY = upload_vec(hhaY), d_hay = upload_vec(hhay), d_aA = upload_vec(aA), d_aY = upload_vec(aY);
   DBuf d_oa = upload_vec(out_a), d_oy = upload_vec(out_y), d_ot = upload_vec(out_t);
   p.hhAy = d_hAy.as<double>(); p.hhaY = d_haY.as<double>(); p.hhay = d_hay.as<double>();
   p.aA = d_aA.as<double>(); p.aY = d_aY.as<double>();
   p.out_a = d_oa.as<unsigned long long>(); p.out_y = d_oy.as<unsigned long long>(); p.out_t = d_ot.as<unsigned long long>();
-  DBuf d_out(length * sizeof(double));
-  d_out.zero();
-  p.out = d_out.as<double>();
+  DBuf d_out;
+  if (mo) {
+    p.out = mo->d;
+  } else {
+    d_out = DBuf(length * sizeof(double));
+    d_out.zero();
+    p.out = d_out.as<double>();
+  }
   const size_t smem = (size_t)(kTY_M + kTY_N) * kLd * sizeof(uint32_t);
   dim3 grid((nY + kTY_N - 1) / kTY_N, (nA + kTY_M - 1) / kTY_M, nT);
+  st.flush();
   attyn_kernel<<<grid, kTY_T, smem, stream()>>>(p);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
+  if (mo) return (int)length;
   copy_back(out->lf, d_out, length);
   return (int)length;
 }

@@ -27,12 +27,15 @@
 
 #include "abi_common.cuh"
 #include "bcc_model.h"
+#include "lmirror.cuh"
 
 namespace lakgb {
 
 namespace {
 
-long long g_d_mlt = 4294967296LL;  // GLOBAL_D_MLT default (lakcluster_ver18.c:83)
+// GLOBAL_D_MLT (default lakcluster_ver18.c:83), per host thread: concurrent
+// solves may use different B_MLT.
+thread_local long long g_d_mlt = 4294967296LL;
 
 struct XcalcParams {
   const double *lf;
@@ -309,19 +312,32 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
   for (long long o : cols_j) max_coff = o > max_coff ? o : max_coff;
   const size_t lf_elems = (size_t)(max_off + max_coff + 1);
 
-  DBuf d_lf, d_rows, d_cols;
+  DBuf d_lf, d_rows, d_cols, d_roff_all;
   double min_data = 0.0, max_data = 0.0;
   const int nr = (int)rows_j.size(), nc = (int)cols_j.size();
+  // A mirrored matrix (lmirror.cu) is read in place.
+  Mirror *mlf = (lf_YnWt && YnWt == lf_YnWt->lf) ? find_mirror(lf_YnWt) : nullptr;
+  const double *plf = nullptr;
   if (nr > 0 && nc > 0 && YnWt) {
-    d_lf = DBuf(lf_elems * sizeof(double));
-    d_lf.upload(YnWt, lf_elems * sizeof(double));
-    d_rows = upload_vec(rows_j);
-    d_cols = upload_vec(cols_j);
+    if (mlf && lf_elems <= mlf->n) {
+      plf = mlf->d;
+    } else {
+      d_lf = DBuf(lf_elems * sizeof(double));
+      d_lf.upload(YnWt, lf_elems * sizeof(double));
+      plf = d_lf.as<double>();
+    }
+    {
+      Stager st;
+      d_rows = upload_vec(rows_j);
+      d_cols = upload_vec(cols_j);
+      d_roff_all = upload_vec(row_off_a);
+      st.flush();
+    }
     const long long total = (long long)nr * nc;
     int blocks = (int)((total + 255) / 256);
     if (blocks > 1024) blocks = 1024;
     DBuf d_min(blocks * sizeof(double)), d_max(blocks * sizeof(double)), d_any(blocks * sizeof(int));
-    xcalc_minmax_kernel<<<blocks, 256, 0, stream()>>>(d_lf.as<double>(), d_rows.as<long long>(), nr,
+    xcalc_minmax_kernel<<<blocks, 256, 0, stream()>>>(plf, d_rows.as<long long>(), nr,
                                                        d_cols.as<long long>(), nc, d_min.as<double>(),
                                                        d_max.as<double>(), d_any.as<int>());
     LAKGB_CUDA(cudaGetLastError());
@@ -364,9 +380,8 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
     if (nbytes) planes.upload(row0.data(), (size_t)brows);
     if (nr > 0 && nc > 0 && YnWt) {
       XcalcParams p{};
-      p.lf = d_lf.as<double>();
-      DBuf d_roff = upload_vec(row_off_a);
-      p.row_off = d_roff.as<long long>(); p.nrows_a = Yn_nrows;
+      p.lf = plf;
+      p.row_off = d_roff_all.as<long long>(); p.nrows_a = Yn_nrows;
       p.col_off = d_cols.as<long long>(); p.ncols_j = nc;
       p.min = min; p.mlt = mlt; p.dmax = (unsigned long long)(g_d_mlt - 1);
       p.ncols_per = ncols_per; p.brows = brows; p.planes = planes.as<uint8_t>();

@@ -15,6 +15,7 @@ Configurations (rows x SNP columns):
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -65,4 +66,68 @@ def case_control(n_case=4096, n_ctrl=4096, n_cols=16384, k_rows=256, k_cols=512,
     for b in range(nbins):
         inst.A_bins.append(np.ascontiguousarray(A[bA == b]))
         inst.Z_bins.append(np.ascontiguousarray(Z[bZ == b]))
+    return inst
+
+
+def log_uniform_int(rng, lo, hi):
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def null_instance(seed, rows=(1024, 8192), cols=(4096, 32768), maf=(0.05, 0.5), k_rows=None, k_cols=None,
+                  flip=0.05):
+    """One label-shuffled null instance of the case/control setup: a pooled
+    sample of r rows x c SNPs (MAF U[maf]), with a planted bicluster in the
+    first half, then case/control labels assigned by a random permutation of
+    the pooled rows (so the planted rows are spread over both groups).
+    r ~ logU[rows], c ~ logU[cols]; one covariate bin."""
+    rng = np.random.default_rng(seed)
+    r = log_uniform_int(rng, *rows)
+    c = log_uniform_int(rng, *cols)
+    f = maf[0] + (maf[1] - maf[0]) * rng.random(c)
+    X = _bernoulli_cols(rng, r, f)
+    kr = k_rows or max(2, r // 16)
+    kc = k_cols or max(2, c // 32)
+    rr = rng.permutation(r // 2)[:kr]
+    cc = rng.permutation(c)[:kc]
+    pat = (rng.random(kc) < 0.5).astype(np.uint8)
+    X[np.ix_(rr, cc)] = np.tile(pat, (kr, 1)) ^ (rng.random((kr, kc)) < flip).astype(np.uint8)
+    perm = rng.permutation(r)
+    A = np.ascontiguousarray(X[perm[: r // 2]])
+    Z = np.ascontiguousarray(X[perm[r // 2:]])
+    inst = BccInstance("null_%d" % seed, c)
+    inst.A_bins.append(A)
+    inst.Z_bins.append(Z)
+    return inst
+
+
+def served_request(seed, rows=(512, 16384), cols=(2048, 65536), maf=(0.05, 0.5), case_fraction=0.5,
+                   max_categories=3, flip=0.05):
+    """One request of the served stream: r ~ logU[rows] rows (case fraction
+    0.5), c ~ logU[cols] SNPs, MAF U[maf], k ~ U{0..3} covariate categories
+    (NBINS = max(1, k), rows assigned uniformly), a planted bicluster in the
+    cases."""
+    rng = np.random.default_rng(seed)
+    r = log_uniform_int(rng, *rows)
+    c = log_uniform_int(rng, *cols)
+    k = int(rng.integers(0, max_categories + 1))
+    nb = max(1, k)
+    n_case = max(2, int(round(r * case_fraction)))
+    n_ctrl = max(2, r - n_case)
+    f = maf[0] + (maf[1] - maf[0]) * rng.random(c)
+    A = _bernoulli_cols(rng, n_case, f)
+    Z = _bernoulli_cols(rng, n_ctrl, f)
+    kr, kc = max(2, n_case // 16), max(2, c // 32)
+    rr = rng.permutation(n_case)[:kr]
+    cc = rng.permutation(c)[:kc]
+    pat = (rng.random(kc) < 0.5).astype(np.uint8)
+    A[np.ix_(rr, cc)] = np.tile(pat, (kr, 1)) ^ (rng.random((kr, kc)) < flip).astype(np.uint8)
+    bA = (rng.random(n_case) * nb).astype(np.int64)
+    bZ = (rng.random(n_ctrl) * nb).astype(np.int64)
+    inst = BccInstance("req_%d" % seed, c)
+    for b in range(nb):
+        a, z = A[bA == b], Z[bZ == b]
+        if a.shape[0] == 0 or z.shape[0] == 0:   # keep every bin populated
+            a, z = A[:2], Z[:2]
+        inst.A_bins.append(np.ascontiguousarray(a))
+        inst.Z_bins.append(np.ascontiguousarray(z))
     return inst

@@ -133,3 +133,46 @@ def run_in_file(path: str) -> None:
         buf = C.create_string_buffer(512)
         lib.lakgb_bcc_last_error(buf, 512)
         raise RuntimeError("lakgb_bcc_run_in_file failed (%d): %s" % (rc, buf.value.decode()))
+
+
+WORKLOADS = {
+    # name: description (see workload())
+    "case_only_1024x1024": "cases 1024 x 1024 SNPs, 45 x 45 planted, gamma 0.05 (config 1)",
+    "case_control_4096x4096x16384": "cases 4096 + controls 4096 x 16384 SNPs, 2 bins, gamma 0.05 (config 2)",
+    "case_control_1024x1024x4096": "cases 1024 + controls 1024 x 4096 SNPs, 2 bins, gamma 0.05 (small config 2)",
+}
+
+
+def workload(name):
+    """Synthetic problems of the benchmark configurations, as solve arguments."""
+    from . import synth
+    if name == "case_only_1024x1024":
+        inst = synth.case_only(1024, 1024, k=45, flip=0.1, seed=1)
+        return inst.A_bins, None, 0.05
+    if name == "case_control_4096x4096x16384":
+        inst = synth.case_control(4096, 4096, 16384, 256, 512, 0.05, nbins=2, seed=2)
+        return inst.A_bins, inst.Z_bins, 0.05
+    if name == "case_control_1024x1024x4096":
+        inst = synth.case_control(1024, 1024, 4096, 64, 128, 0.05, nbins=2, seed=2)
+        return inst.A_bins, inst.Z_bins, 0.05
+    raise KeyError(name)
+
+
+def main(argv=None):
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description="Solve a synthetic bcc workload on the GPU and print its timing.")
+    ap.add_argument("--workload", default="case_control_1024x1024x4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--reps", type=int, default=1)
+    args = ap.parse_args(argv)
+    A, Z, gamma = workload(args.workload)
+    p = Problem(A, Z, gamma=gamma)
+    for r in range(args.reps):
+        t0 = time.perf_counter()
+        out = p.solve()
+        print("%s rep %d: %.3f s, %d iterations, %d eliminations" %
+              (args.workload, r, time.perf_counter() - t0, len(out["trace"]), len(out["xdrop_a"])), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -208,6 +208,9 @@ def run_reference(args):
 # GPU
 
 
+GRAM_POPCOUNT, GRAM_TENSOR = 0, 1  # lakgb_set_gram_impl
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -269,21 +272,33 @@ def run_gpu(args):
         ms = float(t.item())
     value = world * work / (ms / 1000.0)
 
-    # dominant kernel alone: the largest AnZt launch, timed on its stream
+    # dominant kernel alone: the largest AnZt launch, timed on its stream,
+    # with each of the two Gram kernels (the pass above ran the default one)
     big = dev.args[0]
-    for _ in range(3):
-        lib.lakgb_gram_device(C.byref(big))
-    torch.cuda.synchronize()
-    kt = []
-    for i in range(args.steps):
-        flush.zero_()
-        kstart[i].record(stream)
-        big.stream = sh
-        lib.lakgb_gram_device(C.byref(big))
-        kend[i].record(stream)
-    torch.cuda.synchronize()
-    kt = [s.elapsed_time(e) for s, e in zip(kstart, kend)]
-    k_ms = sum(kt) / len(kt)
+    big.stream = sh
+    lib.lakgb_set_gram_impl.argtypes = [C.c_int]
+    lib.lakgb_gram_impl.restype = C.c_int
+    lib.lakgb_device_status.restype = C.c_int
+    default_impl = lib.lakgb_gram_impl()
+
+    def time_big(impl):
+        lib.lakgb_set_gram_impl(impl)
+        for _ in range(3):
+            lib.lakgb_gram_device(C.byref(big))
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            kstart[i].record(stream)
+            lib.lakgb_gram_device(C.byref(big))
+            kend[i].record(stream)
+        torch.cuda.synchronize()
+        kt = [s.elapsed_time(e) for s, e in zip(kstart, kend)]
+        return sum(kt) / len(kt)
+
+    k_ms_popc = time_big(GRAM_POPCOUNT)
+    k_ms = time_big(default_impl)
+    lib.lakgb_set_gram_impl(default_impl)
+    device_status = lib.lakgb_device_status()
     k_work = float(big.nA) * float(big.nZ) * float(inst.ncols)
 
     # e2e through the reference-facing C entry points, host buffers, no residency
@@ -354,7 +369,9 @@ def run_gpu(args):
                              "frac": (k_work / (k_ms / 1000.0)) / popc_peak,
                              "note": "POPC issue-rate bound, 16 lanes/clk/SM x 32 bits at the sampled SM clock"},
                 "kernel_ms": k_ms,
+                "popcount_kernel_ms": k_ms_popc,
             },
+            "device_status": device_status,
             "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s},
             "clocks": clocks,

@@ -325,6 +325,19 @@ unsigned long long lakgb_kernel_launches(void);
 /* Device time (ms) of the most recent Gram kernel launch, timed with CUDA
  * events on the launching stream. */
 double lakgb_last_gram_ms(void);
+/* Kernel of the +/-1 Gram (AnZt_vv / AnAt_vv and the Grams inside the bcc
+ * solve): LAKGB_GRAM_TENSOR (default) runs the integer counts on the tcgen05
+ * tensor cores, LAKGB_GRAM_POPCOUNT on the CUDA cores' popcount; both give
+ * bit-identical outputs.  Process-wide. */
+#define LAKGB_GRAM_POPCOUNT 0
+#define LAKGB_GRAM_TENSOR 1
+void lakgb_set_gram_impl(int impl);
+int lakgb_gram_impl(void);
+/* Device status word of the tensor-core kernels: 0, or the code of the first
+ * pipeline wait that ran out of time (the kernel then skipped its remaining
+ * work, so its outputs are invalid).  Synchronises the device; reading it
+ * clears it. */
+int lakgb_device_status(void);
 
 #ifdef __cplusplus
 }

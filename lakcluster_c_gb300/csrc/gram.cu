@@ -14,6 +14,8 @@
 // shared memory (row pitch 61 words: conflict-free column reads), every
 // thread accumulates a TM x TN micro-tile of integer counts over the block's
 // 60 words, then folds them into FP64 accumulators with the block weight.
+#include <atomic>
+
 #include "gram.cuh"
 #include "lakgb_runtime.cuh"
 
@@ -149,11 +151,15 @@ void launch_tile(const GramParams &p) {
 
 }  // namespace
 
+std::atomic<int> g_gram_impl{LAKGB_GRAM_TENSOR};
+
 void launch_gram(const GramParams &p) {
   if (p.nA <= 0 || p.nZ <= 0 || p.P <= 0) return;
   cudaStream_t s = p.stream ? p.stream : stream();
   gram_timer_begin(s);
-  if (p.type == 1)
+  if (g_gram_impl.load(std::memory_order_relaxed) == LAKGB_GRAM_TENSOR)
+    launch_gram_tc(p, s);
+  else if (p.type == 1)
     launch_tile<128, 64, 8, 4, 1>(p);
   else
     launch_tile<128, 64, 8, 4, 2>(p);
@@ -161,6 +167,14 @@ void launch_gram(const GramParams &p) {
 }
 
 }  // namespace lakgb
+
+extern "C" void lakgb_set_gram_impl(int impl) {
+  lakgb::g_gram_impl.store(impl == LAKGB_GRAM_POPCOUNT ? LAKGB_GRAM_POPCOUNT : LAKGB_GRAM_TENSOR);
+}
+
+extern "C" int lakgb_gram_impl(void) { return lakgb::g_gram_impl.load(); }
+
+extern "C" int lakgb_device_status(void) { return lakgb::tc_status_take(); }
 
 extern "C" int lakgb_gram_device(const lakgb_gram_args *a) {
   using namespace lakgb;

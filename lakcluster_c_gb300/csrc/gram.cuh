@@ -31,8 +31,16 @@ struct GramParams {
   cudaStream_t stream;     // launch stream (null: the library stream)
 };
 
-// Enqueue the Gram kernel on the library stream.
+// Enqueue the Gram kernel on the library stream: the tensor-core kernel
+// (gram_tc.cu) or the popcount kernel (gram.cu), as lakgb_set_gram_impl selects.
 void launch_gram(const GramParams &p);
+
+// The tensor-core Gram (gram_tc.cu) on stream s.
+void launch_gram_tc(const GramParams &p, cudaStream_t s);
+
+// Read and clear the device status word of the tensor-core kernels
+// (0 = no pipeline error).
+int tc_status_take();
 
 // Algorithmic bit-ops of one Gram launch: rows_A * rows_Z * retained columns
 // (the full square for the symmetric variant, as the reference counts it).

@@ -314,8 +314,11 @@ int lakgb_xcalc_noalloc(const struct lakgb_xcalc_noalloc_args *args);
  * it clears it. */
 int lakgb_last_error(char *msg, int msg_len);
 /* Keep uploaded wX bit matrices resident on the device between calls, keyed
- * by their host address (1, default) or re-upload on every call (0).  A caller
- * that rewrites a wX buffer in place must call lakgb_forget_host_buffer. */
+ * by their host address and size (1), or upload them afresh on every call (0,
+ * default).  With 1, a caller that rewrites a wX buffer in place, or frees one
+ * whose address may be reused, must call lakgb_forget_host_buffer first.
+ * lakgb_bcc_solve and lakgb_bcc_run_in_file keep their own matrices resident
+ * for the length of the solve whatever this setting is. */
 void lakgb_set_residency(int on);
 void lakgb_forget_host_buffer(const void *host_ptr);
 /* D_MLT used by wrap_xcalc (the reference's GLOBAL_D_MLT, default 2^32). */

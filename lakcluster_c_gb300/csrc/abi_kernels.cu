@@ -60,8 +60,8 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   }
   if (nA == 0 || nZ == 0 || P == 0) return (int)length;
 
-  const void *wA = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   Stager st;
+  const void *wA = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   const void *wZ = resident(M_Zn->wX, (size_t)M_Zn->rpop_b * M_Zn->mc_length);
   DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> arow(M_An->m_b_, M_An->m_b_ + nA), zrow(M_Zn->m_b_, M_Zn->m_b_ + nZ);
@@ -149,8 +149,8 @@ extern "C" int wrap_An_v__run(int *tidx, void **vpra, pthread_t *thread_in, int 
   const int n = (int)M_An->rpop_j;
   if (n == 0) return (int)length;
   const int P = (int)(M_An->mc_length / kBlockBytes);
-  const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   Stager st;
+  const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> rows(M_An->m_b_, M_An->m_b_ + n);
   DBuf d_rows = upload_vec(rows), d_outr = upload_vec(spacing_index(output_spacing_r, M_An));
@@ -190,8 +190,8 @@ extern "C" int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int 
   }
   const int n = (int)M_An->rpop_j;
   if (n == 0) return (int)length;
-  const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   Stager st;
+  const void *w = resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
   DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> rows(M_An->m_b_, M_An->m_b_ + n);
   DBuf d_rows = upload_vec(rows), d_outr = upload_vec(spacing_index(output_spacing_r, M_An));

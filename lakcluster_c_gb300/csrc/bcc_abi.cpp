@@ -36,7 +36,20 @@ extern "C" void lakgb_bcc_problem_init(struct lakgb_bcc_problem *p) {
   p->test_sparse = 1;
 }
 
+extern "C" void lakgb_residency_scope(int enter);  // lakgb_runtime.cu
+
+namespace {
+// Device residency of the solve's matrices for the length of one solve: the
+// driver forgets each buffer it frees or rewrites, and whatever is still
+// cached when the solve ends is dropped.
+struct SolveResidency {
+  SolveResidency() { lakgb_residency_scope(1); }
+  ~SolveResidency() { lakgb_residency_scope(0); }
+};
+}  // namespace
+
 extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakgb_bcc_result *res) {
+  SolveResidency residency;
   g_err.clear();
   if (!prob || !res) { g_err = "null argument"; return 2; }
   memset(res, 0, sizeof(*res));
@@ -103,6 +116,7 @@ extern "C" void lakgb_bcc_result_free(struct lakgb_bcc_result *res) {
 }
 
 extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
+  SolveResidency residency;
   g_err.clear();
   lakbcc::Params P;
   lakbcc::Input I;

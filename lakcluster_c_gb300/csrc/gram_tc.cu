@@ -50,6 +50,7 @@ namespace {
 constexpr int kBM = 128, kBN = 128;
 constexpr int kStages = 4;
 constexpr int kChunks = 15;               // 128-bit chunks per 1920-bit block
+constexpr int kPrefetch = 5;              // producer loads in flight (divides kChunks)
 constexpr int kStageA = kBM * 128;        // bytes: 128 rows x 128 e4m3
 constexpr int kStageB = kBN * 128;
 constexpr int kStageBytes = kStageA + kStageB;
@@ -90,6 +91,16 @@ __device__ __forceinline__ uint4 and4(uint4 a, uint4 b) {
 // Counts decoded from the accumulator: n * 2^-12 -> n (exact for n < 2^22).
 __device__ __forceinline__ int decode_count(uint32_t bits) {
   return __float_as_int(__fmaf_rn(__uint_as_float(bits), 4096.0f, 12582912.0f)) - 0x4B400000;
+}
+
+// 2.0 * x, exactly as __dmul_rn(2.0, x) rounds it: for a normal x whose
+// double does not overflow, one more in the exponent field; otherwise (zero,
+// subnormal, near-overflow, inf, nan) the multiply itself.  Keeps the FP64
+// pipe for the adds.
+__device__ __forceinline__ double twice(double x) {
+  const long long bits = __double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7FF);
+  return (e >= 1 && e <= 2045) ? __longlong_as_double(bits + (1ll << 52)) : __dmul_rn(2.0, x);
 }
 
 template <int TYPE>
@@ -141,17 +152,29 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
     const long long ao = sm.a_off[r], zo = sm.z_off[r];
     const uint32_t row_in_stage = (uint32_t)((r >> 3) * kSBO + (r & 7) * 16);
     const uint32_t st0 = tc::smem_u32(stages);
+    const int G = P * kChunks;
+    // Loads run kPrefetch chunks ahead of the expansion (register ring).
+    uint4 rm[kPrefetch], ra[kPrefetch], rz[kPrefetch];
+    auto load = [&](int g, uint4 &m, uint4 &xa, uint4 &xz) {
+      m = xa = xz = make_uint4(0, 0, 0, 0);
+      if (g < G) {
+        const long long off = (long long)(g / kChunks) * kBlockBytes + (g % kChunks) * 16;
+        m = __ldg(reinterpret_cast<const uint4 *>(p.mask + off));
+        if (ao >= 0) xa = __ldg(reinterpret_cast<const uint4 *>(p.wA + ao + off));
+        if (zo >= 0) xz = __ldg(reinterpret_cast<const uint4 *>(p.wZ + zo + off));
+      }
+    };
+#pragma unroll
+    for (int u = 0; u < kPrefetch; ++u) load(u, rm[u], ra[u], rz[u]);
     bool ok = true;
-    for (int b = 0; b < P; ++b) {
-      int pa = 0, pz = 0;
-      const long long boff = (long long)b * kBlockBytes;
-      for (int ch = 0; ch < kChunks; ++ch) {
-        const int g = b * kChunks + ch, s = g % kStages, it = g / kStages;
-        const long long off = boff + ch * 16;
-        uint4 m = __ldg(reinterpret_cast<const uint4 *>(p.mask + off));
-        uint4 xa = ao >= 0 ? __ldg(reinterpret_cast<const uint4 *>(p.wA + ao + off)) : make_uint4(0, 0, 0, 0);
-        uint4 xz = zo >= 0 ? __ldg(reinterpret_cast<const uint4 *>(p.wZ + zo + off)) : make_uint4(0, 0, 0, 0);
-        xa = and4(xa, m);
+    int pa = 0, pz = 0;
+    for (int g0 = 0; g0 < G; g0 += kPrefetch) {
+#pragma unroll
+      for (int u = 0; u < kPrefetch; ++u) {
+        const int g = g0 + u, s = g % kStages, it = g / kStages;
+        const uint4 m = rm[u], xz = rz[u];
+        const uint4 xa = and4(ra[u], m);
+        load(g + kPrefetch, rm[u], ra[u], rz[u]);
         if (TYPE == 1) {
           pa += popc4(xa);
           pz += popc4(and4(xz, m));
@@ -164,12 +187,16 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
           tc::fence_proxy_async();
         }
         tc::mbar_arrive(&sm.full[s]);
+        if ((g + 1) % kChunks == 0) {
+          // end of block b: publish its row counts
+          const int b = g / kChunks, t = b & 1;
+          if (b >= 2 && ok) ok = tc::mbar_wait(&sm.aux_empty[t], ((b >> 1) - 1) & 1, abort, &g_tc_status, 2);
+          s_pa[t * kBM + r] = pa;
+          s_pz[t * kBN + r] = pz;
+          tc::mbar_arrive(&sm.aux_full[t]);
+          pa = pz = 0;
+        }
       }
-      const int t = b & 1;
-      if (b >= 2 && ok) ok = tc::mbar_wait(&sm.aux_empty[t], ((b >> 1) - 1) & 1, abort, &g_tc_status, 2);
-      s_pa[t * kBM + r] = pa;
-      s_pz[t * kBN + r] = pz;
-      tc::mbar_arrive(&sm.aux_full[t]);
     }
   } else if (warp == 4) {
     // ---------------- MMA issue ----------------
@@ -244,9 +271,16 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
       const int *pzb = s_pz + t * kBN;
 #pragma unroll 1
       for (int c0 = 0; c0 < kBN; c0 += 32) {
-        uint32_t cnt[32];
+        // counts of columns c0..c0+31 and their accumulators (TMEM columns
+        // 256 + 2*c0 + 2j low word, + 2j + 1 high word), one wait for all
+        uint32_t cnt[32], aw[2][32];
+        const uint32_t acol = lane_base + 256 + 2 * c0;
         if (ok) {
           tc::tmem_ld32(lane_base + t * kBN + c0, cnt);
+          if (b > 0) {
+            tc::tmem_ld32(acol, aw[0]);
+            tc::tmem_ld32(acol + 32, aw[1]);
+          }
           tc::tmem_wait_ld();
         } else {
 #pragma unroll
@@ -259,14 +293,6 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
         }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          // accumulators of columns c0+16h .. c0+16h+15: TMEM columns
-          // 256 + 2*(c0+16h) + 2j (low word) and + 2j + 1 (high word)
-          const uint32_t acol = lane_base + 256 + 2 * (c0 + 16 * h);
-          uint32_t aw[32];
-          if (ok && b > 0) {
-            tc::tmem_ld32(acol, aw);
-            tc::tmem_wait_ld();
-          }
           double acc[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
@@ -274,28 +300,29 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
             int c = (TYPE == 1) ? pa + pzb[c0 + 16 * h + j] - 2 * n : n;
             c = min(max(c, 0), kTabStride - 1);
             const double x = Tb[c];
-            acc[j] = (b > 0) ? __dadd_rn(__hiloint2double((int)aw[2 * j + 1], (int)aw[2 * j]), x) : x;
+            acc[j] = (b > 0) ? __dadd_rn(__hiloint2double((int)aw[h][2 * j + 1], (int)aw[h][2 * j]), x) : x;
           }
           if (b + 1 < P) {
-            if (ok) {
 #pragma unroll
-              for (int j = 0; j < 16; ++j) {
-                aw[2 * j] = (uint32_t)__double2loint(acc[j]);
-                aw[2 * j + 1] = (uint32_t)__double2hiint(acc[j]);
-              }
-              tc::tmem_st32(acol, aw);
+            for (int j = 0; j < 16; ++j) {
+              aw[h][2 * j] = (uint32_t)__double2loint(acc[j]);
+              aw[h][2 * j + 1] = (uint32_t)__double2hiint(acc[j]);
             }
           } else if (ok && ga < p.nA) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               const int gz = tile_n + c0 + 16 * h + j;
               if (gz >= p.nZ || (p.symmetric && ga > gz)) continue;
-              double o = (TYPE == 1) ? __dsub_rn(p.a0d1, __dmul_rn(2.0, acc[j])) : acc[j];
+              double o = (TYPE == 1) ? __dsub_rn(p.a0d1, twice(acc[j])) : acc[j];
               if (p.lfA && p.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(lfa, p.lfZ[gz]), p.a2d1));
               p.out[orow + (long long)p.out_c[gz] * p.out_stride] = o;
               if (p.symmetric) p.out[(long long)p.out_r2[gz] + ocol2] = o;
             }
           }
+        }
+        if (ok && b + 1 < P) {
+          tc::tmem_st32(acol, aw[0]);
+          tc::tmem_st32(acol + 32, aw[1]);
         }
       }
       if (ok) tc::tmem_wait_st();

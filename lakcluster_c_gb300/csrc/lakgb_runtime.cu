@@ -17,7 +17,7 @@ std::mutex g_mu;
 int g_err = 0;
 char g_msg[512] = {0};
 std::atomic<unsigned long long> g_launches{0};
-bool g_residency = true;
+bool g_residency = false;
 struct ResEntry { void *d; size_t n; };
 std::map<std::pair<const void *, size_t>, ResEntry> g_res;
 cudaEvent_t g_ev0 = nullptr, g_ev1 = nullptr;
@@ -73,6 +73,10 @@ Arena &arena() {
 
 namespace {
 thread_local Stager *t_active = nullptr;
+// Residency scope of this thread (a whole solve): depth, and the cache keys
+// inserted inside it, which are dropped when the outermost scope ends.
+thread_local int t_scope_depth = 0;
+thread_local std::vector<std::pair<const void *, size_t>> t_scope_keys;
 }
 
 Stager *active_stager() { return t_active; }
@@ -148,23 +152,33 @@ void DBuf::zero() {
   if (n) LAKGB_CUDA(cudaMemsetAsync(p, 0, n, stream()));
 }
 
+// Caching is on for a thread inside a residency scope (a whole solve, which
+// forgets every buffer it frees or rewrites) or process-wide after
+// lakgb_set_residency(1).  Otherwise a call's matrices are uploaded afresh
+// into its staging arena: a host buffer freed and reallocated at the same
+// address must never be served from an old device copy.
+bool residency_enabled() { return t_scope_depth > 0 || g_residency; }
+
 const void *resident(const void *host, size_t bytes) {
   if (bytes == 0) return nullptr;
   stream();  // create the stream before taking the lock
   std::lock_guard<std::mutex> lk(g_mu);
   auto key = std::make_pair(host, bytes);
   auto it = g_res.find(key);
-  if (g_residency && it != g_res.end()) return it->second.d;
+  const bool on = residency_enabled();
+  if (on && it != g_res.end()) return it->second.d;
   if (it != g_res.end()) {
     cudaFreeAsync(it->second.d, stream());
     g_res.erase(it);
   }
+  if (!on && t_active) return t_active->put_bytes(host, bytes);
   void *d = nullptr;
   LAKGB_CUDA(cudaMallocAsync(&d, bytes, stream()));
   LAKGB_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, stream()));
   // Complete before other threads' streams may read it.
   LAKGB_CUDA(cudaStreamSynchronize(stream()));
   g_res[key] = ResEntry{d, bytes};
+  if (t_scope_depth > 0) t_scope_keys.push_back(key);
   return d;
 }
 
@@ -179,10 +193,27 @@ void resident_put(const void *host, size_t bytes, DBuf &&d) {
       ++it;
     }
   }
-  if (!g_residency || bytes == 0 || !d.p) return;  // d frees itself
-  g_res[std::make_pair(host, bytes)] = ResEntry{d.p, bytes};
+  if (!residency_enabled() || bytes == 0 || !d.p) return;  // d frees itself
+  const auto key = std::make_pair(host, bytes);
+  g_res[key] = ResEntry{d.p, bytes};
+  if (t_scope_depth > 0) t_scope_keys.push_back(key);
   d.p = nullptr;
   d.n = 0;
+}
+
+ResidencyScope::ResidencyScope() { ++t_scope_depth; }
+
+ResidencyScope::~ResidencyScope() {
+  if (--t_scope_depth > 0) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (const auto &key : t_scope_keys) {
+    auto it = g_res.find(key);
+    if (it != g_res.end()) {
+      cudaFreeAsync(it->second.d, stream());
+      g_res.erase(it);
+    }
+  }
+  t_scope_keys.clear();
 }
 
 void gram_timer_begin(cudaStream_t s) {
@@ -221,6 +252,16 @@ extern "C" void lakgb_set_residency(int on) {
   if (!g_residency) {
     for (auto &kv : g_res) cudaFreeAsync(kv.second.d, stream());
     g_res.clear();
+  }
+}
+
+extern "C" void lakgb_residency_scope(int enter) {
+  thread_local std::vector<lakgb::ResidencyScope *> scopes;
+  if (enter) {
+    scopes.push_back(new lakgb::ResidencyScope());
+  } else if (!scopes.empty()) {
+    delete scopes.back();
+    scopes.pop_back();
   }
 }
 

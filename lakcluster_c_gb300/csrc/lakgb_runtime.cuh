@@ -31,9 +31,21 @@ void count_launch(unsigned long long n = 1);
 void *dalloc(size_t bytes);
 void dfree(void *p);
 
-// Device copy of a host buffer.  With residency on, buffers are cached by
-// (host pointer, size) and reused without re-upload.
+// Device copy of a host buffer.  With residency on (residency_enabled()),
+// buffers are cached by (host pointer, size) and reused without re-upload;
+// otherwise the copy goes into the call's staging arena (the caller holds a
+// Stager across the call).
 const void *resident(const void *host, size_t bytes);
+bool residency_enabled();
+
+// Residency on for this thread while the object lives; cache entries this
+// thread inserts meanwhile are dropped when the outermost scope ends.
+struct ResidencyScope {
+  ResidencyScope();
+  ~ResidencyScope();
+  ResidencyScope(const ResidencyScope &) = delete;
+  ResidencyScope &operator=(const ResidencyScope &) = delete;
+};
 
 // A device buffer freed when the object goes out of scope (after the stream
 // has drained the work that uses it).
@@ -86,8 +98,10 @@ class Stager {
   }
   template <class V> const typename V::value_type *put(const V &v) { return put(v.data(), v.size()); }
   void flush();
- private:
+  // Copy n host bytes in (arena or a dedicated buffer); the returned device
+  // pointer is valid for kernels enqueued after flush().
   const void *put_bytes(const void *h, size_t n);
+ private:
   bool active_ = false;
   std::vector<DBuf> spill_;
   friend DBuf upload_bytes(const void *h, size_t n);

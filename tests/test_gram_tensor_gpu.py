@@ -90,3 +90,20 @@ def test_tensor_extreme_counts(impl_switch, oracle_lib, density, mask_keep, dead
             outs = _run_both(impl_switch, False, t, MA, MZ, aj, None, None)
             assert _bits_equal(outs[TENSOR], want), (t, aj is None)
             assert _bits_equal(outs[POPCOUNT], want), (t, aj is None)
+
+
+def test_host_buffer_rewritten_in_place(impl_switch, oracle_lib):
+    """A wX buffer rewritten in place (same address, same size) between two
+    reference-API calls is read afresh: no stale device copy by default."""
+    rng = np.random.default_rng(77)
+    m = 2 * 1920
+    MA, MZ = _case(rng, 150, 130, m, False)
+    A_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(m)))
+    for impl in (TENSOR, POPCOUNT):
+        impl_switch.lakgb_set_gram_impl(impl)
+        first = kc.call_gram("gpu", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
+        MA.wX[:] = rng.integers(0, 256, MA.wX.shape, dtype=np.uint8)
+        want = kc.call_gram("oracle", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
+        got = kc.call_gram("gpu", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
+        assert not _bits_equal(first, want)
+        assert _bits_equal(got, want), impl

@@ -25,18 +25,23 @@
 // table T_b[c] (c = 0..1920), built once per launch with the same rounded
 // multiply, so the FP64 pipe -- slow on this part -- does only the add.
 //
-// CTA: a 128 (A rows) x 128 (Z rows) tile, 9 warps.
-//   warps 0-3  producers: per 128-column chunk, load each tile row's 16
-//              bytes, mask, expand to 128 e4m3 bytes in shared memory
-//              (K-major core matrices, no swizzle), count pa / pz.
-//   warp 4     owns TMEM; lane 0 issues the MMAs (M=128, N=128, K=32; 4 per
-//              chunk, 15 chunks per block) into one of two count buffers.
-//   warps 5-8  fold: per block, read the counts from TMEM (warp w reads
-//              lanes 32*(w%4)..+31), look up T_b[c], add into the FP64
-//              accumulators, which live in TMEM as well (columns 256..511,
-//              two 32-bit halves per value).
-// Shared memory: 4 stages x (16 KB A + 16 KB B) + 2 x T_b (15 KB) + counts.
+// Persistent CTAs, one per SM, each looping over 128 (A rows) x 128 (Z rows)
+// output tiles; the pipeline runs on across tile boundaries.  25 warps:
+//   warps 0-7   producers, one tile row each (A rows 0-127, then Z rows
+//               0-127): per 128-column chunk, load the row's 16 bytes, mask,
+//               expand to 128 e4m3 bytes in shared memory (K-major, 128-byte
+//               swizzle), count pa / pz.
+//   warp 8      owns TMEM; lane 0 issues the MMAs (M=128, N=128, K=32; 4 per
+//               chunk, 15 chunks per block) into one of two count buffers.
+//   warps 9-24  fold, four warps per lane quadrant (warp w reads TMEM lanes
+//               32*(w%4)..+31), each for 32 of the 128 columns: per block,
+//               read the counts from TMEM, look up T_b[c], add into the FP64
+//               accumulators, which live in TMEM as well (columns 256..511,
+//               two 32-bit halves per value).
+// Shared memory: 6 stages x (16 KB A + 16 KB B) + 2 x T_b (15 KB) + counts.
 // TMEM: 512 columns (2 x 128 count columns + 256 accumulator columns).
+#include <algorithm>
+
 #include "gram.cuh"
 #include "lakgb_runtime.cuh"
 #include "tc_ptx.cuh"
@@ -48,37 +53,42 @@ __device__ int g_tc_status;  // first pipeline error code of any tensor-core ker
 namespace {
 
 constexpr int kBM = 128, kBN = 128;
-constexpr int kStages = 4;
+constexpr int kStages = 6;
 constexpr int kChunks = 15;               // 128-bit chunks per 1920-bit block
-constexpr int kPrefetch = 5;              // producer loads in flight (divides kChunks)
+constexpr int kPrefetch = 3;              // producer loads in flight (divides kChunks)
 constexpr int kStageA = kBM * 128;        // bytes: 128 rows x 128 e4m3
 constexpr int kStageB = kBN * 128;
 constexpr int kStageBytes = kStageA + kStageB;
 constexpr int kTabStride = 1922;          // doubles per block table (1921 used, 16-byte multiple)
 constexpr int kTabBytes = kTabStride * 8;
-constexpr int kSBO = 8 * 128;             // bytes between 8-row core-matrix groups (8 k-groups of 16 B)
-constexpr int kThreads = 288;
+constexpr int kSBO = 8 * 128;             // bytes between 8-row swizzle atoms (8 rows of 128 B)
+constexpr int kProducers = 256;           // warps 0-7
+constexpr int kMmaWarp = 8;
+constexpr int kFold = 512;                // warps 9-24
+constexpr int kRound = 8;                 // columns per TMEM round of a fold warp
+constexpr int kFoldCols = kBN / (kFold / 128);  // tile columns per fold warp
+constexpr int kThreads = kProducers + 32 + kFold;
 constexpr uint32_t kTmemCols = 512;
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 2 * kTabBytes + 2 * (kBM + kBN) * 4 + 128;
+constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 2 * kTabBytes + 2 * (kBM + kBN) * 4 + 1024;
 
 struct Smem {
   uint64_t full[kStages], empty[kStages];
   uint64_t acc_full[2], acc_empty[2], aux_full[2], aux_empty[2], done;
   uint32_t tmem_base;
   int abort;
-  long long a_off[kBM], z_off[kBN];
 };
 
-// Expand the 128 bits of x into 128 e4m3 bytes of one tile row: words q of x
-// fill k-groups 2q and 2q+1 (16 bytes each) at row_base + g*128.
-__device__ __forceinline__ void expand_row(uint32_t row_base, uint4 x) {
+// Expand the 128 bits of x into the 128 e4m3 bytes of one tile row (a
+// 128-byte row of a 128-byte-swizzled atom): word q of x fills the 16-byte
+// chunks 2q and 2q+1, stored at chunk index c ^ sw (sw = row % 8).
+__device__ __forceinline__ void expand_row(uint32_t row_base, uint32_t sw, uint4 x) {
   const uint32_t w[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const uint32_t v = w[q];
-    tc::st_shared_v4(row_base + (2 * q) * 128, (v << 3) & 0x08080808u, (v << 2) & 0x08080808u,
+    tc::st_shared_v4(row_base + (((2 * q) ^ sw) << 4), (v << 3) & 0x08080808u, (v << 2) & 0x08080808u,
                      (v << 1) & 0x08080808u, v & 0x08080808u);
-    tc::st_shared_v4(row_base + (2 * q + 1) * 128, (v >> 1) & 0x08080808u, (v >> 2) & 0x08080808u,
+    tc::st_shared_v4(row_base + (((2 * q + 1) ^ sw) << 4), (v >> 1) & 0x08080808u, (v >> 2) & 0x08080808u,
                      (v >> 3) & 0x08080808u, (v >> 4) & 0x08080808u);
   }
 }
@@ -103,126 +113,161 @@ __device__ __forceinline__ double twice(double x) {
   return (e >= 1 && e <= 2045) ? __longlong_as_double(bits + (1ll << 52)) : __dmul_rn(2.0, x);
 }
 
+// Tile order shared by every role: tile i of the CTA's sequence is
+// blockIdx.x + i*gridDim.x in row-major (A tile row, Z tile column) order;
+// tiles wholly below the diagonal of a symmetric Gram are skipped.
+struct TileWalk {
+  int ntn, ntiles, tile;
+  __device__ TileWalk(const GramParams &p)
+      : ntn((p.nZ + kBN - 1) / kBN), ntiles(((p.nA + kBM - 1) / kBM) * ((p.nZ + kBN - 1) / kBN)),
+        tile((int)blockIdx.x - (int)gridDim.x) {}
+  __device__ bool next(const GramParams &p, int &tile_m, int &tile_n) {
+    for (;;) {
+      tile += gridDim.x;
+      if (tile >= ntiles) return false;
+      tile_m = (tile / ntn) * kBM;
+      tile_n = (tile % ntn) * kBN;
+      if (!(p.symmetric && tile_m > tile_n + kBN - 1)) return true;
+    }
+  }
+};
+
 template <int TYPE>
 __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, const double *__restrict__ T) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ Smem sm;
-  uint8_t *stages = dsm;
-  double *sT = reinterpret_cast<double *>(dsm + (size_t)kStages * kStageBytes);  // [2][kTabStride]
-  int *s_pa = reinterpret_cast<int *>(dsm + (size_t)kStages * kStageBytes + 2 * kTabBytes);  // [2][kBM]
-  int *s_pz = s_pa + 2 * kBM;                                                                   // [2][kBN]
-
-  const int tile_n = blockIdx.x * kBN;
-  const int tile_m = blockIdx.y * kBM;
-  if (p.symmetric && tile_m > tile_n + kBN - 1) return;
+  // stages first, on a 1024-byte boundary (swizzle atoms)
+  uint8_t *stages = dsm + ((1024 - (tc::smem_u32(dsm) & 1023)) & 1023);
+  double *sT = reinterpret_cast<double *>(stages + (size_t)kStages * kStageBytes);  // [2][kTabStride]
+  int *s_cnt = reinterpret_cast<int *>(stages + (size_t)kStages * kStageBytes + 2 * kTabBytes);  // [2][256]
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   volatile int *abort = &sm.abort;
   const int P = p.P;
 
-  for (int i = tid; i < kBM; i += kThreads)
-    sm.a_off[i] = (tile_m + i < p.nA) ? (long long)p.a_rowb[tile_m + i] * p.a_row_bytes : -1;
-  for (int i = tid; i < kBN; i += kThreads)
-    sm.z_off[i] = (tile_n + i < p.nZ) ? (long long)p.z_rowb[tile_n + i] * p.z_row_bytes : -1;
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      tc::mbar_init(&sm.full[s], 128);
+      tc::mbar_init(&sm.full[s], kProducers);
       tc::mbar_init(&sm.empty[s], 1);
     }
     for (int t = 0; t < 2; ++t) {
       tc::mbar_init(&sm.acc_full[t], 1);
-      tc::mbar_init(&sm.acc_empty[t], 128);
-      tc::mbar_init(&sm.aux_full[t], 128);
-      tc::mbar_init(&sm.aux_empty[t], 128);
+      tc::mbar_init(&sm.acc_empty[t], kFold);
+      tc::mbar_init(&sm.aux_full[t], kProducers);
+      tc::mbar_init(&sm.aux_empty[t], kFold);
     }
     tc::mbar_init(&sm.done, 1);
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 4) tc::tmem_alloc(&sm.tmem_base, kTmemCols);
+  if (warp == kMmaWarp) tc::tmem_alloc(&sm.tmem_base, kTmemCols);
   tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = sm.tmem_base;
+  TileWalk walk(p);
+  int tile_m, tile_n;
 
-  if (warp < 4) {
+  if (tid < kProducers) {
     // ---------------- producers ----------------
-    const int r = tid;  // A row r and Z row r of the tile
-    const long long ao = sm.a_off[r], zo = sm.z_off[r];
-    const uint32_t row_in_stage = (uint32_t)((r >> 3) * kSBO + (r & 7) * 16);
+    const int side = tid >> 7, rr = tid & 127;  // side 0: A row rr, side 1: Z row rr
+    const uint8_t *base = side ? p.wZ : p.wA;
+    const uint32_t *rowb = side ? p.z_rowb : p.a_rowb;
+    const long long row_bytes = side ? p.z_row_bytes : p.a_row_bytes;
+    const int nrows = side ? p.nZ : p.nA;
     const uint32_t st0 = tc::smem_u32(stages);
+    const uint32_t my_row = st0 + side * kStageA + (uint32_t)((rr >> 3) * kSBO + (rr & 7) * 128);
+    const uint32_t my_sw = (uint32_t)(rr & 7);
     const int G = P * kChunks;
-    // Loads run kPrefetch chunks ahead of the expansion (register ring).
-    uint4 rm[kPrefetch], ra[kPrefetch], rz[kPrefetch];
-    auto load = [&](int g, uint4 &m, uint4 &xa, uint4 &xz) {
-      m = xa = xz = make_uint4(0, 0, 0, 0);
-      if (g < G) {
-        const long long off = (long long)(g / kChunks) * kBlockBytes + (g % kChunks) * 16;
-        m = __ldg(reinterpret_cast<const uint4 *>(p.mask + off));
-        if (ao >= 0) xa = __ldg(reinterpret_cast<const uint4 *>(p.wA + ao + off));
-        if (zo >= 0) xz = __ldg(reinterpret_cast<const uint4 *>(p.wZ + zo + off));
-      }
-    };
-#pragma unroll
-    for (int u = 0; u < kPrefetch; ++u) load(u, rm[u], ra[u], rz[u]);
     bool ok = true;
-    int pa = 0, pz = 0;
-    for (int g0 = 0; g0 < G; g0 += kPrefetch) {
+    // ring position of the next chunk: stage s, in pass `wrap` over the ring
+    int s = 0, wrap = 0;
+    int gbb = 0;  // blocks this CTA has produced
+    while (walk.next(p, tile_m, tile_n)) {
+      const int grow = (side ? tile_n : tile_m) + rr;
+      const long long ro = grow < nrows ? (long long)rowb[grow] * row_bytes : -1;
+      uint4 rm[kPrefetch], rx[kPrefetch];
+      // chunk g of the tile covers bytes 16g..16g+15 of each row (blocks of
+      // 240 bytes are contiguous)
+      auto load = [&](int g, uint4 &m, uint4 &x) {
+        m = x = make_uint4(0, 0, 0, 0);
+        if (g < G) {
+          m = __ldg(reinterpret_cast<const uint4 *>(p.mask) + g);
+          if (ro >= 0) x = __ldg(reinterpret_cast<const uint4 *>(base + ro) + g);
+        }
+      };
 #pragma unroll
-      for (int u = 0; u < kPrefetch; ++u) {
-        const int g = g0 + u, s = g % kStages, it = g / kStages;
-        const uint4 m = rm[u], xz = rz[u];
-        const uint4 xa = and4(ra[u], m);
-        load(g + kPrefetch, rm[u], ra[u], rz[u]);
-        if (TYPE == 1) {
-          pa += popc4(xa);
-          pz += popc4(and4(xz, m));
-        }
-        if (it > 0 && ok) ok = tc::mbar_wait(&sm.empty[s], (it - 1) & 1, abort, &g_tc_status, 1);
-        if (ok) {
-          const uint32_t sa = st0 + s * kStageBytes + row_in_stage;
-          expand_row(sa, xa);
-          expand_row(sa + kStageA, xz);
-          tc::fence_proxy_async();
-        }
-        tc::mbar_arrive(&sm.full[s]);
-        if ((g + 1) % kChunks == 0) {
-          // end of block b: publish its row counts
-          const int b = g / kChunks, t = b & 1;
-          if (b >= 2 && ok) ok = tc::mbar_wait(&sm.aux_empty[t], ((b >> 1) - 1) & 1, abort, &g_tc_status, 2);
-          s_pa[t * kBM + r] = pa;
-          s_pz[t * kBN + r] = pz;
-          tc::mbar_arrive(&sm.aux_full[t]);
-          pa = pz = 0;
+      for (int u = 0; u < kPrefetch; ++u) load(u, rm[u], rx[u]);
+      int cnt = 0, ch = 0;
+      for (int g0 = 0; g0 < G; g0 += kPrefetch) {
+#pragma unroll
+        for (int u = 0; u < kPrefetch; ++u) {
+          const int g = g0 + u;
+          const uint4 m = rm[u];
+          const uint4 xm = and4(rx[u], m);
+          // A rows enter masked; Z rows unmasked (the mask on A already
+          // restricts every product), their count masked
+          const uint4 x = side ? rx[u] : xm;
+          load(g + kPrefetch, rm[u], rx[u]);
+          if (TYPE == 1) cnt += popc4(xm);
+          if (wrap > 0 && ok) ok = tc::mbar_wait(&sm.empty[s], (uint32_t)((wrap - 1) & 1), abort, &g_tc_status, 1);
+          if (ok) {
+            expand_row(my_row + s * kStageBytes, my_sw, x);
+            tc::fence_proxy_async();
+          }
+          tc::mbar_arrive(&sm.full[s]);
+          if (++s == kStages) {
+            s = 0;
+            ++wrap;
+          }
+          if (++ch == kChunks) {
+            // end of a block: publish the row counts
+            const int t = gbb & 1;
+            if (gbb >= 2 && ok)
+              ok = tc::mbar_wait(&sm.aux_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, &g_tc_status, 2);
+            s_cnt[t * 256 + tid] = cnt;
+            tc::mbar_arrive(&sm.aux_full[t]);
+            cnt = 0;
+            ch = 0;
+            ++gbb;
+          }
         }
       }
     }
-  } else if (warp == 4) {
+  } else if (warp == kMmaWarp) {
     // ---------------- MMA issue ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_e4m3_f32(kBM, kBN);
       const uint32_t st0 = tc::smem_u32(stages);
       bool ok = true;
-      for (int b = 0; b < P && ok; ++b) {
-        const int t = b & 1;
-        if (b >= 2) ok = tc::mbar_wait(&sm.acc_empty[t], ((b >> 1) - 1) & 1, abort, &g_tc_status, 3);
-        tc::fence_after_sync();
-        for (int ch = 0; ch < kChunks && ok; ++ch) {
-          const int g = b * kChunks + ch, s = g % kStages, it = g / kStages;
-          ok = tc::mbar_wait(&sm.full[s], it & 1, abort, &g_tc_status, 4);
-          if (!ok) break;
+      int s = 0, wrap = 0, gbb = 0;
+      while (ok && walk.next(p, tile_m, tile_n)) {
+        for (int b = 0; b < P && ok; ++b, ++gbb) {
+          const int t = gbb & 1;
+          if (gbb >= 2)
+            ok = tc::mbar_wait(&sm.acc_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, &g_tc_status, 3);
           tc::fence_after_sync();
-          const uint32_t sa = st0 + s * kStageBytes, sb = sa + kStageA;
+          for (int ch = 0; ch < kChunks && ok; ++ch) {
+            const int cs = s;
+            ok = tc::mbar_wait(&sm.full[cs], (uint32_t)(wrap & 1), abort, &g_tc_status, 4);
+            if (++s == kStages) {
+              s = 0;
+              ++wrap;
+            }
+            if (!ok) break;
+            tc::fence_after_sync();
+            const uint32_t sa = st0 + cs * kStageBytes, sb = sa + kStageA;
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint64_t ad = tc::smem_desc(sa + kk * 256, 128, kSBO);
-            const uint64_t bd = tc::smem_desc(sb + kk * 256, 128, kSBO);
-            tc::mma_e4m3(tmem + t * kBN, ad, bd, idesc, (ch | kk) != 0);
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ad = tc::smem_desc_sw128(sa + kk * 32, kSBO);
+              const uint64_t bd = tc::smem_desc_sw128(sb + kk * 32, kSBO);
+              tc::mma_e4m3(tmem + t * kBN, ad, bd, idesc, (ch | kk) != 0);
+            }
+            tc::mma_commit(&sm.empty[cs]);
           }
-          tc::mma_commit(&sm.empty[s]);
+          if (ok) tc::mma_commit(&sm.acc_full[t]);
         }
-        if (ok) tc::mma_commit(&sm.acc_full[t]);
       }
       // every issued MMA has completed before TMEM is released (waited for
       // even after an abort, within the same time limit)
@@ -237,102 +282,98 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
     }
   } else {
     // ---------------- FP64 fold ----------------
+    const int et = tid - (kProducers + 32);  // 0..kFold-1
     const int q = warp & 3;
-    const int et = tid - 160;  // 0..127
+    const int col0 = (et >> 7) * kFoldCols;   // this warp's columns of the tile
     const int row = 32 * q + lane;
-    const int ga = tile_m + row;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    for (int i = et; i < kTabBytes / 16; i += 128)
+    for (int i = et; i < kTabBytes / 16; i += kFold)
       tc::cp_async16(reinterpret_cast<uint8_t *>(sT) + 16 * i, reinterpret_cast<const uint8_t *>(T) + 16 * i);
     tc::cp_async_commit();
-    const double lfa = (p.lfA && ga < p.nA) ? p.lfA[ga] : 0.0;
-    const long long orow = ga < p.nA ? (long long)p.out_r[ga] : 0;
-    const long long ocol2 = (p.symmetric && ga < p.nA) ? (long long)p.out_c2[ga] * p.out_stride : 0;
     bool ok = true;
-    for (int b = 0; b < P; ++b) {
-      const int t = b & 1;
-      if (b + 1 < P) {
-        tc::named_bar_sync(1, 128);  // block b-1 no longer reads its table buffer
-        const uint8_t *src = reinterpret_cast<const uint8_t *>(T + (size_t)(b + 1) * kTabStride);
-        uint8_t *dst = reinterpret_cast<uint8_t *>(sT + (t ^ 1) * kTabStride);
-        for (int i = et; i < kTabBytes / 16; i += 128) tc::cp_async16(dst + 16 * i, src + 16 * i);
-        tc::cp_async_commit();
-        tc::cp_async_wait<1>();
-      } else {
-        tc::cp_async_wait<0>();
-      }
-      tc::named_bar_sync(1, 128);  // T_b is in shared memory
-      bool w = ok && tc::mbar_wait(&sm.aux_full[t], (b >> 1) & 1, abort, &g_tc_status, 6);
-      w = w && tc::mbar_wait(&sm.acc_full[t], (b >> 1) & 1, abort, &g_tc_status, 7);
-      ok = __all_sync(0xffffffffu, w);
-      tc::fence_after_sync();
-      const double *Tb = sT + t * kTabStride;
-      const int pa = s_pa[t * kBM + row];
-      const int *pzb = s_pz + t * kBN;
+    long long gb0 = 0;
+    while (walk.next(p, tile_m, tile_n)) {
+      const int ga = tile_m + row;
+      const bool row_in = ga < p.nA;
+      const double lfa = (p.lfA && row_in) ? p.lfA[ga] : 0.0;
+      const long long orow = row_in ? (long long)p.out_r[ga] : 0;
+      const long long ocol2 = (p.symmetric && row_in) ? (long long)p.out_c2[ga] * p.out_stride : 0;
+      for (int b = 0; b < P; ++b) {
+        const long long gbb = gb0 + b;
+        const int t = (int)(gbb & 1);
+        {
+          // the next block's table (block 0 of the next tile after the last)
+          const int nb = (b + 1 < P) ? b + 1 : 0;
+          tc::named_bar_sync(1, kFold);  // the previous block no longer reads buffer t^1
+          const uint8_t *src = reinterpret_cast<const uint8_t *>(T + (size_t)nb * kTabStride);
+          uint8_t *dst = reinterpret_cast<uint8_t *>(sT + (t ^ 1) * kTabStride);
+          for (int i = et; i < kTabBytes / 16; i += kFold) tc::cp_async16(dst + 16 * i, src + 16 * i);
+          tc::cp_async_commit();
+          tc::cp_async_wait<1>();
+          tc::named_bar_sync(1, kFold);  // T_b is in shared memory
+        }
+        bool w = ok && tc::mbar_wait(&sm.aux_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 6);
+        w = w && tc::mbar_wait(&sm.acc_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 7);
+        ok = __all_sync(0xffffffffu, w);
+        tc::fence_after_sync();
+        const double *Tb = sT + t * kTabStride;
+        const int pa = s_cnt[t * 256 + row];
+        const int *pzb = s_cnt + t * 256 + 128;
 #pragma unroll 1
-      for (int c0 = 0; c0 < kBN; c0 += 32) {
-        // counts of columns c0..c0+31 and their accumulators (TMEM columns
-        // 256 + 2*c0 + 2j low word, + 2j + 1 high word), one wait for all
-        uint32_t cnt[32], aw[2][32];
-        const uint32_t acol = lane_base + 256 + 2 * c0;
-        if (ok) {
-          tc::tmem_ld32(lane_base + t * kBN + c0, cnt);
-          if (b > 0) {
-            tc::tmem_ld32(acol, aw[0]);
-            tc::tmem_ld32(acol + 32, aw[1]);
+        for (int c0 = col0; c0 < col0 + kFoldCols; c0 += kRound) {
+          // counts of columns c0..c0+7 and their accumulators (TMEM columns
+          // 256 + 2*c0 + 2j low word, + 2j + 1 high word), one wait for both
+          uint32_t cn[kRound], a[2 * kRound];
+          const uint32_t acol = lane_base + 256 + 2 * c0;
+          if (ok) {
+            tc::tmem_ld8(lane_base + t * kBN + c0, cn);
+            if (b > 0) tc::tmem_ld16(acol, a);
+            tc::tmem_wait_ld();
+          } else {
+#pragma unroll
+            for (int j = 0; j < kRound; ++j) cn[j] = 0;
           }
-          tc::tmem_wait_ld();
-        } else {
+          if (c0 == col0 + kFoldCols - kRound) {
+            // all this warp's count columns of buffer t read
+            tc::fence_before_sync();
+            tc::mbar_arrive(&sm.acc_empty[t]);
+          }
 #pragma unroll
-          for (int j = 0; j < 32; ++j) cnt[j] = 0;
-        }
-        if (c0 == kBN - 32) {
-          // all count columns of buffer t read: the MMA may refill it
-          tc::fence_before_sync();
-          tc::mbar_arrive(&sm.acc_empty[t]);
-        }
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          double acc[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = decode_count(cnt[16 * h + j]);
-            int c = (TYPE == 1) ? pa + pzb[c0 + 16 * h + j] - 2 * n : n;
+          for (int j = 0; j < kRound; ++j) {
+            const int n = decode_count(cn[j]);
+            int c = (TYPE == 1) ? pa + pzb[c0 + j] - 2 * n : n;
             c = min(max(c, 0), kTabStride - 1);
             const double x = Tb[c];
-            acc[j] = (b > 0) ? __dadd_rn(__hiloint2double((int)aw[h][2 * j + 1], (int)aw[h][2 * j]), x) : x;
+            const double v = (b > 0) ? __dadd_rn(__hiloint2double((int)a[2 * j + 1], (int)a[2 * j]), x) : x;
+            a[2 * j] = (uint32_t)__double2loint(v);
+            a[2 * j + 1] = (uint32_t)__double2hiint(v);
           }
           if (b + 1 < P) {
+            if (ok) tc::tmem_st16(acol, a);
+          } else if (ok && row_in) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              aw[h][2 * j] = (uint32_t)__double2loint(acc[j]);
-              aw[h][2 * j + 1] = (uint32_t)__double2hiint(acc[j]);
-            }
-          } else if (ok && ga < p.nA) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int gz = tile_n + c0 + 16 * h + j;
+            for (int j = 0; j < kRound; ++j) {
+              const int gz = tile_n + c0 + j;
               if (gz >= p.nZ || (p.symmetric && ga > gz)) continue;
-              double o = (TYPE == 1) ? __dsub_rn(p.a0d1, twice(acc[j])) : acc[j];
+              const double v = __hiloint2double((int)a[2 * j + 1], (int)a[2 * j]);
+              double o = (TYPE == 1) ? __dsub_rn(p.a0d1, twice(v)) : v;
               if (p.lfA && p.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(lfa, p.lfZ[gz]), p.a2d1));
               p.out[orow + (long long)p.out_c[gz] * p.out_stride] = o;
               if (p.symmetric) p.out[(long long)p.out_r2[gz] + ocol2] = o;
             }
           }
         }
-        if (ok && b + 1 < P) {
-          tc::tmem_st32(acol, aw[0]);
-          tc::tmem_st32(acol + 32, aw[1]);
-        }
+        if (ok) tc::tmem_wait_st();
+        tc::mbar_arrive(&sm.aux_empty[t]);
       }
-      if (ok) tc::tmem_wait_st();
-      tc::mbar_arrive(&sm.aux_empty[t]);
+      gb0 += P;
     }
+    tc::cp_async_wait<0>();
   }
 
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 4) {
+  if (warp == kMmaWarp) {
     __syncwarp();
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, kTmemCols);
@@ -346,6 +387,26 @@ __global__ void gram_table_kernel(const double *__restrict__ D, int P, double *_
     T[(size_t)b * kTabStride + c] = c < kTabStride - 1 ? __dmul_rn(d, (double)c) : __longlong_as_double(0x7ff8dead00000000ll);
 }
 
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    LAKGB_CUDA(cudaGetDevice(&dev));
+    LAKGB_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+
+// Tiles a launch computes (symmetric Grams skip the tiles below the diagonal).
+int active_tiles(const GramParams &p) {
+  const int ntm = (p.nA + kBM - 1) / kBM, ntn = (p.nZ + kBN - 1) / kBN;
+  if (!p.symmetric) return ntm * ntn;
+  int n = 0;
+  for (int i = 0; i < ntm; ++i)
+    for (int j = 0; j < ntn; ++j) n += !(i * kBM > j * kBN + kBN - 1);
+  return n;
+}
+
 template <int TYPE>
 void launch_tc_type(const GramParams &p, const double *T, cudaStream_t s) {
   static bool configured = false;
@@ -354,7 +415,7 @@ void launch_tc_type(const GramParams &p, const double *T, cudaStream_t s) {
                                     (int)kSmemBytes));
     configured = true;
   }
-  dim3 grid((p.nZ + kBN - 1) / kBN, (p.nA + kBM - 1) / kBM);
+  const int grid = std::max(1, std::min(active_tiles(p), sm_count()));
   gram_tc_kernel<TYPE><<<grid, kThreads, kSmemBytes, s>>>(p, T);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();

@@ -211,6 +211,24 @@ def run_reference(args):
 GRAM_POPCOUNT, GRAM_TENSOR = 0, 1  # lakgb_set_gram_impl
 
 
+def _ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` recorded by the committed ncu summary
+    (a line 'traffic_bytes_per_launch: N' in profiles/<kernel>_*.md), or None."""
+    prof = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(prof):
+        return None
+    for name in sorted(os.listdir(prof)):
+        if name.startswith(kernel) and name.endswith(".md"):
+            with open(os.path.join(prof, name)) as f:
+                for line in f:
+                    if line.strip().startswith("traffic_bytes_per_launch:"):
+                        try:
+                            return float(line.split(":", 1)[1].split()[0])
+                        except ValueError:
+                            return None
+    return None
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -346,6 +364,14 @@ def run_gpu(args):
     peaks, src = _peaks()
     tflops = 2.0 * k_work / (k_ms / 1000.0) / 1e12
     peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    # The fold of the tensor-core kernel: per output element, one FP64 add per
+    # 1920-column block after the first, then the score combine (a0d1 - 2S,
+    # and three more operations with the row/column terms).
+    P = (inst.ncols + 1919) // 1920
+    fp64_per_elem = (P - 1) + 1 + (3 if (big.lfA and big.lfZ) else 0)
+    fp64_ops = float(big.nA) * float(big.nZ) * fp64_per_elem
+    fp64_rate = lib.lakgb_measure_fp64_add_rate()
+    traffic = _ncu_traffic("gram_tc_kernel")
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     clocks = clk.summary()
     mhz = clocks.get("sm_mhz") or 1920.0
@@ -354,7 +380,7 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u32-popcount+f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "e4m3-bit-mma+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "bins": inst.nbins, "cases": 4096, "controls": 4096,
                        "snps": inst.ncols, "launches_per_step": len(dev.args),
                        "l2": "flushed before each step (256 MB write)",
@@ -362,14 +388,23 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "roofline": {
                 "bound": "tensor", "achieved": tflops, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": tflops / peak_tf, "traffic": None,
-                "kernel": "gram_popc_kernel (largest AnZt launch, %dx%d rows)" % (big.nA, big.nZ),
-                "note": "bit-pair products counted as 2 ops (one MAC) against the %s dense bf16 tensor peak" % src,
-                "int_pipe": {"achieved_bitops": k_work / (k_ms / 1000.0), "peak_bitops": popc_peak,
-                             "frac": (k_work / (k_ms / 1000.0)) / popc_peak,
-                             "note": "POPC issue-rate bound, 16 lanes/clk/SM x 32 bits at the sampled SM clock"},
+                "frac": tflops / peak_tf, "traffic": traffic,
+                "kernel": "gram_tc_kernel (tcgen05 e4m3, largest AnZt launch, %dx%d rows, %d blocks)"
+                          % (big.nA, big.nZ, P),
+                "note": ("bit-pair products counted as 2 ops (one MAC) against the %s dense bf16 tensor peak; "
+                         "the e4m3 MMA this kernel issues is nominally 2x the bf16 rate. traffic: DRAM bytes of "
+                         "one launch from the committed ncu capture (profiles/), null when absent" % src),
+                "fp64_pipe": {"achieved_ops_per_s": fp64_ops / (k_ms / 1000.0), "peak_adds_per_s": fp64_rate,
+                              "frac": fp64_ops / (k_ms / 1000.0) / fp64_rate, "ops_per_launch": fp64_ops,
+                              "note": "the binding unit: FP64 adds of the block-weighted fold (%d per element) "
+                                      "against the add rate measured live on this GPU "
+                                      "(lakgb_measure_fp64_add_rate)" % fp64_per_elem},
+                "popcount_kernel": {"kernel_ms": k_ms_popc, "achieved_bitops": k_work / (k_ms_popc / 1000.0),
+                                    "int_pipe_peak_bitops": popc_peak,
+                                    "int_pipe_frac": (k_work / (k_ms_popc / 1000.0)) / popc_peak,
+                                    "note": "the CUDA-core kernel on the same launch; POPC issue-rate bound, "
+                                            "16 lanes/clk/SM x 32 bits at the sampled SM clock"},
                 "kernel_ms": k_ms,
-                "popcount_kernel_ms": k_ms_popc,
             },
             "device_status": device_status,
             "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

@@ -341,6 +341,11 @@ int lakgb_gram_impl(void);
  * work, so its outputs are invalid).  Synchronises the device; reading it
  * clears it. */
 int lakgb_device_status(void);
+/* Measured FP64 add throughput of the current device (adds per second):
+ * independent add chains on every SM, best of three timed launches.  The fold
+ * of the tensor-core Gram performs one FP64 add per output element per
+ * 1920-column block, so this rate bounds it. */
+double lakgb_measure_fp64_add_rate(void);
 
 #ifdef __cplusplus
 }

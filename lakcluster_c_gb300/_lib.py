@@ -40,6 +40,10 @@ def load() -> C.CDLL:
     lib.lakgb_forget_host_buffer.argtypes = [C.c_void_p]
     lib.lakgb_kernel_launches.restype = C.c_ulonglong
     lib.lakgb_last_gram_ms.restype = C.c_double
+    lib.lakgb_measure_fp64_add_rate.restype = C.c_double
+    lib.lakgb_set_gram_impl.argtypes = [C.c_int]
+    lib.lakgb_gram_impl.restype = C.c_int
+    lib.lakgb_device_status.restype = C.c_int
     _lib = lib
     return lib
 

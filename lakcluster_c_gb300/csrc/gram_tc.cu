@@ -448,3 +448,54 @@ int tc_status_take() {
 }
 
 }  // namespace lakgb
+
+// ---------------------------------------------------------------------------
+// Throughput of the FP64 add on this device: the pipe that bounds the fold of
+// the tensor-core Gram (one add per element per block).  Independent add
+// chains on every SM, timed with CUDA events.
+
+namespace lakgb {
+namespace {
+
+__global__ void fp64_add_rate_kernel(double *out, double y, int iters) {
+  double a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = threadIdx.x * 1e-3 + j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = __dadd_rn(a[j], y);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s = __dadd_rn(s, a[j]);
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+}  // namespace lakgb
+
+extern "C" double lakgb_measure_fp64_add_rate(void) {
+  using namespace lakgb;
+  const int blocks = sm_count() * 4, threads = 256, iters = 4096;
+  double *d = nullptr;
+  cudaEvent_t e0, e1;
+  LAKGB_CUDA(cudaMalloc(&d, sizeof(double) * blocks * threads));
+  LAKGB_CUDA(cudaEventCreate(&e0));
+  LAKGB_CUDA(cudaEventCreate(&e1));
+  float best = 0.f;
+  for (int rep = 0; rep < 4; ++rep) {
+    LAKGB_CUDA(cudaEventRecord(e0, stream()));
+    fp64_add_rate_kernel<<<blocks, threads, 0, stream()>>>(d, 1.5e-9, iters);
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch();
+    LAKGB_CUDA(cudaEventRecord(e1, stream()));
+    LAKGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    LAKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  LAKGB_CUDA(cudaEventDestroy(e0));
+  LAKGB_CUDA(cudaEventDestroy(e1));
+  LAKGB_CUDA(cudaFree(d));
+  return (double)blocks * threads * iters * 8 / (best * 1e-3);
+}

@@ -36,8 +36,11 @@ inline std::vector<uint32_t> spacing_index(int spacing, const M_handle *M) {
 }
 
 // Allocate (malloc, zero-filled) or check-and-zero the output, as the
-// reference wrappers do (AnZt_vv.c:203-204).
-inline L_handle *ensure_output(L_handle **pp, unsigned long long length, const char *who) {
+// reference wrappers do (AnZt_vv.c:203-204).  zero_host = false leaves an
+// existing buffer's zero-fill to a HostOutputFill (below), for calls whose
+// device result, zeros included, is copied over the whole output anyway.
+inline L_handle *ensure_output(L_handle **pp, unsigned long long length, const char *who,
+                               bool zero_host = true) {
   if (*pp == nullptr) {
     L_handle *L = (L_handle *)calloc(1, sizeof(L_handle));
     L->length = length;
@@ -54,9 +57,23 @@ inline L_handle *ensure_output(L_handle **pp, unsigned long long length, const c
     set_error(2, "output length %llu < %llu in %s", L->length, length, who);
     return nullptr;
   }
-  memset(L->lf, 0, length * sizeof(double));
+  if (zero_host) memset(L->lf, 0, length * sizeof(double));
   return L;
 }
+
+// The zero-fill of a host output that ensure_output(..., false) skipped: done
+// when the call returns without copying the full device result over it.
+struct HostOutputFill {
+  L_handle *L = nullptr;
+  unsigned long long n = 0;
+  bool copied = false;
+  HostOutputFill() = default;
+  HostOutputFill(const HostOutputFill &) = delete;
+  HostOutputFill &operator=(const HostOutputFill &) = delete;
+  ~HostOutputFill() {
+    if (L && !copied && n) memset(L->lf, 0, n * sizeof(double));
+  }
+};
 
 inline int popcount_bytes(const unsigned char *p, long n) {
   int c = 0;
@@ -75,7 +92,8 @@ inline DBuf upload_vec(const std::vector<T> &v) {
   return upload_bytes(v.data(), v.size() * sizeof(T));
 }
 
-inline void copy_back(double *host, const DBuf &dev, unsigned long long length) {
+inline void copy_back(double *host, const DBuf &dev, unsigned long long length, HostOutputFill *fill = nullptr) {
+  if (fill) fill->copied = true;
   if (length) LAKGB_CUDA(cudaMemcpyAsync(host, dev.p, length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
   LAKGB_CUDA(cudaStreamSynchronize(stream()));
 }

@@ -31,6 +31,7 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   // A mirrored output (lmirror.cu) is produced on the device only.
   Mirror *mo = *out_p ? find_mirror(*out_p) : nullptr;
   L_handle *out = nullptr;
+  HostOutputFill fill;
   if (mo) {
     out = *out_p;
     if (out->length < length || mo->n < length) {
@@ -40,7 +41,9 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
     if (length) LAKGB_CUDA(cudaMemsetAsync(mo->d, 0, length * sizeof(double), stream()));
     mo->host_stale = true;
   } else {
-    out = ensure_output(out_p, length, who);
+    out = ensure_output(out_p, length, who, false);
+    fill.L = out;
+    fill.n = length;
   }
   if (!out) return (int)length;
   out->spacing_row = spacing_r; out->row_stride = length_r;
@@ -111,7 +114,7 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   st.flush();
   launch_gram(p);
   if (mo) return (int)length;
-  copy_back(out->lf, d_out, length);
+  copy_back(out->lf, d_out, length, &fill);
   return (int)length;
 }
 

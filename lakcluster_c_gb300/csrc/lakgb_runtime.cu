@@ -109,8 +109,10 @@ void Stager::begin() {
 const void *Stager::put_bytes(const void *h, size_t n) {
   Arena &a = arena();
   const size_t off = (a.used + 255) & ~(size_t)255;
-  if (!active_ || off + n > a.cap) {
-    // Too large for the arena: a dedicated buffer, uploaded in order.
+  if (!active_ || off + n > a.cap || n >= kDirectUploadBytes) {
+    // Too large for the arena, or large enough that a direct copy from the
+    // caller's memory beats a host-side copy into the arena first: a
+    // dedicated buffer, uploaded in order.
     spill_.emplace_back(n ? n : 1);
     spill_.back().upload(h, n);
     return spill_.back().p;

@@ -86,6 +86,8 @@ struct DBuf {
 // their own.  One Stager per call; the arena is reused by the next call once
 // its copy has completed.
 constexpr size_t kStageBytes = 32u << 20;
+// Arrays of at least this many bytes skip the arena (one direct copy each).
+constexpr size_t kDirectUploadBytes = 1u << 20;
 class Stager {
  public:
   Stager() { begin(); }

@@ -339,6 +339,7 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   // A mirrored output (lmirror.cu) is produced on the device only.
   Mirror *mo = *output_p ? find_mirror(*output_p) : nullptr;
   L_handle *out = nullptr;
+  HostOutputFill fill;
   if (mo) {
     out = *output_p;
     if (out->length < length || mo->n < length) {
@@ -348,7 +349,9 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
     if (length) LAKGB_CUDA(cudaMemsetAsync(mo->d, 0, length * sizeof(double), stream()));
     mo->host_stale = true;
   } else {
-    out = ensure_output(output_p, length, "wrap_AtTYn_vv__run");
+    out = ensure_output(output_p, length, "wrap_AtTYn_vv__run", false);
+    fill.L = out;
+    fill.n = length;
   }
   if (!out) return (int)length;
   out->spacing_row = output_spacing_a; out->row_stride = la;
@@ -415,6 +418,6 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
   if (mo) return (int)length;
-  copy_back(out->lf, d_out, length);
+  copy_back(out->lf, d_out, length, &fill);
   return (int)length;
 }

@@ -332,10 +332,17 @@ double lakgb_last_gram_ms(void);
  * solve): LAKGB_GRAM_TENSOR (default) runs the integer counts on the tcgen05
  * tensor cores, LAKGB_GRAM_POPCOUNT on the CUDA cores' popcount; both give
  * bit-identical outputs.  Process-wide. */
-#define LAKGB_GRAM_POPCOUNT 0
-#define LAKGB_GRAM_TENSOR 1
+#define LAKGB_IMPL_POPCOUNT 0
+#define LAKGB_IMPL_TENSOR 1
+#define LAKGB_GRAM_POPCOUNT LAKGB_IMPL_POPCOUNT
+#define LAKGB_GRAM_TENSOR LAKGB_IMPL_TENSOR
 void lakgb_set_gram_impl(int impl);
 int lakgb_gram_impl(void);
+/* Kernel of the bit-plane loop product (wrap_At_T_YnWt_S_Zn_ww__run):
+ * LAKGB_IMPL_TENSOR (default; B_MLT of 8, 16 or 32, otherwise the CUDA-core
+ * kernel runs) or LAKGB_IMPL_POPCOUNT; bit-identical outputs.  Process-wide. */
+void lakgb_set_bitplane_impl(int impl);
+int lakgb_bitplane_impl(void);
 /* Device status word of the tensor-core kernels: 0, or the code of the first
  * pipeline wait that ran out of time (the kernel then skipped its remaining
  * work, so its outputs are invalid).  Synchronises the device; reading it

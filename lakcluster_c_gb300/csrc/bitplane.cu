@@ -28,10 +28,12 @@
 // popcount(a' & plane).  With pmpm0 = 2*popcount(a' & y) - popcount(y & mask),
 // the chunk's counts fold into exact At_tmp values, and 32 threads (one per
 // SNP) then run the FP64 recurrence over the chunk's Wn rows in order.
+#include <atomic>
 #include <mutex>
 
 #include "abi_common.cuh"
 #include "bcc_model.h"
+#include "bitplane.cuh"
 
 namespace lakgb {
 
@@ -41,28 +43,6 @@ constexpr int kLd = kBlockWords + 1;   // smem row pitch (words)
 constexpr int kBP_M = 32;              // SNP pairs per CTA
 constexpr int kBP_N = 256;             // plane rows per chunk
 constexpr int kBP_T = 256;             // threads
-
-struct BitplaneParams {
-  // At / Tt / planes share the row length `kbytes` (patients, a-space bits).
-  const uint8_t *At; const uint32_t *at_rowb;   // per pair: At row (b index)
-  long long at_row_bytes;
-  const uint8_t *Tt; long long tt_row_bytes; const uint32_t *tt_rowb;  // per t
-  const uint8_t *planes; long long plane_bytes;
-  const uint8_t *mask;                          // M_At->mc_j
-  int P;                                        // 1920-bit blocks per row
-  int npairs;
-  const uint8_t *Zt; const uint32_t *zt_rowb; long long zt_row_bytes;
-  const uint32_t *mw_a;                         // a-index of each Wn row (j order)
-  int nW; int B; int ncols_per;
-  const int8_t *vS;                             // [t][mw] +/-1
-  const double *aA; const double *aZ;           // per pair
-  const int *ycnt;                              // per plane row: popcount(y & mask)
-  const double *T_base; const double *T_tmp;    // [t], [t][mw]
-  double min_d, mlt_d;
-  const unsigned long long *out_off;            // per pair: row index in the output
-  const unsigned long long *t_off;              // per t: column offset (index * row_stride)
-  double *out;
-};
 
 __device__ __forceinline__ int plane_row(int mw, int k, int ncols_per) {
   return mw * ncols_per + ncols_per - 1 - k;
@@ -330,6 +310,16 @@ inline unsigned long long pick_u(int s, unsigned long long j, unsigned long long
 
 using namespace lakgb;
 
+namespace lakgb {
+std::atomic<int> g_bitplane_impl{LAKGB_IMPL_TENSOR};
+}
+
+extern "C" void lakgb_set_bitplane_impl(int impl) {
+  g_bitplane_impl.store(impl == LAKGB_IMPL_POPCOUNT ? LAKGB_IMPL_POPCOUNT : LAKGB_IMPL_TENSOR);
+}
+
+extern "C" int lakgb_bitplane_impl(void) { return g_bitplane_impl.load(); }
+
 extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a,
                                            int spacing_t, M_handle *M_At, M_handle *M_Tt, M_handle *M_Yn,
                                            M_handle *M_Wn, M_handle *M_St, M_handle *M_Zt, double *A_ajdk,
@@ -423,10 +413,14 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   std::call_once(attr, [&] {
     LAKGB_CUDA(cudaFuncSetAttribute(bitplane_main_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   });
-  dim3 grid((npairs + kBP_M - 1) / kBP_M, nT);
-  bitplane_main_kernel<<<grid, kBP_T, smem, stream()>>>(p);
-  LAKGB_CUDA(cudaGetLastError());
-  count_launch();
+  if (g_bitplane_impl.load(std::memory_order_relaxed) == LAKGB_IMPL_TENSOR && (B == 8 || B == 16 || B == 32)) {
+    launch_bitplane_tc(p, nT, stream());
+  } else {
+    dim3 grid((npairs + kBP_M - 1) / kBP_M, nT);
+    bitplane_main_kernel<<<grid, kBP_T, smem, stream()>>>(p);
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch();
+  }
   copy_back(out->lf, d_out, length);
   return (int)length;
 }

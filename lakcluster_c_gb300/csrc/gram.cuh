@@ -41,6 +41,9 @@ void launch_gram_tc(const GramParams &p, cudaStream_t s);
 // Read and clear the device status word of the tensor-core kernels
 // (0 = no pipeline error).
 int tc_status_take();
+// Device address of that status word, for tensor-core kernels of other
+// translation units.
+int *tc_status_device_ptr();
 
 // Algorithmic bit-ops of one Gram launch: rows_A * rows_Z * retained columns
 // (the full square for the symmetric variant, as the reference counts it).

@@ -436,6 +436,12 @@ void launch_gram_tc(const GramParams &p, cudaStream_t s) {
   LAKGB_CUDA(cudaFreeAsync(T, s));
 }
 
+int *tc_status_device_ptr() {
+  static int *ptr = nullptr;
+  if (!ptr) LAKGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_tc_status));
+  return ptr;
+}
+
 int tc_status_take() {
   int v = 0;
   LAKGB_CUDA(cudaDeviceSynchronize());

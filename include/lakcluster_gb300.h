@@ -170,6 +170,29 @@ int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *thread_in,
                                 struct L_handle *lf_AtTYn, struct L_handle *lf_ZtSWn,
                                 struct L_handle **output_p);
 
+/* The SNP x SNP x covariate product with Yt = At, each pair computed once and
+ * stored at both (na, ny) and (ny, na).  Replaces wrap_AtTAn_vv__run,
+ * dir_h/lakcluster_header.h:376 (kernel dir_c/AtTAn_vv.c:5-172). */
+int wrap_AtTAn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                       int output_spacing_y, int output_spacing_t, struct M_handle *M_At,
+                       struct M_handle *M_Tt, struct M_handle *M_Yt, double *A_ajdk, double *Y_ajdk,
+                       struct L_handle *lf_AtTn, struct L_handle *lf_YtTn, struct L_handle **output_AtTAn_p);
+
+/* The loop product element by element from the FP64 YnWt (no quantisation):
+ * the reference's ground truth for wrap_At_T_YnWt_S_Zn_ww__run.  Replaces
+ * wrap_At_T_YnWt_S_Zn_vv__run, dir_c/At_T_YnWt_S_Zn_vv.c:87 (kernel :5-85). */
+int wrap_At_T_YnWt_S_Zn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                                int output_spacing_s, struct M_handle *M_At, struct M_handle *M_Tt,
+                                struct M_handle *M_St, struct M_handle *M_Zt, double *A_ajdk,
+                                struct L_handle *lf_YnWt, struct L_handle **output_p);
+
+/* (An - a) D ZtSWn D (Yt - a) element by element, An row paired with Yn row.
+ * Replaces wrap_An_ZtSWn_Yt_vv__run, dir_c/An_ZtSWn_Yt_vv.c:131 (kernel :5-130). */
+int wrap_An_ZtSWn_Yt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                             int output_spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                             struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk,
+                             struct L_handle *lf_ZtSWn, struct L_handle **output_p);
+
 /* ---------------------------------------------------------------------------
  * Whole solves.
  * ------------------------------------------------------------------------- */

@@ -116,6 +116,10 @@ struct AtTYnParams {
   const double *aA; const double *aY;
   const unsigned long long *out_a; const unsigned long long *out_y; const unsigned long long *out_t;
   double *out;
+  // AtTAn (Yt = At): pairs na <= ny only, each also stored at
+  // out_a2[ny] + out_y2[na] (the transposed position).
+  int symmetric;
+  const unsigned long long *out_a2; const unsigned long long *out_y2;
 };
 
 __global__ void __launch_bounds__(kTY_T, 2) attyn_kernel(AtTYnParams p) {
@@ -124,6 +128,7 @@ __global__ void __launch_bounds__(kTY_T, 2) attyn_kernel(AtTYnParams p) {
   __shared__ long long a_off[kTY_M], y_off[kTY_N];
   const int t = blockIdx.z;
   const int n0 = blockIdx.x * kTY_N, m0 = blockIdx.y * kTY_M;
+  if (p.symmetric && m0 > n0 + kTY_N - 1) return;  // wholly below the diagonal
   const int tid = threadIdx.x, tx = tid % (kTY_N / kTY_TN), ty = tid / (kTY_N / kTY_TN);
   for (int i = tid; i < kTY_M; i += kTY_T) a_off[i] = m0 + i < p.nA ? (long long)p.a_rowb[m0 + i] * p.a_row_bytes : -1;
   for (int i = tid; i < kTY_N; i += kTY_T) y_off[i] = n0 + i < p.nY ? (long long)p.y_rowb[n0 + i] * p.y_row_bytes : -1;
@@ -183,12 +188,13 @@ __global__ void __launch_bounds__(kTY_T, 2) attyn_kernel(AtTYnParams p) {
 #pragma unroll
     for (int j = 0; j < kTY_TN; ++j) {
       const int ny = n0 + tx + 16 * j;
-      if (ny >= p.nY) continue;
+      if (ny >= p.nY || (p.symmetric && na > ny)) continue;
       const double hhaY = p.hhaY[(long long)t * p.nY + ny], aY = p.aY[ny];
       const double hhAY = (double)(2ll * c[i][j] - p.cpop);
       const double v = __dadd_rn(__dsub_rn(__dsub_rn(hhAY, __dmul_rn(hhAy, aY)), __dmul_rn(aA, hhaY)),
                                  __dmul_rn(__dmul_rn(aA, hhay), aY));
       p.out[p.out_a[na] + p.out_y[ny] + p.out_t[t]] = v;
+      if (p.symmetric) p.out[p.out_a2[ny] + p.out_y2[na] + p.out_t[t]] = v;
     }
   }
 }
@@ -327,11 +333,11 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
   return (int)length;
 }
 
-extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
-                                  int output_spacing_y, int output_spacing_t, M_handle *M_At, M_handle *M_Tt,
-                                  M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, L_handle *lf_AtTn,
-                                  L_handle *lf_YtTn, L_handle **output_p) {
-  (void)tidx; (void)vpra; (void)thread_in;
+namespace {
+
+int attyn_entry(bool symmetric, const char *who, int output_spacing_a, int output_spacing_y, int output_spacing_t,
+                M_handle *M_At, M_handle *M_Tt, M_handle *M_Yt, double *A_ajdk, double *Y_ajdk,
+                L_handle *lf_AtTn, L_handle *lf_YtTn, L_handle **output_p) {
   const unsigned long long la = spacing_length(output_spacing_a, M_At);
   const unsigned long long ly = spacing_length(output_spacing_y, M_Yt);
   const unsigned long long lt = spacing_length(output_spacing_t, M_Tt);
@@ -343,13 +349,13 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   if (mo) {
     out = *output_p;
     if (out->length < length || mo->n < length) {
-      set_error(2, "output length %llu < %llu in wrap_AtTYn_vv__run", out->length, length);
+      set_error(2, "output length %llu < %llu in %s", out->length, length, who);
       return (int)length;
     }
     if (length) LAKGB_CUDA(cudaMemsetAsync(mo->d, 0, length * sizeof(double), stream()));
     mo->host_stale = true;
   } else {
-    out = ensure_output(output_p, length, "wrap_AtTYn_vv__run", false);
+    out = ensure_output(output_p, length, who, false);
     fill.L = out;
     fill.n = length;
   }
@@ -360,7 +366,7 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   const int nA = (int)M_At->rpop_j, nY = (int)M_Yt->rpop_j, nT = (int)M_Tt->rpop_j;
   if (nA == 0 || nY == 0 || nT == 0) return (int)length;
   if (M_Yt->mc_length != M_At->mc_length || M_Tt->mc_length != M_At->mc_length) {
-    set_error(4, "wrap_AtTYn_vv__run: rows of unequal length");
+    set_error(4, "%s: rows of unequal length", who);
     return (int)length;
   }
   const int A_pcols = (int)lakbcc::psize(M_At->nrows), Y_pcols = (int)lakbcc::psize(M_Yt->nrows);
@@ -403,6 +409,18 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   p.hhAy = d_hAy.as<double>(); p.hhaY = d_haY.as<double>(); p.hhay = d_hay.as<double>();
   p.aA = d_aA.as<double>(); p.aY = d_aY.as<double>();
   p.out_a = d_oa.as<unsigned long long>(); p.out_y = d_oy.as<unsigned long long>(); p.out_t = d_ot.as<unsigned long long>();
+  DBuf d_oa2, d_oy2;
+  if (symmetric) {
+    // transposed positions: Yt row k as an output row, At row i as a column
+    std::vector<unsigned long long> out_a2(nY), out_y2(nA);
+    for (int k = 0; k < nY; ++k) out_a2[k] = pick_u(output_spacing_a, k, M_Yt->m_b_[k], M_Yt->m_a_[k]);
+    for (int i = 0; i < nA; ++i) out_y2[i] = pick_u(output_spacing_y, i, M_At->m_b_[i], M_At->m_a_[i]) * la;
+    d_oa2 = upload_vec(out_a2);
+    d_oy2 = upload_vec(out_y2);
+    p.symmetric = 1;
+    p.out_a2 = d_oa2.as<unsigned long long>();
+    p.out_y2 = d_oy2.as<unsigned long long>();
+  }
   DBuf d_out;
   if (mo) {
     p.out = mo->d;
@@ -420,4 +438,24 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
   if (mo) return (int)length;
   copy_back(out->lf, d_out, length, &fill);
   return (int)length;
+}
+
+}  // namespace
+
+extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                                  int output_spacing_y, int output_spacing_t, M_handle *M_At, M_handle *M_Tt,
+                                  M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, L_handle *lf_AtTn,
+                                  L_handle *lf_YtTn, L_handle **output_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  return attyn_entry(false, "wrap_AtTYn_vv__run", output_spacing_a, output_spacing_y, output_spacing_t, M_At, M_Tt,
+                     M_Yt, A_ajdk, Y_ajdk, lf_AtTn, lf_YtTn, output_p);
+}
+
+extern "C" int wrap_AtTAn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
+                                  int output_spacing_y, int output_spacing_t, M_handle *M_At, M_handle *M_Tt,
+                                  M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, L_handle *lf_AtTn,
+                                  L_handle *lf_YtTn, L_handle **output_AtTAn_p) {
+  (void)tidx; (void)vpra; (void)thread_in;
+  return attyn_entry(true, "wrap_AtTAn_vv__run", output_spacing_a, output_spacing_y, output_spacing_t, M_At, M_Tt,
+                     M_Yt, A_ajdk, Y_ajdk, lf_AtTn, lf_YtTn, output_AtTAn_p);
 }

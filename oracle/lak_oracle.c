@@ -561,3 +561,130 @@ int lako_AtTYn____WtSZn_vv(int spacing_a, int spacing_s, struct M_handle *M_At, 
   }
   return (int)(la * ls);
 }
+
+/* dir_c/AtTAn_vv.c:5-172: AtTYn_vv with Yt = At; each pair na_j <= ny_j is
+   computed once and stored at (na, ny) and at (ny, na) (:99-113). */
+int lako_AtTAn_vv(int spacing_a, int spacing_y, int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                  struct M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_AtTn,
+                  struct L_handle *lf_YtTn, struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_At), ly = spacing_len(spacing_y, M_Yt),
+                     lt = spacing_len(spacing_t, M_Tt);
+  struct L_handle *out = ensure(out_p, la * ly * lt);
+  if (!out) return (int)(la * ly * lt);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_y; out->col_stride = ly;
+  out->spacing_lyr = spacing_t; out->lyr_stride = lt;
+  const double *a_An = A_ajdk + 1 * psize_c(M_At->nrows), *a_Yn = Y_ajdk + 1 * psize_c(M_Yt->nrows);
+  const long nb = (long)M_At->mc_length;
+  for (long long t = 0; t < M_Tt->rpop_j; t++) {
+    const unsigned t_a = M_Tt->m_a_[t], t_b = M_Tt->m_b_[t];
+    const unsigned char *Tt = M_Tt->wX + (long long)t_b * M_Tt->mc_length;
+    const long long hhay = -M_Tt->cpop_j + 2 * row_and(Tt, M_Tt->mc_j, (long)M_Tt->mc_length);
+    const unsigned long long tab_t = pick(spacing_t, t, t_b, t_a);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+    for (long long na = 0; na < M_At->rpop_j; na++) {
+      const unsigned na_a = M_At->m_a_[na], na_b = M_At->m_b_[na];
+      const unsigned char *At = M_At->wX + (long long)na_b * M_At->mc_length;
+      const long long hhAy = (long long)*L2(lf_AtTn, na, na_b, na_a, t, t_b, t_a);
+      for (long long ny = na; ny < M_Yt->rpop_j; ny++) {
+        const unsigned ny_a = M_Yt->m_a_[ny], ny_b = M_Yt->m_b_[ny];
+        const long long hhaY = (long long)*L2(lf_YtTn, ny, ny_b, ny_a, t, t_b, t_a);
+        long long hhAY = M_At->cpop_j;
+        hhAY -= 2 * row_notxorxor(At, Tt, M_Yt->wX + (long long)ny_b * M_Yt->mc_length, M_At->mc_j, nb);
+        const double v =
+            (hhAY - hhAy * a_Yn[ny_a / 1920] - a_An[na_a / 1920] * hhaY + a_An[na_a / 1920] * hhay * a_Yn[ny_a / 1920]);
+        out->lf[pick(spacing_a, na, na_b, na_a) + pick(spacing_y, ny, ny_b, ny_a) * la + tab_t * la * ly] = v;
+        out->lf[pick(spacing_a, ny, ny_b, ny_a) + pick(spacing_y, na, na_b, na_a) * la + tab_t * la * ly] = v;
+      }
+    }
+  }
+  return (int)(la * ly * lt);
+}
+
+/* dir_c/At_T_YnWt_S_Zn_vv.c:5-85: the loop product element by element from
+   the FP64 YnWt (no quantisation):
+   out[na, ns] = sum_my (vA - a_An[na]) * vT * (sum_mw YnWt[my, mw] * vS * (vZ - a_An[nz])),
+   At row na paired with Zt row nz, both sums in index order (:62-77). */
+int lako_At_T_YnWt_S_Zn_vv(int spacing_a, int spacing_s, struct M_handle *M_At, struct M_handle *M_Tt,
+                           struct M_handle *M_St, struct M_handle *M_Zt, double *A_ajdk,
+                           struct L_handle *lf_YnWt, struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_At), ls = spacing_len(spacing_s, M_St);
+  struct L_handle *out = ensure(out_p, la * ls);
+  if (!out) return (int)(la * ls);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_s; out->col_stride = ls;
+  const double *a_An = A_ajdk + 1 * psize_c(M_At->nrows); /* AJDK_1_0 */
+  const long long nP = M_At->rpop_j < M_Zt->rpop_j ? M_At->rpop_j : M_Zt->rpop_j;
+  for (long long s = 0; s < M_St->rpop_j; s++) {
+    const unsigned s_a = M_St->m_a_[s], s_b = M_St->m_b_[s];
+    const unsigned char *Tt = M_Tt->wX + (long long)s_b * M_Tt->mc_length;
+    const unsigned char *St = M_St->wX + (long long)s_b * M_St->mc_length;
+    const unsigned long long ts = pick(spacing_s, s, s_b, s_a);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+    for (long long i = 0; i < nP; i++) {
+      const unsigned na_a = M_At->m_a_[i], na_b = M_At->m_b_[i], nz_a = M_Zt->m_a_[i], nz_b = M_Zt->m_b_[i];
+      const unsigned char *At = M_At->wX + (long long)na_b * M_At->mc_length;
+      const unsigned char *Zt = M_Zt->wX + (long long)nz_b * M_Zt->mc_length;
+      double acc = 0;
+      for (long long my = 0; my < M_At->cpop_j; my++) {
+        const unsigned my_a = M_At->n_a_[my], my_b = M_At->n_b_[my];
+        const int vA = bit_pm(At, my_a), vT = bit_pm(Tt, my_a);
+        double tmp = 0;
+        for (long long mw = 0; mw < M_Zt->cpop_j; mw++) {
+          const unsigned mw_a = M_Zt->n_a_[mw], mw_b = M_Zt->n_b_[mw];
+          const int vS = bit_pm(St, mw_a), vZ = bit_pm(Zt, mw_a);
+          tmp += (*L2(lf_YnWt, my, my_b, my_a, mw, mw_b, mw_a)) * vS * (vZ - a_An[nz_a / 1920]);
+        }
+        acc += (vA - a_An[na_a / 1920]) * vT * tmp;
+      }
+      out->lf[pick(spacing_a, i, na_b, na_a) + ts * la] = acc;
+    }
+  }
+  return (int)(la * ls);
+}
+
+/* dir_c/An_ZtSWn_Yt_vv.c:5-130: out[ma, ns] = sum_ny [ (sum_na (vA - a_An[na]) * D_An[na] *
+   ZtSWn[na, ny, ns]) * (D_Yn[ny] * (vY - a_Yn[ny])) ], An row ma paired with Yn row my,
+   both sums in index order (:69-79; the OpenMP branch :95-115 keeps the same order per output). */
+int lako_An_ZtSWn_Yt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                        struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_ZtSWn,
+                        struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_An), ls = spacing_len(spacing_s, M_St);
+  struct L_handle *out = ensure(out_p, la * ls);
+  if (!out) return (int)(la * ls);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_s; out->col_stride = ls;
+  if (!lf_ZtSWn) return (int)(la * ls);
+  const long A_pcols = psize_c(M_An->ncols), Y_pcols = psize_c(M_Yn->ncols);
+  const double *D_An = A_ajdk + 5 * A_pcols, *a_An = A_ajdk + 1 * A_pcols; /* AJDK_0_1, AJDK_1_0 */
+  const double *D_Yn = Y_ajdk + 5 * Y_pcols, *a_Yn = Y_ajdk + 1 * Y_pcols;
+  const long long nP = M_An->rpop_j < M_Yn->rpop_j ? M_An->rpop_j : M_Yn->rpop_j;
+  for (long long s = 0; s < M_St->rpop_j; s++) {
+    const unsigned s_a = M_St->m_a_[s], s_b = M_St->m_b_[s];
+    const unsigned long long ts = pick(spacing_s, s, s_b, s_a);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+    for (long long i = 0; i < nP; i++) {
+      const unsigned ma_a = M_An->m_a_[i], ma_b = M_An->m_b_[i], my_b = M_Yn->m_b_[i];
+      const unsigned char *An = M_An->wX + (long long)ma_b * M_An->mc_length;
+      const unsigned char *Yn = M_Yn->wX + (long long)my_b * M_Yn->mc_length;
+      double acc = 0;
+      for (long long ny = 0; ny < M_Yn->cpop_j; ny++) {
+        const unsigned ny_a = M_Yn->n_a_[ny], ny_b = M_Yn->n_b_[ny];
+        const int vY = bit_pm(Yn, ny_a);
+        double tmp = 0;
+        for (long long na = 0; na < M_An->cpop_j; na++) {
+          const unsigned na_a = M_An->n_a_[na], na_b = M_An->n_b_[na];
+          const int vA = bit_pm(An, na_a);
+          tmp += (vA - a_An[na_a / 1920]) * D_An[na_a / 1920] * (*L3(lf_ZtSWn, na, na_b, na_a, ny, ny_b, ny_a, s, s_b, s_a));
+        }
+        tmp *= D_Yn[ny_a / 1920] * (vY - a_Yn[ny_a / 1920]);
+        acc += tmp;
+      }
+      out->lf[pick(spacing_a, i, ma_b, ma_a) + ts * la] = acc;
+    }
+  }
+  return (int)(la * ls);
+}

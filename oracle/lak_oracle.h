@@ -62,6 +62,19 @@ int lako_AtTYn____WtSZn_vv(int spacing_a, int spacing_s, struct M_handle *M_At, 
                            struct M_handle *M_Zt, double *Y_ajdk, struct L_handle *lf_AtTYn,
                            struct L_handle *lf_ZtSWn, struct L_handle **out_p);
 
+/* dir_c/AtTAn_vv.c:5-172 */
+int lako_AtTAn_vv(int spacing_a, int spacing_y, int spacing_t, struct M_handle *M_At, struct M_handle *M_Tt,
+                  struct M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_AtTn,
+                  struct L_handle *lf_YtTn, struct L_handle **out_p);
+/* dir_c/At_T_YnWt_S_Zn_vv.c:5-85 */
+int lako_At_T_YnWt_S_Zn_vv(int spacing_a, int spacing_s, struct M_handle *M_At, struct M_handle *M_Tt,
+                           struct M_handle *M_St, struct M_handle *M_Zt, double *A_ajdk,
+                           struct L_handle *lf_YnWt, struct L_handle **out_p);
+/* dir_c/An_ZtSWn_Yt_vv.c:5-130 */
+int lako_An_ZtSWn_Yt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                        struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_ZtSWn,
+                        struct L_handle **out_p);
+
 /* Threads used by the OpenMP loops (default: all). */
 void lako_set_threads(int n);
 

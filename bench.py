@@ -355,6 +355,10 @@ def run_gpu(args):
         cpu = {"value": w / secs, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": CPU_SAMPLE + ", 3 passes, %.1f s" % secs}
 
+    large = None
+    if rank == 0 and not args.no_large:
+        large = large_pass_measurement(args, stream, sh, flush)
+
     solves = None
     if rank == 0 and not args.no_solves:
         solves = solve_measurements(args, with_cpu=(world == 1 and not args.no_cpu_baseline))
@@ -413,12 +417,52 @@ def run_gpu(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if large is not None:
+            line["large_gram_pass"] = large
         if solves is not None:
             line["solves"] = solves
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def large_pass_measurement(args, stream, sh, flush):
+    """The Gram pass of the large configuration (cases 32768 + controls 32768 x
+    131072 SNPs, 3 bins; 15 launches), inputs drawn on the device: every
+    product run with both Gram kernels and compared bit for bit, sampled
+    entries recomputed on the host, then the pass timed with each kernel."""
+    import torch
+    from lakcluster_c_gb300.large_pass import POPCOUNT, TENSOR, LargeGramPass
+
+    t0 = time.perf_counter()
+    lp = LargeGramPass()
+    setup_s = time.perf_counter() - t0
+    checks = lp.run_checks()
+    work = lp.work_bitops()
+    lib = lp.lib
+    default_impl = lib.lakgb_gram_impl()
+    timings = {}
+    for impl, name, reps in ((TENSOR, "tensor", 3), (POPCOUNT, "popcount", 1)):
+        lib.lakgb_set_gram_impl(impl)
+        lp.run(sh)  # warm
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lp.run(sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        timings[name] = {"ms_per_pass": statistics.median(ms), "bitops_per_s": work / (statistics.median(ms) / 1e3),
+                         "reps": reps}
+    lib.lakgb_set_gram_impl(default_impl)
+    return {"workload": "case_control_32768x32768x131072_3bins_gram_pass", "launches": len(lp.args),
+            "bitops_per_pass": work, "setup_seconds": setup_s, "checks": checks, **timings,
+            "note": "operands drawn on the device (MAF U[0.01,0.5], 2048x4096 planted, 5% flips); row terms from "
+                    "wrap_An_ajdk_v; host recomputation of sampled entries in block order"}
 
 
 def solve_measurements(args, with_cpu: bool):
@@ -540,6 +584,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solves", action="store_true", help="skip the whole-solve timings")
     ap.add_argument("--no-many", action="store_true", help="skip the batched / served timings")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the large-configuration Gram pass (32768 + 32768 x 131072)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -1,0 +1,208 @@
+"""The Gram pass of the large single-solve configuration on one GPU:
+cases 32768 and controls 32768 x 131072 SNPs, MAF U[0.01, 0.5], a
+2048 x 4096 planted bicluster with 5 % flips, rows in 3 covariate bins.
+
+At this size the 0/1 matrices (4.3 G entries each) never exist: the packed
+rows are drawn on the device, chunk by chunk (torch as plumbing: a seeded
+generator, comparisons, an MSB-first bit pack).  The pass is the reference's
+bcc_lf_YnWt Gram pass (dir_c/bcc_lf.c:223-270): AnZt for every bin pair and
+AnAt for nb1 <= nb2, D-weighted, with the AJDK_1_1 row terms.  The row terms
+come from the library's own wrap_An_ajdk_v on host copies of the packed bins.
+
+``run_checks`` runs every product with both Gram kernels and compares the
+outputs bit for bit, and recomputes sampled entries on the host from the
+packed bits (XOR popcounts per 1920-column block and the FP64 fold in block
+order, in Python floats, which are IEEE binary64).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import load
+from .gram_pass import AJDK_0_1, AJDK_1_1, AJDK_2_1, GramArgs, products
+
+TENSOR, POPCOUNT = 1, 0
+
+
+def _pack_rows(bits, row_bytes):
+    """(rows, m) bool tensor -> (rows, row_bytes) uint8, MSB first, zero padded."""
+    import torch
+    rows, m = bits.shape
+    pad = row_bytes * 8 - m
+    if pad:
+        bits = torch.cat([bits, torch.zeros(rows, pad, dtype=torch.bool, device=bits.device)], dim=1)
+    w = torch.tensor([128, 64, 32, 16, 8, 4, 2, 1], dtype=torch.uint8, device=bits.device)
+    return (bits.view(rows, row_bytes, 8).to(torch.uint8) * w).sum(dim=2, dtype=torch.uint8)
+
+
+class LargeGramPass:
+    def __init__(self, n_cases=32768, n_controls=32768, ncols=131072, nbins=3, planted=(2048, 4096),
+                 flip=0.05, maf=(0.01, 0.5), seed=3, device="cuda", chunk_rows=2048):
+        import torch
+        self.torch = torch
+        self.ncols, self.nbins = ncols, nbins
+        self.P = abi.psize(ncols)
+        self.row_bytes = abi.bsize(ncols)
+        g = torch.Generator(device=device)
+        g.manual_seed(seed)
+        p = maf[0] + (maf[1] - maf[0]) * torch.rand(ncols, generator=g, device=device)
+        pr, pc = planted
+        pattern = torch.rand(pc, generator=g, device=device) < 0.5
+        # bin of every row (uniform), cases then controls
+        bin_a = torch.randint(0, nbins, (n_cases,), generator=g, device=device)
+        bin_z = torch.randint(0, nbins, (n_controls,), generator=g, device=device)
+        self.A = [[] for _ in range(nbins)]
+        self.Z = [[] for _ in range(nbins)]
+        colsum = torch.zeros(ncols, dtype=torch.float64, device=device)
+        for side, n, bins, store in (("A", n_cases, bin_a, self.A), ("Z", n_controls, bin_z, self.Z)):
+            for r0 in range(0, n, chunk_rows):
+                r1 = min(n, r0 + chunk_rows)
+                bits = torch.rand(r1 - r0, ncols, generator=g, device=device) < p
+                if side == "A" and r0 < pr:
+                    k = min(r1, pr) - r0
+                    noise = torch.rand(k, pc, generator=g, device=device) < flip
+                    bits[:k, :pc] = pattern ^ noise
+                if side == "A":
+                    colsum += bits.sum(dim=0, dtype=torch.float64)
+                packed = _pack_rows(bits, self.row_bytes)
+                b = bins[r0:r1]
+                for nb in range(nbins):
+                    store[nb].append(packed[b == nb])
+                del bits
+        self.A = [torch.cat(x) for x in self.A]
+        self.Z = [torch.cat(x) for x in self.Z]
+        # per-block allele frequency over all case rows (bcc_load_A_p)
+        A_p = np.full(self.P, 0.5)
+        cs = colsum.cpu().numpy()
+        for blk in range(self.P):
+            lo, hi = blk * abi.POPLENGTH, min((blk + 1) * abi.POPLENGTH, ncols)
+            if hi > lo:
+                A_p[blk] = cs[lo:hi].sum() / max(1, (hi - lo) * n_cases)
+        self.A_ajdk = abi.calc_A_ajdk(A_p)
+        mask = np.zeros(self.row_bytes, np.uint8)
+        mask[: ncols // 8] = 0xFF
+        if ncols % 8:
+            mask[ncols // 8] = (0xFF << (8 - ncols % 8)) & 0xFF
+        self.mask_host = mask
+        self.mask = torch.from_numpy(mask).to(device)
+        self.D = torch.from_numpy(self.A_ajdk[AJDK_0_1 * self.P:(AJDK_0_1 + 1) * self.P].copy()).to(device)
+        a0 = a2 = 0.0
+        for nc in range(self.P):
+            c = float(np.unpackbits(mask[nc * 240:(nc + 1) * 240]).sum())
+            a0 += self.A_ajdk[nc + AJDK_0_1 * self.P] * c
+            a2 += self.A_ajdk[nc + AJDK_2_1 * self.P] * c
+        self.a0d1, self.a2d1 = a0, a2
+        self.lib = load()
+        self.lib.lakgb_gram_device.argtypes = [C.POINTER(GramArgs)]
+        self.lib.lakgb_gram_device.restype = C.c_int
+        self.lf11 = {}
+        self.lf11_host = {}
+        for nb in range(nbins):
+            for key, W in (("A", self.A[nb]), ("Z", self.Z[nb])):
+                v = self._row_terms(W)
+                self.lf11_host[(key, nb)] = v
+                self.lf11[(key, nb)] = torch.from_numpy(v).to(device)
+        self.rows = {}
+        for nb in range(nbins):
+            for key, W in (("A", self.A[nb]), ("Z", self.Z[nb])):
+                self.rows[(key, nb)] = torch.arange(W.shape[0], dtype=torch.int32, device=device)
+        self.args = []
+        for kind, nb1, nb2, sym in products(nbins):
+            W1 = self.A[nb1]
+            zkey = ("Z", nb2) if kind == "AnZt" else ("A", nb2)
+            W2 = self.Z[nb2] if kind == "AnZt" else self.A[nb2]
+            a = GramArgs()
+            a.wA = W1.data_ptr(); a.a_rowb = self.rows[("A", nb1)].data_ptr()
+            a.nA = W1.shape[0]; a.a_row_bytes = self.row_bytes
+            a.wZ = W2.data_ptr(); a.z_rowb = self.rows[zkey].data_ptr()
+            a.nZ = W2.shape[0]; a.z_row_bytes = self.row_bytes
+            a.mask = self.mask.data_ptr(); a.P = self.P
+            a.D = self.D.data_ptr(); a.type_flag = abi.TYPE_pm
+            a.a0d1, a.a2d1 = self.a0d1, self.a2d1
+            a.lfA = self.lf11[("A", nb1)].data_ptr(); a.lfZ = self.lf11[zkey].data_ptr()
+            a.out_r = self.rows[("A", nb1)].data_ptr(); a.out_c = self.rows[zkey].data_ptr()
+            a.out_r2 = self.rows[zkey].data_ptr(); a.out_c2 = self.rows[("A", nb1)].data_ptr()
+            a.out_stride = W1.shape[0]; a.symmetric = int(sym)
+            self.args.append(((kind, nb1, nb2, sym), a, W1.shape[0] * W2.shape[0]))
+        self.max_out = max(n for _, _, n in self.args)
+        self.out = torch.empty(self.max_out, dtype=torch.float64, device=device)
+        self.out2 = None
+
+    def _row_terms(self, W):
+        """AJDK_1_1 row terms of packed rows W through wrap_An_ajdk_v."""
+        lib = self.lib
+        w = W.cpu().numpy()
+        M = abi.MHandle(None, wX=w, nrows=w.shape[0], ncols=self.ncols)
+        out = C.POINTER(abi.L_handle)()
+        lib.wrap_An_ajdk_v(C.byref(C.c_int(0)), None, None, abi.TYPE_pm, abi.SPACING_b, M.ptr,
+                           self.A_ajdk.ctypes.data_as(C.POINTER(C.c_double)), C.byref(out))
+        n = M.rpop_b * abi.AJDK_TOT
+        v = np.ctypeslib.as_array(C.cast(out.contents.lf, C.POINTER(C.c_double)), shape=(n,)).copy()
+        return np.ascontiguousarray(v[np.arange(M.rpop_b) + AJDK_1_1 * M.rpop_b])
+
+    def work_bitops(self) -> float:
+        return float(sum(n for _, _, n in self.args)) * float(self.ncols)
+
+    def run(self, stream_handle=0, out=None):
+        """One pass; every product writes into the same output buffer."""
+        out = self.out if out is None else out
+        for _, a, _ in self.args:
+            a.stream = stream_handle
+            a.out = out.data_ptr()
+            if self.lib.lakgb_gram_device(C.byref(a)) != 0:
+                raise RuntimeError("lakgb_gram_device failed")
+
+    def _host_entry(self, kind, nb1, nb2, i, k):
+        """One output entry recomputed on the host (reference order)."""
+        ra = self.A[nb1][i].cpu().numpy()
+        rz = (self.Z[nb2] if kind == "AnZt" else self.A[nb2])[k].cpu().numpy()
+        x = np.unpackbits(ra ^ rz) & np.unpackbits(self.mask_host)
+        acc = 0.0
+        D = self.A_ajdk[AJDK_0_1 * self.P:(AJDK_0_1 + 1) * self.P]
+        for b in range(self.P):
+            c = float(x[b * 1920:(b + 1) * 1920].sum())
+            acc = acc + float(D[b]) * c
+        zkey = ("Z", nb2) if kind == "AnZt" else ("A", nb2)
+        o = self.a0d1 - 2.0 * acc
+        return o - ((float(self.lf11_host[("A", nb1)][i]) + float(self.lf11_host[zkey][k])) - self.a2d1)
+
+    def run_checks(self, samples_per_product=4, seed=0):
+        """Both kernels on every product: identical outputs; sampled entries
+        equal to the host recomputation.  Returns a summary dict."""
+        torch = self.torch
+        rng = np.random.default_rng(seed)
+        self.lib.lakgb_set_gram_impl.argtypes = [C.c_int]
+        self.lib.lakgb_gram_impl.restype = C.c_int
+        self.lib.lakgb_device_status.restype = C.c_int
+        before = self.lib.lakgb_gram_impl()
+        out_t = torch.empty(self.max_out, dtype=torch.float64, device=self.out.device)
+        out_p = torch.empty_like(out_t)
+        identical, sampled, sample_ok = 0, 0, 0
+        try:
+            for (kind, nb1, nb2, sym), a, n in self.args:
+                res = {}
+                for impl, buf in ((TENSOR, out_t), (POPCOUNT, out_p)):
+                    buf.zero_()
+                    self.lib.lakgb_set_gram_impl(impl)
+                    a.stream = 0
+                    a.out = buf.data_ptr()
+                    if self.lib.lakgb_gram_device(C.byref(a)) != 0:
+                        raise RuntimeError("lakgb_gram_device failed")
+                torch.cuda.synchronize()
+                if torch.equal(out_t[:n].view(torch.int64), out_p[:n].view(torch.int64)):
+                    identical += 1
+                nA = a.nA
+                for _ in range(samples_per_product):
+                    i = int(rng.integers(0, a.nA))
+                    k = int(rng.integers(i if sym else 0, a.nZ))
+                    got = float(out_t[i + k * nA].item())
+                    want = self._host_entry(kind, nb1, nb2, i, k)
+                    sampled += 1
+                    sample_ok += int(np.float64(got).view(np.uint64) == np.float64(want).view(np.uint64))
+        finally:
+            self.lib.lakgb_set_gram_impl(before)
+        return {"products": len(self.args), "tensor_equals_popcount": identical, "sampled_entries": sampled,
+                "sampled_equal_host": sample_ok, "device_status": self.lib.lakgb_device_status()}

@@ -419,6 +419,9 @@ def run_gpu(args):
             line["cpu_baseline"] = cpu
         if large is not None:
             line["large_gram_pass"] = large
+        buf = C.create_string_buffer(1 << 16)
+        lib.lakgb_gram_autotune_table(buf, len(buf))
+        line["gram_autotune"] = json.loads(buf.value.decode() or "[]")
         if solves is not None:
             line["solves"] = solves
         print(json.dumps(line), flush=True)

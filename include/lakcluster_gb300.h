@@ -352,15 +352,27 @@ unsigned long long lakgb_kernel_launches(void);
  * events on the launching stream. */
 double lakgb_last_gram_ms(void);
 /* Kernel of the +/-1 Gram (AnZt_vv / AnAt_vv and the Grams inside the bcc
- * solve): LAKGB_GRAM_TENSOR (default) runs the integer counts on the tcgen05
- * tensor cores, LAKGB_GRAM_POPCOUNT on the CUDA cores' popcount; both give
- * bit-identical outputs.  Process-wide. */
+ * solve): LAKGB_GRAM_TENSOR runs the integer counts on the tcgen05 tensor
+ * cores, LAKGB_GRAM_POPCOUNT on the CUDA cores' popcount, LAKGB_GRAM_AUTO
+ * (default) chooses per shape class by measurement; all give bit-identical
+ * outputs.  Process-wide. */
 #define LAKGB_IMPL_POPCOUNT 0
 #define LAKGB_IMPL_TENSOR 1
+#define LAKGB_IMPL_AUTO 2
 #define LAKGB_GRAM_POPCOUNT LAKGB_IMPL_POPCOUNT
 #define LAKGB_GRAM_TENSOR LAKGB_IMPL_TENSOR
+#define LAKGB_GRAM_AUTO LAKGB_IMPL_AUTO
 void lakgb_set_gram_impl(int impl);
 int lakgb_gram_impl(void);
+/* LAKGB_GRAM_AUTO (the default) picks the Gram kernel and tile shape by
+ * measurement: the first launch of each shape class (type, symmetric, log2 of
+ * the A rows, Z rows and blocks) runs every candidate -- the tensor-core
+ * kernel and three tile shapes of the popcount kernel, all bit-identical --
+ * timed with CUDA events, and the fastest serves that class afterwards.
+ * lakgb_gram_autotune_table writes the table as JSON into buf (returns its
+ * full length); lakgb_gram_autotune_reset clears it. */
+int lakgb_gram_autotune_table(char *buf, int buf_len);
+void lakgb_gram_autotune_reset(void);
 /* Kernel of the bit-plane loop product (wrap_At_T_YnWt_S_Zn_ww__run):
  * LAKGB_IMPL_TENSOR (default; B_MLT of 8, 16 or 32, otherwise the CUDA-core
  * kernel runs) or LAKGB_IMPL_POPCOUNT; bit-identical outputs.  Process-wide. */

@@ -14,7 +14,13 @@
 // shared memory (row pitch 61 words: conflict-free column reads), every
 // thread accumulates a TM x TN micro-tile of integer counts over the block's
 // 60 words, then folds them into FP64 accumulators with the block weight.
+#include <string.h>
+
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 
 #include "gram.cuh"
 #include "lakgb_runtime.cuh"
@@ -151,25 +157,145 @@ void launch_tile(const GramParams &p) {
 
 }  // namespace
 
-std::atomic<int> g_gram_impl{LAKGB_GRAM_TENSOR};
+// ---------------------------------------------------------------------------
+// Kernel choice.  Every candidate computes the same outputs bit for bit, so
+// the choice is a matter of speed only.  With LAKGB_IMPL_AUTO (the default)
+// the first launch of each shape class -- (type, symmetric, log2 of the A
+// rows, of the Z rows and of the blocks) -- runs every candidate on its real
+// arguments, timed with CUDA events on the launching stream, and the fastest
+// is used for that class from then on.
+
+enum GramVariant { kTensor = 0, kPopc128x64, kPopc64x64, kPopc64x128, kNumVariants };
+const char *const kVariantName[kNumVariants] = {"tensor_128x128", "popcount_128x64", "popcount_64x64",
+                                                "popcount_64x128"};
+
+void launch_variant(int v, const GramParams &p, cudaStream_t s) {
+  GramParams q = p;
+  q.stream = s;
+  if (v == kTensor) {
+    launch_gram_tc(q, s);
+  } else if (q.type == 1) {
+    if (v == kPopc128x64) launch_tile<128, 64, 8, 4, 1>(q);
+    else if (v == kPopc64x64) launch_tile<64, 64, 4, 4, 1>(q);
+    else launch_tile<64, 128, 4, 8, 1>(q);
+  } else {
+    if (v == kPopc128x64) launch_tile<128, 64, 8, 4, 2>(q);
+    else if (v == kPopc64x64) launch_tile<64, 64, 4, 4, 2>(q);
+    else launch_tile<64, 128, 4, 8, 2>(q);
+  }
+}
+
+inline int log2_bucket(long long n) {
+  int b = 0;
+  while ((1ll << b) < n) ++b;
+  return b;
+}
+
+struct TuneKey {
+  int type, sym, la, lz, lp;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(type, sym, la, lz, lp) < std::tie(o.type, o.sym, o.la, o.lz, o.lp);
+  }
+};
+
+struct TuneEntry {
+  int choice;
+  float ms[kNumVariants];
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune;
+
+int tuned_variant(const GramParams &p, cudaStream_t s, bool *ran) {
+  const TuneKey key{p.type, p.symmetric ? 1 : 0, log2_bucket(p.nA), log2_bucket(p.nZ), log2_bucket(p.P)};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second.choice;
+  }
+  // Measure every candidate on this launch; each overwrites the same output
+  // elements with the same values, so the call's result is unaffected.
+  TuneEntry e{};
+  cudaEvent_t ev[kNumVariants + 1];
+  for (auto &x : ev) LAKGB_CUDA(cudaEventCreate(&x));
+  LAKGB_CUDA(cudaEventRecord(ev[0], s));
+  for (int v = 0; v < kNumVariants; ++v) {
+    launch_variant(v, p, s);
+    LAKGB_CUDA(cudaEventRecord(ev[v + 1], s));
+  }
+  LAKGB_CUDA(cudaEventSynchronize(ev[kNumVariants]));
+  int best = 0;
+  for (int v = 0; v < kNumVariants; ++v) {
+    LAKGB_CUDA(cudaEventElapsedTime(&e.ms[v], ev[v], ev[v + 1]));
+    if (e.ms[v] < e.ms[best]) best = v;
+  }
+  for (auto &x : ev) LAKGB_CUDA(cudaEventDestroy(x));
+  e.choice = best;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.emplace(key, e);
+  }
+  *ran = true;
+  return best;
+}
+
+std::atomic<int> g_gram_impl{LAKGB_IMPL_AUTO};
 
 void launch_gram(const GramParams &p) {
   if (p.nA <= 0 || p.nZ <= 0 || p.P <= 0) return;
   cudaStream_t s = p.stream ? p.stream : stream();
   gram_timer_begin(s);
-  if (g_gram_impl.load(std::memory_order_relaxed) == LAKGB_GRAM_TENSOR)
-    launch_gram_tc(p, s);
-  else if (p.type == 1)
-    launch_tile<128, 64, 8, 4, 1>(p);
-  else
-    launch_tile<128, 64, 8, 4, 2>(p);
+  const int impl = g_gram_impl.load(std::memory_order_relaxed);
+  if (impl == LAKGB_IMPL_TENSOR) {
+    launch_variant(kTensor, p, s);
+  } else if (impl == LAKGB_IMPL_POPCOUNT) {
+    launch_variant(kPopc128x64, p, s);
+  } else {
+    bool ran = false;
+    const int v = tuned_variant(p, s, &ran);
+    if (!ran) launch_variant(v, p, s);
+  }
   gram_timer_end(s);
 }
 
 }  // namespace lakgb
 
 extern "C" void lakgb_set_gram_impl(int impl) {
-  lakgb::g_gram_impl.store(impl == LAKGB_GRAM_POPCOUNT ? LAKGB_GRAM_POPCOUNT : LAKGB_GRAM_TENSOR);
+  lakgb::g_gram_impl.store(impl == LAKGB_IMPL_POPCOUNT ? LAKGB_IMPL_POPCOUNT
+                                                       : (impl == LAKGB_IMPL_TENSOR ? LAKGB_IMPL_TENSOR
+                                                                                    : LAKGB_IMPL_AUTO));
+}
+
+extern "C" int lakgb_gram_autotune_table(char *buf, int buf_len) {
+  using namespace lakgb;
+  std::string out = "[";
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    bool first = true;
+    for (const auto &kv : g_tune) {
+      char line[512];
+      int n = snprintf(line, sizeof line, "%s{\"type\":%d,\"symmetric\":%d,\"log2_rows_a\":%d,\"log2_rows_z\":%d,"
+                       "\"log2_blocks\":%d,\"choice\":\"%s\",\"ms\":{",
+                       first ? "" : ",", kv.first.type, kv.first.sym, kv.first.la, kv.first.lz, kv.first.lp,
+                       kVariantName[kv.second.choice]);
+      for (int v = 0; v < kNumVariants; ++v)
+        n += snprintf(line + n, sizeof line - n, "%s\"%s\":%.4f", v ? "," : "", kVariantName[v], kv.second.ms[v]);
+      snprintf(line + n, sizeof line - n, "}}");
+      out += line;
+      first = false;
+    }
+  }
+  out += "]";
+  if (buf && buf_len > 0) {
+    strncpy(buf, out.c_str(), (size_t)buf_len - 1);
+    buf[buf_len - 1] = 0;
+  }
+  return (int)out.size();
+}
+
+extern "C" void lakgb_gram_autotune_reset(void) {
+  std::lock_guard<std::mutex> lk(lakgb::g_tune_mu);
+  lakgb::g_tune.clear();
 }
 
 extern "C" int lakgb_gram_impl(void) { return lakgb::g_gram_impl.load(); }

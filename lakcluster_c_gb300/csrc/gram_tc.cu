@@ -113,22 +113,39 @@ __device__ __forceinline__ double twice(double x) {
   return (e >= 1 && e <= 2045) ? __longlong_as_double(bits + (1ll << 52)) : __dmul_rn(2.0, x);
 }
 
-// Tile order shared by every role: tile i of the CTA's sequence is
-// blockIdx.x + i*gridDim.x in row-major (A tile row, Z tile column) order;
-// tiles wholly below the diagonal of a symmetric Gram are skipped.
+// Tile order shared by every role: tile k of the launch's list goes to CTA
+// k % gridDim.x.  The list is every (A tile row, Z tile column) pair in
+// row-major order, or, for a symmetric Gram (square tile grid), only the
+// pairs on or above the diagonal -- so the active tiles, not all tiles, are
+// spread evenly over the CTAs.
 struct TileWalk {
-  int ntn, ntiles, tile;
-  __device__ TileWalk(const GramParams &p)
-      : ntn((p.nZ + kBN - 1) / kBN), ntiles(((p.nA + kBM - 1) / kBM) * ((p.nZ + kBN - 1) / kBN)),
-        tile((int)blockIdx.x - (int)gridDim.x) {}
+  int ntn, ntiles, k;
+  bool tri;
+  __device__ TileWalk(const GramParams &p) : ntn((p.nZ + kBN - 1) / kBN), k((int)blockIdx.x - (int)gridDim.x) {
+    const int ntm = (p.nA + kBM - 1) / kBM;
+    tri = p.symmetric && ntm == ntn;
+    ntiles = tri ? ntn * (ntn + 1) / 2 : ntm * ntn;
+  }
   __device__ bool next(const GramParams &p, int &tile_m, int &tile_n) {
-    for (;;) {
-      tile += gridDim.x;
-      if (tile >= ntiles) return false;
-      tile_m = (tile / ntn) * kBM;
-      tile_n = (tile % ntn) * kBN;
-      if (!(p.symmetric && tile_m > tile_n + kBN - 1)) return true;
+    if (!tri) {
+      for (;;) {  // a symmetric call with unequal row counts: skip tiles below the diagonal
+        k += gridDim.x;
+        if (k >= ntiles) return false;
+        tile_m = (k / ntn) * kBM;
+        tile_n = (k % ntn) * kBN;
+        if (!(p.symmetric && tile_m > tile_n + kBN - 1)) return true;
+      }
     }
+    k += gridDim.x;
+    if (k >= ntiles) return false;
+    int i = 0, r = k;
+    while (r >= ntn - i) {  // row i of the upper triangle holds ntn - i tiles
+      r -= ntn - i;
+      ++i;
+    }
+    tile_m = i * kBM;
+    tile_n = (i + r) * kBN;
+    return true;
   }
 };
 
@@ -397,14 +414,11 @@ int sm_count() {
   return n;
 }
 
-// Tiles a launch computes (symmetric Grams skip the tiles below the diagonal).
+// Tiles a launch computes (symmetric Grams: the tiles on or above the
+// diagonal of the square tile grid).
 int active_tiles(const GramParams &p) {
   const int ntm = (p.nA + kBM - 1) / kBM, ntn = (p.nZ + kBN - 1) / kBN;
-  if (!p.symmetric) return ntm * ntn;
-  int n = 0;
-  for (int i = 0; i < ntm; ++i)
-    for (int j = 0; j < ntn; ++j) n += !(i * kBM > j * kBN + kBN - 1);
-  return n;
+  return (p.symmetric && ntm == ntn) ? ntn * (ntn + 1) / 2 : ntm * ntn;
 }
 
 template <int TYPE>

@@ -107,3 +107,26 @@ def test_host_buffer_rewritten_in_place(impl_switch, oracle_lib):
         got = kc.call_gram("gpu", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
         assert not _bits_equal(first, want)
         assert _bits_equal(got, want), impl
+
+
+def test_autotuned_dispatch_matches_oracle(impl_switch, oracle_lib):
+    """LAKGB_GRAM_AUTO: the first launch of a shape class times every
+    candidate; results equal the oracle's before and after the class is
+    tuned, and the table records a choice with a time per candidate."""
+    import json
+    lib = impl_switch
+    lib.lakgb_set_gram_impl(2)
+    lib.lakgb_gram_autotune_reset()
+    rng = np.random.default_rng(4242)
+    MA, MZ = _case(rng, 333, 222, 4000, False)
+    A_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(4000)))
+    want = kc.call_gram("oracle", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
+    for _ in range(2):
+        got = kc.call_gram("gpu", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
+        assert _bits_equal(got, want)
+        assert lib.lakgb_device_status() == 0
+    buf = C.create_string_buffer(1 << 14)
+    lib.lakgb_gram_autotune_table(buf, len(buf))
+    table = json.loads(buf.value.decode())
+    assert len(table) == 1
+    assert table[0]["choice"] in table[0]["ms"] and len(table[0]["ms"]) == 4

@@ -293,6 +293,9 @@ int lakgb_gram_device(const struct lakgb_gram_args *args);
  * when both handles are mirrored.  The bcc solve mirrors its Gram matrices
  * (AnZt, AnAt and their low-rank updates) for the whole solve. */
 void lakgb_L_mirror(struct L_handle *L);
+/* lakgb_L_mirror for an L whose values are all zero (e.g. just allocated):
+ * the device copy is zero-filled instead of uploaded. */
+void lakgb_L_mirror_zero(struct L_handle *L);
 void lakgb_L_release_mirror(struct L_handle *L);
 void lakgb_L_to_host(struct L_handle *L);
 void lakgb_L_sub(struct L_handle *dst, const struct L_handle *src);
@@ -351,6 +354,11 @@ unsigned long long lakgb_kernel_launches(void);
 /* Device time (ms) of the most recent Gram kernel launch, timed with CUDA
  * events on the launching stream. */
 double lakgb_last_gram_ms(void);
+/* Per-entry-point call counts and wall seconds (host clock, each call's own
+ * synchronisations included) as JSON, collected only when the environment
+ * sets LAKGB_PROFILE_CALLS; returns the full length.  Reset clears them. */
+int lakgb_call_profile(char *buf, int buf_len);
+void lakgb_call_profile_reset(void);
 /* Kernel of the +/-1 Gram (AnZt_vv / AnAt_vv and the Grams inside the bcc
  * solve): LAKGB_GRAM_TENSOR runs the integer counts on the tcgen05 tensor
  * cores, LAKGB_GRAM_POPCOUNT on the CUDA cores' popcount, LAKGB_GRAM_AUTO

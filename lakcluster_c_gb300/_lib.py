@@ -44,6 +44,8 @@ def load() -> C.CDLL:
     lib.lakgb_set_gram_impl.argtypes = [C.c_int]
     lib.lakgb_gram_impl.restype = C.c_int
     lib.lakgb_device_status.restype = C.c_int
+    lib.lakgb_call_profile.argtypes = [C.c_char_p, C.c_int]
+    lib.lakgb_call_profile.restype = C.c_int
     lib.lakgb_gram_autotune_table.argtypes = [C.c_char_p, C.c_int]
     lib.lakgb_gram_autotune_table.restype = C.c_int
     lib.lakgb_set_bitplane_impl.argtypes = [C.c_int]

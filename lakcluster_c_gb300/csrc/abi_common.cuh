@@ -93,6 +93,7 @@ inline DBuf upload_vec(const std::vector<T> &v) {
 }
 
 inline void copy_back(double *host, const DBuf &dev, unsigned long long length, HostOutputFill *fill = nullptr) {
+  LAKGB_PROFILE_CALL("(copy back + sync)");
   if (fill) fill->copied = true;
   if (length) LAKGB_CUDA(cudaMemcpyAsync(host, dev.p, length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
   LAKGB_CUDA(cudaStreamSynchronize(stream()));

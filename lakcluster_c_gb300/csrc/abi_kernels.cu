@@ -124,6 +124,7 @@ extern "C" int wrap_AnZt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, i
                                  int output_spacing_r, int output_spacing_c, M_handle *M_An,
                                  M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk,
                                  L_handle *lf_Zn_ajdk, L_handle **output_AnZt_p) {
+  LAKGB_PROFILE_CALL("wrap_AnZt_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   return gram_entry(false, type_flag, output_spacing_r, output_spacing_c, M_An, M_Zn, A_ajdk,
                     lf_An_ajdk, lf_Zn_ajdk, output_AnZt_p, "wrap_AnZt_vv__run");
@@ -133,6 +134,7 @@ extern "C" int wrap_AnAt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, i
                                  int output_spacing_r, int output_spacing_c, M_handle *M_An,
                                  M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk,
                                  L_handle *lf_Zn_ajdk, L_handle **output_AnAt_p) {
+  LAKGB_PROFILE_CALL("wrap_AnAt_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   return gram_entry(true, type_flag, output_spacing_r, output_spacing_c, M_An, M_Zn, A_ajdk,
                     lf_An_ajdk, lf_Zn_ajdk, output_AnAt_p, "wrap_AnAt_vv__run");
@@ -140,6 +142,7 @@ extern "C" int wrap_AnAt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, i
 
 extern "C" int wrap_An_v__run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
                               int output_spacing_r, M_handle *M_An, L_handle **output_An_v_p) {
+  LAKGB_PROFILE_CALL("wrap_An_v__run");
   (void)tidx; (void)vpra; (void)thread_in;
   const unsigned long long length = spacing_length(output_spacing_r, M_An);
   L_handle *out = ensure_output(output_An_v_p, length, "wrap_An_v__run");
@@ -172,6 +175,7 @@ extern "C" int wrap_An_v__run(int *tidx, void **vpra, pthread_t *thread_in, int 
 extern "C" int wrap_An_ajdk_v(int *tidx, void **vpra, pthread_t *thread_in, int type_flag,
                               int output_spacing_r, M_handle *M_An, double *A_ajdk,
                               L_handle **output_An_ajdk_p) {
+  LAKGB_PROFILE_CALL("wrap_An_ajdk_v");
   (void)tidx; (void)vpra; (void)thread_in;
   const unsigned long long length_r = spacing_length(output_spacing_r, M_An);
   const unsigned long long length = length_r * LAKGB_AJDK_TOT;

@@ -148,6 +148,16 @@ struct State {
     hooks->L_mirror(L);
     mirrored.push_back(L);
   }
+  // Mirror a freshly allocated (all-zero) L without uploading it.
+  void mirror_zero(L_handle *L) {
+    if (!hooks || !hooks->L_mirror || !L) return;
+    if (std::find(mirrored.begin(), mirrored.end(), L) != mirrored.end()) return;
+    if (hooks->L_mirror_zero)
+      hooks->L_mirror_zero(L);
+    else
+      hooks->L_mirror(L);
+    mirrored.push_back(L);
+  }
   void to_host(L_handle *L) {
     if (hooks && hooks->L_to_host && L) hooks->L_to_host(L);
   }
@@ -491,8 +501,9 @@ int load(State &S, const Input &I, std::string &err) {
       F->QR_AnZtSZnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
       F->QR_AnAtTAnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
       F->QC_AtTAnZtSZn = S.L(AT); F->QC_AtTAnAtTAn = S.L(AT);
-      S.mirror(F->lf_AnZt); S.mirror(F->lf_AnAt); S.mirror(F->lf_jnvt); S.mirror(F->lf_jnjt);
-      S.mirror(F->lf_knzt); S.mirror(F->lf_hnvt); S.mirror(F->lf_ankt); S.mirror(F->lf_knat); S.mirror(F->lf_knkt);
+      S.mirror_zero(F->lf_AnZt); S.mirror_zero(F->lf_AnAt); S.mirror_zero(F->lf_jnvt); S.mirror_zero(F->lf_jnjt);
+      S.mirror_zero(F->lf_knzt); S.mirror_zero(F->lf_hnvt); S.mirror_zero(F->lf_ankt); S.mirror_zero(F->lf_knat);
+      S.mirror_zero(F->lf_knkt);
       S.F[nb1 + nb2 * S.nbins] = std::move(F);
     }
   }

@@ -62,6 +62,9 @@ struct Hooks {
   void (*L_to_host)(L_handle *L) = nullptr;
   void (*L_sub)(L_handle *dst, const L_handle *src) = nullptr;
   void (*L_transpose)(L_handle *dst, const L_handle *src) = nullptr;
+  // As L_mirror for an L whose values are all zero (freshly allocated): the
+  // device copy is zero-filled, nothing is uploaded.  Null: L_mirror is used.
+  void (*L_mirror_zero)(L_handle *L) = nullptr;
 };
 
 // Parse a reference .in file (updateglobals.c syntax) and load its .b16 files.

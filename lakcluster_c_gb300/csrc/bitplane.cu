@@ -324,6 +324,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
                                            int spacing_t, M_handle *M_At, M_handle *M_Tt, M_handle *M_Yn,
                                            M_handle *M_Wn, M_handle *M_St, M_handle *M_Zt, double *A_ajdk,
                                            M_handle *M_YnWt, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_At_T_YnWt_S_Zn_ww__run");
   (void)tidx; (void)vpra; (void)thread_in; (void)M_Yn;
   const unsigned long long length_a = spacing_length(spacing_a, M_At);
   const unsigned long long length_t = spacing_length(spacing_t, M_Tt);
@@ -428,6 +429,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
 extern "C" int wrap_An_ZtSn_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a, int spacing_s,
                                     M_handle *M_An, L_handle *lf_ZtSn, M_handle *M_ZtSn, M_handle *M_St,
                                     L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_An_ZtSn_ww__run");
   (void)tidx; (void)vpra; (void)thread_in; (void)lf_ZtSn;
   const unsigned long long length_a = spacing_length(spacing_a, M_An);
   const unsigned long long length_s = spacing_length(spacing_s, M_St);

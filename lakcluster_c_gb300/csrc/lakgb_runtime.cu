@@ -6,8 +6,10 @@
 #include <string.h>
 
 #include <atomic>
+#include <chrono>
 #include <map>
 #include <mutex>
+#include <string>
 #include <utility>
 
 namespace lakgb {
@@ -107,6 +109,7 @@ void Stager::begin() {
 }
 
 const void *Stager::put_bytes(const void *h, size_t n) {
+  LAKGB_PROFILE_CALL("(stage copy)");
   Arena &a = arena();
   const size_t off = (a.used + 255) & ~(size_t)255;
   if (!active_ || off + n > a.cap || n >= kDirectUploadBytes) {
@@ -123,6 +126,7 @@ const void *Stager::put_bytes(const void *h, size_t n) {
 }
 
 void Stager::flush() {
+  LAKGB_PROFILE_CALL("(staged upload)");
   Arena &a = arena();
   if (t_active == this) t_active = nullptr;
   if (!active_) return;
@@ -137,12 +141,14 @@ void Stager::flush() {
 void count_launch(unsigned long long n) { g_launches += n; }
 
 void *dalloc(size_t bytes) {
+  LAKGB_PROFILE_CALL("(device alloc)");
   void *p = nullptr;
   LAKGB_CUDA(cudaMallocAsync(&p, bytes, stream()));
   return p;
 }
 
 void dfree(void *p) {
+  LAKGB_PROFILE_CALL("(device free)");
   if (p) LAKGB_CUDA(cudaFreeAsync(p, stream()));
 }
 
@@ -218,6 +224,45 @@ ResidencyScope::~ResidencyScope() {
   t_scope_keys.clear();
 }
 
+namespace {
+bool profile_calls_on() {
+  static const bool on = [] {
+    const char *e = getenv("LAKGB_PROFILE_CALLS");
+    return e && *e && *e != '0';
+  }();
+  return on;
+}
+long long now_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+struct CallStat {
+  long long calls = 0, ns = 0, self_ns = 0;
+};
+std::mutex g_call_mu;
+std::map<std::string, CallStat> g_calls;
+thread_local long long t_child_ns = 0;  // time of the calls nested in the open one
+}  // namespace
+
+CallTimer::CallTimer(const char *n) : name(n), t0(0) {
+  if (!profile_calls_on()) return;
+  saved = t_child_ns;
+  t_child_ns = 0;
+  t0 = now_ns();
+}
+
+CallTimer::~CallTimer() {
+  if (!t0) return;
+  const long long dt = now_ns() - t0;
+  const long long self = dt - t_child_ns;
+  t_child_ns = saved + dt;
+  std::lock_guard<std::mutex> lk(g_call_mu);
+  CallStat &c = g_calls[name];
+  c.calls += 1;
+  c.ns += dt;
+  c.self_ns += self;
+}
+
 void gram_timer_begin(cudaStream_t s) {
   if (!g_ev0) {
     LAKGB_CUDA(cudaEventCreate(&g_ev0));
@@ -281,6 +326,32 @@ extern "C" void lakgb_forget_host_buffer(const void *host_ptr) {
 }
 
 extern "C" unsigned long long lakgb_kernel_launches(void) { return g_launches.load(); }
+
+extern "C" int lakgb_call_profile(char *buf, int buf_len) {
+  std::string out = "{";
+  {
+    std::lock_guard<std::mutex> lk(g_call_mu);
+    bool first = true;
+    for (const auto &kv : g_calls) {
+      char line[256];
+      snprintf(line, sizeof line, "%s\"%s\":{\"calls\":%lld,\"seconds\":%.6f,\"self_seconds\":%.6f}",
+               first ? "" : ",", kv.first.c_str(), kv.second.calls, kv.second.ns * 1e-9, kv.second.self_ns * 1e-9);
+      out += line;
+      first = false;
+    }
+  }
+  out += "}";
+  if (buf && buf_len > 0) {
+    strncpy(buf, out.c_str(), (size_t)buf_len - 1);
+    buf[buf_len - 1] = 0;
+  }
+  return (int)out.size();
+}
+
+extern "C" void lakgb_call_profile_reset(void) {
+  std::lock_guard<std::mutex> lk(g_call_mu);
+  g_calls.clear();
+}
 
 extern "C" double lakgb_last_gram_ms(void) {
   if (!g_ev_pending) return 0.0;

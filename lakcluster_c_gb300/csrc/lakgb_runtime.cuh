@@ -122,6 +122,20 @@ DBuf upload_bytes(const void *h, size_t n);
 // residency off the buffer is simply released.
 void resident_put(const void *host, size_t bytes, DBuf &&d);
 
+// Per-entry-point call counts and wall time (host clock, the call's own
+// synchronisations included), collected when LAKGB_PROFILE_CALLS is set in
+// the environment; read with lakgb_call_profile.
+struct CallTimer {
+  const char *name;
+  long long t0;
+  long long saved = 0;
+  explicit CallTimer(const char *n);
+  ~CallTimer();
+  CallTimer(const CallTimer &) = delete;
+  CallTimer &operator=(const CallTimer &) = delete;
+};
+#define LAKGB_PROFILE_CALL(name) ::lakgb::CallTimer lakgb_call_timer_(name)
+
 // Events bracketing the most recent Gram launch.
 void gram_timer_begin(cudaStream_t s);
 void gram_timer_end(cudaStream_t s);

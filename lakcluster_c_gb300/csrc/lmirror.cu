@@ -60,6 +60,7 @@ Mirror *find_mirror(const L_handle *L) {
 using namespace lakgb;
 
 extern "C" void lakgb_L_mirror(L_handle *L) {
+  LAKGB_PROFILE_CALL("lakgb_L_mirror");
   if (!L || find_mirror(L)) return;
   Mirror m{};
   m.n = L->length;
@@ -71,7 +72,21 @@ extern "C" void lakgb_L_mirror(L_handle *L) {
   g_mirrors[L] = m;
 }
 
+extern "C" void lakgb_L_mirror_zero(L_handle *L) {
+  LAKGB_PROFILE_CALL("lakgb_L_mirror_zero");
+  if (!L || find_mirror(L)) return;
+  Mirror m{};
+  m.n = L->length;
+  LAKGB_CUDA(cudaMallocAsync((void **)&m.d, (m.n ? m.n : 1) * sizeof(double), stream()));
+  if (m.n) LAKGB_CUDA(cudaMemsetAsync(m.d, 0, m.n * sizeof(double), stream()));
+  LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  m.host_stale = false;
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_mirrors[L] = m;
+}
+
 extern "C" void lakgb_L_to_host(L_handle *L) {
+  LAKGB_PROFILE_CALL("lakgb_L_to_host");
   Mirror *m = find_mirror(L);
   if (!m || !m->host_stale) return;
   if (m->n) LAKGB_CUDA(cudaMemcpyAsync(L->lf, m->d, m->n * sizeof(double), cudaMemcpyDeviceToHost, stream()));
@@ -80,6 +95,7 @@ extern "C" void lakgb_L_to_host(L_handle *L) {
 }
 
 extern "C" void lakgb_L_release_mirror(L_handle *L) {
+  LAKGB_PROFILE_CALL("lakgb_L_release_mirror");
   Mirror m{};
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -92,6 +108,7 @@ extern "C" void lakgb_L_release_mirror(L_handle *L) {
 }
 
 extern "C" void lakgb_L_sub(L_handle *dst, const L_handle *src) {
+  LAKGB_PROFILE_CALL("lakgb_L_sub");
   Mirror *md = find_mirror(dst), *ms = find_mirror(src);
   const unsigned long long n = dst->length;
   if (md && ms && ms->n >= n) {
@@ -114,6 +131,7 @@ extern "C" void lakgb_L_sub(L_handle *dst, const L_handle *src) {
 }
 
 extern "C" void lakgb_L_transpose(L_handle *dst, const L_handle *src) {
+  LAKGB_PROFILE_CALL("lakgb_L_transpose");
   dst->spacing_row = src->spacing_col; dst->spacing_col = src->spacing_row; dst->spacing_lyr = src->spacing_lyr;
   dst->row_stride = src->col_stride; dst->col_stride = src->row_stride; dst->lyr_stride = src->lyr_stride;
   Mirror *md = find_mirror(dst), *ms = find_mirror(src);

@@ -208,6 +208,7 @@ using namespace lakgb;
 extern "C" int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
                                         int output_spacing_s, M_handle *M_An, M_handle *M_St, M_handle *M_Zn,
                                         L_handle *lf_AnZt, L_handle *lf_YnWt, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_AnZt_S_WnYt_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   const unsigned long long length_a = spacing_length(output_spacing_a, M_An);
   const unsigned long long length_s = spacing_length(output_spacing_s, M_St);
@@ -270,6 +271,7 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
                                            int output_spacing_s, M_handle *M_At, M_handle *M_Tt, M_handle *M_Yt,
                                            M_handle *M_Wt, M_handle *M_St, M_handle *M_Zt, double *Y_ajdk,
                                            L_handle *lf_AtTYn, L_handle *lf_ZtSWn, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_AtTYn____WtSZn_vv__run");
   (void)tidx; (void)vpra; (void)thread_in; (void)M_Tt;
   const unsigned long long length_a = spacing_length(output_spacing_a, M_At);
   const unsigned long long length_s = spacing_length(output_spacing_s, M_St);
@@ -446,6 +448,7 @@ extern "C" int wrap_AtTYn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
                                   int output_spacing_y, int output_spacing_t, M_handle *M_At, M_handle *M_Tt,
                                   M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, L_handle *lf_AtTn,
                                   L_handle *lf_YtTn, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_AtTYn_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   return attyn_entry(false, "wrap_AtTYn_vv__run", output_spacing_a, output_spacing_y, output_spacing_t, M_At, M_Tt,
                      M_Yt, A_ajdk, Y_ajdk, lf_AtTn, lf_YtTn, output_p);
@@ -455,6 +458,7 @@ extern "C" int wrap_AtTAn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, 
                                   int output_spacing_y, int output_spacing_t, M_handle *M_At, M_handle *M_Tt,
                                   M_handle *M_Yt, double *A_ajdk, double *Y_ajdk, L_handle *lf_AtTn,
                                   L_handle *lf_YtTn, L_handle **output_AtTAn_p) {
+  LAKGB_PROFILE_CALL("wrap_AtTAn_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   return attyn_entry(true, "wrap_AtTAn_vv__run", output_spacing_a, output_spacing_y, output_spacing_t, M_At, M_Tt,
                      M_Yt, A_ajdk, Y_ajdk, lf_AtTn, lf_YtTn, output_AtTAn_p);

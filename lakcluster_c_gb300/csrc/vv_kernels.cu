@@ -183,6 +183,7 @@ using namespace lakgb;
 extern "C" int wrap_At_T_YnWt_S_Zn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
                                            int output_spacing_s, M_handle *M_At, M_handle *M_Tt, M_handle *M_St,
                                            M_handle *M_Zt, double *A_ajdk, L_handle *lf_YnWt, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_At_T_YnWt_S_Zn_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   const unsigned long long la = spacing_length(output_spacing_a, M_At);
   const unsigned long long ls = spacing_length(output_spacing_s, M_St);
@@ -249,6 +250,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_vv__run(int *tidx, void **vpra, pthread_t *th
 extern "C" int wrap_An_ZtSWn_Yt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
                                         int output_spacing_s, M_handle *M_An, M_handle *M_St, M_handle *M_Yn,
                                         double *A_ajdk, double *Y_ajdk, L_handle *lf_ZtSWn, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_An_ZtSWn_Yt_vv__run");
   (void)tidx; (void)vpra; (void)thread_in;
   const unsigned long long la = spacing_length(output_spacing_a, M_An);
   const unsigned long long ls = spacing_length(output_spacing_s, M_St);

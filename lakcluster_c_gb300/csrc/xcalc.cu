@@ -265,6 +265,7 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
                            unsigned char *mr_b, unsigned char *mc_j, unsigned char *mc_b,
                            L_handle *lf_YnWt, double *YnWt, int *Yn_nrows_p, int *Wn_nrows_p,
                            M_handle **M_X_p, int *b_mlt_p, int trm_flag) {
+  LAKGB_PROFILE_CALL("wrap_xcalc");
   (void)tidx; (void)vpra; (void)thread_in;
   const int Yn_nrows = *Yn_nrows_p, Wn_nrows = *Wn_nrows_p, b_mlt = *b_mlt_p;
   if (!M_X_p || !*M_X_p) {

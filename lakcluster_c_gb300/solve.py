@@ -165,13 +165,24 @@ def main(argv=None):
     ap.add_argument("--workload", default="case_control_1024x1024x4096", choices=sorted(WORKLOADS))
     ap.add_argument("--reps", type=int, default=1)
     args = ap.parse_args(argv)
+    import json
+    import os
     A, Z, gamma = workload(args.workload)
     p = Problem(A, Z, gamma=gamma)
+    profile = os.environ.get("LAKGB_PROFILE_CALLS", "0") not in ("", "0")
     for r in range(args.reps):
+        if profile:
+            p.lib.lakgb_call_profile_reset()
         t0 = time.perf_counter()
         out = p.solve()
         print("%s rep %d: %.3f s, %d iterations, %d eliminations" %
               (args.workload, r, time.perf_counter() - t0, len(out["trace"]), len(out["xdrop_a"])), flush=True)
+        if profile:
+            buf = C.create_string_buffer(1 << 16)
+            p.lib.lakgb_call_profile(buf, len(buf))
+            for name, v in sorted(json.loads(buf.value.decode()).items(), key=lambda kv: -kv[1]["seconds"]):
+                print("  %-32s %6d calls %8.3f s (self %.3f s)" % (name, v["calls"], v["seconds"], v["self_seconds"]),
+                      flush=True)
 
 
 if __name__ == "__main__":

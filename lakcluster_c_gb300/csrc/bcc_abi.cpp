@@ -36,15 +36,25 @@ extern "C" void lakgb_bcc_problem_init(struct lakgb_bcc_problem *p) {
   p->test_sparse = 1;
 }
 
-extern "C" void lakgb_residency_scope(int enter);  // lakgb_runtime.cu
+extern "C" void lakgb_residency_scope(int enter);   // lakgb_runtime.cu
+extern "C" void lakgb_device_only_planes(int on);   // lakgb_runtime.cu
 
 namespace {
 // Device residency of the solve's matrices for the length of one solve: the
 // driver forgets each buffer it frees or rewrites, and whatever is still
-// cached when the solve ends is dropped.
+// cached when the solve ends is dropped.  Unless the solve traces its stages
+// (LAKBCC_TRACE, which digests bit planes on the host), xcalc's planes stay on
+// the device.
 struct SolveResidency {
-  SolveResidency() { lakgb_residency_scope(1); }
-  ~SolveResidency() { lakgb_residency_scope(0); }
+  SolveResidency() {
+    lakgb_residency_scope(1);
+    const char *trace = getenv("LAKBCC_TRACE");
+    lakgb_device_only_planes(!(trace && *trace));
+  }
+  ~SolveResidency() {
+    lakgb_device_only_planes(0);
+    lakgb_residency_scope(0);
+  }
 };
 }  // namespace
 

@@ -302,6 +302,17 @@ extern "C" void lakgb_set_residency(int on) {
   }
 }
 
+namespace lakgb {
+namespace {
+thread_local int t_device_only_planes = 0;
+}
+bool host_planes_wanted() { return !t_device_only_planes || !residency_enabled(); }
+}  // namespace lakgb
+
+// Inside a solve: bit planes made by wrap_xcalc stay on the device only (the
+// driver reads them through the residency cache, never on the host).
+extern "C" void lakgb_device_only_planes(int on) { lakgb::t_device_only_planes = on ? 1 : 0; }
+
 extern "C" void lakgb_residency_scope(int enter) {
   thread_local std::vector<lakgb::ResidencyScope *> scopes;
   if (enter) {

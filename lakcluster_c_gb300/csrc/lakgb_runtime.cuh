@@ -38,6 +38,10 @@ void dfree(void *p);
 const void *resident(const void *host, size_t bytes);
 bool residency_enabled();
 
+// Whether wrap_xcalc copies its bit planes back into the host M_X (always,
+// except inside a solve that does not trace its stages).
+bool host_planes_wanted();
+
 // Residency on for this thread while the object lives; cache entries this
 // thread inserts meanwhile are dropped when the outermost scope ends.
 struct ResidencyScope {

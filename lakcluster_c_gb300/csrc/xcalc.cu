@@ -392,8 +392,10 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
       LAKGB_CUDA(cudaGetLastError());
       count_launch();
     }
-    if (nbytes) LAKGB_CUDA(cudaMemcpyAsync(M_X->Ara, planes.p, nbytes, cudaMemcpyDeviceToHost, stream()));
-    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    if (host_planes_wanted()) {
+      if (nbytes) LAKGB_CUDA(cudaMemcpyAsync(M_X->Ara, planes.p, nbytes, cudaMemcpyDeviceToHost, stream()));
+      LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    }
     resident_put(M_X->Ara, nbytes, std::move(planes));
   }
   // M_X fields (xcalc.c:231-241).

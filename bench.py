@@ -284,6 +284,30 @@ def run_gpu(args):
     launches = lib.lakgb_kernel_launches() - launches0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(step_ms) / len(step_ms)
+
+    # The same pass captured once into a CUDA graph and replayed (every shape
+    # class was tuned by the warm-up steps, so nothing in it synchronises).
+    graph = None
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            dev.run(sh)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        gms = []
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            g.replay()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        gms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+        gm = sum(gms) / len(gms)
+        graph = {"ms_per_step": gm, "value": world * work / (gm / 1000.0),
+                 "note": "the seven launches of the pass captured once and replayed as one CUDA graph"}
+    except Exception as e:  # capture unsupported here: report why, keep the eager numbers
+        graph = {"unavailable": str(e)[:200]}
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -411,6 +435,7 @@ def run_gpu(args):
                 "kernel_ms": k_ms,
             },
             "device_status": device_status,
+            "cuda_graph": graph,
             "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s},
             "clocks": clocks,
@@ -494,9 +519,16 @@ def solve_measurements(args, with_cpu: bool):
     inst = synth.case_control(seed=2)
     p2 = sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05)
     t0 = time.perf_counter()
-    r2 = p2.solve()
-    s2 = time.perf_counter() - t0
-    c2 = {"seconds": s2, "solves_per_s": 1.0 / s2, "iterations": len(r2["trace"]), "reps": 1}
+    r2 = p2.solve()  # first solve of the process: includes the Gram autotuner's one-time measurements
+    first = time.perf_counter() - t0
+    t = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        r2b = p2.solve()
+        t.append(time.perf_counter() - t0)
+    s2 = statistics.median(t)
+    c2 = {"seconds": s2, "solves_per_s": 1.0 / s2, "iterations": len(r2["trace"]), "reps": len(t),
+          "first_solve_seconds": first, "repeat_identical": r2b == r2}
     if "case_control_4096x4096x16384" in golden:  # from the oracle port (reference too slow)
         g = golden["case_control_4096x4096x16384"]
         c2["matches_oracle_port"] = all(r2[k] == g[k] for k in ("trace", "xdrop_a", "xdrop_b"))
@@ -514,15 +546,15 @@ def many_solves_measurements(args):
     workers = max(2, min(16, os.cpu_count() or 2))
     out = {}
     # Batched nulls: label-shuffled case/control instances of uneven sizes.
-    n_null = 12
+    n_null = 24
     probs = []
     for i in range(n_null):
-        inst = synth.null_instance(1000 + i, rows=(1024, 8192), cols=(4096, 16384))
+        inst = synth.null_instance(1000 + i, rows=(1024, 8192), cols=(4096, 32768))
         probs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05))
     plain, t_plain = serve.solve_plain(probs)
     batched, t_batch, peak = serve.solve_batched(probs, workers=workers)
     out["batched_nulls"] = {
-        "instances": n_null, "rows": "logU[1024,8192]", "cols": "logU[4096,16384]", "workers": workers,
+        "instances": n_null, "rows": "logU[1024,8192]", "cols": "logU[4096,32768]", "workers": workers,
         "plain_solves_per_s": n_null / t_plain, "batched_solves_per_s": n_null / t_batch,
         "speedup": t_plain / t_batch, "peak_concurrency": peak, "identical_to_plain": batched == plain}
     # Served stream: Poisson arrivals at twice the plain path's throughput.

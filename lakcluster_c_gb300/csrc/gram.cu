@@ -16,6 +16,7 @@
 // 60 words, then folds them into FP64 accumulators with the block weight.
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -160,12 +161,16 @@ void launch_tile(const GramParams &p) {
 // ---------------------------------------------------------------------------
 // Kernel choice.  Every candidate computes the same outputs bit for bit, so
 // the choice is a matter of speed only.  With LAKGB_IMPL_AUTO (the default)
-// the first launch of each shape class -- (type, symmetric, log2 of the A
-// rows, of the Z rows and of the blocks) -- runs every candidate on its real
-// arguments, timed with CUDA events on the launching stream, and the fastest
-// is used for that class from then on.
+// a launch with at least kTensorRows rows on both sides takes the tensor-core
+// kernel (it wins there by 3x or more); for smaller launches the first one of
+// each shape class -- (type, symmetric, log2 of the A rows, of the Z rows and
+// of the blocks) -- runs the candidates on its real arguments, timed with CUDA
+// events on the launching stream, and the fastest serves that class from
+// then on.
 
 enum GramVariant { kTensor = 0, kPopc128x64, kPopc64x64, kPopc64x128, kNumVariants };
+constexpr int kTunedVariants = 3;   // tensor, popcount 128x64, popcount 64x64
+constexpr int kTensorRows = 512;
 const char *const kVariantName[kNumVariants] = {"tensor_128x128", "popcount_128x64", "popcount_64x64",
                                                 "popcount_64x128"};
 
@@ -207,29 +212,47 @@ std::mutex g_tune_mu;
 std::map<TuneKey, TuneEntry> g_tune;
 
 int tuned_variant(const GramParams &p, cudaStream_t s, bool *ran) {
+  if (p.nA >= kTensorRows && p.nZ >= kTensorRows) return kTensor;
   const TuneKey key{p.type, p.symmetric ? 1 : 0, log2_bucket(p.nA), log2_bucket(p.nZ), log2_bucket(p.P)};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second.choice;
   }
-  // Measure every candidate on this launch; each overwrites the same output
-  // elements with the same values, so the call's result is unaffected.
+  // Under stream capture nothing can be timed: an untuned class takes the
+  // tensor-core kernel (tune by running the launch once before capturing).
+  if (capturing(s)) return kTensor;
+  // Measure the candidates on this launch; each overwrites the same output
+  // elements with the same values, so the call's result is unaffected.  One
+  // untimed round first (first launches can carry one-time costs such as
+  // module loading), then one timed round.
   TuneEntry e{};
-  cudaEvent_t ev[kNumVariants + 1];
-  for (auto &x : ev) LAKGB_CUDA(cudaEventCreate(&x));
-  LAKGB_CUDA(cudaEventRecord(ev[0], s));
-  for (int v = 0; v < kNumVariants; ++v) {
-    launch_variant(v, p, s);
-    LAKGB_CUDA(cudaEventRecord(ev[v + 1], s));
+  for (int v = 0; v < kNumVariants; ++v) e.ms[v] = -1.f;  // not measured
+  for (int v = 0; v < kTunedVariants; ++v) launch_variant(v, p, s);
+  constexpr int kRounds = 1;
+  cudaEvent_t ev[kRounds][kTunedVariants + 1];
+  for (auto &r : ev)
+    for (auto &x : r) LAKGB_CUDA(cudaEventCreate(&x));
+  for (int r = 0; r < kRounds; ++r) {
+    LAKGB_CUDA(cudaEventRecord(ev[r][0], s));
+    for (int v = 0; v < kTunedVariants; ++v) {
+      launch_variant(v, p, s);
+      LAKGB_CUDA(cudaEventRecord(ev[r][v + 1], s));
+    }
   }
-  LAKGB_CUDA(cudaEventSynchronize(ev[kNumVariants]));
+  LAKGB_CUDA(cudaEventSynchronize(ev[kRounds - 1][kTunedVariants]));
   int best = 0;
-  for (int v = 0; v < kNumVariants; ++v) {
-    LAKGB_CUDA(cudaEventElapsedTime(&e.ms[v], ev[v], ev[v + 1]));
+  for (int v = 0; v < kTunedVariants; ++v) {
+    e.ms[v] = 1e30f;
+    for (int r = 0; r < kRounds; ++r) {
+      float ms = 0.f;
+      LAKGB_CUDA(cudaEventElapsedTime(&ms, ev[r][v], ev[r][v + 1]));
+      e.ms[v] = std::min(e.ms[v], ms);
+    }
     if (e.ms[v] < e.ms[best]) best = v;
   }
-  for (auto &x : ev) LAKGB_CUDA(cudaEventDestroy(x));
+  for (auto &r : ev)
+    for (auto &x : r) LAKGB_CUDA(cudaEventDestroy(x));
   e.choice = best;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);

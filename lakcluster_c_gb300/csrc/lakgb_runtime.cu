@@ -263,7 +263,16 @@ CallTimer::~CallTimer() {
   c.self_ns += self;
 }
 
+// True while s is being captured into a CUDA graph: nothing may synchronise
+// or time it then.
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  LAKGB_CUDA(cudaStreamIsCapturing(s, &st));
+  return st != cudaStreamCaptureStatusNone;
+}
+
 void gram_timer_begin(cudaStream_t s) {
+  if (capturing(s)) return;
   if (!g_ev0) {
     LAKGB_CUDA(cudaEventCreate(&g_ev0));
     LAKGB_CUDA(cudaEventCreate(&g_ev1));
@@ -272,6 +281,7 @@ void gram_timer_begin(cudaStream_t s) {
 }
 
 void gram_timer_end(cudaStream_t s) {
+  if (capturing(s)) return;
   LAKGB_CUDA(cudaEventRecord(g_ev1, s));
   g_ev_pending = true;
 }

@@ -140,7 +140,11 @@ struct CallTimer {
 };
 #define LAKGB_PROFILE_CALL(name) ::lakgb::CallTimer lakgb_call_timer_(name)
 
-// Events bracketing the most recent Gram launch.
+// True while stream s is being captured into a CUDA graph.
+bool capturing(cudaStream_t s);
+
+// Events bracketing the most recent Gram launch (not recorded while s is
+// being captured).
 void gram_timer_begin(cudaStream_t s);
 void gram_timer_end(cudaStream_t s);
 

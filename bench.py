@@ -444,15 +444,26 @@ def run_gpu(args):
             line["cpu_baseline"] = cpu
         if large is not None:
             line["large_gram_pass"] = large
-        buf = C.create_string_buffer(1 << 16)
-        lib.lakgb_gram_autotune_table(buf, len(buf))
-        line["gram_autotune"] = json.loads(buf.value.decode() or "[]")
+        line["gram_autotune"] = autotune_summary(lib)
         if solves is not None:
             line["solves"] = solves
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def autotune_summary(lib):
+    """The Gram autotuner's decisions: how many shape classes took each
+    kernel, and the first few classes with the times seen."""
+    n = lib.lakgb_gram_autotune_table(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    lib.lakgb_gram_autotune_table(buf, len(buf))
+    table = json.loads(buf.value.decode() or "[]")
+    chosen = {}
+    for e in table:
+        chosen[e["choice"]] = chosen.get(e["choice"], 0) + 1
+    return {"classes": len(table), "chosen": chosen, "first_classes": table[:6]}
 
 
 def large_pass_measurement(args, stream, sh, flush):

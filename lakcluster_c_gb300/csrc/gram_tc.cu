@@ -39,6 +39,9 @@
 //               accumulators, which live in TMEM as well (columns 256..511,
 //               two 32-bit halves per value).
 // Shared memory: 6 stages x (16 KB A + 16 KB B) + 2 x T_b (15 KB) + counts.
+// The T_b buffers are filled by bulk copies on mbarriers, issued by whichever
+// fold warp finishes a block last, so fold warps drift apart by up to a block
+// instead of meeting at every block boundary.
 // TMEM: 512 columns (2 x 128 count columns + 256 accumulator columns).
 #include <algorithm>
 
@@ -65,6 +68,7 @@ constexpr int kSBO = 8 * 128;             // bytes between 8-row swizzle atoms (
 constexpr int kProducers = 256;           // warps 0-7
 constexpr int kMmaWarp = 8;
 constexpr int kFold = 512;                // warps 9-24
+constexpr int kFoldWarps = kFold / 32;
 constexpr int kRound = 8;                 // columns per TMEM round of a fold warp
 constexpr int kFoldCols = kBN / (kFold / 128);  // tile columns per fold warp
 constexpr int kThreads = kProducers + 32 + kFold;
@@ -74,6 +78,9 @@ constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 2 * kTabBytes + 2 
 struct Smem {
   uint64_t full[kStages], empty[kStages];
   uint64_t acc_full[2], acc_empty[2], aux_full[2], aux_empty[2], done;
+  uint64_t tab_full[2];            // T_b buffer t loaded (bulk copy)
+  unsigned tab_read[2];            // fold warps done with buffer t (monotonic)
+  unsigned tab_issued[2];          // bulk copies issued into buffer t
   uint32_t tmem_base;
   int abort;
 };
@@ -172,6 +179,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
       tc::mbar_init(&sm.acc_empty[t], kFold);
       tc::mbar_init(&sm.aux_full[t], kProducers);
       tc::mbar_init(&sm.aux_empty[t], kFold);
+      tc::mbar_init(&sm.tab_full[t], 1);
+      sm.tab_read[t] = sm.tab_issued[t] = 0;
     }
     tc::mbar_init(&sm.done, 1);
     sm.abort = 0;
@@ -304,9 +313,21 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
     const int col0 = (et >> 7) * kFoldCols;   // this warp's columns of the tile
     const int row = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    for (int i = et; i < kTabBytes / 16; i += kFold)
-      tc::cp_async16(reinterpret_cast<uint8_t *>(sT) + 16 * i, reinterpret_cast<const uint8_t *>(T) + 16 * i);
-    tc::cp_async_commit();
+    // T_b of the CTA's g-th block (every tile has P blocks, so block g % P)
+    // into buffer g & 1 by one bulk copy.  Copies g = 0, 1 start here; the
+    // last fold warp to finish block g issues g + 2 into the buffer g read, so
+    // the fold warps are never held together at block boundaries.  (The two
+    // copies issued after the CTA's last block are waited for at the end.)
+    auto issue_table = [&](int t, long long g) {
+      tc::fence_proxy_async();
+      tc::mbar_arrive_expect_tx(&sm.tab_full[t], kTabBytes);
+      tc::bulk_g2s(sT + t * kTabStride, T + (size_t)(g % P) * kTabStride, kTabBytes, &sm.tab_full[t]);
+      atomicAdd(&sm.tab_issued[t], 1u);
+    };
+    if (et == 0) {
+      issue_table(0, 0);
+      issue_table(1, 1);
+    }
     bool ok = true;
     long long gb0 = 0;
     while (walk.next(p, tile_m, tile_n)) {
@@ -318,18 +339,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
       for (int b = 0; b < P; ++b) {
         const long long gbb = gb0 + b;
         const int t = (int)(gbb & 1);
-        {
-          // the next block's table (block 0 of the next tile after the last)
-          const int nb = (b + 1 < P) ? b + 1 : 0;
-          tc::named_bar_sync(1, kFold);  // the previous block no longer reads buffer t^1
-          const uint8_t *src = reinterpret_cast<const uint8_t *>(T + (size_t)nb * kTabStride);
-          uint8_t *dst = reinterpret_cast<uint8_t *>(sT + (t ^ 1) * kTabStride);
-          for (int i = et; i < kTabBytes / 16; i += kFold) tc::cp_async16(dst + 16 * i, src + 16 * i);
-          tc::cp_async_commit();
-          tc::cp_async_wait<1>();
-          tc::named_bar_sync(1, kFold);  // T_b is in shared memory
-        }
-        bool w = ok && tc::mbar_wait(&sm.aux_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 6);
+        bool w = ok && tc::mbar_wait(&sm.tab_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 8);
+        w = w && tc::mbar_wait(&sm.aux_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 6);
         w = w && tc::mbar_wait(&sm.acc_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 7);
         ok = __all_sync(0xffffffffu, w);
         tc::fence_after_sync();
@@ -380,12 +391,38 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
             }
           }
         }
+        // this warp no longer reads T buffer t; the last of the fold warps
+        // to get here loads block gbb + 2 into it (after the copy it read
+        // has landed; no new copies once the CTA has aborted)
+        __syncwarp();
+        if (lane == 0) {
+          __threadfence_block();
+          const unsigned prev = atomicAdd(&sm.tab_read[t], 1u);
+          if ((prev + 1) % kFoldWarps == 0) {
+            __threadfence_block();
+            if (!*abort) {
+              if (tc::mbar_wait_landed(&sm.tab_full[t], (uint32_t)((gbb >> 1) & 1)))
+                issue_table(t, gbb + 2);
+              else
+                atomicCAS(&g_tc_status, 0, 9);
+            }
+          }
+        }
+        __syncwarp();
         if (ok) tc::tmem_wait_st();
         tc::mbar_arrive(&sm.aux_empty[t]);
       }
       gb0 += P;
     }
-    tc::cp_async_wait<0>();
+    // every bulk copy into the tables has landed before the CTA exits (each
+    // copy was issued after the previous one into its buffer landed)
+    tc::named_bar_sync(1, kFold);
+    if (et == 0) {
+      for (int t = 0; t < 2; ++t) {
+        const unsigned n = *(volatile unsigned *)&sm.tab_issued[t];
+        if (n && !tc::mbar_wait_landed(&sm.tab_full[t], (n - 1) & 1)) atomicCAS(&g_tc_status, 0, 10);
+      }
+    }
   }
 
   tc::fence_before_sync();

@@ -69,8 +69,9 @@ constexpr int kProducers = 256;           // warps 0-7
 constexpr int kMmaWarp = 8;
 constexpr int kFold = 512;                // warps 9-24
 constexpr int kFoldWarps = kFold / 32;
-constexpr int kRound = 8;                 // columns per TMEM round of a fold warp
+constexpr int kRound = 4;                 // columns per TMEM round of a fold warp
 constexpr int kFoldCols = kBN / (kFold / 128);  // tile columns per fold warp
+constexpr int kRounds = kFoldCols / kRound;
 constexpr int kThreads = kProducers + 32 + kFold;
 constexpr uint32_t kTmemCols = 512;
 constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 2 * kTabBytes + 2 * (kBM + kBN) * 4 + 1024;
@@ -98,6 +99,20 @@ __device__ __forceinline__ void expand_row(uint32_t row_base, uint32_t sw, uint4
     tc::st_shared_v4(row_base + (((2 * q + 1) ^ sw) << 4), (v >> 1) & 0x08080808u, (v >> 2) & 0x08080808u,
                      (v >> 3) & 0x08080808u, (v >> 4) & 0x08080808u);
   }
+}
+
+template <int R>
+__device__ __forceinline__ void tmem_ld_n(uint32_t taddr, uint32_t (&v)[R]) {
+  if constexpr (R == 4) tc::tmem_ld4(taddr, v);
+  else if constexpr (R == 8) tc::tmem_ld8(taddr, v);
+  else if constexpr (R == 16) tc::tmem_ld16(taddr, v);
+  else tc::tmem_ld32(taddr, v);
+}
+template <int R>
+__device__ __forceinline__ void tmem_st_n(uint32_t taddr, const uint32_t (&v)[R]) {
+  if constexpr (R == 8) tc::tmem_st8(taddr, v);
+  else if constexpr (R == 16) tc::tmem_st16(taddr, v);
+  else tc::tmem_st32(taddr, v);
 }
 
 __device__ __forceinline__ int popc4(uint4 x) { return __popc(x.x) + __popc(x.y) + __popc(x.z) + __popc(x.w); }
@@ -171,14 +186,14 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      tc::mbar_init(&sm.full[s], kProducers);
+      tc::mbar_init(&sm.full[s], kProducers / 32);  // one arrival per warp
       tc::mbar_init(&sm.empty[s], 1);
     }
     for (int t = 0; t < 2; ++t) {
       tc::mbar_init(&sm.acc_full[t], 1);
-      tc::mbar_init(&sm.acc_empty[t], kFold);
-      tc::mbar_init(&sm.aux_full[t], kProducers);
-      tc::mbar_init(&sm.aux_empty[t], kFold);
+      tc::mbar_init(&sm.acc_empty[t], kFoldWarps);
+      tc::mbar_init(&sm.aux_full[t], kProducers / 32);
+      tc::mbar_init(&sm.aux_empty[t], kFoldWarps);
       tc::mbar_init(&sm.tab_full[t], 1);
       sm.tab_read[t] = sm.tab_issued[t] = 0;
     }
@@ -242,7 +257,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
             expand_row(my_row + s * kStageBytes, my_sw, x);
             tc::fence_proxy_async();
           }
-          tc::mbar_arrive(&sm.full[s]);
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&sm.full[s]);
           if (++s == kStages) {
             s = 0;
             ++wrap;
@@ -253,7 +269,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
             if (gbb >= 2 && ok)
               ok = tc::mbar_wait(&sm.aux_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, &g_tc_status, 2);
             s_cnt[t * 256 + tid] = cnt;
-            tc::mbar_arrive(&sm.aux_full[t]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&sm.aux_full[t]);
             cnt = 0;
             ch = 0;
             ++gbb;
@@ -347,48 +364,67 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
         const double *Tb = sT + t * kTabStride;
         const int pa = s_cnt[t * 256 + row];
         const int *pzb = s_cnt + t * 256 + 128;
-#pragma unroll 1
-        for (int c0 = col0; c0 < col0 + kFoldCols; c0 += kRound) {
-          // counts of columns c0..c0+7 and their accumulators (TMEM columns
-          // 256 + 2*c0 + 2j low word, + 2j + 1 high word), one wait for both
-          uint32_t cn[kRound], a[2 * kRound];
-          const uint32_t acol = lane_base + 256 + 2 * c0;
-          if (ok) {
-            tc::tmem_ld8(lane_base + t * kBN + c0, cn);
-            if (b > 0) tc::tmem_ld16(acol, a);
-            tc::tmem_wait_ld();
-          } else {
+        // Rounds of kRound columns, software-pipelined: the TMEM loads of
+        // round r + 1 (counts, and accumulators after block 0) are in flight
+        // while round r is added, so their latency hides behind the adds.
+        uint32_t cn[2][kRound], a[2][2 * kRound];
+        auto load_round = [&](int r, int buf) {
+          const int c0 = col0 + r * kRound;
+          tmem_ld_n<kRound>(lane_base + t * kBN + c0, cn[buf]);
+          if (b > 0) tmem_ld_n<2 * kRound>(lane_base + 256 + 2 * c0, a[buf]);
+        };
+        if (ok) {
+          load_round(0, 0);
+          tc::tmem_wait_ld();
+          tc::reg_fence(cn[0]);
+          tc::reg_fence(a[0]);
+        }
 #pragma unroll
-            for (int j = 0; j < kRound; ++j) cn[j] = 0;
+        for (int r = 0; r < kRounds; ++r) {
+          const int cur = r & 1, nxt = cur ^ 1;
+          const int c0 = col0 + r * kRound;
+          if (!ok) {
+#pragma unroll
+            for (int j = 0; j < kRound; ++j) cn[cur][j] = 0;
           }
-          if (c0 == col0 + kFoldCols - kRound) {
-            // all this warp's count columns of buffer t read
+          if (ok && r + 1 < kRounds) load_round(r + 1, nxt);
+          if (r == kRounds - 1) {
+            // all this warp's count columns of buffer t have been read
             tc::fence_before_sync();
-            tc::mbar_arrive(&sm.acc_empty[t]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&sm.acc_empty[t]);
           }
 #pragma unroll
           for (int j = 0; j < kRound; ++j) {
-            const int n = decode_count(cn[j]);
+            const int n = decode_count(cn[cur][j]);
             int c = (TYPE == 1) ? pa + pzb[c0 + j] - 2 * n : n;
             c = min(max(c, 0), kTabStride - 1);
             const double x = Tb[c];
-            const double v = (b > 0) ? __dadd_rn(__hiloint2double((int)a[2 * j + 1], (int)a[2 * j]), x) : x;
-            a[2 * j] = (uint32_t)__double2loint(v);
-            a[2 * j + 1] = (uint32_t)__double2hiint(v);
+            const double v =
+                (b > 0) ? __dadd_rn(__hiloint2double((int)a[cur][2 * j + 1], (int)a[cur][2 * j]), x) : x;
+            a[cur][2 * j] = (uint32_t)__double2loint(v);
+            a[cur][2 * j + 1] = (uint32_t)__double2hiint(v);
           }
           if (b + 1 < P) {
-            if (ok) tc::tmem_st16(acol, a);
+            // accumulators of columns c0 + j: TMEM columns 256 + 2 (c0 + j)
+            // (low word) and + 1 (high word)
+            if (ok) tmem_st_n<2 * kRound>(lane_base + 256 + 2 * c0, a[cur]);
           } else if (ok && row_in) {
 #pragma unroll
             for (int j = 0; j < kRound; ++j) {
               const int gz = tile_n + c0 + j;
               if (gz >= p.nZ || (p.symmetric && ga > gz)) continue;
-              const double v = __hiloint2double((int)a[2 * j + 1], (int)a[2 * j]);
+              const double v = __hiloint2double((int)a[cur][2 * j + 1], (int)a[cur][2 * j]);
               double o = (TYPE == 1) ? __dsub_rn(p.a0d1, twice(v)) : v;
               if (p.lfA && p.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(lfa, p.lfZ[gz]), p.a2d1));
               p.out[orow + (long long)p.out_c[gz] * p.out_stride] = o;
               if (p.symmetric) p.out[(long long)p.out_r2[gz] + ocol2] = o;
             }
+          }
+          if (ok && r + 1 < kRounds) {
+            tc::tmem_wait_ld();
+            tc::reg_fence(cn[nxt]);
+            tc::reg_fence(a[nxt]);
           }
         }
         // this warp no longer reads T buffer t; the last of the fold warps
@@ -410,7 +446,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
         }
         __syncwarp();
         if (ok) tc::tmem_wait_st();
-        tc::mbar_arrive(&sm.aux_empty[t]);
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&sm.aux_empty[t]);
       }
       gb0 += P;
     }

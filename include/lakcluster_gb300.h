@@ -367,6 +367,10 @@ void lakgb_call_profile_reset(void);
 #define LAKGB_IMPL_POPCOUNT 0
 #define LAKGB_IMPL_TENSOR 1
 #define LAKGB_IMPL_AUTO 2
+/* Gram only: the popcount kernel split over blocks (every 1920-column block
+ * of every output tile counted by its own CTA, then the FP64 fold over the
+ * blocks in order); for launches with few output tiles.  Bit-identical. */
+#define LAKGB_IMPL_SPLIT 3
 #define LAKGB_GRAM_POPCOUNT LAKGB_IMPL_POPCOUNT
 #define LAKGB_GRAM_TENSOR LAKGB_IMPL_TENSOR
 #define LAKGB_GRAM_AUTO LAKGB_IMPL_AUTO
@@ -375,7 +379,8 @@ int lakgb_gram_impl(void);
 /* LAKGB_GRAM_AUTO (the default) picks the Gram kernel and tile shape by
  * measurement: the first launch of each shape class (type, symmetric, log2 of
  * the A rows, Z rows and blocks) runs every candidate -- the tensor-core
- * kernel and three tile shapes of the popcount kernel, all bit-identical --
+ * kernel, two tile shapes of the popcount kernel and the popcount kernel
+ * split over blocks, all bit-identical --
  * timed with CUDA events, and the fastest serves that class afterwards.
  * lakgb_gram_autotune_table writes the table as JSON into buf (returns its
  * full length); lakgb_gram_autotune_reset clears it. */

@@ -14,6 +14,9 @@
 // shared memory (row pitch 61 words: conflict-free column reads), every
 // thread accumulates a TM x TN micro-tile of integer counts over the block's
 // 60 words, then folds them into FP64 accumulators with the block weight.
+// For launches with few tiles the same staging and counting run split over
+// blocks (one CTA per tile and block, counts to a scratch array), followed by
+// a kernel that does the fold in block order.
 #include <string.h>
 
 #include <algorithm>
@@ -31,6 +34,81 @@ namespace lakgb {
 namespace {
 
 constexpr int kLd = kBlockWords + 1;  // smem row pitch in words
+
+// Stage the masked 240-byte segments of block `blk` of the tile's BM + BN
+// rows in shared memory (zeros for rows past the end).
+template <int BM, int BN, int NT>
+__device__ __forceinline__ void stage_block(const GramParams &p, int blk, uint32_t *As, uint32_t *Zs,
+                                            const long long *a_off, const long long *z_off, int tid) {
+  const long long boff = (long long)blk * kBlockBytes;
+  const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + boff);
+  for (int idx = tid; idx < BM * 15; idx += NT) {
+    const int r = idx / 15, v = idx - r * 15;
+    uint4 x = make_uint4(0u, 0u, 0u, 0u);
+    const long long o = a_off[r];
+    if (o >= 0) {
+      const uint4 m = __ldg(mk + v);
+      x = __ldg(reinterpret_cast<const uint4 *>(p.wA + o + boff) + v);
+      x.x &= m.x; x.y &= m.y; x.z &= m.z; x.w &= m.w;
+    }
+    uint32_t *d = As + r * kLd + 4 * v;
+    d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
+  }
+  for (int idx = tid; idx < BN * 15; idx += NT) {
+    const int r = idx / 15, v = idx - r * 15;
+    uint4 x = make_uint4(0u, 0u, 0u, 0u);
+    const long long o = z_off[r];
+    if (o >= 0) {
+      const uint4 m = __ldg(mk + v);
+      x = __ldg(reinterpret_cast<const uint4 *>(p.wZ + o + boff) + v);
+      x.x &= m.x; x.y &= m.y; x.z &= m.z; x.w &= m.w;
+    }
+    uint32_t *d = Zs + r * kLd + 4 * v;
+    d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
+  }
+}
+
+// Integer counts of one staged block for this thread's TM x TN micro-tile
+// (rows ty + i*TY of A, tx + j*TX of Z).
+template <int TM, int TN, int TX, int TY, int TYPE>
+__device__ __forceinline__ void count_block(const uint32_t *As, const uint32_t *Zs, int tx, int ty,
+                                            int (&cnt)[TM][TN]) {
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) cnt[i][j] = 0;
+#pragma unroll 4
+  for (int w = 0; w < kBlockWords; ++w) {
+    uint32_t a[TM], z[TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) a[i] = As[(ty + i * TY) * kLd + w];
+#pragma unroll
+    for (int j = 0; j < TN; ++j) z[j] = Zs[(tx + j * TX) * kLd + w];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) cnt[i][j] += __popc(TYPE == 1 ? (a[i] ^ z[j]) : (a[i] & z[j]));
+  }
+}
+
+// The score combine of one output element and its store (and its mirror for
+// a symmetric Gram), in the reference's operation order.
+template <int TYPE>
+__device__ __forceinline__ void store_element(const GramParams &p, int ga, int gz, double acc) {
+  double o = (TYPE == 1) ? __dsub_rn(p.a0d1, __dmul_rn(2.0, acc)) : acc;
+  if (p.lfA && p.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(p.lfA[ga], p.lfZ[gz]), p.a2d1));
+  p.out[(long long)p.out_r[ga] + (long long)p.out_c[gz] * p.out_stride] = o;
+  if (p.symmetric) p.out[(long long)p.out_r2[gz] + (long long)p.out_c2[ga] * p.out_stride] = o;
+}
+
+template <int BM, int BN>
+__device__ __forceinline__ void row_offsets(const GramParams &p, int tile_m, int tile_n, long long *a_off,
+                                            long long *z_off, int tid, int nt) {
+  for (int i = tid; i < BM; i += nt)
+    a_off[i] = (tile_m + i < p.nA) ? (long long)p.a_rowb[tile_m + i] * p.a_row_bytes : -1;
+  for (int i = tid; i < BN; i += nt)
+    z_off[i] = (tile_n + i < p.nZ) ? (long long)p.z_rowb[tile_n + i] * p.z_row_bytes : -1;
+}
 
 template <int BM, int BN, int TM, int TN, int TYPE>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN), 2)
@@ -53,11 +131,7 @@ gram_popc_kernel(GramParams p) {
   const int tid = threadIdx.x;
   const int tx = tid % TX;
   const int ty = tid / TX;
-
-  for (int i = tid; i < BM; i += NT)
-    a_off[i] = (tile_m + i < p.nA) ? (long long)p.a_rowb[tile_m + i] * p.a_row_bytes : -1;
-  for (int i = tid; i < BN; i += NT)
-    z_off[i] = (tile_n + i < p.nZ) ? (long long)p.z_rowb[tile_n + i] * p.z_row_bytes : -1;
+  row_offsets<BM, BN>(p, tile_m, tile_n, a_off, z_off, tid, NT);
 
   double acc[TM][TN];
 #pragma unroll
@@ -67,53 +141,10 @@ gram_popc_kernel(GramParams p) {
 
   for (int blk = 0; blk < p.P; ++blk) {
     __syncthreads();
-    const long long boff = (long long)blk * kBlockBytes;
-    const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + boff);
-    for (int idx = tid; idx < BM * 15; idx += NT) {
-      const int r = idx / 15, v = idx - r * 15;
-      uint4 x = make_uint4(0u, 0u, 0u, 0u);
-      const long long o = a_off[r];
-      if (o >= 0) {
-        const uint4 m = __ldg(mk + v);
-        x = __ldg(reinterpret_cast<const uint4 *>(p.wA + o + boff) + v);
-        x.x &= m.x; x.y &= m.y; x.z &= m.z; x.w &= m.w;
-      }
-      uint32_t *d = As + r * kLd + 4 * v;
-      d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
-    }
-    for (int idx = tid; idx < BN * 15; idx += NT) {
-      const int r = idx / 15, v = idx - r * 15;
-      uint4 x = make_uint4(0u, 0u, 0u, 0u);
-      const long long o = z_off[r];
-      if (o >= 0) {
-        const uint4 m = __ldg(mk + v);
-        x = __ldg(reinterpret_cast<const uint4 *>(p.wZ + o + boff) + v);
-        x.x &= m.x; x.y &= m.y; x.z &= m.z; x.w &= m.w;
-      }
-      uint32_t *d = Zs + r * kLd + 4 * v;
-      d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
-    }
+    stage_block<BM, BN, NT>(p, blk, As, Zs, a_off, z_off, tid);
     __syncthreads();
-
     int cnt[TM][TN];
-#pragma unroll
-    for (int i = 0; i < TM; ++i)
-#pragma unroll
-      for (int j = 0; j < TN; ++j) cnt[i][j] = 0;
-
-#pragma unroll 4
-    for (int w = 0; w < kBlockWords; ++w) {
-      uint32_t a[TM], z[TN];
-#pragma unroll
-      for (int i = 0; i < TM; ++i) a[i] = As[(ty + i * TY) * kLd + w];
-#pragma unroll
-      for (int j = 0; j < TN; ++j) z[j] = Zs[(tx + j * TX) * kLd + w];
-#pragma unroll
-      for (int i = 0; i < TM; ++i)
-#pragma unroll
-        for (int j = 0; j < TN; ++j)
-          cnt[i][j] += __popc(TYPE == 1 ? (a[i] ^ z[j]) : (a[i] & z[j]));
-    }
+    count_block<TM, TN, TX, TY, TYPE>(As, Zs, tx, ty, cnt);
     const double d = p.D ? p.D[blk] : 1.0;
 #pragma unroll
     for (int i = 0; i < TM; ++i)
@@ -131,12 +162,68 @@ gram_popc_kernel(GramParams p) {
       const int gz = tile_n + tx + j * TX;
       if (gz >= p.nZ) continue;
       if (p.symmetric && ga > gz) continue;
-      double o = (TYPE == 1) ? __dsub_rn(p.a0d1, __dmul_rn(2.0, acc[i][j])) : acc[i][j];
-      if (p.lfA && p.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(p.lfA[ga], p.lfZ[gz]), p.a2d1));
-      p.out[(long long)p.out_r[ga] + (long long)p.out_c[gz] * p.out_stride] = o;
-      if (p.symmetric)
-        p.out[(long long)p.out_r2[gz] + (long long)p.out_c2[ga] * p.out_stride] = o;
+      store_element<TYPE>(p, ga, gz, acc[i][j]);
     }
+  }
+}
+
+// Split over blocks, for launches with few output tiles (a few hundred rows
+// or fewer on a side), where one CTA per tile would walk all P blocks alone
+// while most SMs idle.  Every (tile, block) pair is its own CTA and writes
+// the tile's integer counts of that block (<= 1920, uint16) to a scratch
+// array cnt[(b * nZ + k) * nA + i]; the fold kernel then adds each element's
+// weighted counts over the blocks in ascending order, with the same multiply
+// and add as above, so the outputs are the same bit for bit.
+template <int BM, int BN, int TM, int TN, int TYPE>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+gram_split_counts_kernel(GramParams p, uint16_t *__restrict__ cnt_out) {
+  constexpr int TX = BN / TN;
+  constexpr int TY = BM / TM;
+  constexpr int NT = TX * TY;
+  extern __shared__ uint32_t smem[];
+  uint32_t *As = smem;
+  uint32_t *Zs = smem + BM * kLd;
+  __shared__ long long a_off[BM];
+  __shared__ long long z_off[BN];
+
+  const int tile_n = blockIdx.x * BN;
+  const int tile_m = blockIdx.y * BM;
+  const int blk = blockIdx.z;
+  if (p.symmetric && tile_m > tile_n + BN - 1) return;
+  const int tid = threadIdx.x;
+  const int tx = tid % TX;
+  const int ty = tid / TX;
+  row_offsets<BM, BN>(p, tile_m, tile_n, a_off, z_off, tid, NT);
+  __syncthreads();
+  stage_block<BM, BN, NT>(p, blk, As, Zs, a_off, z_off, tid);
+  __syncthreads();
+  int cnt[TM][TN];
+  count_block<TM, TN, TX, TY, TYPE>(As, Zs, tx, ty, cnt);
+  uint16_t *o = cnt_out + (size_t)blk * p.nZ * p.nA;
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int ga = tile_m + ty + i * TY;
+    if (ga >= p.nA) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int gz = tile_n + tx + j * TX;
+      if (gz < p.nZ) o[(size_t)gz * p.nA + ga] = (uint16_t)cnt[i][j];
+    }
+  }
+}
+
+template <int TYPE>
+__global__ void __launch_bounds__(256) gram_split_fold_kernel(GramParams p, const uint16_t *__restrict__ cnt) {
+  const long long n = (long long)p.nA * p.nZ, plane = n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int gz = (int)(e / p.nA), ga = (int)(e - (long long)gz * p.nA);
+    if (p.symmetric && ga > gz) continue;
+    double acc = 0.0;
+    for (int b = 0; b < p.P; ++b) {
+      const double d = p.D ? p.D[b] : 1.0;
+      acc = __dadd_rn(acc, __dmul_rn(d, (double)cnt[(size_t)b * plane + e]));
+    }
+    store_element<TYPE>(p, ga, gz, acc);
   }
 }
 
@@ -156,6 +243,33 @@ void launch_tile(const GramParams &p) {
   count_launch();
 }
 
+// Scratch bytes of the split launch; above kSplitMaxBytes it is not used.
+constexpr size_t kSplitMaxBytes = size_t(256) << 20;
+size_t split_bytes(const GramParams &p) { return (size_t)p.P * (size_t)p.nA * (size_t)p.nZ * sizeof(uint16_t); }
+
+template <int TYPE>
+void launch_split(const GramParams &p, cudaStream_t s) {
+  constexpr int BM = 64, BN = 64, TM = 4, TN = 4, NT = (BM / TM) * (BN / TN);
+  const size_t smem = (size_t)(BM + BN) * kLd * sizeof(uint32_t);
+  static bool configured = false;
+  if (!configured) {
+    LAKGB_CUDA(cudaFuncSetAttribute(gram_split_counts_kernel<BM, BN, TM, TN, TYPE>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  uint16_t *cnt = nullptr;
+  LAKGB_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&cnt), split_bytes(p), s));
+  dim3 grid((p.nZ + BN - 1) / BN, (p.nA + BM - 1) / BM, p.P);
+  gram_split_counts_kernel<BM, BN, TM, TN, TYPE><<<grid, NT, smem, s>>>(p, cnt);
+  LAKGB_CUDA(cudaGetLastError());
+  const long long n = (long long)p.nA * p.nZ;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 152ll * 8);
+  gram_split_fold_kernel<TYPE><<<blocks, 256, 0, s>>>(p, cnt);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch(2);
+  LAKGB_CUDA(cudaFreeAsync(cnt, s));
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -164,21 +278,28 @@ void launch_tile(const GramParams &p) {
 // a launch with at least kTensorRows rows on both sides takes the tensor-core
 // kernel (it wins there by 3x or more); for smaller launches the first one of
 // each shape class -- (type, symmetric, log2 of the A rows, of the Z rows and
-// of the blocks) -- runs the candidates on its real arguments, timed with CUDA
-// events on the launching stream, and the fastest serves that class from
-// then on.
+// of the blocks) -- runs the candidates (tensor kernel, popcount kernel with
+// two tile shapes, popcount kernel split over blocks) on its real arguments,
+// timed with CUDA events on the launching stream, and the fastest serves that
+// class from then on.
 
-enum GramVariant { kTensor = 0, kPopc128x64, kPopc64x64, kPopc64x128, kNumVariants };
-constexpr int kTunedVariants = 3;   // tensor, popcount 128x64, popcount 64x64
+enum GramVariant { kTensor = 0, kPopc128x64, kPopc64x64, kSplit64x64, kPopc64x128, kNumVariants };
+constexpr int kTunedVariants = 4;   // tensor, popcount 128x64, popcount 64x64, split over blocks
 constexpr int kTensorRows = 512;
 const char *const kVariantName[kNumVariants] = {"tensor_128x128", "popcount_128x64", "popcount_64x64",
-                                                "popcount_64x128"};
+                                                "split_64x64", "popcount_64x128"};
 
 void launch_variant(int v, const GramParams &p, cudaStream_t s) {
   GramParams q = p;
   q.stream = s;
+  if (v == kSplit64x64 && (split_bytes(q) > kSplitMaxBytes || q.P > 65535)) v = kPopc64x64;
   if (v == kTensor) {
     launch_gram_tc(q, s);
+  } else if (v == kSplit64x64) {
+    if (q.type == 1)
+      launch_split<1>(q, s);
+    else
+      launch_split<2>(q, s);
   } else if (q.type == 1) {
     if (v == kPopc128x64) launch_tile<128, 64, 8, 4, 1>(q);
     else if (v == kPopc64x64) launch_tile<64, 64, 4, 4, 1>(q);
@@ -271,6 +392,8 @@ void launch_gram(const GramParams &p) {
   const int impl = g_gram_impl.load(std::memory_order_relaxed);
   if (impl == LAKGB_IMPL_TENSOR) {
     launch_variant(kTensor, p, s);
+  } else if (impl == LAKGB_IMPL_SPLIT) {
+    launch_variant(kSplit64x64, p, s);
   } else if (impl == LAKGB_IMPL_POPCOUNT) {
     launch_variant(kPopc128x64, p, s);
   } else {
@@ -284,9 +407,9 @@ void launch_gram(const GramParams &p) {
 }  // namespace lakgb
 
 extern "C" void lakgb_set_gram_impl(int impl) {
-  lakgb::g_gram_impl.store(impl == LAKGB_IMPL_POPCOUNT ? LAKGB_IMPL_POPCOUNT
-                                                       : (impl == LAKGB_IMPL_TENSOR ? LAKGB_IMPL_TENSOR
-                                                                                    : LAKGB_IMPL_AUTO));
+  lakgb::g_gram_impl.store((impl == LAKGB_IMPL_POPCOUNT || impl == LAKGB_IMPL_TENSOR || impl == LAKGB_IMPL_SPLIT)
+                               ? impl
+                               : LAKGB_IMPL_AUTO);
 }
 
 extern "C" int lakgb_gram_autotune_table(char *buf, int buf_len) {

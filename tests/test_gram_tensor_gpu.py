@@ -1,5 +1,6 @@
-"""GPU parity of the two Gram kernels: the tcgen05 tensor-core kernel and the
-popcount kernel give bit-identical outputs to each other and to the C oracle
+"""GPU parity of the Gram kernels: the tcgen05 tensor-core kernel, the
+popcount kernel and the popcount kernel split over blocks give bit-identical
+outputs to each other and to the C oracle
 (AnZt_vv / AnAt_vv, both types), including partial tiles, full blocks
 (counts of 1920), fully masked blocks and unweighted (D = NULL) calls, and the
 tensor-core kernels' device status word stays 0."""
@@ -13,7 +14,7 @@ from lakcluster_c_gb300 import abi
 
 pytestmark = pytest.mark.gpu
 
-POPCOUNT, TENSOR = 0, 1
+POPCOUNT, TENSOR, SPLIT = 0, 1, 3
 
 
 def _bits_equal(a, b):
@@ -48,7 +49,7 @@ def _case(rng, nA, nZ, m, sym, density=0.5, mask_keep=0.9, dead_blocks=()):
 
 def _run_both(lib, sym, t, MA, MZ, A_ajdk, lfA, lfZ):
     outs = {}
-    for impl in (POPCOUNT, TENSOR):
+    for impl in (POPCOUNT, TENSOR, SPLIT):
         lib.lakgb_set_gram_impl(impl)
         outs[impl] = kc.call_gram("gpu", sym, t, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, lfA, lfZ)
         assert lib.lakgb_device_status() == 0
@@ -72,6 +73,7 @@ def test_tensor_matches_popcount_and_oracle(impl_switch, oracle_lib, nA, nZ, m, 
             want = kc.call_gram("oracle", sym, t, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, *lf)
             outs = _run_both(impl_switch, sym, t, MA, MZ, A_ajdk, *lf)
             assert _bits_equal(outs[TENSOR], outs[POPCOUNT]), (t, lf[0] is None)
+            assert _bits_equal(outs[SPLIT], outs[POPCOUNT]), (t, lf[0] is None)
             assert _bits_equal(outs[TENSOR], want), (t, lf[0] is None)
 
 
@@ -90,6 +92,7 @@ def test_tensor_extreme_counts(impl_switch, oracle_lib, density, mask_keep, dead
             outs = _run_both(impl_switch, False, t, MA, MZ, aj, None, None)
             assert _bits_equal(outs[TENSOR], want), (t, aj is None)
             assert _bits_equal(outs[POPCOUNT], want), (t, aj is None)
+            assert _bits_equal(outs[SPLIT], want), (t, aj is None)
 
 
 def test_host_buffer_rewritten_in_place(impl_switch, oracle_lib):
@@ -99,7 +102,7 @@ def test_host_buffer_rewritten_in_place(impl_switch, oracle_lib):
     m = 2 * 1920
     MA, MZ = _case(rng, 150, 130, m, False)
     A_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(m)))
-    for impl in (TENSOR, POPCOUNT):
+    for impl in (TENSOR, POPCOUNT, SPLIT):
         impl_switch.lakgb_set_gram_impl(impl)
         first = kc.call_gram("gpu", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, None, None)
         MA.wX[:] = rng.integers(0, 256, MA.wX.shape, dtype=np.uint8)
@@ -129,4 +132,4 @@ def test_autotuned_dispatch_matches_oracle(impl_switch, oracle_lib):
     lib.lakgb_gram_autotune_table(buf, len(buf))
     table = json.loads(buf.value.decode())
     assert len(table) == 1
-    assert table[0]["choice"] in table[0]["ms"] and len(table[0]["ms"]) == 4
+    assert table[0]["choice"] in table[0]["ms"] and len(table[0]["ms"]) == 5

@@ -424,9 +424,16 @@ def run_gpu(args):
                          "one launch from the committed ncu capture (profiles/), null when absent" % src),
                 "fp64_pipe": {"achieved_ops_per_s": fp64_ops / (k_ms / 1000.0), "peak_adds_per_s": fp64_rate,
                               "frac": fp64_ops / (k_ms / 1000.0) / fp64_rate, "ops_per_launch": fp64_ops,
-                              "note": "the binding unit: FP64 adds of the block-weighted fold (%d per element) "
-                                      "against the add rate measured live on this GPU "
-                                      "(lakgb_measure_fp64_add_rate)" % fp64_per_elem},
+                              "note": "FP64 adds of the block-weighted fold (%d per element) against the add "
+                                      "rate measured live on this GPU (lakgb_measure_fp64_add_rate); not the "
+                                      "sole bound: copies of the kernel without the adds, or without the table "
+                                      "loads, run at most 6 %% faster" % fp64_per_elem},
+                "vs_int_pipe_roofline": {
+                    "achieved_bitops": k_work / (k_ms / 1000.0), "int_pipe_peak_bitops": popc_peak,
+                    "ratio": (k_work / (k_ms / 1000.0)) / popc_peak,
+                    "note": "the tensor kernel against the integer-pipe roofline of a popcount Gram (POPC at "
+                            "16 lanes/clk/SM x 32 bits, sampled SM clock): above 1 means faster than any "
+                            "popcount kernel can run"},
                 "popcount_kernel": {"kernel_ms": k_ms_popc, "achieved_bitops": k_work / (k_ms_popc / 1000.0),
                                     "int_pipe_peak_bitops": popc_peak,
                                     "int_pipe_frac": (k_work / (k_ms_popc / 1000.0)) / popc_peak,

@@ -164,11 +164,14 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description="Solve a synthetic bcc workload on the GPU and print its timing.")
     ap.add_argument("--workload", default="case_control_1024x1024x4096", choices=sorted(WORKLOADS))
     ap.add_argument("--reps", type=int, default=1)
+    ap.add_argument("--gram-impl", default="auto", choices=["auto", "tensor", "popcount", "split"],
+                    help="Gram kernel for every launch (default: autotuned per shape class)")
     args = ap.parse_args(argv)
     import json
     import os
     A, Z, gamma = workload(args.workload)
     p = Problem(A, Z, gamma=gamma)
+    p.lib.lakgb_set_gram_impl({"popcount": 0, "tensor": 1, "auto": 2, "split": 3}[args.gram_impl])
     profile = os.environ.get("LAKGB_PROFILE_CALLS", "0") not in ("", "0")
     for r in range(args.reps):
         if profile:

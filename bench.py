@@ -382,6 +382,9 @@ def run_gpu(args):
     large = None
     if rank == 0 and not args.no_large:
         large = large_pass_measurement(args, stream, sh, flush)
+    grouped = None
+    if rank == 0 and not args.no_grouped:
+        grouped = grouped_gram_measurement(stream, sh, flush)
 
     solves = None
     if rank == 0 and not args.no_solves:
@@ -451,6 +454,8 @@ def run_gpu(args):
             line["cpu_baseline"] = cpu
         if large is not None:
             line["large_gram_pass"] = large
+        if grouped is not None:
+            line["grouped_null_gram_passes"] = grouped
         line["gram_autotune"] = autotune_summary(lib)
         if solves is not None:
             line["solves"] = solves
@@ -509,6 +514,75 @@ def large_pass_measurement(args, stream, sh, flush):
             "bitops_per_pass": work, "setup_seconds": setup_s, "checks": checks, **timings,
             "note": "operands drawn on the device (MAF U[0.01,0.5], 2048x4096 planted, 5% flips); row terms from "
                     "wrap_An_ajdk_v; host recomputation of sampled entries in block order"}
+
+
+def grouped_gram_measurement(stream, sh, flush):
+    """The Gram passes of the batched-null instances (24 label-shuffled
+    case/control problems, rows logU[1024,8192], SNPs logU[4096,32768], one
+    bin; 48 launches): one launch per product (the plain path, default kernel
+    choice) against one grouped persistent launch of the tensor-core kernel
+    (lakgb_gram_group_run), direct and replayed from a CUDA graph.  Outputs of
+    the grouped launch are compared bit for bit with the plain path's."""
+    import torch
+    from lakcluster_c_gb300 import synth
+    from lakcluster_c_gb300.large_pass import GroupedGramPasses, LargeGramPass
+
+    passes = []
+    for i in range(24):
+        rng = np.random.default_rng(1000 + i)
+        r = synth.log_uniform_int(rng, 1024, 8192)
+        c = synth.log_uniform_int(rng, 4096, 32768)
+        na = r // 2
+        passes.append(LargeGramPass(n_cases=na, n_controls=r - na, ncols=c, nbins=1,
+                                    planted=(min(na, max(2, r // 16)), max(2, c // 32)), maf=(0.05, 0.5),
+                                    seed=1000 + i))
+    g = GroupedGramPasses(passes)
+    work = g.work_bitops()
+    nan = float("nan")
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+
+    plain_ms = timed(lambda: g.run_plain(sh))
+    want = [o.view(torch.int64).clone() for o in g.outputs()]
+
+    def reset():
+        for o in g.outputs():
+            o.fill_(nan)
+        torch.cuda.synchronize()
+
+    reset()
+    grouped_ms = timed(lambda: g.run_grouped(sh))
+    same = all(torch.equal(o.view(torch.int64), w) for o, w in zip(g.outputs(), want))
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        g.run_grouped(stream.cuda_stream)
+    reset()
+    graph_ms = timed(lambda: graph.replay())
+    graph_same = all(torch.equal(o.view(torch.int64), w) for o, w in zip(g.outputs(), want))
+    launches = g.n
+    g.close()
+    del want, graph
+    return {"workload": "24 null instances' Gram passes (rows logU[1024,8192], SNPs logU[4096,32768], 1 bin)",
+            "launches_plain": launches, "bitops": work,
+            "plain": {"ms": plain_ms, "bitops_per_s": work / (plain_ms / 1e3)},
+            "grouped": {"ms": grouped_ms, "bitops_per_s": work / (grouped_ms / 1e3), "identical_to_plain": same},
+            "grouped_cuda_graph": {"ms": graph_ms, "bitops_per_s": work / (graph_ms / 1e3),
+                                   "identical_to_plain": graph_same},
+            "speedup_grouped_graph": plain_ms / graph_ms,
+            "note": "operands drawn on the device with the instances' shapes; one grouped launch = the table "
+                    "kernel for every instance's blocks + one persistent tcgen05 launch over all instances' tiles"}
 
 
 def solve_measurements(args, with_cpu: bool):
@@ -637,6 +711,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solves", action="store_true", help="skip the whole-solve timings")
     ap.add_argument("--no-many", action="store_true", help="skip the batched / served timings")
+    ap.add_argument("--no-grouped", action="store_true",
+                    help="skip the grouped Gram passes of the batched-null instances")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the large-configuration Gram pass (32768 + 32768 x 131072)")
     args = ap.parse_args()

@@ -284,6 +284,22 @@ struct lakgb_gram_args {
 };
 int lakgb_gram_device(const struct lakgb_gram_args *args);
 
+/* Grouped Gram (no reference counterpart): n independent Grams, each as
+ * lakgb_gram_device would compute it (bit-identical outputs), run as ONE
+ * persistent launch of the tensor-core kernel over all their tiles (plus one
+ * launch that builds every instance's block tables) -- for many instances at
+ * once, e.g. the Gram passes of label-shuffled null problems.  create copies
+ * the descriptors to the device (the pointers in them must stay valid; the
+ * data they point to may change between runs); run enqueues the two launches
+ * on `stream` (NULL: the library stream) and does nothing else, so it can be
+ * captured in a CUDA graph.  All instances must have the same type_flag; a
+ * symmetric instance must have as many 128-row tiles of A rows as of Z rows.
+ * create returns NULL on bad arguments (lakgb_last_error says why). */
+typedef struct lakgb_gram_group lakgb_gram_group;
+lakgb_gram_group *lakgb_gram_group_create(const struct lakgb_gram_args *args, int n);
+int lakgb_gram_group_run(lakgb_gram_group *group, void *stream);
+void lakgb_gram_group_destroy(lakgb_gram_group *group);
+
 /* Device mirrors of L_handles (no reference counterpart).  After
  * lakgb_L_mirror(L) the values of L live on the device: the kernel entry
  * points above write a mirrored output there (not into L->lf) and read a

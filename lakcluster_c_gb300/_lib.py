@@ -50,6 +50,12 @@ def load() -> C.CDLL:
     lib.lakgb_gram_autotune_table.restype = C.c_int
     lib.lakgb_set_bitplane_impl.argtypes = [C.c_int]
     lib.lakgb_bitplane_impl.restype = C.c_int
+    lib.lakgb_gram_group_create.argtypes = [C.c_void_p, C.c_int]
+    lib.lakgb_gram_group_create.restype = C.c_void_p
+    lib.lakgb_gram_group_run.argtypes = [C.c_void_p, C.c_void_p]
+    lib.lakgb_gram_group_run.restype = C.c_int
+    lib.lakgb_gram_group_destroy.argtypes = [C.c_void_p]
+    lib.lakgb_gram_group_destroy.restype = None
     _lib = lib
     return lib
 

@@ -25,6 +25,8 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <vector>
+#include <climits>
 
 #include "gram.cuh"
 #include "lakgb_runtime.cuh"
@@ -448,23 +450,112 @@ extern "C" int lakgb_gram_impl(void) { return lakgb::g_gram_impl.load(); }
 
 extern "C" int lakgb_device_status(void) { return lakgb::tc_status_take(); }
 
+namespace {
+
+bool params_from_args(const lakgb_gram_args *a, lakgb::GramParams *p) {
+  if (!a || (a->type_flag != LAKGB_TYPE_pm && a->type_flag != LAKGB_TYPE_00)) return false;
+  *p = lakgb::GramParams{};
+  p->wA = a->wA; p->a_rowb = a->a_rowb; p->nA = a->nA; p->a_row_bytes = a->a_row_bytes;
+  p->wZ = a->wZ; p->z_rowb = a->z_rowb; p->nZ = a->nZ; p->z_row_bytes = a->z_row_bytes;
+  p->mask = a->mask; p->P = a->P; p->D = a->D;
+  p->type = (a->type_flag == LAKGB_TYPE_pm) ? 1 : 2;
+  p->a0d1 = a->a0d1; p->a2d1 = a->a2d1; p->lfA = a->lfA; p->lfZ = a->lfZ;
+  p->out_r = a->out_r; p->out_c = a->out_c; p->out_r2 = a->out_r2; p->out_c2 = a->out_c2;
+  p->out_stride = a->out_stride; p->out = a->out; p->symmetric = a->symmetric;
+  p->stream = (cudaStream_t)a->stream;
+  return true;
+}
+
+}  // namespace
+
 extern "C" int lakgb_gram_device(const lakgb_gram_args *a) {
   using namespace lakgb;
-  if (!a || (a->type_flag != LAKGB_TYPE_pm && a->type_flag != LAKGB_TYPE_00)) {
+  GramParams p;
+  if (!params_from_args(a, &p)) {
     set_error(3, "lakgb_gram_device: bad arguments");
     return -1;
   }
-  GramParams p{};
-  p.wA = a->wA; p.a_rowb = a->a_rowb; p.nA = a->nA; p.a_row_bytes = a->a_row_bytes;
-  p.wZ = a->wZ; p.z_rowb = a->z_rowb; p.nZ = a->nZ; p.z_row_bytes = a->z_row_bytes;
-  p.mask = a->mask; p.P = a->P; p.D = a->D;
-  p.type = (a->type_flag == LAKGB_TYPE_pm) ? 1 : 2;
-  p.a0d1 = a->a0d1; p.a2d1 = a->a2d1; p.lfA = a->lfA; p.lfZ = a->lfZ;
-  p.out_r = a->out_r; p.out_c = a->out_c; p.out_r2 = a->out_r2; p.out_c2 = a->out_c2;
-  p.out_stride = a->out_stride; p.out = a->out; p.symmetric = a->symmetric;
-  p.stream = (cudaStream_t)a->stream;
   launch_gram(p);
   return 0;
+}
+
+// Grouped Gram: the descriptors live on the device for the group's lifetime,
+// so a run is two kernel launches and nothing else (capturable in a graph).
+struct lakgb_gram_group {
+  int n = 0, type = 1, total_tiles = 0;
+  long long total_blocks = 0;
+  lakgb::GramParams *d_ps = nullptr;
+  int *d_tile0 = nullptr;
+  long long *d_blk0 = nullptr;
+  double *d_T = nullptr;
+};
+
+extern "C" lakgb_gram_group *lakgb_gram_group_create(const lakgb_gram_args *args, int n) {
+  using namespace lakgb;
+  if (!args || n <= 0) {
+    set_error(3, "lakgb_gram_group_create: no instances");
+    return nullptr;
+  }
+  std::vector<GramParams> ps((size_t)n);
+  std::vector<int> tile0((size_t)n + 1, 0);
+  std::vector<long long> blk0((size_t)n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    if (!params_from_args(&args[i], &ps[i]) || ps[i].type != ps[0].type) {
+      set_error(3, "lakgb_gram_group_create: instance %d: bad arguments or a type unlike instance 0", i);
+      return nullptr;
+    }
+    const GramParams &p = ps[i];
+    const bool empty = p.nA <= 0 || p.nZ <= 0 || p.P <= 0;
+    const int ntm = (p.nA + 127) / 128, ntn = (p.nZ + 127) / 128;
+    if (!empty && p.symmetric && ntm != ntn) {
+      set_error(3, "lakgb_gram_group_create: instance %d: symmetric with unequal tile rows and columns", i);
+      return nullptr;
+    }
+    const long long tiles = empty ? 0 : gram_tc_tiles(p);
+    if ((long long)tile0[i] + tiles > INT_MAX) {
+      set_error(3, "lakgb_gram_group_create: too many tiles");
+      return nullptr;
+    }
+    tile0[i + 1] = tile0[i] + (int)tiles;
+    blk0[i + 1] = blk0[i] + (empty ? 0 : p.P);
+  }
+  if (blk0[n] > INT_MAX) {
+    set_error(3, "lakgb_gram_group_create: too many blocks");
+    return nullptr;
+  }
+  auto *g = new lakgb_gram_group;
+  g->n = n;
+  g->type = ps[0].type;
+  g->total_tiles = tile0[n];
+  g->total_blocks = blk0[n];
+  LAKGB_CUDA(cudaMalloc(&g->d_ps, sizeof(GramParams) * n));
+  LAKGB_CUDA(cudaMalloc(&g->d_tile0, sizeof(int) * (n + 1)));
+  LAKGB_CUDA(cudaMalloc(&g->d_blk0, sizeof(long long) * (n + 1)));
+  LAKGB_CUDA(cudaMalloc(&g->d_T, gram_tc_table_row_bytes() * (size_t)std::max(1ll, g->total_blocks)));
+  LAKGB_CUDA(cudaMemcpy(g->d_ps, ps.data(), sizeof(GramParams) * n, cudaMemcpyHostToDevice));
+  LAKGB_CUDA(cudaMemcpy(g->d_tile0, tile0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  LAKGB_CUDA(cudaMemcpy(g->d_blk0, blk0.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice));
+  return g;
+}
+
+extern "C" int lakgb_gram_group_run(lakgb_gram_group *g, void *stream) {
+  using namespace lakgb;
+  if (!g) return -1;
+  cudaStream_t s = stream ? (cudaStream_t)stream : lakgb::stream();
+  gram_timer_begin(s);
+  launch_gram_tc_group(GramGroupDev{g->d_ps, g->d_tile0, g->d_blk0, g->n}, g->type, g->total_tiles,
+                       g->total_blocks, g->d_T, s);
+  gram_timer_end(s);
+  return 0;
+}
+
+extern "C" void lakgb_gram_group_destroy(lakgb_gram_group *g) {
+  if (!g) return;
+  cudaFree(g->d_ps);
+  cudaFree(g->d_tile0);
+  cudaFree(g->d_blk0);
+  cudaFree(g->d_T);
+  delete g;
 }
 
 namespace lakgb {

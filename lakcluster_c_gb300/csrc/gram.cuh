@@ -31,6 +31,30 @@ struct GramParams {
   cudaStream_t stream;     // launch stream (null: the library stream)
 };
 
+// Several independent Grams launched as one (the tensor-core kernel's grouped
+// form): their parameters, the prefix sums of their tile counts (n + 1) and
+// of their block counts (n + 1, rows of the table array), all in device
+// memory.  Every instance has the same type; a symmetric instance has a
+// square tile grid.
+struct GramGroupDev {
+  const GramParams *ps;
+  const int *tile0;
+  const long long *blk0;
+  int n;
+};
+
+// Tiles of one Gram on the tensor-core kernel's 128 x 128 grid (symmetric
+// with a square grid: the upper triangle).
+int gram_tc_tiles(const GramParams &p);
+
+// Enqueue the grouped tensor-core Gram on stream s: the table kernel for all
+// instances' blocks into T (total_blocks x 1922 doubles), then one
+// persistent launch over all instances' tiles.
+void launch_gram_tc_group(const GramGroupDev &g, int type, int total_tiles, long long total_blocks, double *T,
+                          cudaStream_t s);
+// Bytes of one table row (per instance block) of the grouped launch.
+size_t gram_tc_table_row_bytes();
+
 // Enqueue the Gram kernel on the library stream: the tensor-core kernel
 // (gram_tc.cu) or the popcount kernel (gram.cu), as lakgb_set_gram_impl selects.
 void launch_gram(const GramParams &p);

@@ -135,44 +135,87 @@ __device__ __forceinline__ double twice(double x) {
   return (e >= 1 && e <= 2045) ? __longlong_as_double(bits + (1ll << 52)) : __dmul_rn(2.0, x);
 }
 
+// (tile_m, tile_n) of tile r of one Gram's list: every (A tile row, Z tile
+// column) pair in row-major order, or, for a symmetric Gram with a square
+// tile grid, only the pairs on or above the diagonal.
+__device__ __forceinline__ void tile_coords(int ntn, bool tri, int r, int &tile_m, int &tile_n) {
+  if (!tri) {
+    tile_m = (r / ntn) * kBM;
+    tile_n = (r % ntn) * kBN;
+    return;
+  }
+  int i = 0;
+  while (r >= ntn - i) {  // row i of the upper triangle holds ntn - i tiles
+    r -= ntn - i;
+    ++i;
+  }
+  tile_m = i * kBM;
+  tile_n = (i + r) * kBN;
+}
+
+// The instance of a grouped launch that holds global tile (or table row) k:
+// the last i with start[i] <= k.
+template <typename I>
+__device__ __forceinline__ int find_instance(const I *start, int n, long long k) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((long long)start[mid] <= k) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Tile order shared by every role: tile k of the launch's list goes to CTA
-// k % gridDim.x.  The list is every (A tile row, Z tile column) pair in
-// row-major order, or, for a symmetric Gram (square tile grid), only the
-// pairs on or above the diagonal -- so the active tiles, not all tiles, are
-// spread evenly over the CTAs.
+// k % gridDim.x, so the active tiles, not all tiles, are spread evenly over
+// the CTAs.  A single Gram lists its own tiles (tile_coords; a symmetric call
+// with unequal row counts skips the tiles below the diagonal as it walks); a
+// grouped launch lists the tiles of its instances one instance after another.
+template <bool GRP>
 struct TileWalk {
   int ntn, ntiles, k;
   bool tri;
-  __device__ TileWalk(const GramParams &p) : ntn((p.nZ + kBN - 1) / kBN), k((int)blockIdx.x - (int)gridDim.x) {
-    const int ntm = (p.nA + kBM - 1) / kBM;
-    tri = p.symmetric && ntm == ntn;
-    ntiles = tri ? ntn * (ntn + 1) / 2 : ntm * ntn;
+  __device__ TileWalk(const GramParams &p, const GramGroupDev &g) : k((int)blockIdx.x - (int)gridDim.x) {
+    if (GRP) {
+      ntiles = g.tile0[g.n];
+      ntn = 0;
+      tri = false;
+    } else {
+      ntn = (p.nZ + kBN - 1) / kBN;
+      const int ntm = (p.nA + kBM - 1) / kBM;
+      tri = p.symmetric && ntm == ntn;
+      ntiles = tri ? ntn * (ntn + 1) / 2 : ntm * ntn;
+    }
   }
-  __device__ bool next(const GramParams &p, int &tile_m, int &tile_n) {
-    if (!tri) {
-      for (;;) {  // a symmetric call with unequal row counts: skip tiles below the diagonal
-        k += gridDim.x;
-        if (k >= ntiles) return false;
-        tile_m = (k / ntn) * kBM;
-        tile_n = (k % ntn) * kBN;
-        if (!(p.symmetric && tile_m > tile_n + kBN - 1)) return true;
-      }
+  __device__ bool next(const GramParams &p, const GramGroupDev &g, int &inst, int &tile_m, int &tile_n) {
+    if (GRP) {
+      k += gridDim.x;
+      if (k >= ntiles) return false;
+      inst = find_instance(g.tile0, g.n, k);
+      const GramParams &q = g.ps[inst];
+      const int n_z = (q.nZ + kBN - 1) / kBN, n_m = (q.nA + kBM - 1) / kBM;
+      tile_coords(n_z, q.symmetric && n_m == n_z, k - g.tile0[inst], tile_m, tile_n);
+      return true;
     }
-    k += gridDim.x;
-    if (k >= ntiles) return false;
-    int i = 0, r = k;
-    while (r >= ntn - i) {  // row i of the upper triangle holds ntn - i tiles
-      r -= ntn - i;
-      ++i;
+    inst = 0;
+    for (;;) {
+      k += gridDim.x;
+      if (k >= ntiles) return false;
+      tile_coords(ntn, tri, k, tile_m, tile_n);
+      if (tri || !(p.symmetric && tile_m > tile_n + kBN - 1)) return true;
     }
-    tile_m = i * kBM;
-    tile_n = (i + r) * kBN;
-    return true;
   }
 };
 
-template <int TYPE>
-__global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, const double *__restrict__ T) {
+// The parameters of instance `inst` (a grouped launch) or the launch's own.
+template <bool GRP>
+__device__ __forceinline__ const GramParams &params_of(const GramParams &p, const GramGroupDev &g, int inst) {
+  if constexpr (GRP) return g.ps[inst];
+  else return p;
+}
+
+template <int TYPE, bool GRP>
+__global__ void __launch_bounds__(kThreads, 1)
+    gram_tc_kernel(GramParams p, GramGroupDev grp, const double *__restrict__ T) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ Smem sm;
   // stages first, on a 1024-byte boundary (swizzle atoms)
@@ -182,7 +225,6 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   volatile int *abort = &sm.abort;
-  const int P = p.P;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -207,25 +249,27 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = sm.tmem_base;
-  TileWalk walk(p);
-  int tile_m, tile_n;
+  TileWalk<GRP> walk(p, grp);
+  int inst, tile_m, tile_n;
 
   if (tid < kProducers) {
     // ---------------- producers ----------------
     const int side = tid >> 7, rr = tid & 127;  // side 0: A row rr, side 1: Z row rr
-    const uint8_t *base = side ? p.wZ : p.wA;
-    const uint32_t *rowb = side ? p.z_rowb : p.a_rowb;
-    const long long row_bytes = side ? p.z_row_bytes : p.a_row_bytes;
-    const int nrows = side ? p.nZ : p.nA;
     const uint32_t st0 = tc::smem_u32(stages);
     const uint32_t my_row = st0 + side * kStageA + (uint32_t)((rr >> 3) * kSBO + (rr & 7) * 128);
     const uint32_t my_sw = (uint32_t)(rr & 7);
-    const int G = P * kChunks;
     bool ok = true;
     // ring position of the next chunk: stage s, in pass `wrap` over the ring
     int s = 0, wrap = 0;
     int gbb = 0;  // blocks this CTA has produced
-    while (walk.next(p, tile_m, tile_n)) {
+    while (walk.next(p, grp, inst, tile_m, tile_n)) {
+      const GramParams &q = params_of<GRP>(p, grp, inst);
+      const uint8_t *base = side ? q.wZ : q.wA;
+      const uint32_t *rowb = side ? q.z_rowb : q.a_rowb;
+      const long long row_bytes = side ? q.z_row_bytes : q.a_row_bytes;
+      const int nrows = side ? q.nZ : q.nA;
+      const uint8_t *mask = q.mask;
+      const int G = q.P * kChunks;
       const int grow = (side ? tile_n : tile_m) + rr;
       const long long ro = grow < nrows ? (long long)rowb[grow] * row_bytes : -1;
       uint4 rm[kPrefetch], rx[kPrefetch];
@@ -234,7 +278,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
       auto load = [&](int g, uint4 &m, uint4 &x) {
         m = x = make_uint4(0, 0, 0, 0);
         if (g < G) {
-          m = __ldg(reinterpret_cast<const uint4 *>(p.mask) + g);
+          m = __ldg(reinterpret_cast<const uint4 *>(mask) + g);
           if (ro >= 0) x = __ldg(reinterpret_cast<const uint4 *>(base + ro) + g);
         }
       };
@@ -285,7 +329,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
       const uint32_t st0 = tc::smem_u32(stages);
       bool ok = true;
       int s = 0, wrap = 0, gbb = 0;
-      while (ok && walk.next(p, tile_m, tile_n)) {
+      while (ok && walk.next(p, grp, inst, tile_m, tile_n)) {
+        const int P = params_of<GRP>(p, grp, inst).P;
         for (int b = 0; b < P && ok; ++b, ++gbb) {
           const int t = gbb & 1;
           if (gbb >= 2)
@@ -330,29 +375,53 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
     const int col0 = (et >> 7) * kFoldCols;   // this warp's columns of the tile
     const int row = 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    // T_b of the CTA's g-th block (every tile has P blocks, so block g % P)
-    // into buffer g & 1 by one bulk copy.  Copies g = 0, 1 start here; the
-    // last fold warp to finish block g issues g + 2 into the buffer g read, so
-    // the fold warps are never held together at block boundaries.  (The two
-    // copies issued after the CTA's last block are waited for at the end.)
-    auto issue_table = [&](int t, long long g) {
+    // The table T_b of the CTA's g-th block goes into buffer g & 1 by one
+    // bulk copy.  Copies g = 0, 1 start here; the last fold warp to finish
+    // block g issues g + 2 into the buffer g read, so the fold warps are never
+    // held together at block boundaries.  issue_table(t, jt, boff) loads the
+    // block `boff` blocks after the start of this CTA's tile jt: block
+    // boff % P of a single Gram (every tile has P blocks); in a grouped launch
+    // it is found by walking on through this CTA's tiles, and nothing is
+    // loaded past its last block.  (Copies issued past the CTA's last block
+    // of a single Gram are waited for at the end.)
+    const int ntiles_grp = GRP ? grp.tile0[grp.n] : 0;
+    auto issue_table = [&](int t, int jt, int boff) {
+      int in = 0, blk = 0;
+      if constexpr (GRP) {
+        for (;;) {
+          const int k = (int)blockIdx.x + jt * (int)gridDim.x;
+          if (k >= ntiles_grp) return;
+          in = find_instance(grp.tile0, grp.n, k);
+          const int pj = grp.ps[in].P;
+          if (boff < pj) break;
+          boff -= pj;
+          ++jt;
+        }
+        blk = boff;
+      } else {
+        blk = boff % p.P;
+      }
+      const double *src = T + ((GRP ? grp.blk0[in] : 0ll) + blk) * (long long)kTabStride;
       tc::fence_proxy_async();
       tc::mbar_arrive_expect_tx(&sm.tab_full[t], kTabBytes);
-      tc::bulk_g2s(sT + t * kTabStride, T + (size_t)(g % P) * kTabStride, kTabBytes, &sm.tab_full[t]);
+      tc::bulk_g2s(sT + t * kTabStride, src, kTabBytes, &sm.tab_full[t]);
       atomicAdd(&sm.tab_issued[t], 1u);
     };
     if (et == 0) {
-      issue_table(0, 0);
-      issue_table(1, 1);
+      issue_table(0, 0, 0);
+      issue_table(1, 0, 1);
     }
     bool ok = true;
     long long gb0 = 0;
-    while (walk.next(p, tile_m, tile_n)) {
+    int jt = 0;  // this CTA's tiles so far
+    while (walk.next(p, grp, inst, tile_m, tile_n)) {
+      const GramParams &pp = params_of<GRP>(p, grp, inst);
+      const int P = pp.P;
       const int ga = tile_m + row;
-      const bool row_in = ga < p.nA;
-      const double lfa = (p.lfA && row_in) ? p.lfA[ga] : 0.0;
-      const long long orow = row_in ? (long long)p.out_r[ga] : 0;
-      const long long ocol2 = (p.symmetric && row_in) ? (long long)p.out_c2[ga] * p.out_stride : 0;
+      const bool row_in = ga < pp.nA;
+      const double lfa = (pp.lfA && row_in) ? pp.lfA[ga] : 0.0;
+      const long long orow = row_in ? (long long)pp.out_r[ga] : 0;
+      const long long ocol2 = (pp.symmetric && row_in) ? (long long)pp.out_c2[ga] * pp.out_stride : 0;
       for (int b = 0; b < P; ++b) {
         const long long gbb = gb0 + b;
         const int t = (int)(gbb & 1);
@@ -413,12 +482,12 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
 #pragma unroll
             for (int j = 0; j < kRound; ++j) {
               const int gz = tile_n + c0 + j;
-              if (gz >= p.nZ || (p.symmetric && ga > gz)) continue;
+              if (gz >= pp.nZ || (pp.symmetric && ga > gz)) continue;
               const double v = __hiloint2double((int)a[cur][2 * j + 1], (int)a[cur][2 * j]);
-              double o = (TYPE == 1) ? __dsub_rn(p.a0d1, twice(v)) : v;
-              if (p.lfA && p.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(lfa, p.lfZ[gz]), p.a2d1));
-              p.out[orow + (long long)p.out_c[gz] * p.out_stride] = o;
-              if (p.symmetric) p.out[(long long)p.out_r2[gz] + ocol2] = o;
+              double o = (TYPE == 1) ? __dsub_rn(pp.a0d1, twice(v)) : v;
+              if (pp.lfA && pp.lfZ) o = __dsub_rn(o, __dsub_rn(__dadd_rn(lfa, pp.lfZ[gz]), pp.a2d1));
+              pp.out[orow + (long long)pp.out_c[gz] * pp.out_stride] = o;
+              if (pp.symmetric) pp.out[(long long)pp.out_r2[gz] + ocol2] = o;
             }
           }
           if (ok && r + 1 < kRounds) {
@@ -438,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
             __threadfence_block();
             if (!*abort) {
               if (tc::mbar_wait_landed(&sm.tab_full[t], (uint32_t)((gbb >> 1) & 1)))
-                issue_table(t, gbb + 2);
+                issue_table(t, jt, b + 2);
               else
                 atomicCAS(&g_tc_status, 0, 9);
             }
@@ -450,6 +519,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
         if (lane == 0) tc::mbar_arrive(&sm.aux_empty[t]);
       }
       gb0 += P;
+      ++jt;
     }
     // every bulk copy into the tables has landed before the CTA exits (each
     // copy was issued after the previous one into its buffer landed)
@@ -471,11 +541,22 @@ __global__ void __launch_bounds__(kThreads, 1) gram_tc_kernel(GramParams p, cons
   }
 }
 
+__device__ __forceinline__ void write_table_row(double d, double *__restrict__ row) {
+  for (int c = threadIdx.x; c < kTabStride; c += blockDim.x)
+    row[c] = c < kTabStride - 1 ? __dmul_rn(d, (double)c) : __longlong_as_double(0x7ff8dead00000000ll);
+}
+
 __global__ void gram_table_kernel(const double *__restrict__ D, int P, double *__restrict__ T) {
   const int b = blockIdx.x;
-  const double d = D ? D[b] : 1.0;
-  for (int c = threadIdx.x; c < kTabStride; c += blockDim.x)
-    T[(size_t)b * kTabStride + c] = c < kTabStride - 1 ? __dmul_rn(d, (double)c) : __longlong_as_double(0x7ff8dead00000000ll);
+  write_table_row(D ? D[b] : 1.0, T + (size_t)b * kTabStride);
+}
+
+// Table rows of a grouped launch: row r is block r - blk0[i] of instance i.
+__global__ void gram_table_group_kernel(GramGroupDev g, double *__restrict__ T) {
+  const long long r = blockIdx.x;
+  const int in = find_instance(g.blk0, g.n, r);
+  const double *D = g.ps[in].D;
+  write_table_row(D ? D[r - g.blk0[in]] : 1.0, T + (size_t)r * kTabStride);
 }
 
 int sm_count() {
@@ -495,16 +576,30 @@ int active_tiles(const GramParams &p) {
   return (p.symmetric && ntm == ntn) ? ntn * (ntn + 1) / 2 : ntm * ntn;
 }
 
-template <int TYPE>
-void launch_tc_type(const GramParams &p, const double *T, cudaStream_t s) {
+template <int TYPE, bool GRP>
+void configure_tc() {
   static bool configured = false;
   if (!configured) {
-    LAKGB_CUDA(cudaFuncSetAttribute(gram_tc_kernel<TYPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    LAKGB_CUDA(cudaFuncSetAttribute(gram_tc_kernel<TYPE, GRP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kSmemBytes));
     configured = true;
   }
+}
+
+template <int TYPE>
+void launch_tc_type(const GramParams &p, const double *T, cudaStream_t s) {
+  configure_tc<TYPE, false>();
   const int grid = std::max(1, std::min(active_tiles(p), sm_count()));
-  gram_tc_kernel<TYPE><<<grid, kThreads, kSmemBytes, s>>>(p, T);
+  gram_tc_kernel<TYPE, false><<<grid, kThreads, kSmemBytes, s>>>(p, GramGroupDev{}, T);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+template <int TYPE>
+void launch_tc_group_type(const GramGroupDev &g, int total_tiles, const double *T, cudaStream_t s) {
+  configure_tc<TYPE, true>();
+  const int grid = std::max(1, std::min(total_tiles, sm_count()));
+  gram_tc_kernel<TYPE, true><<<grid, kThreads, kSmemBytes, s>>>(GramParams{}, g, T);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
 }
@@ -522,6 +617,22 @@ void launch_gram_tc(const GramParams &p, cudaStream_t s) {
   else
     launch_tc_type<2>(p, T, s);
   LAKGB_CUDA(cudaFreeAsync(T, s));
+}
+
+int gram_tc_tiles(const GramParams &p) { return active_tiles(p); }
+
+size_t gram_tc_table_row_bytes() { return (size_t)kTabBytes; }
+
+void launch_gram_tc_group(const GramGroupDev &g, int type, int total_tiles, long long total_blocks, double *T,
+                          cudaStream_t s) {
+  if (total_tiles <= 0 || total_blocks <= 0) return;
+  gram_table_group_kernel<<<(unsigned)total_blocks, 256, 0, s>>>(g, T);
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+  if (type == 1)
+    launch_tc_group_type<1>(g, total_tiles, T, s);
+  else
+    launch_tc_group_type<2>(g, total_tiles, T, s);
 }
 
 int *tc_status_device_ptr() {

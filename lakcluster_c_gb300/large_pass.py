@@ -206,3 +206,52 @@ class LargeGramPass:
             self.lib.lakgb_set_gram_impl(before)
         return {"products": len(self.args), "tensor_equals_popcount": identical, "sampled_entries": sampled,
                 "sampled_equal_host": sample_ok, "device_status": self.lib.lakgb_device_status()}
+
+
+class GroupedGramPasses:
+    """The Gram passes of several independent problems (e.g. label-shuffled
+    null instances), each product with its own output buffer, run either one
+    launch per product (``run_plain``) or as one grouped persistent launch of
+    the tensor-core kernel (``run_grouped``, lakgb_gram_group_run), which
+    gives the same outputs bit for bit."""
+
+    def __init__(self, passes):
+        import torch
+        self.torch = torch
+        self.passes = passes
+        self.lib = passes[0].lib
+        self.items = []
+        for ps in passes:
+            for key, a, n in ps.args:
+                out = torch.empty(n, dtype=torch.float64, device=ps.out.device)
+                a.out = out.data_ptr()
+                self.items.append((ps, key, a, out))
+        self.n = len(self.items)
+        arr = (GramArgs * self.n)()
+        for i, (_, _, a, _) in enumerate(self.items):
+            arr[i] = a
+        self._arr = arr
+        self.group = self.lib.lakgb_gram_group_create(C.cast(arr, C.c_void_p), self.n)
+        if not self.group:
+            raise RuntimeError("lakgb_gram_group_create failed")
+
+    def work_bitops(self) -> float:
+        return float(sum(ps.work_bitops() for ps in self.passes))
+
+    def outputs(self):
+        return [out for _, _, _, out in self.items]
+
+    def run_plain(self, stream_handle=0):
+        for _, _, a, _ in self.items:
+            a.stream = stream_handle
+            if self.lib.lakgb_gram_device(C.byref(a)) != 0:
+                raise RuntimeError("lakgb_gram_device failed")
+
+    def run_grouped(self, stream_handle=0):
+        if self.lib.lakgb_gram_group_run(self.group, C.c_void_p(stream_handle or None)) != 0:
+            raise RuntimeError("lakgb_gram_group_run failed")
+
+    def close(self):
+        if self.group:
+            self.lib.lakgb_gram_group_destroy(self.group)
+            self.group = None

@@ -212,3 +212,22 @@ class GramPassDevice:
             if rc != 0:
                 raise RuntimeError("lakgb_gram_device failed")
         return len(self.args)
+
+    def run_grouped(self, stream_handle: int = 0) -> int:
+        """The whole pass as one grouped persistent launch of the tensor-core
+        kernel (lakgb_gram_group_run): same outputs, one tile list over all
+        products instead of one launch per product."""
+        if getattr(self, "_group", None) is None:
+            arr = (GramArgs * len(self.args))(*self.args)
+            self._group_args = arr
+            self._group = self.lib.lakgb_gram_group_create(C.cast(arr, C.c_void_p), len(self.args))
+            if not self._group:
+                raise RuntimeError("lakgb_gram_group_create failed")
+        if self.lib.lakgb_gram_group_run(self._group, C.c_void_p(stream_handle or None)) != 0:
+            raise RuntimeError("lakgb_gram_group_run failed")
+        return 1
+
+    def close(self):
+        if getattr(self, "_group", None):
+            self.lib.lakgb_gram_group_destroy(self._group)
+            self._group = None

@@ -444,7 +444,12 @@ def run_gpu(args):
     fp64_per_elem = (P - 1) + 1 + (3 if (big.lfA and big.lfZ) else 0)
     fp64_ops = float(big.nA) * float(big.nZ) * fp64_per_elem
     fp64_rate = lib.lakgb_measure_fp64_add_rate()
-    traffic = _ncu_traffic("gram_tc_kernel")
+    traffic = _ncu_traffic("gram_tc_kernel_case_control")
+    g_traffic = _ncu_traffic("gram_tc_kernel_grouped")
+    g_tflops = 2.0 * work / (ms / 1000.0) / 1e12
+    # computed elements of the pass (symmetric products: the upper triangle)
+    pass_fp64 = sum((float(a.nA) * (a.nA + 1) / 2 if a.symmetric else float(a.nA) * a.nZ) for a in dev.args)
+    pass_fp64 *= fp64_per_elem
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     clocks = clk.summary()
     mhz = clocks.get("sm_mhz") or 1920.0
@@ -463,31 +468,37 @@ def run_gpu(args):
                        "parallelism": "replicas" if world > 1 else "single"},
             "gpu_launches": int(launches),
             "roofline": {
-                "bound": "tensor", "achieved": tflops, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": tflops / peak_tf, "traffic": traffic,
-                "kernel": "gram_tc_kernel (tcgen05 e4m3, largest AnZt launch, %dx%d rows, %d blocks)"
-                          % (big.nA, big.nZ, P),
-                "note": ("bit-pair products counted as 2 ops (one MAC) against the %s dense bf16 tensor peak; "
-                         "the e4m3 MMA this kernel issues is nominally 2x the bf16 rate. traffic: DRAM bytes of "
-                         "one launch from the committed ncu capture (profiles/), null when absent" % src),
-                "fp64_pipe": {"achieved_ops_per_s": fp64_ops / (k_ms / 1000.0), "peak_adds_per_s": fp64_rate,
-                              "frac": fp64_ops / (k_ms / 1000.0) / fp64_rate, "ops_per_launch": fp64_ops,
-                              "note": "FP64 adds of the block-weighted fold (%d per element) against the add "
-                                      "rate measured live on this GPU (lakgb_measure_fp64_add_rate); not the "
-                                      "sole bound: copies of the kernel without the adds, or without the table "
-                                      "loads, run at most 6 %% faster" % fp64_per_elem},
+                "bound": "tensor", "achieved": g_tflops, "peak": peak_tf, "unit": "TFLOP/s",
+                "frac": g_tflops / peak_tf, "traffic": g_traffic,
+                "kernel": "gram_tc_kernel<1, grouped> (tcgen05 e4m3): the pass's one persistent launch over "
+                          "the seven products' tiles",
+                "note": ("bit-pair products counted as 2 ops (one MAC) against the %s dense bf16 tensor peak "
+                         "(the e4m3 MMA the kernel issues is nominally 2x the bf16 rate); launch time = the "
+                         "step's CUDA-event time, which also holds the table launch (about 4 us). traffic: DRAM "
+                         "bytes of one launch from the committed ncu capture (profiles/), null when absent" % src),
+                "fp64_pipe": {"achieved_ops_per_s": pass_fp64 / (ms / 1000.0), "peak_adds_per_s": fp64_rate,
+                              "frac": pass_fp64 / (ms / 1000.0) / fp64_rate, "ops_per_launch": pass_fp64,
+                              "note": "FP64 operations of the fold and score combine (%d per computed element) "
+                                      "against the add rate measured live on this GPU "
+                                      "(lakgb_measure_fp64_add_rate)" % fp64_per_elem},
                 "vs_int_pipe_roofline": {
-                    "achieved_bitops": k_work / (k_ms / 1000.0), "int_pipe_peak_bitops": popc_peak,
-                    "ratio": (k_work / (k_ms / 1000.0)) / popc_peak,
-                    "note": "the tensor kernel against the integer-pipe roofline of a popcount Gram (POPC at "
-                            "16 lanes/clk/SM x 32 bits, sampled SM clock): above 1 means faster than any "
-                            "popcount kernel can run"},
+                    "achieved_bitops": work / (ms / 1000.0), "int_pipe_peak_bitops": popc_peak,
+                    "ratio": (work / (ms / 1000.0)) / popc_peak,
+                    "note": "the pass against the integer-pipe roofline of a popcount Gram (POPC at 16 lanes/clk/SM "
+                            "x 32 bits, sampled SM clock): above 1 means faster than any popcount kernel can run"},
+                "largest_single_launch": {
+                    "kernel": "gram_tc_kernel<1> alone on the largest AnZt product, %dx%d rows, %d blocks"
+                              % (big.nA, big.nZ, P),
+                    "kernel_ms": k_ms, "achieved": tflops, "frac": tflops / peak_tf, "traffic": traffic,
+                    "fp64_pipe_frac": fp64_ops / (k_ms / 1000.0) / fp64_rate,
+                    "vs_int_pipe_roofline": (k_work / (k_ms / 1000.0)) / popc_peak,
+                    "note": "not the sole bound: copies of the kernel without the FP64 adds, or without the "
+                            "table loads, run at most 6 % faster"},
                 "popcount_kernel": {"kernel_ms": k_ms_popc, "achieved_bitops": k_work / (k_ms_popc / 1000.0),
                                     "int_pipe_peak_bitops": popc_peak,
                                     "int_pipe_frac": (k_work / (k_ms_popc / 1000.0)) / popc_peak,
-                                    "note": "the CUDA-core kernel on the same launch; POPC issue-rate bound, "
+                                    "note": "the CUDA-core kernel on the largest product; POPC issue-rate bound, "
                                             "16 lanes/clk/SM x 32 bits at the sampled SM clock"},
-                "kernel_ms": k_ms,
             },
             "device_status": device_status,
             "per_launch_pass": per_launch,

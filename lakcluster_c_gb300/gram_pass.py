@@ -231,3 +231,30 @@ class GramPassDevice:
         if getattr(self, "_group", None):
             self.lib.lakgb_gram_group_destroy(self._group)
             self._group = None
+
+
+def main(argv=None):
+    """Run the case/control Gram pass on the GPU a few times, per product or as
+    one grouped launch (for profiling a single form of the pass)."""
+    import argparse
+    import time
+
+    ap = argparse.ArgumentParser(description="Run the case/control Gram pass (4096 + 4096 x 16384, 2 bins).")
+    ap.add_argument("--grouped", action="store_true", help="one grouped launch per pass")
+    ap.add_argument("--reps", type=int, default=3)
+    args = ap.parse_args(argv)
+    import torch
+    from . import synth
+    gp = GramPassHost(synth.case_control(seed=2))
+    dev = GramPassDevice(gp)
+    for r in range(args.reps):
+        t0 = time.perf_counter()
+        (dev.run_grouped if args.grouped else dev.run)(0)
+        torch.cuda.synchronize()
+        print("pass %d (%s): %.3f ms" % (r, "grouped" if args.grouped else "per product",
+                                         1e3 * (time.perf_counter() - t0)), flush=True)
+    dev.close()
+
+
+if __name__ == "__main__":
+    main()

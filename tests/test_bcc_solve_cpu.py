@@ -75,7 +75,9 @@ def test_library_exports_every_declared_entry_point():
     lib = ctypes.CDLL(lib_path)
     hdr = open(os.path.join(bc.ROOT, "include", "lakcluster_gb300.h")).read()
     hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
-    names = re.findall(r"^\s*(?:int|void|double|unsigned long long)\s+\**(\w+)\s*\(", hdr, flags=re.M)
+    names = re.findall(r"^\s*(?:int|void|double|unsigned long long|long long|lakgb_\w+|struct \w+)\s*\**\s*(\w+)\s*\(",
+                       hdr, flags=re.M)
+    assert "lakgb_gram_group_create" in names and "lakgb_server_create" in names
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing

@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "gram.cuh"
@@ -21,6 +22,9 @@ namespace {
 constexpr int kAjdk_0_1 = 5;
 constexpr int kAjdk_1_1 = 6;
 constexpr int kAjdk_2_1 = 7;
+
+// Host outputs at least this large come back in two parts (gram_entry).
+constexpr size_t kSplitDownloadBytes = size_t(8) << 20;
 
 int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_handle *M_An,
                M_handle *M_Zn, double *A_ajdk, L_handle *lf_An_ajdk, L_handle *lf_Zn_ajdk,
@@ -69,8 +73,9 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
   std::vector<uint32_t> arow(M_An->m_b_, M_An->m_b_ + nA), zrow(M_Zn->m_b_, M_Zn->m_b_ + nZ);
   DBuf d_arow = upload_vec(arow), d_zrow = upload_vec(zrow);
+  const std::vector<uint32_t> outc = spacing_index(spacing_c, M_Zn);
   DBuf d_outr = upload_vec(spacing_index(spacing_r, M_An));
-  DBuf d_outc = upload_vec(spacing_index(spacing_c, M_Zn));
+  DBuf d_outc = upload_vec(outc);
   DBuf d_outr2, d_outc2;
   if (symmetric) {
     d_outr2 = upload_vec(spacing_index(spacing_r, M_Zn));
@@ -112,6 +117,42 @@ int gram_entry(bool symmetric, int type_flag, int spacing_r, int spacing_c, M_ha
   p.out_stride = (long long)length_r; p.out = dout;
   p.symmetric = symmetric ? 1 : 0;
   st.flush();
+  // A large host output of a non-symmetric Gram comes back in two parts: the
+  // Z rows are split at a multiple of 128 rows (whole tensor-core tiles) into
+  // two launches, and the output columns of the first part (a contiguous
+  // range: column indices grow with the Z row) are downloaded while the
+  // second part computes.  Every element is computed exactly as by one
+  // launch.  (A symmetric Gram also writes the mirrored elements, which
+  // cross the column split, so it comes back in one piece.)
+  const int zsplit = ((nZ / 2) + 127) / 128 * 128;
+  if (!mo && !symmetric && length * sizeof(double) >= kSplitDownloadBytes && zsplit > 0 && zsplit < nZ &&
+      std::is_sorted(outc.begin(), outc.end())) {
+    GramParams q0 = p, q1 = p;
+    q0.nZ = zsplit;
+    q1.nZ = nZ - zsplit;
+    q1.z_rowb = p.z_rowb + zsplit;
+    q1.out_c = p.out_c + zsplit;
+    if (p.lfZ) q1.lfZ = p.lfZ + zsplit;
+    const unsigned long long c_mid = outc[zsplit];  // first output column of the second part
+    cudaEvent_t e0;
+    LAKGB_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+    launch_gram(q0);
+    LAKGB_CUDA(cudaEventRecord(e0, stream()));
+    launch_gram(q1);
+    {
+      LAKGB_PROFILE_CALL("(copy back + sync)");
+      fill.copied = true;
+      LAKGB_CUDA(cudaStreamWaitEvent(copy_stream(), e0, 0));
+      LAKGB_CUDA(cudaMemcpyAsync(out->lf, dout, c_mid * length_r * sizeof(double), cudaMemcpyDeviceToHost,
+                                 copy_stream()));
+      LAKGB_CUDA(cudaMemcpyAsync(out->lf + c_mid * length_r, dout + c_mid * length_r,
+                                 (length - c_mid * length_r) * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+      LAKGB_CUDA(cudaStreamSynchronize(copy_stream()));
+      LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    }
+    LAKGB_CUDA(cudaEventDestroy(e0));
+    return (int)length;
+  }
   launch_gram(p);
   if (mo) return (int)length;
   copy_back(out->lf, d_out, length, &fill);

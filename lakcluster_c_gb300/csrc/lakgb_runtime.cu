@@ -57,6 +57,12 @@ cudaStream_t stream() {
   return s;
 }
 
+cudaStream_t copy_stream() {
+  thread_local cudaStream_t s = nullptr;
+  if (!s) LAKGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  return s;
+}
+
 // --- per-thread staging arena -----------------------------------------------
 
 namespace {

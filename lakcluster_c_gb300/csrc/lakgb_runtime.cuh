@@ -25,6 +25,9 @@ void check_cuda(cudaError_t e, const char *what, const char *file, int line);
 #define LAKGB_CUDA(x) ::lakgb::check_cuda((x), #x, __FILE__, __LINE__)
 
 cudaStream_t stream();
+// A second per-thread stream (non-blocking) for downloads that overlap the
+// kernels on stream().
+cudaStream_t copy_stream();
 void count_launch(unsigned long long n = 1);
 
 // Device allocation on the library stream (stream-ordered allocator).

@@ -133,3 +133,26 @@ def test_autotuned_dispatch_matches_oracle(impl_switch, oracle_lib):
     table = json.loads(buf.value.decode())
     assert len(table) == 1
     assert table[0]["choice"] in table[0]["ms"] and len(table[0]["ms"]) == 5
+
+
+@pytest.mark.parametrize("sa,sb", [(abi.SPACING_b, abi.SPACING_b), (abi.SPACING_j, abi.SPACING_j),
+                                   (abi.SPACING_a, abi.SPACING_b), (abi.SPACING_b, abi.SPACING_a)])
+def test_large_host_output_two_part_download(impl_switch, oracle_lib, sa, sb):
+    """Host outputs of 8 MB or more of a non-symmetric Gram come back in two
+    parts (two launches over halves of the Z rows, the first half's columns
+    downloaded while the second computes): same values as the oracle for
+    every output spacing, with masked rows and columns."""
+    rng = np.random.default_rng(9000 + sa * 3 + sb)
+    MA, MZ = _case(rng, 1250, 1150, 3 * 1920 + 77, False)
+    A_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(3 * 1920 + 77)))
+    vA = kc.call_an_ajdk("oracle", abi.TYPE_pm, abi.SPACING_a, MA, A_ajdk)
+    vZ = kc.call_an_ajdk("oracle", abi.TYPE_pm, abi.SPACING_a, MZ, A_ajdk)
+    lfA = kc.lhandle_from(vA, MA.nrows, abi.AJDK_TOT, abi.SPACING_a)
+    lfZ = kc.lhandle_from(vZ, MZ.nrows, abi.AJDK_TOT, abi.SPACING_a)
+    want = kc.call_gram("oracle", False, abi.TYPE_pm, sa, sb, MA, MZ, A_ajdk, lfA, lfZ)
+    assert want.size * 8 >= 8 << 20  # large enough for the two-part download
+    for impl in (TENSOR, 2):
+        impl_switch.lakgb_set_gram_impl(impl)
+        got = kc.call_gram("gpu", False, abi.TYPE_pm, sa, sb, MA, MZ, A_ajdk, lfA, lfZ)
+        assert _bits_equal(got, want), impl
+        assert impl_switch.lakgb_device_status() == 0

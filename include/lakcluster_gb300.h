@@ -284,6 +284,21 @@ struct lakgb_gram_args {
 };
 int lakgb_gram_device(const struct lakgb_gram_args *args);
 
+/* .b16 bit-matrix transpose, file to file: the reference's wrap_transpose
+ * (dir_c/binary_read.c:174) with its signature.  Reads fname_0in (header
+ * bitj, n_row, n_col; n_col records of n_row bits padded to bitj), writes
+ * fname_out (header bitj, n_col, n_row; n_row records of n_col bits, padding
+ * bits zero), transposing on the GPU.  n_bytes_per_read (the reference's
+ * workspace chunk) is accepted and not needed.  Errors: a printed warning,
+ * as the reference does, and lakgb_last_error. */
+void wrap_transpose(char *fname_0in, char *fname_out, int n_bytes_per_read);
+/* The same transpose on device memory (no reference counterpart): n_records
+ * records of n_bits bits, each padded to 16 bits, into n_bits records of
+ * n_records bits padded to 16 bits, enqueued on `stream` (NULL: the library
+ * stream).  Returns 0, or -1 on bad arguments. */
+int lakgb_bits_transpose_device(const unsigned char *in, int n_records, int n_bits, unsigned char *out,
+                                void *stream);
+
 /* Grouped Gram (no reference counterpart): n independent Grams, each as
  * lakgb_gram_device would compute it (bit-identical outputs), run as ONE
  * persistent launch of the tensor-core kernel over all their tiles (plus one

@@ -56,6 +56,10 @@ def load() -> C.CDLL:
     lib.lakgb_gram_group_run.restype = C.c_int
     lib.lakgb_gram_group_destroy.argtypes = [C.c_void_p]
     lib.lakgb_gram_group_destroy.restype = None
+    lib.wrap_transpose.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+    lib.wrap_transpose.restype = None
+    lib.lakgb_bits_transpose_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    lib.lakgb_bits_transpose_device.restype = C.c_int
     _lib = lib
     return lib
 

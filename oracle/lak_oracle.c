@@ -688,3 +688,21 @@ int lako_An_ZtSWn_Yt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, str
   }
   return (int)(la * ls);
 }
+
+/* dir_c/binary_read.c:174-269: wrap_transpose sets bit (7 - nc % 8) of byte
+ * nc / 8 of output row nf from bit (7 - nf % 8) of byte nf / 8 of input record
+ * nc, and clears the bits of the padding columns n_col..n_col+extend-1.  Here
+ * every output byte starts at zero, so the padding bits stay zero. */
+void lako_bits_transpose(const unsigned char *in, long long in_rec_bytes, int n_in_rec, unsigned char *out,
+                         long long out_rec_bytes, int n_out_rec)
+{
+  memset(out, 0, (size_t)out_rec_bytes * (size_t)(n_out_rec > 0 ? n_out_rec : 0));
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < n_out_rec; ++r) {
+    unsigned char *o = out + (size_t)r * (size_t)out_rec_bytes;
+    for (int c = 0; c < n_in_rec; ++c) {
+      const unsigned char b = (in[(size_t)c * (size_t)in_rec_bytes + (size_t)(r / 8)] >> (7 - r % 8)) & 1;
+      o[c / 8] |= (unsigned char)(b << (7 - c % 8));
+    }
+  }
+}

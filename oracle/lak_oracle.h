@@ -75,6 +75,13 @@ int lako_An_ZtSWn_Yt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, str
                         struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_ZtSWn,
                         struct L_handle **out_p);
 
+/* dir_c/binary_read.c:174-269 (wrap_transpose), on memory: n_in_rec records
+ * of in_rec_bytes bytes (bits MSB first) into n_out_rec records of
+ * out_rec_bytes bytes, out record r bit c = in record c bit r; bits of out
+ * records past the last input record are zero. */
+void lako_bits_transpose(const unsigned char *in, long long in_rec_bytes, int n_in_rec, unsigned char *out,
+                         long long out_rec_bytes, int n_out_rec);
+
 /* Threads used by the OpenMP loops (default: all). */
 void lako_set_threads(int n);
 

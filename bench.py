@@ -427,6 +427,9 @@ def run_gpu(args):
     grouped = None
     if rank == 0 and not args.no_grouped:
         grouped = grouped_gram_measurement(stream, sh, flush)
+    transpose = None
+    if rank == 0 and not args.no_transpose:
+        transpose = transpose_measurement(stream, sh, with_cpu=not args.no_cpu_baseline)
 
     solves = None
     if rank == 0 and not args.no_solves:
@@ -513,6 +516,8 @@ def run_gpu(args):
             line["large_gram_pass"] = large
         if grouped is not None:
             line["grouped_null_gram_passes"] = grouped
+        if transpose is not None:
+            line["b16_transpose"] = transpose
         line["gram_autotune"] = autotune_summary(lib)
         if solves is not None:
             line["solves"] = solves
@@ -642,6 +647,73 @@ def grouped_gram_measurement(stream, sh, flush):
                     "kernel for every instance's blocks + one persistent tcgen05 launch over all instances' tiles"}
 
 
+def transpose_measurement(stream, sh, with_cpu: bool):
+    """The .b16 transposer (wrap_transpose, dir_c/binary_read.c:174): the
+    kernel on a matrix of the large configuration's size (131072 records of
+    32768 bits, 512 MB each way) against the measured HBM copy bandwidth; the
+    file-to-file call on a 64 MB file; the C oracle on the host cores on an
+    8192 x 8192-bit sample."""
+    import tempfile
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from lakcluster_c_gb300 import infiles
+    from lakcluster_c_gb300._lib import load
+
+    lib = load()
+    peaks, src = _peaks()
+    n_rec, n_bits = 131072, 32768
+    nbytes = n_rec * n_bits // 8
+    d_in = torch.randint(0, 256, (nbytes,), dtype=torch.uint8, device="cuda")
+    d_out = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        lib.lakgb_bits_transpose_device(d_in.data_ptr(), n_rec, n_bits, d_out.data_ptr(), C.c_void_p(sh))
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.lakgb_bits_transpose_device(d_in.data_ptr(), n_rec, n_bits, d_out.data_ptr(), C.c_void_p(sh))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    k_ms = statistics.median(ms)
+    gbs = 2.0 * nbytes / (k_ms / 1e3) / 1e9
+    del d_in, d_out
+    out = {"kernel": {"records": n_rec, "bits_per_record": n_bits, "bytes_each_way": nbytes, "ms": k_ms,
+                      "achieved_gbs": gbs, "peak_gbs": float(peaks.get("hbm_gbs", 6800.0)),
+                      "frac": gbs / float(peaks.get("hbm_gbs", 6800.0)),
+                      "note": "bytes read + bytes written per launch over its CUDA-event time, against the %s "
+                              "HBM copy bandwidth (inputs 512 MB, larger than L2)" % src}}
+    rng = np.random.default_rng(11)
+    x = (rng.random((8192, 65536)) < 0.5).astype(np.uint8)
+    with tempfile.TemporaryDirectory() as td:
+        p_in, p_out = os.path.join(td, "x.b16"), os.path.join(td, "x_t.b16")
+        infiles.write_b16(p_in, x)
+        lib.wrap_transpose(p_in.encode(), p_out.encode(), 1 << 20)  # warm
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            lib.wrap_transpose(p_in.encode(), p_out.encode(), 1 << 20)
+            t.append(time.perf_counter() - t0)
+        fb = os.path.getsize(p_in)
+        out["file_to_file"] = {"file_bytes": fb, "seconds": min(t), "gbs": 2.0 * fb / min(t) / 1e9,
+                               "note": "wrap_transpose on a 64 MB .b16 file (8192 records of 65536 bits): "
+                                       "read, upload, kernel, download, write"}
+    if with_cpu:
+        import kernel_cases as kc
+        n, m = 8192, 8192
+        a = np.random.default_rng(12).integers(0, 256, n * m // 8, dtype=np.uint8)
+        b = np.zeros_like(a)
+        lib_o = kc.load_backend("oracle")
+        t0 = time.perf_counter()
+        lib_o.lako_bits_transpose(a.ctypes.data_as(C.c_void_p), C.c_longlong(m // 8), n,
+                                  b.ctypes.data_as(C.c_void_p), C.c_longlong(n // 8), m)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"gbs": 2.0 * a.size / cs / 1e9, "seconds": cs, "cores": os.cpu_count(),
+                               "kind": "port", "sample": "8192 records of 8192 bits (8 MB) on the C oracle"}
+    return out
+
+
 def solve_measurements(args, with_cpu: bool):
     """Whole-solve timings: config 1 (case-only 1024 x 1024, the reference's
     CPU-runnable case) and the case/control workload above, through
@@ -768,6 +840,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solves", action="store_true", help="skip the whole-solve timings")
     ap.add_argument("--no-many", action="store_true", help="skip the batched / served timings")
+    ap.add_argument("--no-transpose", action="store_true", help="skip the .b16 transposer measurement")
     ap.add_argument("--no-grouped", action="store_true",
                     help="skip the grouped Gram passes of the batched-null instances")
     ap.add_argument("--no-large", action="store_true",

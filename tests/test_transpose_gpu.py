@@ -22,7 +22,8 @@ def test_wrap_transpose_matches_reference_golden(gpu_lib, tmp_path):
         assert tc.file_transpose("gpu", src, dst) == d["case%02d/out" % i].tobytes(), tc.SHAPES[i]
 
 
-@pytest.mark.parametrize("n,m,p", [(3000, 5000, 0.5), (70001, 300, 0.2), (300, 70001, 0.7), (4097, 4111, 0.01)])
+@pytest.mark.parametrize("n,m,p", [(3000, 5000, 0.5), (70001, 300, 0.2), (300, 70001, 0.7), (4097, 4111, 0.01),
+                                   (4096, 8192, 0.5), (96, 1056, 0.4), (33, 4128, 0.6)])
 def test_wrap_transpose_matches_oracle_large(gpu_lib, tmp_path, n, m, p):
     rng = np.random.default_rng(n * 7 + m)
     x = (rng.random((n, m)) < p).astype(np.uint8)
@@ -31,10 +32,10 @@ def test_wrap_transpose_matches_oracle_large(gpu_lib, tmp_path, n, m, p):
     assert tc.file_transpose("gpu", src, dst) == tc.oracle_transpose(raw)
 
 
-def test_device_transpose_round_trip(gpu_lib):
+@pytest.mark.parametrize("n,m", [(2345, 3071), (2048, 3072)])  # byte access; word access
+def test_device_transpose_round_trip(gpu_lib, n, m):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(5)
-    n, m = 2345, 3071
     in_rec, out_rec = 2 * ((m + 15) // 16), 2 * ((n + 15) // 16)
     x = (rng.random((n, m)) < 0.5).astype(np.uint8)
     packed = np.zeros((n, in_rec), np.uint8)

@@ -1689,6 +1689,10 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   S.hooks = hooks;
   S.out = &O;
   const char *prof = getenv("LAKBCC_PROFILE");
+  // LAKBCC_PROGRESS=N: a line on stderr every N iterations (long solves)
+  const char *prog = getenv("LAKBCC_PROGRESS");
+  const int progress = prog ? atoi(prog) : 0;
+  const auto t_start = std::chrono::steady_clock::now();
   g_clock = StageClock();
   g_clock.on = prof && *prof && *prof != '0';
   g_clock.last = std::chrono::steady_clock::now();
@@ -1720,6 +1724,10 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     doublestudy_ww(S); trace_stage(S, "doublestudy");
     flattenloop(S); trace_stage(S, "flattenloop");
     if (O.iterations > 10000000) { err = "iteration limit"; return 5; }
+    if (progress > 0 && O.iterations % progress == 0)
+      fprintf(stderr, " %% iteration %d: %u rows and %u columns left, %.1f s\n", O.iterations,
+              (unsigned)S.A_rpop_j_total, (unsigned)S.A_cpop_j,
+              std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count());
   }
   if (g_clock.on) {
     double tot = 0;

@@ -54,19 +54,22 @@ def pack_rows(bits) -> np.ndarray:
 
 
 class Problem:
-    """A packed bcc problem kept alive for repeated solves."""
+    """A packed bcc problem kept alive for repeated solves.  A_bins / Z_bins
+    are per-bin 0/1 arrays (rows x SNPs), or, with ``packed_ncols`` given,
+    rows already packed as pack_rows packs them (``packed_ncols`` SNPs)."""
 
     def __init__(self, A_bins, Z_bins=None, *, gamma=0.125, B_MLT=32, gamma_type=0, A_masks=None,
-                 Z_masks=None, col_mask=None, test_sparse=1, lib=None):
+                 Z_masks=None, col_mask=None, test_sparse=1, lib=None, packed_ncols=None):
         self.lib = bind(lib or load())
         self._keep = []
         nb = len(A_bins)
         Z_bins = Z_bins if Z_bins is not None else [None] * nb
-        ncols = np.asarray(A_bins[0]).shape[1]
+        ncols = packed_ncols if packed_ncols is not None else np.asarray(A_bins[0]).shape[1]
+        pk = (lambda x: np.ascontiguousarray(x, np.uint8)) if packed_ncols is not None else pack_rows
         self.bins = (BccBin * nb)()
         for b in range(nb):
             a = np.asarray(A_bins[b], np.uint8)
-            pa = self._hold(pack_rows(a))
+            pa = self._hold(pk(a))
             self.bins[b].A_nrows = a.shape[0]
             self.bins[b].A_rows = pa.ctypes.data
             if A_masks is not None:
@@ -75,7 +78,7 @@ class Problem:
             if z is not None and np.asarray(z).shape[0] > 0:
                 z = np.asarray(z, np.uint8)
                 self.bins[b].Z_nrows = z.shape[0]
-                self.bins[b].Z_rows = self._hold(pack_rows(z)).ctypes.data
+                self.bins[b].Z_rows = self._hold(pk(z)).ctypes.data
                 if Z_masks is not None:
                     self.bins[b].Z_mr_b = self._hold(pack_rows(Z_masks[b])).ctypes.data
         self.prob = BccProblem()
@@ -140,7 +143,40 @@ WORKLOADS = {
     "case_only_1024x1024": "cases 1024 x 1024 SNPs, 45 x 45 planted, gamma 0.05 (config 1)",
     "case_control_4096x4096x16384": "cases 4096 + controls 4096 x 16384 SNPs, 2 bins, gamma 0.05 (config 2)",
     "case_control_1024x1024x4096": "cases 1024 + controls 1024 x 4096 SNPs, 2 bins, gamma 0.05 (small config 2)",
+    "case_control_32768x32768x131072": "cases 32768 + controls 32768 x 131072 SNPs, 3 bins, gamma 0.02, "
+                                        "MAF U[0.01,0.5], 2048 x 4096 planted (config 3; drawn on the GPU)",
 }
+
+
+def large_problem(seed=3, lib=None, chunk_rows=2048, n_case=32768, n_ctrl=32768, ncols=131072, planted=(2048, 4096)):
+    """The large single-solve configuration as a Problem of packed rows: the
+    rows are drawn on the device in chunks (torch as plumbing: a seeded
+    generator, comparisons, an MSB-first pack) and copied to host memory,
+    since 4.3 G entries per matrix would not fit a host 0/1 array well."""
+    import torch
+    nbins, (pr, pc), flip = 3, planted, 0.05
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    p = 0.01 + 0.49 * torch.rand(ncols, generator=g, device="cuda")
+    pattern = torch.rand(pc, generator=g, device="cuda") < 0.5
+    w = torch.tensor([128, 64, 32, 16, 8, 4, 2, 1], dtype=torch.uint8, device="cuda")
+    out = {"A": [[] for _ in range(nbins)], "Z": [[] for _ in range(nbins)]}
+    for side, n in (("A", n_case), ("Z", n_ctrl)):
+        bins = torch.randint(0, nbins, (n,), generator=g, device="cuda")
+        for r0 in range(0, n, chunk_rows):
+            r1 = min(n, r0 + chunk_rows)
+            bits = torch.rand(r1 - r0, ncols, generator=g, device="cuda") < p
+            if side == "A" and r0 < pr:
+                k = min(r1, pr) - r0
+                bits[:k, :pc] = pattern ^ (torch.rand(k, pc, generator=g, device="cuda") < flip)
+            packed = (bits.view(r1 - r0, ncols // 8, 8).to(torch.uint8) * w).sum(dim=2, dtype=torch.uint8)
+            b = bins[r0:r1]
+            for nb in range(nbins):
+                out[side][nb].append(packed[b == nb].cpu().numpy())
+            del bits, packed
+    A = [np.concatenate(x) for x in out["A"]]
+    Z = [np.concatenate(x) for x in out["Z"]]
+    return Problem(A, Z, gamma=0.02, lib=lib, packed_ncols=ncols)
 
 
 def workload(name):
@@ -169,8 +205,11 @@ def main(argv=None):
     args = ap.parse_args(argv)
     import json
     import os
-    A, Z, gamma = workload(args.workload)
-    p = Problem(A, Z, gamma=gamma)
+    if args.workload == "case_control_32768x32768x131072":
+        p = large_problem()
+    else:
+        A, Z, gamma = workload(args.workload)
+        p = Problem(A, Z, gamma=gamma)
     p.lib.lakgb_set_gram_impl({"popcount": 0, "tensor": 1, "auto": 2, "split": 3}[args.gram_impl])
     profile = os.environ.get("LAKGB_PROFILE_CALLS", "0") not in ("", "0")
     for r in range(args.reps):

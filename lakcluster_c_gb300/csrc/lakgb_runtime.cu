@@ -250,7 +250,23 @@ std::map<std::string, CallStat> g_calls;
 thread_local long long t_child_ns = 0;  // time of the calls nested in the open one
 }  // namespace
 
+// LAKGB_SYNC_CALLS=1: every profiled entry point synchronises its stream on
+// return and names itself if a device error is pending (a diagnostic for
+// locating a failing kernel; it costs the overlap of host and device work).
+bool sync_calls_on() {
+  static const bool on = [] {
+    const char *e = getenv("LAKGB_SYNC_CALLS");
+    return e && *e && *e != '0';
+  }();
+  return on;
+}
+
+// Names of the profiled calls open on this thread, outermost first (for the
+// LAKGB_SYNC_CALLS report).
+thread_local std::vector<const char *> t_open_calls;
+
 CallTimer::CallTimer(const char *n) : name(n), t0(0) {
+  if (sync_calls_on()) t_open_calls.push_back(n);
   if (!profile_calls_on()) return;
   saved = t_child_ns;
   t_child_ns = 0;
@@ -258,6 +274,16 @@ CallTimer::CallTimer(const char *n) : name(n), t0(0) {
 }
 
 CallTimer::~CallTimer() {
+  if (sync_calls_on()) {
+    const cudaError_t e = cudaStreamSynchronize(stream());
+    if (e != cudaSuccess) {
+      fprintf(stderr, " %% Error! device error detected on leaving");
+      for (const char *c : t_open_calls) fprintf(stderr, " %s", c);
+      fprintf(stderr, ": %s\n", cudaGetErrorString(e));
+      exit(1);
+    }
+    if (!t_open_calls.empty()) t_open_calls.pop_back();
+  }
   if (!t0) return;
   const long long dt = now_ns() - t0;
   const long long self = dt - t_child_ns;

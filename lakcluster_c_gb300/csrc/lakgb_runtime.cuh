@@ -108,7 +108,8 @@ class Stager {
   template <class V> const typename V::value_type *put(const V &v) { return put(v.data(), v.size()); }
   void flush();
   // Copy n host bytes in (arena or a dedicated buffer); the returned device
-  // pointer is valid for kernels enqueued after flush().
+  // pointer is valid for kernels enqueued after flush() and before the
+  // Stager is destroyed (a dedicated buffer is freed with it).
   const void *put_bytes(const void *h, size_t n);
  private:
   bool active_ = false;

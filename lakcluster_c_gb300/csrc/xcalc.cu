@@ -24,6 +24,7 @@
 #include <math.h>
 
 #include <mutex>
+#include <optional>
 
 #include "abi_common.cuh"
 #include "bcc_model.h"
@@ -48,6 +49,8 @@ struct XcalcParams {
   int ncols_per;
   long long brows;           // bytes per plane row
   uint8_t *planes;
+  unsigned long long lf_n, planes_n;  // elements of lf, bytes of planes (bounds checks)
+  int *bad;                  // set when an index would leave its buffer (access skipped)
 };
 
 __global__ void xcalc_minmax_kernel(const double *lf, const long long *rows_j, int nr,
@@ -99,7 +102,9 @@ __global__ void xcalc_planes_kernel(XcalcParams p) {
   unsigned long long cz = 0ull;
   if (r < p.nrows_a) {
     const long long ro = p.row_off[r];
-    if (ro >= 0) {
+    if (ro >= 0 && (unsigned long long)(ro + p.col_off[c]) >= p.lf_n) {
+      atomicCAS(p.bad, 0, 1);
+    } else if (ro >= 0) {
       const double x = p.lf[ro + p.col_off[c]];
       cz = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
       if (cz < 1ull) cz = 1ull;
@@ -113,7 +118,9 @@ __global__ void xcalc_planes_kernel(XcalcParams p) {
       // ballot bit i = row 32w+i; memory wants row 8k+j at byte k, bit 7-j.
       const unsigned word = __byte_perm(__brev(bal), 0u, 0x0123);
       const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - nb;
-      *reinterpret_cast<unsigned *>(p.planes + plane * p.brows + 4ll * w) = word;
+      const unsigned long long off = (unsigned long long)(plane * p.brows + 4ll * w);
+      if (off + 4 > p.planes_n) atomicCAS(p.bad, 0, 2);
+      else *reinterpret_cast<unsigned *>(p.planes + off) = word;
     }
   }
 }
@@ -261,6 +268,20 @@ using namespace lakgb;
 
 extern "C" void lakgb_set_d_mlt(long long d_mlt) { g_d_mlt = d_mlt; }
 
+namespace lakgb {
+namespace {
+// Per-thread device flag of the planes kernel's bounds checks.
+int *bad_flag() {
+  thread_local int *d = nullptr;
+  if (!d) {
+    LAKGB_CUDA(cudaMalloc(&d, sizeof(int)));
+    LAKGB_CUDA(cudaMemset(d, 0, sizeof(int)));
+  }
+  return d;
+}
+}  // namespace
+}  // namespace lakgb
+
 extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigned char *mr_j,
                            unsigned char *mr_b, unsigned char *mc_j, unsigned char *mc_b,
                            L_handle *lf_YnWt, double *YnWt, int *Yn_nrows_p, int *Wn_nrows_p,
@@ -313,6 +334,7 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
   for (long long o : cols_j) max_coff = o > max_coff ? o : max_coff;
   const size_t lf_elems = (size_t)(max_off + max_coff + 1);
 
+  std::optional<Stager> st;
   DBuf d_lf, d_rows, d_cols, d_roff_all;
   double min_data = 0.0, max_data = 0.0;
   const int nr = (int)rows_j.size(), nc = (int)cols_j.size();
@@ -327,13 +349,13 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
       d_lf.upload(YnWt, lf_elems * sizeof(double));
       plf = d_lf.as<double>();
     }
-    {
-      Stager st;
-      d_rows = upload_vec(rows_j);
-      d_cols = upload_vec(cols_j);
-      d_roff_all = upload_vec(row_off_a);
-      st.flush();
-    }
+    // The Stager lives to the end of the call: arrays of 1 MB or more go to
+    // buffers it owns, which must outlive the kernels below.
+    st.emplace();
+    d_rows = upload_vec(rows_j);
+    d_cols = upload_vec(cols_j);
+    d_roff_all = upload_vec(row_off_a);
+    st->flush();
     const long long total = (long long)nr * nc;
     int blocks = (int)((total + 255) / 256);
     if (blocks > 1024) blocks = 1024;
@@ -345,10 +367,17 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
     count_launch();
     std::vector<double> hmin(blocks), hmax(blocks);
     std::vector<int> hany(blocks);
+    int hbad = 0;  // an earlier call's planes kernel met an index outside its buffers
+    LAKGB_CUDA(cudaMemcpyAsync(&hbad, bad_flag(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
     LAKGB_CUDA(cudaMemcpyAsync(hmin.data(), d_min.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
     LAKGB_CUDA(cudaMemcpyAsync(hmax.data(), d_max.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
     LAKGB_CUDA(cudaMemcpyAsync(hany.data(), d_any.p, blocks * sizeof(int), cudaMemcpyDeviceToHost, stream()));
     LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    if (hbad) {
+      printf(" %% Warning! wrap_xcalc: an earlier call skipped an out-of-range index (code %d)\n", hbad);
+      set_error(5, "wrap_xcalc: an earlier call skipped an out-of-range index (code %d)", hbad);
+      LAKGB_CUDA(cudaMemsetAsync(bad_flag(), 0, sizeof(int), stream()));
+    }
     bool set = false;
     for (int i = 0; i < blocks; ++i) {
       if (!hany[i]) continue;
@@ -386,6 +415,9 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
       p.col_off = d_cols.as<long long>(); p.ncols_j = nc;
       p.min = min; p.mlt = mlt; p.dmax = (unsigned long long)(g_d_mlt - 1);
       p.ncols_per = ncols_per; p.brows = brows; p.planes = planes.as<uint8_t>();
+      p.lf_n = (plf == d_lf.p) ? (unsigned long long)lf_elems : (unsigned long long)mlf->n;
+      p.planes_n = (unsigned long long)nbytes;
+      p.bad = bad_flag();
       const long long warps = (long long)((Yn_nrows + 31) / 32) * nc;
       const int blocks = (int)((warps * 32 + 255) / 256);
       xcalc_planes_kernel<<<blocks, 256, 0, stream()>>>(p);

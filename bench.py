@@ -431,6 +431,10 @@ def run_gpu(args):
     if rank == 0 and not args.no_transpose:
         transpose = transpose_measurement(stream, sh, with_cpu=not args.no_cpu_baseline)
 
+    ztswn_ww = None
+    if rank == 0 and not args.no_ww:
+        ztswn_ww = ztswn_ww_measurement(with_cpu=not args.no_cpu_baseline)
+
     solves = None
     if rank == 0 and not args.no_solves:
         solves = solve_measurements(args, with_cpu=(world == 1 and not args.no_cpu_baseline))
@@ -518,6 +522,8 @@ def run_gpu(args):
             line["grouped_null_gram_passes"] = grouped
         if transpose is not None:
             line["b16_transpose"] = transpose
+        if ztswn_ww is not None:
+            line["an_ztswn_yt_ww"] = ztswn_ww
         line["gram_autotune"] = autotune_summary(lib)
         if solves is not None:
             line["solves"] = solves
@@ -831,6 +837,78 @@ def _products(nbins):
     return products(nbins)
 
 
+def ztswn_ww_measurement(with_cpu: bool):
+    """The bit-plane loop product An_ZtSWn_Yt_ww (dir_c/An_ZtSWn_Yt_ww.c:5-111):
+    2048 patient rows x 16384 SNPs against the 32-bit planes of 1024 Wt rows
+    (one covariate column), operands resident; median of 5 calls, each with its
+    small uploads and its 16 KB download.  Work counted as the reference counts
+    it (:108): rows x covariates x Wt rows x ncols_per_z x padded SNP bits,
+    against the integer-pipe roofline (POPC, 16 lanes/clk/SM x 32 bits at the
+    maximum SM clock).  The first 64 rows are checked against the C oracle,
+    which is also timed on them."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from lakcluster_c_gb300 import abi
+    from lakcluster_c_gb300._lib import load
+
+    lib = load()
+    rng = np.random.default_rng(21)
+    n, m, nw, B = 2048, 16384, 1024, 32
+    mcl, ycl = abi.bsize(m), abi.bsize(nw)
+    a_bytes = rng.integers(0, 256, (n, mcl), dtype=np.uint8)
+    y_bytes = rng.integers(0, 256, (n, ycl), dtype=np.uint8)
+
+    def handles(rows):
+        An = abi.MHandle(None, nrows=rows, ncols=m, wX=a_bytes[:rows])
+        Yn = abi.MHandle(None, nrows=rows, ncols=nw, wX=y_bytes[:rows])
+        return An, Yn
+
+    Wt = abi.MHandle(None, nrows=nw, ncols=16, wX=np.zeros((nw, abi.bsize(16)), np.uint8))
+    St = abi.MHandle(None, nrows=1, ncols=16, wX=np.zeros((1, abi.bsize(16)), np.uint8))
+    pl = abi.MHandle(None, nrows=(B + 1) * nw, ncols=m,
+                     wX=rng.integers(0, 256, ((B + 1) * nw, mcl), dtype=np.uint8))
+    pl.s.ncols_per_z, pl.s.min_d, pl.s.mlt_d = B + 1, -2.5, float(2 ** 32) / 7.0
+    arr = (C.POINTER(abi.M_handle) * 1)(C.pointer(pl.s))
+    A_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(m)))
+    Y_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(nw)))
+    dp = C.POINTER(C.c_double)
+
+    def call(fn, An, Yn, gpu):
+        out = C.POINTER(abi.L_handle)()
+        args = (abi.SPACING_a, abi.SPACING_a, An.ptr, St.ptr, arr, Wt.ptr, Yn.ptr, A_ajdk.ctypes.data_as(dp),
+                Y_ajdk.ctypes.data_as(dp), C.byref(out))
+        k = fn(C.byref(C.c_int(0)), (C.c_void_p * 128)(), None, *args) if gpu else fn(*args)
+        return np.ctypeslib.as_array(C.cast(out.contents.lf, dp), (k,)).copy()
+
+    An, Yn = handles(n)
+    lib.lakgb_set_residency(1)
+    try:
+        got = call(lib.wrap_An_ZtSWn_Yt_ww__run, An, Yn, True)
+        t = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            call(lib.wrap_An_ZtSWn_Yt_ww__run, An, Yn, True)
+            t.append(time.perf_counter() - t0)
+    finally:
+        lib.lakgb_set_residency(0)
+    secs = statistics.median(t)
+    work = float(n) * 1 * nw * (B + 1) * mcl * 8
+    peak = 16.0 * 32 * 152 * 2070e6
+    out = {"workload": "2048 rows x 16384 SNPs, 1024 Wt rows x 33 planes, 1 covariate column",
+           "seconds": secs, "bitops": work, "bitops_per_s": work / secs, "int_pipe_peak_bitops": peak,
+           "int_pipe_frac": work / secs / peak, "device_status": int(lib.lakgb_device_status())}
+    import kernel_cases as kc
+    lib_o = kc.load_backend("oracle")
+    As, Ys = handles(64)
+    t0 = time.perf_counter()
+    want = call(lib_o.lako_An_ZtSWn_Yt_ww, As, Ys, False)
+    cs = time.perf_counter() - t0
+    out["first_64_rows_equal_oracle"] = bool(np.array_equal(got[:64].view(np.uint64), want[:64].view(np.uint64)))
+    if with_cpu:
+        out["cpu_baseline"] = {"bitops_per_s": work * 64 / n / cs, "seconds": cs, "cores": os.cpu_count(),
+                               "kind": "port", "sample": "the first 64 rows on the C oracle"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -841,6 +919,7 @@ def main():
     ap.add_argument("--no-solves", action="store_true", help="skip the whole-solve timings")
     ap.add_argument("--no-many", action="store_true", help="skip the batched / served timings")
     ap.add_argument("--no-transpose", action="store_true", help="skip the .b16 transposer measurement")
+    ap.add_argument("--no-ww", action="store_true", help="skip the An_ZtSWn_Yt_ww bit-plane product measurement")
     ap.add_argument("--no-grouped", action="store_true",
                     help="skip the grouped Gram passes of the batched-null instances")
     ap.add_argument("--no-large", action="store_true",

@@ -193,6 +193,16 @@ int wrap_An_ZtSWn_Yt_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int o
                              struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk,
                              struct L_handle *lf_ZtSWn, struct L_handle **output_p);
 
+/* The same product through bit planes: M_ZtSWn_[s] (one per retained St row)
+ * holds the wrap_xcalc planes of that ZtSWn slice, ncols_per_z rows per
+ * retained Wt row; the Wt handle supplies those rows' indices, An row paired
+ * with Yn row.  Replaces wrap_An_ZtSWn_Yt_ww__run, dir_c/An_ZtSWn_Yt_ww.c:113
+ * (kernel :5-111). */
+int wrap_An_ZtSWn_Yt_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a, int spacing_s,
+                             struct M_handle *M_An, struct M_handle *M_St, struct M_handle **M_ZtSWn_,
+                             struct M_handle *M_Wt, struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk,
+                             struct L_handle **output_An_ZtSWn_Yt_ww_p);
+
 /* ---------------------------------------------------------------------------
  * Whole solves.
  * ------------------------------------------------------------------------- */

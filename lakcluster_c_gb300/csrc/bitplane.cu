@@ -304,6 +304,237 @@ inline unsigned long long pick_u(int s, unsigned long long j, unsigned long long
   return s == LAKGB_SPACING_j ? j : (s == LAKGB_SPACING_b ? b : a);
 }
 
+// An_ZtSWn_Yt_ww (dir_c/An_ZtSWn_Yt_ww.c:5-111).  For St row s the planes of
+// one xcalc'd ZtSWn slice (B value planes per Wt row after the mask plane);
+// with pm0_lf(x, y; D) = sum over 1920-bit blocks, in order, of
+// D[block] * pm0_block(x, y) (popcount_pm0_lf, dir_c/popcount.c:556-621):
+//   X(a, w) = (pm0_lf(An_a, p0; D01)*min*mlt + sum_k 2^k pm0_lf(An_a, plane(w, k); D01)) / mlt
+//           - (pm0_lf(p0, p0; D11)*min*mlt + sum_k 2^k pm0_lf(p0, plane(w, k); D11)) / mlt
+//   out[a, s] = sum over w in order of X(a, w) * D_Y[w] * (vY(a, w) - a_Y[w]).
+// Kernels: the pm0_lf terms of p0 and of each An row against p0 (warp per
+// value); then one CTA per (32 paired rows, 256/B Wt rows, s) stages per block
+// the 32 An rows and its 256 masked plane rows in shared memory, each thread
+// folds its 4 x 8 tile of block counts into FP64 sums with the block's D (no
+// FMA), as the reference does per plane row, and the CTA writes X for its
+// rows and Wt rows to a scratch array; a last kernel adds the X terms of each
+// (row, s) in Wt order onto the output.  Wt rows are taken in ranges sized so
+// the scratch stays bounded, the output carrying the running sums between ranges.
+struct AnZtSWnParams {
+  const uint8_t *An; const uint32_t *a_rowb; long long a_row_bytes; int n;
+  const uint8_t *Yn; const uint32_t *y_rowb; long long y_row_bytes;
+  const uint8_t *mask; int P;
+  const uint8_t *const *planes; long long plane_bytes; const double *min_d, *mlt_d;
+  int nS, ncols_per, B, nW;
+  const double *D01, *D11;
+  const uint32_t *w_a; const double *wD, *wa;
+  const double *base_, *t_, *baseA;
+  double *X; int w_lo, w_hi;  // scratch X[(s*(w_hi-w_lo) + w - w_lo)*n + row] for Wt rows [w_lo, w_hi)
+  const unsigned long long *out_r, *s_off;
+  double *out;
+};
+
+__device__ __forceinline__ double pm0_lf_warp(const uint32_t *x, const uint32_t *y, const uint32_t *m,
+                                              const double *D, int P, int lane) {
+  double acc = 0.0;
+  for (int blk = 0; blk < P; ++blk) {
+    int pos = 0, all = 0;
+    for (int i = lane; i < kBlockWords; i += 32) {
+      const int w = blk * kBlockWords + i;
+      const uint32_t ym = __ldg(y + w) & __ldg(m + w);
+      pos += __popc(__ldg(x + w) & ym);
+      all += __popc(ym);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      pos += __shfl_xor_sync(0xffffffffu, pos, o);
+      all += __shfl_xor_sync(0xffffffffu, all, o);
+    }
+    acc = __dadd_rn(acc, __dmul_rn(__ldg(D + blk), (double)(2 * pos - all)));
+  }
+  return acc;
+}
+
+// Warps [0, nS*nq): dq[s][q] = pm0_lf(p0, y_q; D11), y_0 = p0 and
+// y_{1 + w*B + k} = plane(w, k).  Warps [nS*nq, nS*(nq + n)):
+// baseA[s][r] = pm0_lf(An_r, p0; D01) * min * mlt.
+__global__ void an_ztswn_prep_kernel(AnZtSWnParams p, double *dq, double *baseA) {
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long nq = 1 + (long long)p.nW * p.B;
+  const uint32_t *m = reinterpret_cast<const uint32_t *>(p.mask);
+  if (warp < nq * p.nS) {
+    const int s = (int)(warp / nq), q = (int)(warp % nq);
+    const uint8_t *pl = p.planes[s];
+    const int prow = q == 0 ? 0 : plane_row((q - 1) / p.B, (q - 1) % p.B, p.ncols_per);
+    const double v = pm0_lf_warp(reinterpret_cast<const uint32_t *>(pl),
+                                 reinterpret_cast<const uint32_t *>(pl + (long long)prow * p.plane_bytes), m,
+                                 p.D11, p.P, lane);
+    if (lane == 0) dq[warp] = v;
+    return;
+  }
+  const long long e = warp - nq * p.nS;
+  if (e >= (long long)p.nS * p.n) return;
+  const int s = (int)(e / p.n), r = (int)(e % p.n);
+  const double v = pm0_lf_warp(reinterpret_cast<const uint32_t *>(p.An + (long long)p.a_rowb[r] * p.a_row_bytes),
+                               reinterpret_cast<const uint32_t *>(p.planes[s]), m, p.D01, p.P, lane);
+  if (lane == 0) baseA[e] = __dmul_rn(__dmul_rn(v, p.min_d[s]), p.mlt_d[s]);
+}
+
+// base_[s] = dq[s][0]*min*mlt;  t_[s][w] = sum_k 2^k dq[s][1 + w*B + k], k upward.
+__global__ void an_ztswn_tsum_kernel(AnZtSWnParams p, const double *dq, double *base_, double *t_) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)p.nS * (p.nW + 1)) return;
+  const int s = (int)(idx / (p.nW + 1)), w = (int)(idx % (p.nW + 1)) - 1;
+  const double *row = dq + (long long)s * (1 + (long long)p.nW * p.B);
+  if (w < 0) {
+    base_[s] = __dmul_rn(__dmul_rn(row[0], p.min_d[s]), p.mlt_d[s]);
+    return;
+  }
+  double t = 0.0, n2 = 1.0;
+  for (int k = 0; k < p.B; ++k) {
+    t = __dadd_rn(t, __dmul_rn(n2, row[1 + (long long)w * p.B + k]));
+    n2 *= 2.0;
+  }
+  t_[(long long)s * p.nW + w] = t;
+}
+
+// Two CTAs per SM (128 registers, a 32-byte spill): 1.5x the throughput of
+// one CTA per SM with 243 registers on 2048 x 16384 x (1024 x 33 planes).
+__global__ void __launch_bounds__(kBP_T, 2)
+an_ztswn_ww_kernel(AnZtSWnParams p) {
+  // Dynamic shared memory, two phases: As (kBP_M x kLd words) and Ys (kBP_N x
+  // kLd words) during the block loop; then dv (kBP_M x (kBP_N+1) doubles, the
+  // per-plane sums) over the same bytes.
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t *As = smem;
+  uint32_t *Ys = smem + kBP_M * kLd;
+  double *dv = reinterpret_cast<double *>(smem);
+  __shared__ long long a_off[kBP_M];
+  __shared__ int yrow[kBP_N];
+  __shared__ int ycs[kBP_N];
+
+  const int CW = kBP_N / p.B;  // Wt rows per CTA
+  const int s = blockIdx.z;
+  const int r0 = blockIdx.x * kBP_M;
+  const int w0 = p.w_lo + blockIdx.y * CW;
+  const int tid = threadIdx.x;
+  const int tx = tid & 31, ty = tid >> 5;
+  const uint8_t *pl = p.planes[s];
+  const double mlt = p.mlt_d[s];
+
+  for (int i = tid; i < kBP_M; i += kBP_T)
+    a_off[i] = (r0 + i < p.n) ? (long long)p.a_rowb[r0 + i] * p.a_row_bytes : -1;
+  for (int q = tid; q < kBP_N; q += kBP_T) {
+    const int wl = q / p.B, k = q % p.B;
+    yrow[q] = (q < CW * p.B && w0 + wl < p.w_hi) ? plane_row(w0 + wl, k, p.ncols_per) : -1;
+  }
+  double acc[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0;
+
+  for (int blk = 0; blk < p.P; ++blk) {
+    __syncthreads();
+    const long long boff = (long long)blk * kBlockBytes;
+    const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + boff);
+    for (int idx = tid; idx < kBP_M * 15; idx += kBP_T) {
+      const int r = idx / 15, v = idx - r * 15;
+      uint4 x = make_uint4(0u, 0u, 0u, 0u);
+      if (a_off[r] >= 0) x = __ldg(reinterpret_cast<const uint4 *>(p.An + a_off[r] + boff) + v);
+      uint32_t *d = As + r * kLd + 4 * v;
+      d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
+    }
+    for (int idx = tid; idx < kBP_N * 15; idx += kBP_T) {
+      const int r = idx / 15, v = idx - r * 15;
+      uint4 x = make_uint4(0u, 0u, 0u, 0u);
+      const int pr = yrow[r];
+      if (pr >= 0) {
+        const uint4 y = __ldg(reinterpret_cast<const uint4 *>(pl + (long long)pr * p.plane_bytes + boff) + v);
+        const uint4 m = __ldg(mk + v);
+        x.x = y.x & m.x; x.y = y.y & m.y; x.z = y.z & m.z; x.w = y.w & m.w;
+      }
+      uint32_t *d = Ys + r * kLd + 4 * v;
+      d[0] = x.x; d[1] = x.y; d[2] = x.z; d[3] = x.w;
+    }
+    __syncthreads();
+    {
+      int c = 0;
+      for (int w = 0; w < kBlockWords; ++w) c += __popc(Ys[tid * kLd + w]);
+      ycs[tid] = c;
+    }
+    int c[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) c[i][j] = 0;
+#pragma unroll 4
+    for (int w = 0; w < kBlockWords; ++w) {
+      uint32_t a[4], y[8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[(ty * 4 + i) * kLd + w];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) y[j] = Ys[(tx + 32 * j) * kLd + w];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) c[i][j] += __popc(a[i] & y[j]);
+    }
+    __syncthreads();
+    const double D = __ldg(p.D01 + blk);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        acc[i][j] = __dadd_rn(acc[i][j], __dmul_rn(D, (double)(2 * c[i][j] - ycs[tx + 32 * j])));
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) dv[(ty * 4 + i) * (kBP_N + 1) + tx + 32 * j] = acc[i][j];
+  __syncthreads();
+  // X for (row, Wt row): consecutive threads take consecutive rows, so the
+  // scratch writes (rows contiguous per Wt row) coalesce.
+  const double base_ = p.base_[s];
+  const long long wspan = p.w_hi - p.w_lo;
+  for (int e = tid; e < kBP_M * CW; e += kBP_T) {
+    const int r = e % kBP_M, wl = e / kBP_M;
+    const int w = w0 + wl;
+    if (w >= p.w_hi || r0 + r >= p.n) continue;
+    double t = 0.0, n2 = 1.0;
+    for (int k = 0; k < p.B; ++k) {
+      t = __dadd_rn(t, __dmul_rn(n2, dv[r * (kBP_N + 1) + wl * p.B + k]));
+      n2 *= 2.0;
+    }
+    const double X = __dsub_rn(__ddiv_rn(__dadd_rn(p.baseA[(long long)s * p.n + r0 + r], t), mlt),
+                               __ddiv_rn(__dadd_rn(base_, p.t_[(long long)s * p.nW + w]), mlt));
+    p.X[((long long)s * wspan + (w - p.w_lo)) * p.n + r0 + r] = X;
+  }
+}
+
+// out[row, s] += X(row, w) * D_Y[w] * (vY(row, w) - a_Y[w]) for w in [w_lo, w_hi), in order.
+__global__ void an_ztswn_sum_kernel(AnZtSWnParams p) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)p.nS * p.n) return;
+  const int s = (int)(e / p.n), r = (int)(e % p.n);
+  const long long y_off = (long long)p.y_rowb[r] * p.y_row_bytes;
+  double *o = p.out + p.out_r[r] + p.s_off[s];
+  double acc = *o;
+  const long long wspan = p.w_hi - p.w_lo;
+  const double *x = p.X + (long long)s * wspan * p.n + r;
+  for (int w = p.w_lo; w < p.w_hi; ++w) {
+    const uint32_t wa = p.w_a[w];
+    const int vY = ((p.Yn[y_off + (wa >> 3)] >> (7 - (wa & 7))) & 1) ? 1 : -1;
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(x[(long long)(w - p.w_lo) * p.n], p.wD[w]), __dsub_rn((double)vY, p.wa[w])));
+  }
+  *o = acc;
+}
+
+constexpr size_t kAnZtSWnSmem = std::max((size_t)(kBP_M + kBP_N) * kLd * sizeof(uint32_t),
+                                          (size_t)kBP_M * (kBP_N + 1) * sizeof(double));
+constexpr size_t kAnZtSWnScratch = 256ull << 20;  // bytes of X scratch per range of Wt rows
+
 }  // namespace
 
 }  // namespace lakgb
@@ -468,6 +699,132 @@ extern "C" int wrap_An_ZtSn_ww__run(int *tidx, void **vpra, pthread_t *thread_in
   an_ztsn_kernel<<<(n * 32 + 255) / 256, 256, 0, stream()>>>(p);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
+  copy_back(out->lf, d_out, length);
+  return (int)length;
+}
+
+extern "C" int wrap_An_ZtSWn_Yt_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a, int spacing_s,
+                                        M_handle *M_An, M_handle *M_St, M_handle **M_ZtSWn_, M_handle *M_Wt,
+                                        M_handle *M_Yn, double *A_ajdk, double *Y_ajdk, L_handle **output_p) {
+  LAKGB_PROFILE_CALL("wrap_An_ZtSWn_Yt_ww__run");
+  (void)tidx; (void)vpra; (void)thread_in;
+  const unsigned long long length_a = spacing_length(spacing_a, M_An);
+  const unsigned long long length_s = spacing_length(spacing_s, M_St);
+  const unsigned long long length = length_a * length_s;
+  L_handle *out = ensure_output(output_p, length, "wrap_An_ZtSWn_Yt_ww__run");
+  if (!out) return (int)length;
+  out->spacing_row = spacing_a; out->row_stride = length_a;
+  out->spacing_col = spacing_s; out->col_stride = length_s;
+  const int nS = (int)M_St->rpop_j;
+  const int n = (int)std::min(M_An->rpop_j, M_Yn->rpop_j);
+  const int nW = (int)M_Wt->rpop_j;
+  if (nS == 0 || n == 0 || nW == 0) return (int)length;  // empty sums: the zeros ensure_output wrote
+  if (!M_ZtSWn_ || !A_ajdk || !Y_ajdk) {
+    set_error(4, "wrap_An_ZtSWn_Yt_ww__run: planes or allele weights missing");
+    return (int)length;
+  }
+  const int ncols_per = M_ZtSWn_[0] ? M_ZtSWn_[0]->ncols_per_z : 0, B = ncols_per - 1;
+  for (int s = 0; s < nS; ++s) {
+    const M_handle *Z = M_ZtSWn_[s];
+    if (!Z || Z->ncols_per_z != ncols_per || B < 1 || B > 62 || Z->mc_length != M_An->mc_length ||
+        (long long)nW * ncols_per > Z->nrows) {
+      set_error(4, "wrap_An_ZtSWn_Yt_ww__run: planes of St row %d missing, of unequal length or B_MLT out of range", s);
+      return (int)length;
+    }
+  }
+  if ((long long)M_Yn->mc_length * 8 < M_Wt->nrows) {
+    set_error(4, "wrap_An_ZtSWn_Yt_ww__run: Yn rows shorter than the Wt rows they index");
+    return (int)length;
+  }
+  const int P = (int)(M_An->mc_length / kBlockBytes);
+  const int A_pcols = (int)lakbcc::psize(M_An->ncols), Y_pcols = (int)lakbcc::psize(M_Yn->ncols);
+  const double *D01 = A_ajdk + (size_t)lakbcc::AJDK_0_1 * A_pcols;
+  const double *D11 = A_ajdk + (size_t)lakbcc::AJDK_1_1 * A_pcols;
+  const double *D_Yn = Y_ajdk + (size_t)lakbcc::AJDK_0_1 * Y_pcols;
+  const double *a_Yn = Y_ajdk + (size_t)lakbcc::AJDK_1_0 * Y_pcols;
+
+  std::vector<uint32_t> a_rowb(n), y_rowb(n), w_a(nW);
+  std::vector<unsigned long long> out_r(n), s_off(nS);
+  std::vector<double> wD(nW), wa(nW), mins(nS), mlts(nS);
+  std::vector<double> d01(D01, D01 + P), d11(D11, D11 + P);
+  for (int i = 0; i < n; ++i) {
+    a_rowb[i] = M_An->m_b_[i]; y_rowb[i] = M_Yn->m_b_[i];
+    out_r[i] = pick_u(spacing_a, i, M_An->m_b_[i], M_An->m_a_[i]);
+  }
+  for (int w = 0; w < nW; ++w) {
+    w_a[w] = M_Wt->m_a_[w];
+    wD[w] = D_Yn[w_a[w] / lakbcc::POPLENGTH];
+    wa[w] = a_Yn[w_a[w] / lakbcc::POPLENGTH];
+  }
+  AnZtSWnParams p{};
+  Stager st;
+  std::vector<const uint8_t *> planes(nS);
+  for (int s = 0; s < nS; ++s) {
+    s_off[s] = pick_u(spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * length_a;
+    const M_handle *Z = M_ZtSWn_[s];
+    planes[s] = (const uint8_t *)resident(Z->wX, (size_t)Z->nrows * Z->mc_length);
+    mins[s] = Z->min_d; mlts[s] = Z->mlt_d;
+  }
+  p.An = (const uint8_t *)resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
+  p.a_row_bytes = (long long)M_An->mc_length; p.n = n;
+  p.Yn = (const uint8_t *)resident(M_Yn->wX, (size_t)M_Yn->rpop_b * M_Yn->mc_length);
+  p.y_row_bytes = (long long)M_Yn->mc_length;
+  DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
+  p.mask = mask.as<uint8_t>(); p.P = P;
+  DBuf d_pl = upload_vec(planes), d_min = upload_vec(mins), d_mlt = upload_vec(mlts);
+  p.planes = d_pl.as<const uint8_t *const>(); p.plane_bytes = (long long)M_An->mc_length;
+  p.min_d = d_min.as<double>(); p.mlt_d = d_mlt.as<double>();
+  p.nS = nS; p.ncols_per = ncols_per; p.B = B; p.nW = nW;
+  DBuf d_d01 = upload_vec(d01), d_d11 = upload_vec(d11);
+  p.D01 = d_d01.as<double>(); p.D11 = d_d11.as<double>();
+  DBuf d_ar = upload_vec(a_rowb), d_yr = upload_vec(y_rowb), d_wa = upload_vec(w_a);
+  DBuf d_wD = upload_vec(wD), d_wal = upload_vec(wa), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
+  p.a_rowb = d_ar.as<uint32_t>(); p.y_rowb = d_yr.as<uint32_t>(); p.w_a = d_wa.as<uint32_t>();
+  p.wD = d_wD.as<double>(); p.wa = d_wal.as<double>();
+  p.out_r = d_or.as<unsigned long long>(); p.s_off = d_so.as<unsigned long long>();
+
+  const long long nq = 1 + (long long)nW * B;
+  DBuf d_dq((size_t)nS * nq * sizeof(double)), d_bA((size_t)nS * n * sizeof(double));
+  DBuf d_base((size_t)nS * sizeof(double)), d_t((size_t)nS * nW * sizeof(double));
+  DBuf d_out(length * sizeof(double));
+  d_out.zero();
+  p.out = d_out.as<double>();
+  st.flush();
+  {
+    const long long threads = (nq + n) * nS * 32;
+    an_ztswn_prep_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream()>>>(p, d_dq.as<double>(),
+                                                                                d_bA.as<double>());
+    LAKGB_CUDA(cudaGetLastError());
+    const long long m = (long long)nS * (nW + 1);
+    an_ztswn_tsum_kernel<<<(unsigned)((m + 255) / 256), 256, 0, stream()>>>(p, d_dq.as<double>(), d_base.as<double>(),
+                                                                            d_t.as<double>());
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch(2);
+  }
+  p.base_ = d_base.as<double>(); p.t_ = d_t.as<double>(); p.baseA = d_bA.as<double>();
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    LAKGB_CUDA(cudaFuncSetAttribute(an_ztswn_ww_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAnZtSWnSmem));
+  });
+  // Wt rows in ranges whose X scratch (rows x range x covariates doubles) fits
+  // the budget, a whole number of CTA chunks each.
+  const int CW = kBP_N / B;
+  const long long per_w = (long long)n * nS * (long long)sizeof(double);
+  const long long span = std::min<long long>(65535LL * CW,  // grid.y limit
+                                             std::max<long long>(CW, (long long)(kAnZtSWnScratch / per_w) / CW * CW));
+  const int wspan = (int)std::min<long long>(span, nW);
+  DBuf d_X((size_t)wspan * per_w);
+  p.X = d_X.as<double>();
+  for (int w_lo = 0; w_lo < nW; w_lo += wspan) {
+    p.w_lo = w_lo; p.w_hi = std::min(nW, w_lo + wspan);
+    dim3 grid((n + kBP_M - 1) / kBP_M, (p.w_hi - w_lo + CW - 1) / CW, nS);
+    an_ztswn_ww_kernel<<<grid, kBP_T, kAnZtSWnSmem, stream()>>>(p);
+    LAKGB_CUDA(cudaGetLastError());
+    const long long e = (long long)n * nS;
+    an_ztswn_sum_kernel<<<(unsigned)((e + 255) / 256), 256, 0, stream()>>>(p);
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch(2);
+  }
   copy_back(out->lf, d_out, length);
   return (int)length;
 }

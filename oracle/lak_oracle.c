@@ -689,6 +689,85 @@ int lako_An_ZtSWn_Yt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, str
   return (int)(la * ls);
 }
 
+/* popcount_pm0_lf (dir_c/popcount.c:556-621): per 1920-bit block the exact
+   pm0 count d, then dout += D[block] * d in block order. */
+static double row_pm0_lf(const unsigned char *a, const unsigned char *y, const unsigned char *m, long nbytes,
+                         const double *D)
+{
+  double dout = 0;
+  for (long b = 0; b < nbytes / BLK_BYTES; b++) {
+    const long o = b * BLK_BYTES;
+    const long long d = row_pm0(a + o, y + o, m + o, BLK_BYTES);
+    dout += D[b] * (double)d;
+  }
+  return dout;
+}
+
+/* dir_c/An_ZtSWn_Yt_ww.c:5-111: the bit-plane form of An_ZtSWn_Yt_vv.  For
+   each retained St row s, M_ZtSWn_[s] holds the planes (wrap_xcalc layout,
+   ncols_per_z rows per retained Wt row, row 0 = the first mask plane) of one
+   ZtSWn slice.  With pm0_lf(x, y; D) as above (mask M_An->mc_j),
+     X(a, w) = (pm0_lf(An_a, p0; D01)*min*mlt + sum_k 2^k pm0_lf(An_a, plane(w, k); D01)) / mlt
+             - (pm0_lf(p0, p0; D11)*min*mlt + sum_k 2^k pm0_lf(p0, plane(w, k); D11)) / mlt
+     out[a, s] = sum over retained Wt rows w, in order, of X(a, w) * D_Yn[w] * (vY(a, w) - a_Yn[w])
+   with the k sums taken from the least significant plane up (:59-67, :89-97)
+   and An row a paired with Yn row a (:71). */
+int lako_An_ZtSWn_Yt_ww(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                        struct M_handle **M_ZtSWn_, struct M_handle *M_Wt, struct M_handle *M_Yn,
+                        double *A_ajdk, double *Y_ajdk, struct L_handle **out_p)
+{
+  unsigned long long la = spacing_len(spacing_a, M_An), ls = spacing_len(spacing_s, M_St);
+  struct L_handle *out = ensure(out_p, la * ls);
+  if (!out) return (int)(la * ls);
+  out->spacing_row = spacing_a; out->row_stride = la;
+  out->spacing_col = spacing_s; out->col_stride = ls;
+  const long A_pcols = psize_c(M_An->ncols), Y_pcols = psize_c(M_Yn->ncols);
+  const double *D01 = A_ajdk + AJDK_0_1 * A_pcols, *D11 = A_ajdk + AJDK_1_1 * A_pcols;
+  const double *D_Yn = Y_ajdk + AJDK_0_1 * Y_pcols, *a_Yn = Y_ajdk + 1 * Y_pcols; /* AJDK_1_0 */
+  const long nb = (long)M_An->mc_length;
+  const long long nW = M_Wt->rpop_j;
+  const long long nP = M_An->rpop_j < M_Yn->rpop_j ? M_An->rpop_j : M_Yn->rpop_j;
+  double *t_ = (double *)malloc(sizeof(double) * (nW > 0 ? nW : 1));
+  for (long long s = 0; s < M_St->rpop_j; s++) {
+    const struct M_handle *Z = M_ZtSWn_[s];
+    const int ncp = Z->ncols_per_z;
+    const unsigned long long ts = pick(spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]);
+    const unsigned char *p0 = Z->wX;
+    const double base_ = row_pm0_lf(p0, p0, M_An->mc_j, nb, D11) * Z->min_d * Z->mlt_d;
+    for (long long w = 0; w < nW; w++) {
+      double tmp = 0;
+      long long n2 = 1;
+      for (int mx = ncp - 1; mx > 0; mx--) {
+        tmp += n2 * row_pm0_lf(p0, Z->wX + (long long)(ncp * w + mx) * Z->mc_length, M_An->mc_j, nb, D11);
+        n2 *= 2;
+      }
+      t_[w] = tmp;
+    }
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+    for (long long i = 0; i < nP; i++) {
+      const unsigned char *An = M_An->wX + (long long)M_An->m_b_[i] * M_An->mc_length;
+      const unsigned char *Yn = M_Yn->wX + (long long)M_Yn->m_b_[i] * M_Yn->mc_length;
+      const double baseA = row_pm0_lf(An, p0, M_An->mc_j, nb, D01) * Z->min_d * Z->mlt_d;
+      double acc = 0;
+      for (long long w = 0; w < nW; w++) {
+        double tmp = 0;
+        long long n2 = 1;
+        for (int mx = ncp - 1; mx > 0; mx--) {
+          tmp += n2 * row_pm0_lf(An, Z->wX + (long long)(ncp * w + mx) * Z->mc_length, M_An->mc_j, nb, D01);
+          n2 *= 2;
+        }
+        const double X = (double)(baseA + tmp) / Z->mlt_d - (double)(base_ + t_[w]) / Z->mlt_d;
+        const unsigned w_a = M_Wt->m_a_[w];
+        const int vY = bit_pm(Yn, w_a);
+        acc += X * D_Yn[w_a / 1920] * (vY - a_Yn[w_a / 1920]);
+      }
+      out->lf[pick(spacing_a, i, M_An->m_b_[i], M_An->m_a_[i]) + ts * la] = acc;
+    }
+  }
+  free(t_);
+  return (int)(la * ls);
+}
+
 /* dir_c/binary_read.c:174-269: wrap_transpose sets bit (7 - nc % 8) of byte
  * nc / 8 of output row nf from bit (7 - nf % 8) of byte nf / 8 of input record
  * nc, and clears the bits of the padding columns n_col..n_col+extend-1.  Here

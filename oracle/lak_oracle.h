@@ -45,6 +45,10 @@ int lako_At_T_YnWt_S_Zn_ww(int spacing_a, int spacing_t, struct M_handle *M_At, 
                            struct M_handle *M_Yn, struct M_handle *M_Wn, struct M_handle *M_St,
                            struct M_handle *M_Zt, double *A_ajdk, struct M_handle *M_YnWt,
                            struct L_handle **out_p);
+/* dir_c/An_ZtSWn_Yt_ww.c:5-111 */
+int lako_An_ZtSWn_Yt_ww(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_St,
+                        struct M_handle **M_ZtSWn_, struct M_handle *M_Wt, struct M_handle *M_Yn,
+                        double *A_ajdk, double *Y_ajdk, struct L_handle **out_p);
 /* dir_c/An_ZtSn_ww.c:5-136 */
 int lako_An_ZtSn_ww(int spacing_a, int spacing_s, struct M_handle *M_An, struct M_handle *M_ZtSn,
                     struct M_handle *M_St, struct L_handle **out_p);

@@ -1,6 +1,7 @@
-"""Parity cases for the SNP x SNP and element-wise loop products:
-AtTAn_vv, At_T_YnWt_S_Zn_vv and An_ZtSWn_Yt_vv (dir_c/AtTAn_vv.c,
-dir_c/At_T_YnWt_S_Zn_vv.c, dir_c/An_ZtSWn_Yt_vv.c).
+"""Parity cases for the SNP x SNP and element-wise loop products and the
+bit-plane form of the last: AtTAn_vv, At_T_YnWt_S_Zn_vv, An_ZtSWn_Yt_vv and
+An_ZtSWn_Yt_ww (dir_c/AtTAn_vv.c, dir_c/At_T_YnWt_S_Zn_vv.c,
+dir_c/An_ZtSWn_Yt_vv.c, dir_c/An_ZtSWn_Yt_ww.c).
 
 ``build(spec)`` makes seeded inputs (bit matrices with ragged row and column
 masks, allele weights, FP64 score matrices); ``run(backend, name, x, ...)``
@@ -32,7 +33,7 @@ def specs():
     for i, (nsnp, npat, nctl, nt) in enumerate(shapes):
         for masked in (False, True):
             out.append(dict(name=f"p{i}_{int(masked)}", nsnp=nsnp, npat=npat, nctl=nctl, nt=nt,
-                            masked=masked, seed=5000 + 31 * i + int(masked)))
+                            masked=masked, seed=5000 + 31 * i + int(masked), ww_b_index=i))
     return out
 
 
@@ -68,6 +69,17 @@ def build(spec):
     x["lf_AtTn"] = rng.integers(-npat, npat + 1, (nsnp, nt)).astype(np.float64)
     x["lf_YnWt"] = rng.standard_normal((npat, nctl))
     x["lf_ZtSWn"] = rng.standard_normal((nsnp, nsnp + 3, nt))
+    # An_ZtSWn_Yt_ww: Wt (Y SNPs x controls; its retained rows index the
+    # planes) and, per covariate row, one set of bit planes with its own
+    # min / mlt (drawn after everything above, so earlier inputs keep their values)
+    x["Wt"] = (rng.random((nsnp + 3, nctl)) < 0.4).astype(np.uint8)
+    B = (3, 32, 8, 16)[spec.get("ww_b_index", 0) % 4] if "ww_b_index" in spec else 8
+    nwj = int(x["ysnp_j"].sum())
+    mcl = abi.bsize(nsnp)
+    x["ww_B"] = np.array([B], np.int32)
+    x["ww_planes"] = rng.integers(0, 256, (nt, (B + 1) * nwj, mcl), dtype=np.uint8)
+    x["ww_min"] = -5.0 * rng.random(nt)
+    x["ww_mlt"] = float(2 ** B) / (1.0 + 10.0 * rng.random(nt))
     return x
 
 
@@ -91,6 +103,17 @@ def handles(x):
     lz.s.row_stride, lz.s.col_stride, lz.s.lyr_stride = z.shape
     lz.s.spacing_row = lz.s.spacing_col = lz.s.spacing_lyr = abi.SPACING_a
     h["lf_ZtSWn"] = lz
+    h["Wt"] = kc.mhandle(x["Wt"], x["ysnp_b"], x["ysnp_j"], x["ctl_b"], x["ctl_j"])
+    B = int(x["ww_B"][0])
+    planes = []
+    for s in range(x["ww_planes"].shape[0]):
+        w = x["ww_planes"][s]
+        m = abi.MHandle(None, nrows=w.shape[0], ncols=x["An"].shape[1], wX=w)
+        m.s.ncols_per_z = B + 1
+        m.s.min_d, m.s.mlt_d = float(x["ww_min"][s]), float(x["ww_mlt"][s])
+        planes.append(m)
+    h["ww_planes"] = planes
+    h["ww_arr"] = (C.POINTER(abi.M_handle) * len(planes))(*[C.pointer(m.s) for m in planes])
     return h
 
 
@@ -120,12 +143,17 @@ def run(backend, kind, h, sa, sb, st=abi.SPACING_a):
                 h["lf_ZtSWn"].ptr, C.byref(out))
         n = (lib.lako_An_ZtSWn_Yt_vv(*args) if backend == "oracle"
              else lib.wrap_An_ZtSWn_Yt_vv__run(*kc._thread_args(), *args))
+    elif kind == "An_ZtSWn_Yt_ww":
+        args = (sa, sb, h["An"].ptr, h["St"].ptr, h["ww_arr"], h["Wt"].ptr, h["Yn"].ptr, _dptr(h["A_ajdk"]),
+                _dptr(h["Y_ajdk"]), C.byref(out))
+        n = (lib.lako_An_ZtSWn_Yt_ww(*args) if backend == "oracle"
+             else lib.wrap_An_ZtSWn_Yt_ww__run(*kc._thread_args(), *args))
     else:
         raise ValueError(kind)
     return _take(out, n)
 
 
-KINDS = ["AtTAn", "At_T_YnWt_S_Zn_vv", "An_ZtSWn_Yt_vv"]
+KINDS = ["AtTAn", "At_T_YnWt_S_Zn_vv", "An_ZtSWn_Yt_vv", "An_ZtSWn_Yt_ww"]
 SPACING_PAIRS = [(abi.SPACING_a, abi.SPACING_a), (abi.SPACING_j, abi.SPACING_b), (abi.SPACING_b, abi.SPACING_j)]
 
 

@@ -7,9 +7,10 @@
 //          with the block sums accumulated in ascending block order, one multiply
 //          and one add per block and no FMA, as popcount_lf (popcount.c:252-308).
 //
-// One warp per row: lanes 0..29 read the 240-byte block as 8-byte words, the
-// warp reduces the block count with shuffles, and lanes 0..14 each carry one
-// of the 15 FP64 accumulators.
+// An_v: one warp per row; lanes 0..29 read the 240-byte block as 8-byte
+// words and the warp reduces the block count with shuffles.  An_ajdk: the
+// same counts for two rows per warp, whose 2 x 15 FP64 accumulators sit on
+// lanes 0..14 and 16..30.
 #include "lakgb_runtime.cuh"
 #include "rowvec.cuh"
 
@@ -43,19 +44,30 @@ __global__ void an_v_kernel(RowvecParams p) {
   }
 }
 
+// Two rows per warp: lanes 0..14 carry the 15 accumulators of row 2w and
+// lanes 16..30 those of row 2w+1, so each FP64 multiply and add instruction
+// (which holds the sub-partition's FP64 unit whatever its active lanes) serves
+// both rows.
 __global__ void an_ajdk_kernel(RowvecParams p) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= p.n) return;
-  const uint8_t *row = p.w + (long long)p.rowb[warp] * p.row_bytes;
+  const int r0 = 2 * warp;
+  if (r0 >= p.n) return;
+  const bool two = r0 + 1 < p.n;
+  const uint8_t *rowA = p.w + (long long)p.rowb[r0] * p.row_bytes;
+  const uint8_t *rowB = two ? p.w + (long long)p.rowb[r0 + 1] * p.row_bytes : rowA;
+  const int k = lane & 15;
+  const bool mine = k < 15 && (lane < 16 || two);
   double s = 0.0;
   for (int b = 0; b < p.P; ++b) {
-    const int c = block_count(row + (long long)b * kBlockBytes, p.mask + (long long)b * kBlockBytes, lane);
-    if (lane < 15) s = __dadd_rn(s, __dmul_rn(p.ajdk[b + (long long)lane * p.P], (double)c));
+    const long long bo = (long long)b * kBlockBytes;
+    const int cA = block_count(rowA + bo, p.mask + bo, lane);
+    const int cB = block_count(rowB + bo, p.mask + bo, lane);
+    if (mine) s = __dadd_rn(s, __dmul_rn(p.ajdk[b + (long long)k * p.P], (double)(lane < 16 ? cA : cB)));
   }
-  if (lane < 15) {
-    double o = (p.type == 1) ? __dadd_rn(-p.base[lane], __dmul_rn(2.0, s)) : s;
-    p.out[(long long)p.out_r[warp] + (long long)lane * p.out_stride] = o;
+  if (mine) {
+    double o = (p.type == 1) ? __dadd_rn(-p.base[k], __dmul_rn(2.0, s)) : s;
+    p.out[(long long)p.out_r[r0 + (lane >> 4)] + (long long)k * p.out_stride] = o;
   }
 }
 
@@ -73,7 +85,8 @@ void launch_an_v(const RowvecParams &p) {
 void launch_an_ajdk(const RowvecParams &p) {
   if (p.n <= 0) return;
   const int threads = 256;
-  const int blocks = (int)(((long long)p.n * 32 + threads - 1) / threads);
+  const long long warps = ((long long)p.n + 1) / 2;
+  const int blocks = (int)((warps * 32 + threads - 1) / threads);
   an_ajdk_kernel<<<blocks, threads, 0, stream()>>>(p);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();

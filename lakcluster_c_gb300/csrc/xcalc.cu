@@ -27,6 +27,7 @@
 #include <optional>
 
 #include "abi_common.cuh"
+#include "bit_transpose.cuh"
 #include "bcc_model.h"
 #include "lmirror.cuh"
 
@@ -53,18 +54,33 @@ struct XcalcParams {
   int *bad;                  // set when an index would leave its buffer (access skipped)
 };
 
+// Grid: blockIdx.y strides the retained columns, blockIdx.x * blockDim.x +
+// threadIdx.x the retained rows, about four rows per thread and column (the
+// launch sizes gridDim.x so), loaded together; one partial (min, max, any)
+// per block.
 __global__ void xcalc_minmax_kernel(const double *lf, const long long *rows_j, int nr,
                                     const long long *cols_j, int nc, double *pmin, double *pmax,
                                     int *pany) {
   double mn = 0.0, mx = 0.0;
   int any = 0;
-  const long long total = (long long)nr * nc;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(e % nr), c = (int)(e / nr);
-    const double x = lf[rows_j[r] + cols_j[c]];
-    if (!any) { mn = x; mx = x; any = 1; }
-    else { mn = x < mn ? x : mn; mx = x > mx ? x : mx; }
+  const int stride = gridDim.x * blockDim.x;
+  for (int c = blockIdx.y; c < nc; c += gridDim.y) {
+    const long long co = cols_j[c];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += 4 * stride) {
+      double x[4];
+      int n = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int ru = r + u * stride;
+        if (ru < nr) { x[u] = lf[rows_j[ru] + co]; n = u + 1; }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (u >= n) break;
+        if (!any) { mn = x[u]; mx = x[u]; any = 1; }
+        else { mn = x[u] < mn ? x[u] : mn; mx = x[u] > mx ? x[u] : mx; }
+      }
+    }
   }
   __shared__ double smn[32], smx[32];
   __shared__ int sany[32];
@@ -88,39 +104,59 @@ __global__ void xcalc_minmax_kernel(const double *lf, const long long *rows_j, i
       if (!a) { bmn = smn[w]; bmx = smx[w]; a = 1; }
       else { bmn = smn[w] < bmn ? smn[w] : bmn; bmx = smx[w] > bmx ? smx[w] : bmx; }
     }
-    pmin[blockIdx.x] = bmn; pmax[blockIdx.x] = bmx; pany[blockIdx.x] = a;
+    const int b = blockIdx.x + gridDim.x * blockIdx.y;
+    pmin[b] = bmn; pmax[b] = bmx; pany[b] = a;
   }
 }
 
+// Warp per (column, 128-row group): lane l quantises rows 128g + 32k + l,
+// k = 0..3 (four independent coalesced loads).  Per k, the 32 x 32 bit
+// matrix (row l = bits nb0 .. nb0+31 of lane l's value) is transposed in
+// registers, so lane j holds the word of bit nb0+j; lane j then writes its
+// plane's four words (128 rows) as one 16-byte store.  Plane rows are
+// bsize(nrows) bytes, a multiple of 240 and so of 16, and a group that starts
+// inside the rows ends inside the 1920-bit padding, so every store is aligned
+// and within its plane row.
 __global__ void xcalc_planes_kernel(XcalcParams p) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const int nwords = (p.nrows_a + 31) >> 5;
-  if (warp >= nwords * p.ncols_j) return;
-  const int w = warp % nwords, c = warp / nwords;
-  const int r = (w << 5) + lane;
-  unsigned long long cz = 0ull;
-  if (r < p.nrows_a) {
-    const long long ro = p.row_off[r];
-    if (ro >= 0 && (unsigned long long)(ro + p.col_off[c]) >= p.lf_n) {
+  const int ngroups = (p.nrows_a + 127) >> 7;
+  if (warp >= (long long)ngroups * p.ncols_j) return;
+  const int g = (int)(warp % ngroups), c = (int)(warp / ngroups);
+  const long long co = p.col_off[c];
+  unsigned long long cz[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int r = (g << 7) + (k << 5) + lane;
+    cz[k] = 0ull;
+    const long long ro = r < p.nrows_a ? p.row_off[r] : -1;
+    if (ro >= 0 && (unsigned long long)(ro + co) >= p.lf_n) {
       atomicCAS(p.bad, 0, 1);
     } else if (ro >= 0) {
-      const double x = p.lf[ro + p.col_off[c]];
-      cz = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
-      if (cz < 1ull) cz = 1ull;
-      if (cz > p.dmax) cz = p.dmax;
+      const double x = p.lf[ro + co];
+      unsigned long long v = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
+      if (v < 1ull) v = 1ull;
+      if (v > p.dmax) v = p.dmax;
+      cz[k] = v;
     }
   }
   const int nbits = p.ncols_per - 1;
-  for (int nb = 0; nb < nbits; ++nb) {
-    const unsigned bal = __ballot_sync(0xffffffffu, (unsigned)((cz >> nb) & 1ull));
-    if (lane == 0 && bal) {
-      // ballot bit i = row 32w+i; memory wants row 8k+j at byte k, bit 7-j.
-      const unsigned word = __byte_perm(__brev(bal), 0u, 0x0123);
-      const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - nb;
-      const unsigned long long off = (unsigned long long)(plane * p.brows + 4ll * w);
-      if (off + 4 > p.planes_n) atomicCAS(p.bad, 0, 2);
-      else *reinterpret_cast<unsigned *>(p.planes + off) = word;
+  for (int nb0 = 0; nb0 < nbits; nb0 += 32) {
+    const int nr_ = min(32, nbits - nb0);
+    unsigned mine[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mine[k] = transpose32(__brev((uint32_t)(cz[k] >> nb0)), lane);
+    if (lane < nr_ && (mine[0] | mine[1] | mine[2] | mine[3])) {
+      // lane j's word has row i at bit 31-i; memory wants row 8m+q at byte m, bit 7-q.
+      uint4 v;
+      v.x = __byte_perm(mine[0], 0u, 0x0123);
+      v.y = __byte_perm(mine[1], 0u, 0x0123);
+      v.z = __byte_perm(mine[2], 0u, 0x0123);
+      v.w = __byte_perm(mine[3], 0u, 0x0123);
+      const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - (nb0 + lane);
+      const unsigned long long off = (unsigned long long)(plane * p.brows + 16ll * g);
+      if (off + 16 > p.planes_n || (off & 15ull)) atomicCAS(p.bad, 0, 2);
+      else *reinterpret_cast<uint4 *>(p.planes + off) = v;
     }
   }
 }
@@ -356,11 +392,13 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
     d_cols = upload_vec(cols_j);
     d_roff_all = upload_vec(row_off_a);
     st->flush();
-    const long long total = (long long)nr * nc;
-    int blocks = (int)((total + 255) / 256);
-    if (blocks > 1024) blocks = 1024;
+    // About 8 resident blocks per SM: rows across blockIdx.x (about four per
+    // thread), columns across blockIdx.y.
+    const int gx = std::min((nr + 1023) / 1024, 1216);
+    const int gy = std::max(1, std::min(nc, 1216 / gx));
+    const int blocks = gx * gy;
     DBuf d_min(blocks * sizeof(double)), d_max(blocks * sizeof(double)), d_any(blocks * sizeof(int));
-    xcalc_minmax_kernel<<<blocks, 256, 0, stream()>>>(plf, d_rows.as<long long>(), nr,
+    xcalc_minmax_kernel<<<dim3(gx, gy), 256, 0, stream()>>>(plf, d_rows.as<long long>(), nr,
                                                        d_cols.as<long long>(), nc, d_min.as<double>(),
                                                        d_max.as<double>(), d_any.as<int>());
     LAKGB_CUDA(cudaGetLastError());
@@ -418,7 +456,7 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
       p.lf_n = (plf == d_lf.p) ? (unsigned long long)lf_elems : (unsigned long long)mlf->n;
       p.planes_n = (unsigned long long)nbytes;
       p.bad = bad_flag();
-      const long long warps = (long long)((Yn_nrows + 31) / 32) * nc;
+      const long long warps = (long long)((Yn_nrows + 127) / 128) * nc;
       const int blocks = (int)((warps * 32 + 255) / 256);
       xcalc_planes_kernel<<<blocks, 256, 0, stream()>>>(p);
       LAKGB_CUDA(cudaGetLastError());

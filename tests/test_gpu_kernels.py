@@ -45,3 +45,20 @@ def test_gpu_matches_oracle_larger(gpu_lib, oracle_lib, nA, nZ, m, sym):
         want = kc.call_gram("oracle", sym, t, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, lfA, lfZ)
         got = kc.call_gram("gpu", sym, t, abi.SPACING_b, abi.SPACING_j, MA, MZ, A_ajdk, lfA, lfZ)
         assert _bits_equal(got, want)
+
+
+@pytest.mark.parametrize("n,frac", [(21001, 1.0), (23000, 0.9)])
+def test_an_ajdk_two_rows_per_warp(gpu_lib, oracle_lib, n, frac):
+    """Launches of 16384 rows or more take two rows per warp; an odd row count
+    (21001 rows, all retained) leaves the last warp with one row."""
+    rng = np.random.default_rng(n)
+    A, r_b, r_j = kc.make_matrix_case(rng, n, 2500, frac, frac)
+    assert int(r_j.sum()) >= 16384
+    mc_b = (rng.random(2500) < 0.95).astype(np.uint8)
+    mc_j = mc_b & (rng.random(2500) < 0.9).astype(np.uint8)
+    MA = kc.mhandle(A, r_b, r_j, mc_b, mc_j)
+    A_ajdk = abi.calc_A_ajdk(0.05 + 0.9 * rng.random(abi.psize(2500)))
+    for t in (abi.TYPE_pm, abi.TYPE_00):
+        for sp in (abi.SPACING_a, abi.SPACING_j):
+            want = kc.call_an_ajdk("oracle", t, sp, MA, A_ajdk)
+            assert _bits_equal(kc.call_an_ajdk("gpu", t, sp, MA, A_ajdk), want), (t, sp)

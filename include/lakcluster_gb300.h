@@ -353,12 +353,17 @@ void lakgb_L_transpose(struct L_handle *dst, const struct L_handle *src);
  * with an error.  The array is shared by every call on a device: calls whose
  * kernels overlap on the GPU race.  The first call on a device looks the array
  * up (cudaGetSymbolAddress) and should come before any stream capture.
+ * The call is synchronous: it returns once its GPU work is done (it reads
+ * {min, max, mlt} back into host memory).
  * Inputs (device): lf, the element offset of each Yn a-row (-1 = not
  * retained, nrows_a entries), of each retained row (rows_j) and column
  * (cols_j) in j order, and plane 0 (row0, brows bytes, may be NULL).
  * Output: planes ((b_mlt+1)*n_cols_j rows of brows bytes, overwritten) and,
- * in host memory, {min, max, mlt} as wrap_xcalc stores them in M_X.  Returns 0,
- * or non-zero with lakgb_last_error() set. */
+ * in host memory, {min, max, mlt} as wrap_xcalc stores them in M_X.
+ * Requirements: planes 4-byte aligned; brows a multiple of 4 and at least
+ * 4*ceil(nrows_a/32) (wrap_xcalc's plane rows, bsize(nrows_a) bytes, are);
+ * counts >= 0; 1 <= b_mlt <= 62; d_mlt >= 2.  Returns 0, or non-zero with
+ * lakgb_last_error() set and nothing launched. */
 #define LAKGB_XCALC_NOALLOC_MAX_COLS 32768
 struct lakgb_xcalc_noalloc_args {
   const double *lf;

@@ -86,13 +86,12 @@ def build_lib(force: bool = False, verbose: bool = False) -> str:
 
 
 def build_oracle(force: bool = False) -> str:
-    """Compile the plain-C oracle (and the reference, when its sources exist)."""
+    """Compile the plain-C oracle, and the reference where oracle/Makefile
+    finds its sources (LAK_REFERENCE_DIR overrides the Makefile's REF)."""
     odir = os.path.join(ROOT, "oracle")
-    targets = ["oracle"]
-    ref = os.environ.get("LAK_REFERENCE_DIR", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "dir_c")) and os.uname().machine == "x86_64":
-        targets.append("ref")
-    _run(["make", "-s", "-C", odir, "REF=" + ref] + (["-B"] if force else []) + targets)
+    ref = os.environ.get("LAK_REFERENCE_DIR")
+    _run(["make", "-s", "-C", odir] + (["REF=" + ref] if ref else []) + (["-B"] if force else [])
+         + ["oracle", "ref-if-present"])
     return os.path.join(odir, "liblakoracle.so")
 
 

@@ -532,9 +532,14 @@ extern "C" lakgb_gram_group *lakgb_gram_group_create(const lakgb_gram_args *args
   LAKGB_CUDA(cudaMalloc(&g->d_tile0, sizeof(int) * (n + 1)));
   LAKGB_CUDA(cudaMalloc(&g->d_blk0, sizeof(long long) * (n + 1)));
   LAKGB_CUDA(cudaMalloc(&g->d_T, gram_tc_table_row_bytes() * (size_t)std::max(1ll, g->total_blocks)));
-  LAKGB_CUDA(cudaMemcpy(g->d_ps, ps.data(), sizeof(GramParams) * n, cudaMemcpyHostToDevice));
-  LAKGB_CUDA(cudaMemcpy(g->d_tile0, tile0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
-  LAKGB_CUDA(cudaMemcpy(g->d_blk0, blk0.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice));
+  // Copied on this thread's stream and waited for: a plain cudaMemcpy from
+  // pageable memory may return before its DMA lands, and the launches that
+  // read these arrays run on non-blocking streams that do not wait for it.
+  cudaStream_t s = stream();
+  LAKGB_CUDA(cudaMemcpyAsync(g->d_ps, ps.data(), sizeof(GramParams) * n, cudaMemcpyHostToDevice, s));
+  LAKGB_CUDA(cudaMemcpyAsync(g->d_tile0, tile0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  LAKGB_CUDA(cudaMemcpyAsync(g->d_blk0, blk0.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, s));
+  LAKGB_CUDA(cudaStreamSynchronize(s));
   return g;
 }
 

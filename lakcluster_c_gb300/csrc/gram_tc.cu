@@ -647,7 +647,8 @@ int tc_status_take() {
   LAKGB_CUDA(cudaMemcpyFromSymbol(&v, g_tc_status, sizeof v));
   if (v) {
     const int zero = 0;
-    LAKGB_CUDA(cudaMemcpyToSymbol(g_tc_status, &zero, sizeof zero));
+    LAKGB_CUDA(cudaMemcpyToSymbolAsync(g_tc_status, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, stream()));
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
   }
   return v;
 }

@@ -22,7 +22,9 @@
 // device for the products that follow, and are copied into M_X->wX for
 // callers that read them on the host.
 #include <math.h>
+#include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 #include <optional>
 
@@ -240,31 +242,36 @@ __global__ void xcalc_scalars_kernel(int nc, double d_mlt, double *scratch) {
   out[3] = mlt;            // the value wrap_xcalc stores as M_X->mlt_d
 }
 
+// A warp per (32-row word, column); grid-stride over the warps, so any
+// launch size covers every word (the warp index is uniform within a warp, as
+// the ballots need).
 __global__ void xcalc_planes_dev_kernel(XcalcParams p, const double *scalars) {
   p.min = scalars[0];
   p.mlt = scalars[2];
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nwords = (p.nrows_a + 31) >> 5;
-  if (warp >= nwords * p.ncols_j) return;
-  const int w = warp % nwords, c = warp / nwords;
-  const int r = (w << 5) + lane;
-  unsigned long long cz = 0ull;
-  if (r < p.nrows_a) {
-    const long long ro = p.row_off[r];
-    if (ro >= 0) {
-      const double x = p.lf[ro + p.col_off[c]];
-      cz = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
-      if (cz < 1ull) cz = 1ull;
-      if (cz > p.dmax) cz = p.dmax;
+  const long long total = (long long)nwords * p.ncols_j;
+  const long long step = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < total; warp += step) {
+    const int w = (int)(warp % nwords), c = (int)(warp / nwords);
+    const int r = (w << 5) + lane;
+    unsigned long long cz = 0ull;
+    if (r < p.nrows_a) {
+      const long long ro = p.row_off[r];
+      if (ro >= 0) {
+        const double x = p.lf[ro + p.col_off[c]];
+        cz = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
+        if (cz < 1ull) cz = 1ull;
+        if (cz > p.dmax) cz = p.dmax;
+      }
     }
-  }
-  for (int nb = 0; nb < p.ncols_per - 1; ++nb) {
-    const unsigned bal = __ballot_sync(0xffffffffu, (unsigned)((cz >> nb) & 1ull));
-    if (lane == 0 && bal) {
-      const unsigned word = __byte_perm(__brev(bal), 0u, 0x0123);
-      const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - nb;
-      *reinterpret_cast<unsigned *>(p.planes + plane * p.brows + 4ll * w) = word;
+    for (int nb = 0; nb < p.ncols_per - 1; ++nb) {
+      const unsigned bal = __ballot_sync(0xffffffffu, (unsigned)((cz >> nb) & 1ull));
+      if (lane == 0 && bal) {
+        const unsigned word = __byte_perm(__brev(bal), 0u, 0x0123);
+        const long long plane = (long long)p.ncols_per * c + p.ncols_per - 1 - nb;
+        *reinterpret_cast<unsigned *>(p.planes + plane * p.brows + 4ll * w) = word;
+      }
     }
   }
 }
@@ -306,12 +313,16 @@ extern "C" void lakgb_set_d_mlt(long long d_mlt) { g_d_mlt = d_mlt; }
 
 namespace lakgb {
 namespace {
-// Per-thread device flag of the planes kernel's bounds checks.
+// Per-thread device flag of the planes kernel's bounds checks.  It is
+// zeroed on the thread's own stream: that stream does not wait for the
+// legacy default stream (it is created non-blocking), so a plain cudaMemset
+// could still be pending when the first read of the flag runs, which would
+// then see whatever the allocation held before.
 int *bad_flag() {
   thread_local int *d = nullptr;
   if (!d) {
     LAKGB_CUDA(cudaMalloc(&d, sizeof(int)));
-    LAKGB_CUDA(cudaMemset(d, 0, sizeof(int)));
+    LAKGB_CUDA(cudaMemsetAsync(d, 0, sizeof(int), stream()));
   }
   return d;
 }
@@ -490,13 +501,25 @@ extern "C" int lakgb_xcalc_noalloc(const struct lakgb_xcalc_noalloc_args *a) {
     set_error(2, "lakgb_xcalc_noalloc: null argument");
     return 2;
   }
-  if (a->n_cols_j > kNoAllocMaxCols || a->n_cols_j < 0 || a->n_rows_j < 0 || a->nrows_a < 0) {
+  if (a->n_cols_j < 0 || a->n_rows_j < 0 || a->nrows_a < 0) {
+    set_error(2, "lakgb_xcalc_noalloc: negative count (nrows_a %d, n_rows_j %d, n_cols_j %d)", a->nrows_a,
+              a->n_rows_j, a->n_cols_j);
+    return 2;
+  }
+  if (a->n_cols_j > kNoAllocMaxCols) {
     set_error(2, "lakgb_xcalc_noalloc: %d retained columns exceed the scratch limit of %d", a->n_cols_j,
               kNoAllocMaxCols);
     return 2;
   }
-  if (a->b_mlt < 1 || a->b_mlt > 62 || a->brows < (long long)((a->nrows_a + 31) / 32) * 4) {
-    set_error(2, "lakgb_xcalc_noalloc: b_mlt out of range or plane rows too short");
+  if (a->b_mlt < 1 || a->b_mlt > 62 || a->d_mlt < 2) {
+    set_error(2, "lakgb_xcalc_noalloc: b_mlt %d outside [1, 62] or d_mlt %lld below 2", a->b_mlt, a->d_mlt);
+    return 2;
+  }
+  // The plane kernel stores whole 4-byte words at planes + plane * brows + 4 * w.
+  if (a->brows < (long long)((a->nrows_a + 31) / 32) * 4 || (a->brows & 3) ||
+      (reinterpret_cast<uintptr_t>(a->planes) & 3)) {
+    set_error(2, "lakgb_xcalc_noalloc: plane rows of %lld bytes too short or not a multiple of 4, or planes "
+              "not 4-byte aligned", a->brows);
     return 2;
   }
   double *scratch = noalloc_scratch();
@@ -521,7 +544,8 @@ extern "C" int lakgb_xcalc_noalloc(const struct lakgb_xcalc_noalloc_args *a) {
     p.dmax = (unsigned long long)(a->d_mlt - 1); p.ncols_per = ncols_per; p.brows = a->brows;
     p.planes = a->planes;
     const long long warps = (long long)((a->nrows_a + 31) / 32) * nc;
-    xcalc_planes_dev_kernel<<<(int)((warps * 32 + 255) / 256), 256, 0, s>>>(p, scratch + 3 * kNoAllocMaxCols);
+    const long long blocks = std::min<long long>((warps * 32 + 255) / 256, 1ll << 20);  // the kernel grid-strides
+    xcalc_planes_dev_kernel<<<(unsigned)blocks, 256, 0, s>>>(p, scratch + 3 * kNoAllocMaxCols);
     LAKGB_CUDA(cudaGetLastError());
     count_launch();
   }

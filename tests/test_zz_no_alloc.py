@@ -121,6 +121,53 @@ def test_noalloc_matches_wrap_xcalc(gpu_lib, Yn, Wn, trm):
         assert tuple(out) == want_scalars, "min / max / mlt differ on call %d" % call
 
 
+@pytest.mark.parametrize("which", ["no_rows", "no_cols"])
+def test_noalloc_matches_wrap_xcalc_with_nothing_retained(gpu_lib, which):
+    """No retained rows (or columns): min / max / mlt come from the empty-set
+    fallback, and the planes hold plane 0 only (or nothing)."""
+    import torch
+    lib = _bind(gpu_lib)
+    rng = np.random.default_rng(11)
+    Yn, Wn, B = 200, 40, 32
+    d = _case(rng, Yn, Wn, 0)
+    if which == "no_rows":
+        d["mr_j"][:] = False
+        d["row_off_a"][:] = -1
+        d["rows_j"] = np.zeros(0, np.int64)
+    else:
+        d["mc_j"][:] = False
+        d["cols_j"] = np.zeros(0, np.int64)
+    ylen, wlen = abi.bsize(Yn), abi.bsize(Wn)
+    mr_j, mr_b = abi.pack_bits(d["mr_j"], ylen), abi.pack_bits(d["mr_b"], ylen)
+    mc_j, mc_b = abi.pack_bits(d["mc_j"], wlen), abi.pack_bits(d["mc_b"], wlen)
+    MX = abi.MHandle(None, nrows=(B + 1) * Wn, ncols=Yn, wX=np.zeros(((B + 1) * Wn, ylen), np.uint8))
+    px = C.pointer(MX.s)
+    tid, yn, wn, bm = C.c_int(0), C.c_int(Yn), C.c_int(Wn), C.c_int(B)
+    vpra = (C.c_void_p * 128)()
+    lib.wrap_xcalc(C.byref(tid), C.cast(vpra, C.c_void_p), None, mr_j.ctypes.data, mr_b.ctypes.data,
+                   mc_j.ctypes.data, mc_b.ctypes.data, C.byref(d["L"]), d["lf"].ctypes.data, C.byref(yn),
+                   C.byref(wn), C.byref(px), C.byref(bm), 0)
+    nplanes, brows = MX.s.nrows, MX.s.mc_length
+    want = MX.wX.reshape(-1)[: nplanes * brows].copy()
+    want_scalars = (MX.s.min_d, MX.s.max_d, MX.s.mlt_d)
+    dev = torch.device("cuda")
+    keep = [torch.from_numpy(x).to(dev) if x.size else torch.zeros(1, dtype=torch.int64, device=dev)
+            for x in (d["lf"], d["row_off_a"], d["rows_j"], d["cols_j"])]
+    t_row0 = torch.from_numpy(MX.wX.reshape(-1)[:brows].copy()).to(dev)
+    t_planes = torch.full((max(16, nplanes * brows),), 0x77, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    out = (C.c_double * 3)()
+    a = NoAllocArgs(keep[0].data_ptr(), keep[1].data_ptr(), Yn, keep[2].data_ptr(), len(d["rows_j"]),
+                    keep[3].data_ptr(), len(d["cols_j"]), t_row0.data_ptr(), B, 1 << B, brows, t_planes.data_ptr(),
+                    C.cast(out, C.POINTER(C.c_double)), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    for call in range(2):
+        assert lib.lakgb_xcalc_noalloc(C.byref(a)) == 0
+        got = t_planes.cpu().numpy()[: nplanes * brows]
+        assert np.array_equal(got, want), "planes differ on call %d" % call
+        assert tuple(out) == want_scalars, "min / max / mlt differ on call %d: %s vs %s" % (
+            call, tuple(out), want_scalars)
+
+
 def test_noalloc_rejects_oversize(gpu_lib):
     import torch
     lib = _bind(gpu_lib)

@@ -1,33 +1,35 @@
 """Benchmark: bit-ops/s of the bcc Gram pass (bcc_lf_YnWt) on one GB300.
 
-Workload (the case/control configuration): cases 4096 x 16384 SNPs and
-controls 4096 x 16384, MAF U[0.05,0.5], 256 x 512 planted bicluster with 5%
-flips, rows split uniformly over 2 covariate bins.  One step = the full Gram
-pass over all bin pairs (AnZt for every pair, AnAt for nb1 <= nb2): seven
-products of the +/-1 centred D-weighted Gram with FP64 scores.
+Workload (the large single-solve configuration, the largest that the metric
+is quoted on and that fits one GPU): cases 32768 and controls 32768 x 131072
+SNPs, MAF U[0.01,0.5], a 2048 x 4096 planted bicluster with 5% flips, rows
+assigned uniformly to 3 covariate bins.  One step = the full Gram pass over
+all bin pairs (AnZt for every pair, AnAt for nb1 <= nb2): 15 products of the
++/-1 centred D-weighted Gram with FP64 scores, 2.35e14 bit pairs.  The packed
+inputs (1.08 GB) are larger than L2, so no flush is needed between steps.
 
-  value  bit-ops/s with every operand already in HBM, the seven products run
-         as one grouped persistent launch of the tensor-core kernel
+  value  bit-ops/s with every operand already in HBM, the 15 products run as
+         one grouped persistent launch of the tensor-core kernel
          (lakgb_gram_group_run, after one table launch), timed with CUDA
-         events on the launching stream; L2 (129 MB) is flushed before each
-         step because the packed inputs (~18 MB) would fit in it.  The same
-         pass with one launch per product (lakgb_gram_device, default kernel
-         choice) is reported as per_launch_pass, and replayed from a CUDA
-         graph as cuda_graph; the grouped outputs are checked bit for bit
-         against the per-launch ones before timing.
+         events on the launching stream; the grouped outputs are checked bit
+         for bit against one launch per product before timing, and every
+         product is also run with the CUDA-core popcount kernel and compared.
   e2e    the same pass through the reference-facing C entry points
-         (wrap_AnZt_vv__run / wrap_AnAt_vv__run) on host buffers, with the
-         bit-matrix upload and the FP64 result download inside the timed region.
+         (wrap_AnZt_vv__run / wrap_AnAt_vv__run) on host buffers: the packed
+         bins uploaded once per pass from pinned memory, the 14.3 GB of FP64
+         scores copied back, inside the timed region; checked bit for bit
+         against the device-resident pass.
 
-Whole solves ("solves" in the JSON line): config 1 (case-only 1024 x 1024,
-the reference's CPU-runnable case) timed over repeated lakgb_bcc_solve calls
-and checked against the reference's golden trace, and one solve of the
-case/control workload; the config-1 solve is also timed on the host cores.
+The host-core baseline times one product of this shape on a row subset
+(6144 case x 6144 control rows x 131072 SNPs) with the reference's kernels
+where they build (x86-64 with the reference tree) or the plain-C port of the
+same kernels (oracle/liblakoracle.so), OpenMP over all host threads.
+`--impl reference` runs that CPU path as the reference arm.
 
-`--impl reference` times the reference's CPU implementation of the pass on
-this host's cores instead: the reference compiled from its sources when it is
-available here (x86-64 with the reference tree), otherwise the plain-C port of
-the same kernels (oracle/liblakoracle.so), OpenMP over all host threads.
+Extras in the same JSON line: the case/control configuration's pass (cases
+4096 + controls 4096 x 16384, 2 bins), the batched-null Gram passes, the .b16
+transposer, the bit-plane An_ZtSWn_Yt_ww product, whole solves, batched nulls
+and a served stream.
 """
 from __future__ import annotations
 
@@ -46,9 +48,17 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-METRIC = "bit-ops/s of Gram pass (bcc_lf_YnWt, case/control 2x(2048+2048) x 16384, B_MLT=32)"
+METRIC = ("bit-ops/s of Gram pass (bcc_lf_YnWt; large case/control: cases 32768 + controls 32768 x 131072 SNPs, "
+          "3 bins, B_MLT=32)")
 UNIT = "bitop/s"
-WORKLOAD = "case_control_4096x4096x16384_2bins_gram_pass"
+WORKLOAD = "case_control_32768x32768x131072_3bins_gram_pass"
+CONFIG = {"workload": WORKLOAD, "cases": 32768, "controls": 32768, "snps": 131072, "bins": 3,
+          "products_per_step": 15, "maf": "U[0.01,0.5]", "planted": "2048x4096, 5% flips",
+          "l2": "no flush: the packed inputs (1.08 GB) are larger than L2 (129 MB)"}
+LARGE_CPU_ROWS = 6144
+CPU_SAMPLE = ("one AnZt product of the workload's shape on a row subset: %d case x %d control rows x 131072 SNPs "
+              "(MAF U[0.01,0.5], planted rows with 5%% flips), D-weighted with row terms, rows drawn on the host"
+              % (LARGE_CPU_ROWS, LARGE_CPU_ROWS))
 
 
 def _rank_env():
@@ -171,14 +181,59 @@ def cpu_gram_pass(inst, backend: str, threads: int):
     return time.perf_counter() - t0, work
 
 
-CPU_SAMPLE = "full Gram pass of the workload (cases 4096 + controls 4096 x 16384 SNPs, 2 bins)"
+# ---------------------------------------------------------------------------
+# CPU: the reference's own kernels (x86 with sources) or the C port, on a
+# bounded sample of the large workload
 
 
-def cpu_sample_instance():
-    """The CPU sample is the whole workload: one full pass takes a few seconds
-    on the host cores, so no subsampling is needed."""
-    from lakcluster_c_gb300 import synth
-    return synth.case_control(seed=2)
+class CpuLargeSample:
+    """One AnZt product of the large workload's shape on a row subset, on the
+    host cores: LARGE_CPU_ROWS case rows x LARGE_CPU_ROWS control rows x all
+    131072 SNPs, D-weighted with the AJDK_1_1 row terms (the arithmetic of
+    every product of the pass).  Rows are drawn on the host with the
+    workload's distributions; timing does not depend on the bit values."""
+
+    def __init__(self, backend: str, threads: int, n_rows: int, ncols: int = 131072):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from lakcluster_c_gb300 import abi
+        from lakcluster_c_gb300.large_pass import host_rows
+        import kernel_cases as kc
+
+        self.backend, self.kc, self.abi = backend, kc, abi
+        self.lib = kc.load_backend(backend)
+        if backend == "oracle":
+            self.lib.lako_set_threads(threads)
+        else:
+            C.c_int.in_dll(self.lib, "GLOBAL_omp_type").value = 1
+            C.c_int.in_dll(self.lib, "GLOBAL_thread_count").value = threads
+        A = host_rows(n_rows, ncols, seed=3)
+        Z = host_rows(n_rows, ncols, planted=(0, 0), seed=4)
+        self.MA = abi.MHandle(None, wX=A, nrows=n_rows, ncols=ncols)
+        self.MZ = abi.MHandle(None, wX=Z, nrows=n_rows, ncols=ncols)
+        P = abi.psize(ncols)
+        pc = np.unpackbits(np.arange(256, dtype=np.uint8)[:, None], axis=1).sum(1)
+        cnt = pc[A.reshape(n_rows, P, abi.POPLENGTH // 8)].sum(axis=(0, 2)).astype(np.float64)
+        bits = np.minimum(abi.POPLENGTH, ncols - abi.POPLENGTH * np.arange(P)).astype(np.float64)
+        self.A_ajdk = abi.calc_A_ajdk(cnt / (bits * n_rows))
+        self.lfA = kc.lhandle_from(kc.call_an_ajdk(backend, abi.TYPE_pm, abi.SPACING_b, self.MA, self.A_ajdk),
+                                   self.MA.rpop_b, abi.AJDK_TOT, abi.SPACING_b)
+        self.lfZ = kc.lhandle_from(kc.call_an_ajdk(backend, abi.TYPE_pm, abi.SPACING_b, self.MZ, self.A_ajdk),
+                                   self.MZ.rpop_b, abi.AJDK_TOT, abi.SPACING_b)
+        self.work = float(n_rows) * float(n_rows) * float(ncols)
+        self.out = C.POINTER(abi.L_handle)()
+
+    def step(self) -> float:
+        """One product; returns its wall time (s)."""
+        abi, kc = self.abi, self.kc
+        aj = self.A_ajdk.ctypes.data_as(C.POINTER(C.c_double))
+        t0 = time.perf_counter()
+        if self.backend == "oracle":
+            self.lib.lako_AnZt_vv(abi.TYPE_pm, abi.SPACING_b, abi.SPACING_b, self.MA.ptr, self.MZ.ptr, aj,
+                                  self.lfA.ptr, self.lfZ.ptr, C.byref(self.out))
+        else:
+            self.lib.wrap_AnZt_vv__run(*kc._thread_args(), abi.TYPE_pm, abi.SPACING_b, abi.SPACING_b,
+                                       self.MA.ptr, self.MZ.ptr, aj, self.lfA.ptr, self.lfZ.ptr, C.byref(self.out))
+        return time.perf_counter() - t0
 
 
 def run_reference(args):
@@ -187,26 +242,19 @@ def run_reference(args):
         return 0
     backend, kind = _cpu_backend()
     threads = os.cpu_count() or 1
-    inst = cpu_sample_instance()
+    smp = CpuLargeSample(backend, threads, LARGE_CPU_ROWS)
     for _ in range(args.warmup):
-        cpu_gram_pass(inst, backend, threads)
-    secs, work = 0.0, 0.0
-    for _ in range(args.steps):
-        s, w = cpu_gram_pass(inst, backend, threads)
-        secs += s
-        work += w
-    value = work / secs
-    solves = {"case_only_1024x1024": {"cpu": cpu_solve_c1()}} if not args.no_solves else None
+        smp.step()
+    secs = sum(smp.step() for _ in range(args.steps))
+    value = smp.work * args.steps / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64-popcount+f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": CPU_SAMPLE},
+        "data": "synthetic", "config": dict(CONFIG, parallelism="replicas" if world > 1 else "single"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": CPU_SAMPLE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    if solves is not None:
-        line["solves"] = solves
     print(json.dumps(line), flush=True)
     return 0
 
@@ -218,22 +266,271 @@ def run_reference(args):
 GRAM_POPCOUNT, GRAM_TENSOR = 0, 1  # lakgb_set_gram_impl
 
 
-def _ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` recorded by the committed ncu summary
-    (a line 'traffic_bytes_per_launch: N' in profiles/<kernel>_*.md), or None."""
+def _ncu_figures(prefix: str):
+    """Figures recorded by a committed ncu summary profiles/<prefix>*.md as
+    lines 'name: value' (traffic_bytes_per_launch, bitops_per_launch), or {}."""
     prof = os.path.join(ROOT, "profiles")
+    out = {}
     if not os.path.isdir(prof):
-        return None
+        return out
     for name in sorted(os.listdir(prof)):
-        if name.startswith(kernel) and name.endswith(".md"):
+        if name.startswith(prefix) and name.endswith(".md"):
             with open(os.path.join(prof, name)) as f:
                 for line in f:
-                    if line.strip().startswith("traffic_bytes_per_launch:"):
+                    k, _, v = line.strip().partition(":")
+                    if k in ("traffic_bytes_per_launch", "bitops_per_launch") and v.strip():
                         try:
-                            return float(line.split(":", 1)[1].split()[0])
+                            out[k] = float(v.split()[0])
                         except ValueError:
-                            return None
-    return None
+                            pass
+            out["file"] = name
+            break
+    return out
+
+
+def _timed_steps(stream, fn, steps):
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        starts[i].record(stream)
+        fn()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in zip(starts, ends)]
+
+
+def large_pass_headline(args, lib, stream, sh, rank, world, local):
+    """The headline: the Gram pass of the large configuration, one grouped
+    persistent launch over its 15 products' tiles (after one table launch),
+    operands and outputs in HBM; its per-launch form, both Gram kernels on
+    every product, the pass from host buffers through the reference-facing
+    entry points, and the roofline figures."""
+    import torch
+    import torch.distributed as dist
+    from lakcluster_c_gb300.large_pass import POPCOUNT, GroupedGramPasses, LargeGramPass, LargeGramPassHost
+
+    t0 = time.perf_counter()
+    lp = LargeGramPass(seed=3 + rank)
+    setup_s = time.perf_counter() - t0
+    work = lp.work_bitops()
+    g = GroupedGramPasses([lp])
+    # The per-launch pass gives the reference outputs for the grouped launch.
+    g.run_plain(sh)
+    torch.cuda.synchronize()
+    want = [o.view(torch.int64).clone() for o in g.outputs()]
+    for o in g.outputs():
+        o.fill_(float("nan"))
+    g.run_grouped(sh)
+    torch.cuda.synchronize()
+    grouped_same = all(torch.equal(o.view(torch.int64), w) for o, w in zip(g.outputs(), want))
+    del want
+    if not grouped_same:
+        raise RuntimeError("grouped pass differs from the per-launch pass")
+    for _ in range(args.warmup):
+        g.run_grouped(sh)
+    torch.cuda.synchronize()
+    launches0 = lib.lakgb_kernel_launches()
+    with ClockSampler(local) as clk:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        step_ms = _timed_steps(stream, lambda: g.run_grouped(sh), args.steps)
+        if world > 1:
+            dist.barrier()
+    launches = lib.lakgb_kernel_launches() - launches0
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t[0].item())
+    value = world * work / (ms / 1000.0)
+    device_status = lib.lakgb_device_status()
+
+    # the same pass, one launch per product (the reference's call pattern)
+    pl = _timed_steps(stream, lambda: g.run_plain(sh), 3)
+    # both Gram kernels on every product, bit for bit; sampled entries on the host
+    checks = lp.run_checks() if rank == 0 else None
+    popc = None
+    if rank == 0:
+        default_impl = lib.lakgb_gram_impl()
+        lib.lakgb_set_gram_impl(POPCOUNT)
+        try:
+            pms = _timed_steps(stream, lambda: lp.run(sh), 1)[0]
+        finally:
+            lib.lakgb_set_gram_impl(default_impl)
+        popc = {"ms_per_pass": pms, "bitops_per_s": work / (pms / 1e3),
+                "note": "the CUDA-core popcount Gram on every product of the pass, one launch each"}
+
+    # e2e: the reference-facing entry points on host buffers
+    host = LargeGramPassHost(lp)
+    lib.lakgb_set_residency(1)
+    try:
+        host.forget_inputs()
+        d2h = host.run()
+        same_host = True
+        for (key, a, n), out in zip(lp.args, g.outputs()):
+            hv = host.output(key)[:n].view(np.uint64)
+            same_host = same_host and np.array_equal(hv, out[:n].view(torch.int64).cpu().numpy().view(np.uint64))
+        e2e_t = []
+        for _ in range(max(1, min(args.steps, 4))):
+            host.forget_inputs()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d2h = host.run()
+            e2e_t.append(time.perf_counter() - t0)
+    finally:
+        host.forget_inputs()
+        lib.lakgb_set_residency(0)
+    e2e_s = statistics.median(e2e_t)
+    h2d = host.h2d_bytes()
+    e2e = {"value": world * work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s, "identical_to_device_pass": same_host,
+           "note": "15 calls of wrap_AnZt_vv__run / wrap_AnAt_vv__run on host M_handles (pinned packed bins, "
+                   "uploaded once per pass: residency on, the bins forgotten before every pass) into host "
+                   "L_handles (14.3 GB of FP64 scores copied back per pass)"}
+
+    # roofline figures of the dominant kernel (the grouped launch)
+    peaks, src = _peaks()
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    peak_tf_sus = float(peaks.get("bf16_tflops_sustained", peak_tf))
+    tflops = 2.0 * work / (ms / 1000.0) / 1e12
+    P = lp.P
+    fp64_per_elem = (P - 1) + 4  # block adds after the first, then the score combine with row terms
+    elems = 0.0
+    for (kind, nb1, nb2, sym), a, n in lp.args:
+        elems += float(a.nA) * (a.nA + 1) / 2 if sym else float(a.nA) * a.nZ
+    fp64_rate = lib.lakgb_measure_fp64_add_rate()
+    prof = _ncu_figures("gram_tc_kernel_grouped_large")
+    traffic = None
+    if "traffic_bytes_per_launch" in prof and prof.get("bitops_per_launch"):
+        traffic = prof["traffic_bytes_per_launch"] * work / prof["bitops_per_launch"]
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    clocks = clk.summary()
+    mhz = clocks.get("sm_mhz") or 1920.0
+    popc_peak = 16 * 32 * sm_count * mhz * 1e6
+    roof = {
+        "bound": "tensor", "achieved": tflops, "peak": peak_tf, "unit": "TFLOP/s", "frac": tflops / peak_tf,
+        "traffic": traffic,
+        "kernel": "gram_tc_kernel<1, grouped> (tcgen05 e4m3 counts + FP64 fold): the pass's one persistent "
+                  "launch over the 15 products' tiles",
+        "note": ("bit pairs of the pass (full square for AnAt) counted as 2 ops (one MAC) per step time, which "
+                 "also holds the table launch (under 0.1 ms), against the %s dense bf16 burst peak; frac against "
+                 "the sustained peak %.3f. traffic: DRAM bytes per launch scaled by work from the committed ncu "
+                 "capture of the same kernel on a smaller case of this shape (%s)"
+                 % (src, tflops / peak_tf_sus, prof.get("file", "absent"))),
+        "fp64_pipe": {"ops_per_launch": elems * fp64_per_elem,
+                      "achieved_ops_per_s": elems * fp64_per_elem / (ms / 1000.0),
+                      "peak_adds_per_s": fp64_rate,
+                      "frac": elems * fp64_per_elem / (ms / 1000.0) / fp64_rate,
+                      "note": "the fold's FP64 operations (%d per computed element) against the add rate measured "
+                              "live on this GPU" % fp64_per_elem},
+        "vs_int_pipe_roofline": {"achieved_bitops": work / (ms / 1000.0), "int_pipe_peak_bitops": popc_peak,
+                                 "ratio": (work / (ms / 1000.0)) / popc_peak,
+                                 "note": "against the integer-pipe roofline of any popcount Gram (POPC 16 lanes/clk"
+                                         "/SM x 32 bits at the sampled SM clock)"},
+    }
+    out = {"value": value, "ms": ms, "launches": int(launches), "clocks": clocks, "roofline": roof, "e2e": e2e,
+           "device_status": device_status, "setup_seconds": setup_s,
+           "per_launch_pass": {"ms_per_step": statistics.median(pl), "value": world * work / (statistics.median(pl) / 1e3),
+                               "note": "the same 15 products, one lakgb_gram_device launch each, default kernel "
+                                       "choice; identical outputs"},
+           "popcount_pass": popc, "checks": checks}
+    g.close()
+    del g, lp, host
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
+def case_control_pass_measurement(args, lib, stream, sh, world, with_cpu: bool):
+    """The Gram pass of the case/control configuration (cases 4096 +
+    controls 4096 x 16384 SNPs, 2 bins, seven products): one grouped launch
+    (L2 flushed before each step: its inputs fit in L2), one launch per
+    product, a CUDA-graph replay, the pass from host buffers, and the C
+    port / reference on the host cores on the same pass."""
+    import torch
+    from lakcluster_c_gb300 import synth
+    from lakcluster_c_gb300.gram_pass import GramPassDevice, GramPassHost, gram_pass_host
+
+    inst = synth.case_control(seed=2)
+    gp = GramPassHost(inst)
+    dev = GramPassDevice(gp)
+    work = gp.work_bitops()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(fn):
+        def f():
+            flush.zero_()
+            fn()
+        return f
+
+    for _ in range(3):
+        dev.run(sh)
+    torch.cuda.synchronize()
+    per_ms = statistics.mean(_timed_steps(stream, step(lambda: dev.run(sh)), args.steps))
+    graph = None
+    try:
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr, stream=stream):
+            dev.run(sh)
+        torch.cuda.synchronize()
+        gms = statistics.mean(_timed_steps(stream, step(gr.replay), args.steps))
+        graph = {"ms_per_step": gms, "value": work / (gms / 1e3)}
+        del gr
+    except Exception as e:  # capture unsupported here: report why
+        graph = {"unavailable": str(e)[:200]}
+    ref = {k: v.view(torch.int64).clone() for k, v in dev.out.items()}
+    for v in dev.out.values():
+        v.fill_(float("nan"))
+    for _ in range(3):
+        dev.run_grouped(sh)
+    torch.cuda.synchronize()
+    same = all(torch.equal(dev.out[k].view(torch.int64), ref[k]) for k in ref)
+    del ref
+    gms = statistics.mean(_timed_steps(stream, step(lambda: dev.run_grouped(sh)), args.steps))
+    dev.close()
+    lib.lakgb_set_residency(0)
+    outputs = {}
+    gram_pass_host(gp, outputs)
+    e2e_t = []
+    d2h = 0
+    for _ in range(5):
+        t0 = time.perf_counter()
+        d2h = gram_pass_host(gp, outputs)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
+    h2d = 0
+    for kind, nb1, nb2, sym in _products(inst.nbins):
+        MA = gp.MA[nb1]
+        MZ = gp.MZ[nb2] if kind == "AnZt" else gp.MA[nb2]
+        if MZ is not None:
+            h2d += MA.wX.nbytes + (0 if sym else MZ.wX.nbytes) + MA.mc_length
+    peaks, src = _peaks()
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    out = {"workload": "case_control_4096x4096x16384_2bins_gram_pass", "products": len(dev.args),
+           "bitops_per_pass": work, "value": work / (gms / 1e3), "ms_per_step": gms,
+           "grouped_identical_to_per_launch": same,
+           "tflops_frac_of_bf16_peak": 2.0 * work / (gms / 1e3) / 1e12 / peak_tf,
+           "per_launch_pass": {"ms_per_step": per_ms, "value": work / (per_ms / 1e3)},
+           "cuda_graph": graph,
+           "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s},
+           "l2": "flushed before each step (256 MB write)"}
+    if with_cpu:
+        backend, kind = _cpu_backend()
+        threads = os.cpu_count() or 1
+        cpu_gram_pass(inst, backend, threads)
+        secs, w = 0.0, 0.0
+        for _ in range(3):
+            s1, w1 = cpu_gram_pass(inst, backend, threads)
+            secs += s1
+            w += w1
+        out["cpu"] = {"value": w / secs, "unit": UNIT, "cores": threads, "kind": kind,
+                      "sample": "the full pass, 3 passes, %.1f s" % secs}
+    del flush
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_gpu(args):
@@ -244,290 +541,75 @@ def run_gpu(args):
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from lakcluster_c_gb300 import build, synth
+    from lakcluster_c_gb300 import build
     if rank == 0 or world == 1:
         build.build_lib()
     if world > 1:
         dist.barrier()
     from lakcluster_c_gb300._lib import load
-    from lakcluster_c_gb300.gram_pass import GramPassDevice, GramPassHost, gram_pass_host
 
     lib = load()
-    # Replicas: each rank runs its own independent instance (weak scaling).
-    inst = synth.case_control(seed=2 + rank)
-    gp = GramPassHost(inst)
-    dev = GramPassDevice(gp)
-    work = gp.work_bitops()
     # A dedicated stream: its handle is non-zero, so the library launches on it
     # (a zero handle would select the library's own stream) and the CUDA
-    # events below bracket exactly the launched kernels.
+    # events bracket exactly the launched kernels.
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    for _ in range(args.warmup):
-        flush.zero_()
-        dev.run(sh)
-    torch.cuda.synchronize()
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kstart = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kend = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    launches0 = lib.lakgb_kernel_launches()
-    with ClockSampler(local) as clk:
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            dev.run(sh)
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-    launches = lib.lakgb_kernel_launches() - launches0
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
-
-    # The same pass captured once into a CUDA graph and replayed (every shape
-    # class was tuned by the warm-up steps, so nothing in it synchronises).
-    graph = None
-    try:
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=stream):
-            dev.run(sh)
-        torch.cuda.synchronize()
-        g.replay()
-        torch.cuda.synchronize()
-        gms = []
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            g.replay()
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-        gms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-        gm = sum(gms) / len(gms)
-        graph = {"ms_per_step": gm, "value": world * work / (gm / 1000.0),
-                 "note": "the seven launches of the pass captured once and replayed as one CUDA graph"}
-    except Exception as e:  # capture unsupported here: report why, keep the eager numbers
-        graph = {"unavailable": str(e)[:200]}
-
-    # The same pass as ONE grouped persistent launch of the tensor-core kernel
-    # over all seven products' tiles (lakgb_gram_group_run); outputs compared
-    # bit for bit with the per-launch pass above.
-    ref = {k: v.view(torch.int64).clone() for k, v in dev.out.items()}
-    for v in dev.out.values():
-        v.fill_(float("nan"))
-    for _ in range(max(3, args.warmup)):
-        flush.zero_()
-        dev.run_grouped(sh)
-    torch.cuda.synchronize()
-    grouped_same = all(torch.equal(dev.out[k].view(torch.int64), ref[k]) for k in ref)
-    del ref
-    if not grouped_same:
-        raise RuntimeError("grouped pass differs from the per-launch pass")
-    glaunches0 = lib.lakgb_kernel_launches()
-    with ClockSampler(local) as gclk:
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            dev.run_grouped(sh)
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-    glaunches = lib.lakgb_kernel_launches() - glaunches0
-    gpm = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
-    if world > 1:
-        t = torch.tensor([ms, gpm], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, gpm = float(t[0].item()), float(t[1].item())
-    # The headline: the pass as one grouped launch.  The same pass with one
-    # launch per product (the form the reference's call sites make) beside it.
-    per_launch = {"ms_per_step": ms, "value": world * work / (ms / 1000.0), "gpu_launches": int(launches),
-                  "clocks": clk.summary(),
-                  "note": "one lakgb_gram_device launch per product (seven per step), default kernel choice"}
-    ms, launches, clk = gpm, glaunches, gclk
-    value = world * work / (ms / 1000.0)
-
-    # dominant kernel alone: the largest AnZt launch, timed on its stream,
-    # with each of the two Gram kernels (the pass above ran the default one)
-    big = dev.args[0]
-    big.stream = sh
-    lib.lakgb_set_gram_impl.argtypes = [C.c_int]
-    lib.lakgb_gram_impl.restype = C.c_int
-    lib.lakgb_device_status.restype = C.c_int
-    default_impl = lib.lakgb_gram_impl()
-
-    def time_big(impl):
-        lib.lakgb_set_gram_impl(impl)
-        for _ in range(3):
-            lib.lakgb_gram_device(C.byref(big))
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            kstart[i].record(stream)
-            lib.lakgb_gram_device(C.byref(big))
-            kend[i].record(stream)
-        torch.cuda.synchronize()
-        kt = [s.elapsed_time(e) for s, e in zip(kstart, kend)]
-        return sum(kt) / len(kt)
-
-    k_ms_popc = time_big(GRAM_POPCOUNT)
-    k_ms = time_big(default_impl)
-    lib.lakgb_set_gram_impl(default_impl)
-    device_status = lib.lakgb_device_status()
-    k_work = float(big.nA) * float(big.nZ) * float(inst.ncols)
-
-    # e2e through the reference-facing C entry points, host buffers, no residency
-    lib.lakgb_set_residency(0)
-    outputs = {}
-    gram_pass_host(gp, outputs)
-    e2e_t = []
-    d2h = 0
-    for _ in range(max(1, min(args.steps, 10))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        d2h = gram_pass_host(gp, outputs)
-        e2e_t.append(time.perf_counter() - t0)
-    lib.lakgb_set_residency(1)
-    h2d = 0
-    for kind, nb1, nb2, sym in _products(inst.nbins):
-        MA = gp.MA[nb1]
-        MZ = gp.MZ[nb2] if kind == "AnZt" else gp.MA[nb2]
-        if MZ is None:
-            continue
-        h2d += MA.wX.nbytes + (0 if sym else MZ.wX.nbytes) + MA.mc_length
-    e2e_s = statistics.median(e2e_t)
+    head = large_pass_headline(args, lib, stream, sh, rank, world, local)
 
     # CPU baseline on a bounded sample (rank 0, N=1)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         backend, kind = _cpu_backend()
         threads = os.cpu_count() or 1
-        sample = cpu_sample_instance()
-        cpu_gram_pass(sample, backend, threads)  # warm
-        secs, w = 0.0, 0.0
-        for _ in range(3):
-            s1, w1 = cpu_gram_pass(sample, backend, threads)
-            secs += s1
-            w += w1
-        cpu = {"value": w / secs, "unit": UNIT, "cores": threads, "kind": kind,
-               "sample": CPU_SAMPLE + ", 3 passes, %.1f s" % secs}
+        smp = CpuLargeSample(backend, threads, LARGE_CPU_ROWS)
+        smp.step()
+        secs = sum(smp.step() for _ in range(3))
+        cpu = {"value": 3 * smp.work / secs, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": CPU_SAMPLE + "; 3 products, %.1f s" % secs}
+        del smp
 
-    large = None
-    if rank == 0 and not args.no_large:
-        large = large_pass_measurement(args, stream, sh, flush)
-    grouped = None
-    if rank == 0 and not args.no_grouped:
-        grouped = grouped_gram_measurement(stream, sh, flush)
-    transpose = None
-    if rank == 0 and not args.no_transpose:
-        transpose = transpose_measurement(stream, sh, with_cpu=not args.no_cpu_baseline)
+    extras = {}
+    if rank == 0:
+        if not args.no_c2:
+            extras["case_control_gram_pass"] = case_control_pass_measurement(
+                args, lib, stream, sh, world, with_cpu=(world == 1 and not args.no_cpu_baseline))
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        if not args.no_grouped:
+            extras["grouped_null_gram_passes"] = grouped_gram_measurement(stream, sh, flush)
+        if not args.no_transpose:
+            extras["b16_transpose"] = transpose_measurement(stream, sh, with_cpu=not args.no_cpu_baseline)
+        if not args.no_ww:
+            extras["an_ztswn_yt_ww"] = ztswn_ww_measurement(with_cpu=not args.no_cpu_baseline)
+        del flush
+        if not args.no_solves:
+            solves = solve_measurements(args, with_cpu=(world == 1 and not args.no_cpu_baseline))
+            if not args.no_many:
+                solves.update(many_solves_measurements(args))
+            extras["solves"] = solves
+        extras["gram_autotune"] = autotune_summary(lib)
 
-    ztswn_ww = None
-    if rank == 0 and not args.no_ww:
-        ztswn_ww = ztswn_ww_measurement(with_cpu=not args.no_cpu_baseline)
-
-    solves = None
-    if rank == 0 and not args.no_solves:
-        solves = solve_measurements(args, with_cpu=(world == 1 and not args.no_cpu_baseline))
-        if not args.no_many:
-            solves.update(many_solves_measurements(args))
-
-    peaks, src = _peaks()
-    tflops = 2.0 * k_work / (k_ms / 1000.0) / 1e12
-    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
-    # The fold of the tensor-core kernel: per output element, one FP64 add per
-    # 1920-column block after the first, then the score combine (a0d1 - 2S,
-    # and three more operations with the row/column terms).
-    P = (inst.ncols + 1919) // 1920
-    fp64_per_elem = (P - 1) + 1 + (3 if (big.lfA and big.lfZ) else 0)
-    fp64_ops = float(big.nA) * float(big.nZ) * fp64_per_elem
-    fp64_rate = lib.lakgb_measure_fp64_add_rate()
-    traffic = _ncu_traffic("gram_tc_kernel_case_control")
-    g_traffic = _ncu_traffic("gram_tc_kernel_grouped")
-    g_tflops = 2.0 * work / (ms / 1000.0) / 1e12
-    # computed elements of the pass (symmetric products: the upper triangle)
-    pass_fp64 = sum((float(a.nA) * (a.nA + 1) / 2 if a.symmetric else float(a.nA) * a.nZ) for a in dev.args)
-    pass_fp64 *= fp64_per_elem
-    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    clocks = clk.summary()
-    mhz = clocks.get("sm_mhz") or 1920.0
-    popc_peak = 16 * 32 * sm_count * mhz * 1e6  # POPC issue rate: 16 lanes/clk/SM x 32 bits
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "e4m3-bit-mma+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "bins": inst.nbins, "cases": 4096, "controls": 4096,
-                       "snps": inst.ncols, "products_per_step": len(dev.args),
-                       "pass_form": "one grouped persistent tcgen05 launch over all products' tiles "
-                                    "(lakgb_gram_group_run) after one table launch; per_launch_pass has the "
-                                    "same pass as one launch per product",
-                       "l2": "flushed before each step (256 MB write)",
-                       "parallelism": "replicas" if world > 1 else "single"},
-            "gpu_launches": int(launches),
-            "roofline": {
-                "bound": "tensor", "achieved": g_tflops, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": g_tflops / peak_tf, "traffic": g_traffic,
-                "kernel": "gram_tc_kernel<1, grouped> (tcgen05 e4m3): the pass's one persistent launch over "
-                          "the seven products' tiles",
-                "note": ("bit-pair products counted as 2 ops (one MAC) against the %s dense bf16 tensor peak "
-                         "(the e4m3 MMA the kernel issues is nominally 2x the bf16 rate); launch time = the "
-                         "step's CUDA-event time, which also holds the table launch (about 4 us). traffic: DRAM "
-                         "bytes of one launch from the committed ncu capture (profiles/), null when absent" % src),
-                "fp64_pipe": {"achieved_ops_per_s": pass_fp64 / (ms / 1000.0), "peak_adds_per_s": fp64_rate,
-                              "frac": pass_fp64 / (ms / 1000.0) / fp64_rate, "ops_per_launch": pass_fp64,
-                              "note": "FP64 operations of the fold and score combine (%d per computed element) "
-                                      "against the add rate measured live on this GPU "
-                                      "(lakgb_measure_fp64_add_rate)" % fp64_per_elem},
-                "vs_int_pipe_roofline": {
-                    "achieved_bitops": work / (ms / 1000.0), "int_pipe_peak_bitops": popc_peak,
-                    "ratio": (work / (ms / 1000.0)) / popc_peak,
-                    "note": "the pass against the integer-pipe roofline of a popcount Gram (POPC at 16 lanes/clk/SM "
-                            "x 32 bits, sampled SM clock): above 1 means faster than any popcount kernel can run"},
-                "largest_single_launch": {
-                    "kernel": "gram_tc_kernel<1> alone on the largest AnZt product, %dx%d rows, %d blocks"
-                              % (big.nA, big.nZ, P),
-                    "kernel_ms": k_ms, "achieved": tflops, "frac": tflops / peak_tf, "traffic": traffic,
-                    "fp64_pipe_frac": fp64_ops / (k_ms / 1000.0) / fp64_rate,
-                    "vs_int_pipe_roofline": (k_work / (k_ms / 1000.0)) / popc_peak,
-                    "note": "not the sole bound: copies of the kernel without the FP64 adds, or without the "
-                            "table loads, run at most 6 % faster"},
-                "popcount_kernel": {"kernel_ms": k_ms_popc, "achieved_bitops": k_work / (k_ms_popc / 1000.0),
-                                    "int_pipe_peak_bitops": popc_peak,
-                                    "int_pipe_frac": (k_work / (k_ms_popc / 1000.0)) / popc_peak,
-                                    "note": "the CUDA-core kernel on the largest product; POPC issue-rate bound, "
-                                            "16 lanes/clk/SM x 32 bits at the sampled SM clock"},
-            },
-            "device_status": device_status,
-            "per_launch_pass": per_launch,
-            "cuda_graph": graph,
-            "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s},
-            "clocks": clocks,
+            "config": dict(CONFIG, parallelism="replicas" if world > 1 else "single"),
+            "pass_form": "one grouped persistent tcgen05 launch over all 15 products' tiles (lakgb_gram_group_run) "
+                         "after one table launch; per_launch_pass has one launch per product",
+            "gpu_launches": head["launches"],
+            "roofline": head["roofline"],
+            "e2e": head["e2e"],
+            "clocks": head["clocks"],
+            "device_status": head["device_status"],
+            "per_launch_pass": head["per_launch_pass"],
+            "popcount_pass": head["popcount_pass"],
+            "parity_checks": head["checks"],
+            "setup_seconds": head["setup_seconds"],
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
-        if large is not None:
-            line["large_gram_pass"] = large
-        if grouped is not None:
-            line["grouped_null_gram_passes"] = grouped
-        if transpose is not None:
-            line["b16_transpose"] = transpose
-        if ztswn_ww is not None:
-            line["an_ztswn_yt_ww"] = ztswn_ww
-        line["gram_autotune"] = autotune_summary(lib)
-        if solves is not None:
-            line["solves"] = solves
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -545,44 +627,6 @@ def autotune_summary(lib):
     for e in table:
         chosen[e["choice"]] = chosen.get(e["choice"], 0) + 1
     return {"classes": len(table), "chosen": chosen, "first_classes": table[:6]}
-
-
-def large_pass_measurement(args, stream, sh, flush):
-    """The Gram pass of the large configuration (cases 32768 + controls 32768 x
-    131072 SNPs, 3 bins; 15 launches), inputs drawn on the device: every
-    product run with both Gram kernels and compared bit for bit, sampled
-    entries recomputed on the host, then the pass timed with each kernel."""
-    import torch
-    from lakcluster_c_gb300.large_pass import POPCOUNT, TENSOR, LargeGramPass
-
-    t0 = time.perf_counter()
-    lp = LargeGramPass()
-    setup_s = time.perf_counter() - t0
-    checks = lp.run_checks()
-    work = lp.work_bitops()
-    lib = lp.lib
-    default_impl = lib.lakgb_gram_impl()
-    timings = {}
-    for impl, name, reps in ((TENSOR, "tensor", 3), (POPCOUNT, "popcount", 1)):
-        lib.lakgb_set_gram_impl(impl)
-        lp.run(sh)  # warm
-        torch.cuda.synchronize()
-        ms = []
-        for _ in range(reps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            lp.run(sh)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        timings[name] = {"ms_per_pass": statistics.median(ms), "bitops_per_s": work / (statistics.median(ms) / 1e3),
-                         "reps": reps}
-    lib.lakgb_set_gram_impl(default_impl)
-    return {"workload": "case_control_32768x32768x131072_3bins_gram_pass", "launches": len(lp.args),
-            "bitops_per_pass": work, "setup_seconds": setup_s, "checks": checks, **timings,
-            "note": "operands drawn on the device (MAF U[0.01,0.5], 2048x4096 planted, 5% flips); row terms from "
-                    "wrap_An_ajdk_v; host recomputation of sampled entries in block order"}
 
 
 def grouped_gram_measurement(stream, sh, flush):
@@ -913,7 +957,7 @@ def ztswn_ww_measurement(with_cpu: bool):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -923,8 +967,8 @@ def main():
     ap.add_argument("--no-ww", action="store_true", help="skip the An_ZtSWn_Yt_ww bit-plane product measurement")
     ap.add_argument("--no-grouped", action="store_true",
                     help="skip the grouped Gram passes of the batched-null instances")
-    ap.add_argument("--no-large", action="store_true",
-                    help="skip the large-configuration Gram pass (32768 + 32768 x 131072)")
+    ap.add_argument("--no-c2", action="store_true",
+                    help="skip the case/control configuration's Gram pass (4096 + 4096 x 16384)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -208,6 +208,108 @@ class LargeGramPass:
                 "sampled_equal_host": sample_ok, "device_status": self.lib.lakgb_device_status()}
 
 
+class LargeGramPassHost:
+    """The same pass through the reference-facing C entry points
+    (wrap_AnZt_vv__run / wrap_AnAt_vv__run) on host buffers: the packed bins
+    of a LargeGramPass copied once into pinned host memory, M_handles over
+    them (every row and SNP retained), the full AJDK row-term handles from
+    wrap_An_ajdk_v, and FP64 outputs in host L_handles the library allocates
+    on the first call and refills on every later one (the reference's
+    zero-then-fill contract).
+
+    ``run`` makes one call per product.  With residency on, each packed bin
+    is uploaded by the first call that reads it and reused by the others of
+    the same pass; ``forget_inputs`` drops those copies so that the next pass
+    uploads every bin again (the per-step host-to-device copy)."""
+
+    def __init__(self, lp: LargeGramPass):
+        import torch
+        self.lp = lp
+        self.lib = lp.lib
+        self.lib.wrap_An_ajdk_v.restype = C.c_int
+        self.M = {}
+        self._pinned = []
+        for nb in range(lp.nbins):
+            for key, W in (("A", lp.A[nb]), ("Z", lp.Z[nb])):
+                h = torch.empty(tuple(W.shape), dtype=torch.uint8, pin_memory=True)
+                h.copy_(W)
+                self._pinned.append(h)
+                self.M[(key, nb)] = abi.MHandle(None, wX=h.numpy(), nrows=W.shape[0], ncols=lp.ncols)
+        self.lf = {}
+        for k, M in self.M.items():
+            out = C.POINTER(abi.L_handle)()
+            self.lib.wrap_An_ajdk_v(C.byref(C.c_int(0)), None, None, abi.TYPE_pm, abi.SPACING_b, M.ptr,
+                                    lp.A_ajdk.ctypes.data_as(C.POINTER(C.c_double)), C.byref(out))
+            n = M.rpop_b * abi.AJDK_TOT
+            v = np.ctypeslib.as_array(C.cast(out.contents.lf, C.POINTER(C.c_double)), shape=(n,)).copy()
+            h = abi.LHandle(n)
+            h.buf[:] = v
+            h.s.row_stride, h.s.col_stride = M.rpop_b, abi.AJDK_TOT
+            h.s.spacing_row, h.s.spacing_col = abi.SPACING_b, abi.SPACING_a
+            self.lf[k] = h
+        self.outputs = {}
+
+    def calls(self):
+        for kind, nb1, nb2, sym in products(self.lp.nbins):
+            zkey = ("Z", nb2) if kind == "AnZt" else ("A", nb2)
+            yield (kind, nb1, nb2, sym), ("A", nb1), zkey
+
+    def forget_inputs(self):
+        for M in self.M.values():
+            self.lib.lakgb_forget_host_buffer(C.c_void_p(M.wX.ctypes.data))
+
+    def h2d_bytes(self) -> int:
+        """Bytes one pass copies host to device: every packed bin once, and
+        per call the column mask, the row-index and output-index lists, the
+        block weights and the row terms it reads."""
+        n = sum(M.wX.nbytes for M in self.M.values())
+        P = self.lp.P
+        for (kind, nb1, nb2, sym), ka, kz in self.calls():
+            nA, nZ = self.M[ka].rpop_j, self.M[kz].rpop_j
+            n += self.M[ka].mc_length + 8 * P + 4 * 2 * (nA + nZ) * (2 if sym else 1) + 8 * (nA + nZ)
+        return n
+
+    def run(self) -> int:
+        """One pass; returns the FP64 output bytes copied back to the host."""
+        aj = self.lp.A_ajdk.ctypes.data_as(C.POINTER(C.c_double))
+        nbytes = 0
+        for key, ka, kz in self.calls():
+            out = self.outputs.get(key)
+            if out is None:
+                out = self.outputs[key] = C.POINTER(abi.L_handle)()
+            fn = self.lib.wrap_AnAt_vv__run if key[3] else self.lib.wrap_AnZt_vv__run
+            n = fn(C.byref(C.c_int(0)), None, None, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_b,
+                   self.M[ka].ptr, self.M[kz].ptr, aj, self.lf[ka].ptr, self.lf[kz].ptr, C.byref(out))
+            nbytes += 8 * n
+        return nbytes
+
+    def output(self, key) -> np.ndarray:
+        L = self.outputs[key].contents
+        return np.ctypeslib.as_array(C.cast(L.lf, C.POINTER(C.c_double)), shape=(int(L.length),))
+
+
+def host_rows(n_rows, ncols, maf=(0.01, 0.5), planted=(2048, 4096), flip=0.05, seed=3, chunk=512):
+    """Packed rows (n_rows x bsize(ncols) bytes) drawn on the host with the
+    large configuration's distributions: per-SNP MAF U[maf], Bernoulli bits,
+    and the first planted[0] rows sharing a random pattern on the first
+    planted[1] SNPs with `flip` noise (a numpy PCG64 stream; for CPU timing
+    samples, which need the shapes and distributions, not the device bits)."""
+    rng = np.random.default_rng(seed)
+    p = (maf[0] + (maf[1] - maf[0]) * rng.random(ncols)).astype(np.float32)
+    pr, pc = planted
+    pattern = rng.random(pc) < 0.5
+    row_bytes = abi.bsize(ncols)
+    out = np.zeros((n_rows, row_bytes), np.uint8)
+    for r0 in range(0, n_rows, chunk):
+        r1 = min(n_rows, r0 + chunk)
+        bits = rng.random((r1 - r0, ncols), dtype=np.float32) < p
+        if r0 < pr:
+            k = min(r1, pr) - r0
+            bits[:k, :pc] = pattern ^ (rng.random((k, pc)) < flip)
+        out[r0:r1, : (ncols + 7) // 8] = np.packbits(bits, axis=1, bitorder="big")
+    return out
+
+
 class GroupedGramPasses:
     """The Gram passes of several independent problems (e.g. label-shuffled
     null instances), each product with its own output buffer, run either one
@@ -255,3 +357,38 @@ class GroupedGramPasses:
         if self.group:
             self.lib.lakgb_gram_group_destroy(self.group)
             self.group = None
+
+
+def main(argv=None):
+    """Run a large-configuration Gram pass on the GPU a few times (for
+    profiling one form of it on a chosen size)."""
+    import argparse
+    import time
+
+    ap = argparse.ArgumentParser(description="Gram pass of the large configuration, or a smaller one of its shape.")
+    ap.add_argument("--cases", type=int, default=32768)
+    ap.add_argument("--controls", type=int, default=32768)
+    ap.add_argument("--snps", type=int, default=131072)
+    ap.add_argument("--bins", type=int, default=3)
+    ap.add_argument("--grouped", action="store_true", help="one grouped launch per pass")
+    ap.add_argument("--reps", type=int, default=2)
+    args = ap.parse_args(argv)
+    import torch
+    lp = LargeGramPass(n_cases=args.cases, n_controls=args.controls, ncols=args.snps, nbins=args.bins)
+    g = GroupedGramPasses([lp]) if args.grouped else None
+    print("products %d, bit-ops per pass %.6e" % (len(lp.args), lp.work_bitops()), flush=True)
+    for r in range(args.reps):
+        t0 = time.perf_counter()
+        if g is not None:
+            g.run_grouped(0)
+        else:
+            lp.run(0)
+        torch.cuda.synchronize()
+        print("pass %d (%s): %.3f ms" % (r, "grouped" if g else "per product", 1e3 * (time.perf_counter() - t0)),
+              flush=True)
+    if g is not None:
+        g.close()
+
+
+if __name__ == "__main__":
+    main()

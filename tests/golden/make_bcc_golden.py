@@ -19,8 +19,11 @@ reads zeros there; the generator checks that, with the reference program's
 constant injected into that one An_v call, the same driver reproduces the
 reference program's files byte for byte.
 
+The cases in LARGE_CASES (minutes of reference time) are solved by the
+reference program with every host thread; the small cases with one.
+
 usage: python tests/golden/make_bcc_golden.py [case ...]
-       python tests/golden/make_bcc_golden.py --port [case ...]   (PORT_CASES, minutes)
+       python tests/golden/make_bcc_golden.py --large [case ...]   (LARGE_CASES)
 """
 import os
 import subprocess
@@ -68,9 +71,10 @@ def make(names):
             ind, ref_out, rk_out = os.path.join(td, "in"), os.path.join(td, "ref"), os.path.join(td, "rk")
             p_ref = bc.write_case(name, ind, ref_out, "ref.in")
             p_rk = bc.write_case(name, ind, rk_out, "rk.in")
-            bc.run_reference(p_ref)
+            large = name in bc.LARGE_CASES
+            bc.run_reference(p_ref, threads=(os.cpu_count() or 1) if large else 1)
             ref = bc.read_outputs(ref_out)
-            if bc.CASES[name][1]:
+            if large or bc.CASES[name][1]:
                 golden, source = ref, "reference program"
             else:
                 d = bc.build(name)
@@ -95,28 +99,9 @@ def make(names):
     np.savez_compressed(bc.GOLDEN, **out)
 
 
-def make_port(names, threads):
-    """Golden outputs of the cases in PORT_CASES, from oracle/lakbcc_port."""
-    subprocess.run(["make", "-s", "-C", os.path.join(os.path.dirname(bc.GOLDEN), "..", "..", "oracle"), "port"],
-                   check=True)
-    z = np.load(bc.GOLDEN, allow_pickle=False)
-    out = {k: z[k] for k in z.files}
-    for name in names:
-        with tempfile.TemporaryDirectory() as td:
-            p = bc.write_case(name, os.path.join(td, "in"), os.path.join(td, "out"))
-            subprocess.run([os.path.join(os.path.dirname(bc.GOLDEN), "..", "..", "oracle", "lakbcc_port"), p,
-                            str(threads)], check=True, stdout=subprocess.DEVNULL)
-            golden = bc.read_outputs(os.path.join(td, "out"))
-            for key in ("trace", "xdrop_a", "xdrop_b"):
-                out[name + "/" + key] = np.array(golden[key])
-            out[name + "/source"] = np.array(["solve driver on the C oracle kernels"])
-            print("%-34s %4d iterations  %5d drops  (oracle port)" % (name, len(golden["trace"]), len(golden["xdrop_a"])))
-    np.savez_compressed(bc.GOLDEN, **out)
-
-
 if __name__ == "__main__":
     args = sys.argv[1:]
-    if args[:1] == ["--port"]:
-        make_port(args[1:] or list(bc.PORT_CASES), os.cpu_count() or 1)
+    if args[:1] == ["--large"]:
+        make(args[1:] or list(bc.LARGE_CASES))
     else:
         make(args or list(bc.CASES))

@@ -28,9 +28,17 @@ def golden():
 
 
 def test_golden_covers_every_case(golden):
-    assert set(golden) == set(bc.CASES) | set(bc.PORT_CASES)
+    assert set(golden) == set(bc.CASES) | set(bc.LARGE_CASES)
     for name in bc.SMALL:
         assert golden[name]["stages"], name
+
+
+def test_goldens_with_controls_come_from_the_reference_program():
+    z = np.load(bc.GOLDEN, allow_pickle=False)
+    for name in list(bc.CASES) + list(bc.LARGE_CASES):
+        has_controls = (bc.CASES.get(name) or bc.LARGE_CASES.get(name))[1]
+        src = str(z[name + "/source"][0])
+        assert (src == "reference program") == has_controls, (name, src)
 
 
 @needs_ref

@@ -36,8 +36,8 @@ def test_in_memory_solve_matches_reference(solve_lib, golden, name):
             assert got[key] == golden[name][key], key
 
 
-def test_large_case_control_solve_matches_oracle(solve_lib, golden):
-    """The 4096 + 4096 x 16384 two-bin workload against the oracle port."""
+def test_large_case_control_solve_matches_reference(solve_lib, golden):
+    """The 4096 + 4096 x 16384 two-bin workload against the reference program's outputs."""
     name = "case_control_4096x4096x16384"
     got = bc.solve_in_memory(solve_lib, name)
     for key in ("trace", "xdrop_a", "xdrop_b"):

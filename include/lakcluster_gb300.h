@@ -258,10 +258,37 @@ int lakgb_bcc_last_error(char *msg, int msg_len);
 struct lakgb_server;
 struct lakgb_server *lakgb_server_create(int workers, long long hbm_budget_bytes);
 long long lakgb_server_submit(struct lakgb_server *s, const struct lakgb_bcc_problem *p);
+/* As submit, with a deadline `deadline_s` seconds after submission (<= 0:
+ * none): a request still queued at its deadline fails with
+ * LAKGB_E_DEADLINE, and a running one stops with that code at its next
+ * elimination iteration. */
+long long lakgb_server_submit_deadline(struct lakgb_server *s, const struct lakgb_bcc_problem *p,
+                                       double deadline_s);
+/* Returns the solve's status: 0, a lakgb_bcc_solve error code,
+ * LAKGB_E_CANCELLED, LAKGB_E_DEADLINE, or -1 for an id that is not (or no
+ * longer) known.  A request that failed fails alone: the others run on. */
 int lakgb_server_wait(struct lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times3);
+/* As wait, and the failure's message into msg (empty on success). */
+int lakgb_server_wait_msg(struct lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times3,
+                          char *msg, int msg_len);
+/* Cancel a request: a queued one completes at once with LAKGB_E_CANCELLED;
+ * a running one stops with that code at its next elimination iteration.
+ * Returns 0, or -1 for an id that is not known or already finished. */
+int lakgb_server_cancel(struct lakgb_server *s, long long id);
 int lakgb_server_peak_concurrency(struct lakgb_server *s);
+/* Stops the server: queued requests complete with LAKGB_E_CANCELLED (their
+ * waiters return), running ones are cancelled and joined, and the call
+ * returns once every thread inside lakgb_server_wait has left it.  No call on
+ * `s` may start after destroy has begun. */
 void lakgb_server_destroy(struct lakgb_server *s);
+#define LAKGB_E_CANCELLED 6
+#define LAKGB_E_DEADLINE 7
 long long lakgb_bcc_footprint(const struct lakgb_bcc_problem *p);
+/* High-water mark (bytes) of the device memory held by the library's
+ * stream-ordered allocations (the device's default memory pool) since the
+ * last reset; reset != 0 restarts it from the current use.  Lets a caller
+ * compare lakgb_bcc_footprint with what a solve really held. */
+long long lakgb_pool_high_water(int reset);
 /* Solve n problems on a server of `workers` threads; returns the number that
  * failed (per-problem status in rcs, may be NULL). */
 int lakgb_bcc_solve_many(const struct lakgb_bcc_problem *ps, int n, struct lakgb_bcc_result *rs, int *rcs,
@@ -442,6 +469,19 @@ int lakgb_bitplane_impl(void);
  * work, so its outputs are invalid).  Synchronises the device; reading it
  * clears it. */
 int lakgb_device_status(void);
+/* The same status word, but only the calling thread's own: every host thread
+ * has its own word, written by the tensor-core launches it makes.  Waits for
+ * the thread's own stream (not the device); reading clears it.  A whole solve
+ * (lakgb_bcc_solve) checks it on return and fails if it is set. */
+int lakgb_thread_device_status(void);
+/* Test hook of the tensor-core Gram's bounded waits (no reference
+ * counterpart): wall-time limit of one pipeline wait in ns (0 = the default,
+ * 2 s) and, when `withhold` is non-zero, one producer arrival of the first
+ * operand stage of CTA 0 is withheld in every later Gram launch, so that the
+ * MMA warp's wait runs out: the kernel then skips its remaining work, frees
+ * its tensor memory and returns, and the status word reads 4.  Synchronises
+ * the device. */
+void lakgb_debug_tc_pipeline(unsigned long long wait_limit_ns, int withhold);
 /* Measured FP64 add throughput of the current device (adds per second):
  * independent add chains on every SM, best of three timed launches.  The fold
  * of the tensor-core Gram performs one FP64 add per output element per

@@ -26,6 +26,15 @@ const lakbcc::Hooks kHooks = {release_L,       lakgb_forget_host_buffer, lakgb_L
 
 long row_bytes_min(int ncols) { return (long)(ncols + (16 - ncols % 16) % 16) / 8; }
 
+// A tensor-core pipeline wait of this thread's launches that ran out of time
+// invalidates the solve's products: report it as the solve's error.
+int pipeline_status() {
+  const int st = lakgb_thread_device_status();
+  if (!st) return 0;
+  g_err = "a tensor-core pipeline wait ran out of time (code " + std::to_string(st) + "); results invalid";
+  return 8;
+}
+
 }  // namespace
 
 extern "C" void lakgb_bcc_problem_init(struct lakgb_bcc_problem *p) {
@@ -105,6 +114,7 @@ extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakg
   lakbcc::Output O;
   int rc = lakbcc::solve(P, I, O, g_err, &kHooks);
   if (rc) return rc;
+  if ((rc = pipeline_status())) return rc;
   res->iterations = O.iterations;
   res->trace = (double *)malloc(sizeof(double) * (O.trace.size() ? O.trace.size() : 1));
   res->n_xdrop = (int)(O.xdrop_a.size() / 2);
@@ -136,6 +146,7 @@ extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
   lakbcc::Output O;
   rc = lakbcc::solve(P, I, O, g_err, &kHooks);
   if (rc) return rc;
+  if ((rc = pipeline_status())) return rc;
   if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_outputs(P.dir_name, O)) {
     g_err = "cannot write outputs into " + P.dir_name;
     return 2;

@@ -1675,6 +1675,24 @@ void initial_subscores(State &S) {
 
 }  // namespace
 
+namespace {
+thread_local StopCheck t_stop = nullptr;
+thread_local void *t_stop_ctx = nullptr;
+
+int stop_requested(std::string &err) {
+  if (!t_stop) return 0;
+  const char *why = nullptr;
+  const int rc = t_stop(t_stop_ctx, &why);
+  if (rc) err = why ? why : "solve stopped";
+  return rc;
+}
+}  // namespace
+
+void set_stop_check(StopCheck fn, void *ctx) {
+  t_stop = fn;
+  t_stop_ctx = ctx;
+}
+
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks) {
   if (P.Ireq > 0) { err = "GLOBAL_Ireq > 0 is not supported by this build"; return 4; }
   if (P.QR_strategy.find("YnWt") == std::string::npos || P.QC_strategy.find("YnWt") == std::string::npos ||
@@ -1699,10 +1717,12 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   O = Output();
   int rc = load(S, I, err);
   if (rc) return rc;
+  if ((rc = stop_requested(err))) return rc;
   M_mxset_all(S);
   trace_stage(S, "load");
   initial_subscores(S);
   while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
+    if ((rc = stop_requested(err))) return rc;
     sumscores_nrm(S);
     // bcc_sumscores_ifT: no MDS correction with a single covariate column;
     // bcc_sumscores_srt: no per-bin sort with GLOBAL_Ireq <= 0.

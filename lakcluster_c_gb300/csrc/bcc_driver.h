@@ -74,6 +74,12 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err);
 int make_output_dir(const std::string &dir);
 // Run the solve.  Returns 0 on success.
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks = nullptr);
+// A check the solves of the calling thread run before the initial pass and
+// before every elimination iteration: a non-zero return ends the solve with
+// that code (its buffers released as on any return) and `why` as the error.
+// Null clears it.  Used by the serving loop for cancellation and deadlines.
+using StopCheck = int (*)(void *ctx, const char **why);
+void set_stop_check(StopCheck fn, void *ctx);
 // Write out_trace.txt / out_xdrop_a.txt / out_xdrop_b.txt as the reference does.
 int write_outputs(const std::string &dir, const Output &O);
 

@@ -18,6 +18,7 @@
 // alone.
 #include <string.h>
 
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -29,6 +30,7 @@
 #include <vector>
 
 #include "../../include/lakcluster_gb300.h"
+#include "bcc_driver.h"
 #include "bcc_model.h"
 
 namespace {
@@ -88,11 +90,29 @@ struct Job {
   std::unique_ptr<OwnedProblem> prob;
   long long bytes = 0;
   Clock::time_point t_submit, t_start, t_end;
+  bool has_deadline = false;
+  Clock::time_point deadline;
+  std::atomic<int> cancel{0};  // set by lakgb_server_cancel / destroy
   int rc = 0;
   std::string err;
   lakgb_bcc_result res{};
-  bool done = false;
+  bool running = false, done = false;
 };
+
+// The stop check of a worker's solve (lakbcc::set_stop_check): cancellation
+// first, then the deadline.
+int job_stop_check(void *ctx, const char **why) {
+  Job *j = static_cast<Job *>(ctx);
+  if (j->cancel.load()) {
+    *why = "cancelled";
+    return LAKGB_E_CANCELLED;
+  }
+  if (j->has_deadline && Clock::now() > j->deadline) {
+    *why = "deadline passed while solving";
+    return LAKGB_E_DEADLINE;
+  }
+  return 0;
+}
 
 }  // namespace
 
@@ -106,21 +126,44 @@ struct lakgb_server {
   std::vector<std::thread> threads;
   long long next_id = 1;
   int running = 0, peak_running = 0;
+  int waiters = 0;  // threads inside lakgb_server_wait
   bool stop = false;
 
+  // A queued job that will not run: completed at once with `rc`.
+  void fail_pending_locked(Job *j, int rc, const char *why) {
+    j->rc = rc;
+    j->err = why;
+    j->t_start = j->t_end = Clock::now();
+    j->done = true;
+    j->prob.reset();
+  }
+
   // Next admissible job: the oldest that fits the budget (continuous
-  // batching with first-fit admission).
+  // batching with first-fit admission).  Queued jobs past their deadline are
+  // failed on the way.
   Job *admit_locked() {
-    for (auto it = pending.begin(); it != pending.end(); ++it) {
+    const Clock::time_point now = Clock::now();
+    bool failed = false;
+    for (auto it = pending.begin(); it != pending.end();) {
       Job *j = *it;
+      if (j->has_deadline && now > j->deadline) {
+        fail_pending_locked(j, LAKGB_E_DEADLINE, "deadline passed while queued");
+        it = pending.erase(it);
+        failed = true;
+        continue;
+      }
       if (running == 0 || in_use + j->bytes <= budget) {
         pending.erase(it);
         in_use += j->bytes;
         ++running;
         if (running > peak_running) peak_running = running;
+        j->running = true;
+        if (failed) cv_done.notify_all();
         return j;
       }
+      ++it;
     }
+    if (failed) cv_done.notify_all();
     return nullptr;
   }
 
@@ -133,7 +176,9 @@ struct lakgb_server {
         if (!j) return;
       }
       j->t_start = Clock::now();
+      lakbcc::set_stop_check(job_stop_check, j);
       j->rc = lakgb_bcc_solve(&j->prob->p, &j->res);
+      lakbcc::set_stop_check(nullptr, nullptr);
       if (j->rc) {
         char msg[512];
         lakgb_bcc_last_error(msg, sizeof msg);
@@ -143,6 +188,7 @@ struct lakgb_server {
       {
         std::lock_guard<std::mutex> lk(mu);
         j->done = true;
+        j->running = false;
         in_use -= j->bytes;
         --running;
         j->prob.reset();
@@ -161,14 +207,21 @@ extern "C" lakgb_server *lakgb_server_create(int workers, long long hbm_budget_b
   return s;
 }
 
-extern "C" long long lakgb_server_submit(lakgb_server *s, const struct lakgb_bcc_problem *p) {
+extern "C" long long lakgb_server_submit_deadline(lakgb_server *s, const struct lakgb_bcc_problem *p,
+                                                  double deadline_s) {
+  if (!s || !p) return -1;
   auto j = std::make_unique<Job>();
   j->prob = std::make_unique<OwnedProblem>(*p);
   j->bytes = footprint(*p);
   j->t_submit = Clock::now();
+  if (deadline_s > 0) {
+    j->has_deadline = true;
+    j->deadline = j->t_submit + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(deadline_s));
+  }
   long long id;
   {
     std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return -1;
     id = j->id = s->next_id++;
     s->pending.push_back(j.get());
     s->jobs[id] = std::move(j);
@@ -177,17 +230,43 @@ extern "C" long long lakgb_server_submit(lakgb_server *s, const struct lakgb_bcc
   return id;
 }
 
-extern "C" int lakgb_server_wait(lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times) {
+extern "C" long long lakgb_server_submit(lakgb_server *s, const struct lakgb_bcc_problem *p) {
+  return lakgb_server_submit_deadline(s, p, 0.0);
+}
+
+extern "C" int lakgb_server_wait_msg(lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times,
+                                     char *msg, int msg_len) {
+  if (msg && msg_len > 0) msg[0] = 0;
+  if (r) memset(r, 0, sizeof(*r));
   std::unique_ptr<Job> j;
   {
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->jobs.find(id);
     if (it == s->jobs.end()) return -1;
     Job *raw = it->second.get();
-    s->cv_done.wait(lk, [&] { return raw->done; });
-    j = std::move(it->second);
-    s->jobs.erase(it);
+    ++s->waiters;
+    // A queued job fails at its deadline even while every worker is busy.
+    while (!raw->done) {
+      if (raw->has_deadline && !raw->running) {
+        s->cv_done.wait_until(lk, raw->deadline + std::chrono::milliseconds(1));
+        if (!raw->done && !raw->running && Clock::now() > raw->deadline) {
+          for (auto p = s->pending.begin(); p != s->pending.end(); ++p)
+            if (*p == raw) { s->pending.erase(p); break; }
+          s->fail_pending_locked(raw, LAKGB_E_DEADLINE, "deadline passed while queued");
+        }
+      } else {
+        s->cv_done.wait(lk);
+      }
+    }
+    it = s->jobs.find(id);
+    if (it != s->jobs.end()) {  // another waiter on the same id may have taken it
+      j = std::move(it->second);
+      s->jobs.erase(it);
+    }
+    --s->waiters;
+    s->cv_done.notify_all();  // destroy may be waiting for the waiters to leave
   }
+  if (!j) return -1;
   if (r) *r = j->res;
   else lakgb_bcc_result_free(&j->res);
   if (times) {
@@ -195,7 +274,30 @@ extern "C" int lakgb_server_wait(lakgb_server *s, long long id, struct lakgb_bcc
     times[1] = std::chrono::duration<double>(j->t_end - j->t_start).count();     // solving
     times[2] = std::chrono::duration<double>(j->t_end - j->t_submit).count();    // latency
   }
+  if (msg && msg_len > 0) {
+    strncpy(msg, j->err.c_str(), (size_t)msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
   return j->rc;
+}
+
+extern "C" int lakgb_server_wait(lakgb_server *s, long long id, struct lakgb_bcc_result *r, double *times) {
+  return lakgb_server_wait_msg(s, id, r, times, nullptr, 0);
+}
+
+extern "C" int lakgb_server_cancel(lakgb_server *s, long long id) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end() || it->second->done) return -1;
+  Job *j = it->second.get();
+  j->cancel.store(1);
+  if (!j->running) {
+    for (auto p = s->pending.begin(); p != s->pending.end(); ++p)
+      if (*p == j) { s->pending.erase(p); break; }
+    s->fail_pending_locked(j, LAKGB_E_CANCELLED, "cancelled while queued");
+    s->cv_done.notify_all();
+  }
+  return 0;
 }
 
 extern "C" int lakgb_server_peak_concurrency(lakgb_server *s) {
@@ -206,12 +308,24 @@ extern "C" int lakgb_server_peak_concurrency(lakgb_server *s) {
 extern "C" long long lakgb_bcc_footprint(const struct lakgb_bcc_problem *p) { return footprint(*p); }
 
 extern "C" void lakgb_server_destroy(lakgb_server *s) {
+  if (!s) return;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
+    for (Job *j : s->pending) s->fail_pending_locked(j, LAKGB_E_CANCELLED, "server shut down");
+    s->pending.clear();
+    for (auto &kv : s->jobs)
+      if (kv.second->running) kv.second->cancel.store(1);
   }
   s->cv_work.notify_all();
+  s->cv_done.notify_all();
   for (auto &t : s->threads) t.join();
+  {
+    // every job is done now; let the threads inside wait collect theirs
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_done.notify_all();
+    s->cv_done.wait(lk, [&] { return s->waiters == 0; });
+  }
   for (auto &kv : s->jobs) lakgb_bcc_result_free(&kv.second->res);
   delete s;
 }

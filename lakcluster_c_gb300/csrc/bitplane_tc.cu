@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 1) bitplane_tc_kernel(BitplaneParams
       tc::mma_commit(&sm.done);
       const unsigned long long t0 = tc::globaltimer();
       while (!tc::mbar_try(&sm.done, 0)) {
-        if (tc::globaltimer() - t0 > tc::kWaitNs) {
+        if (tc::globaltimer() - t0 > tc::g_wait_ns) {
           atomicCAS(status, 0, 15);
           break;
         }

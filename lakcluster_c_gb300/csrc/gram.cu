@@ -450,6 +450,12 @@ extern "C" int lakgb_gram_impl(void) { return lakgb::g_gram_impl.load(); }
 
 extern "C" int lakgb_device_status(void) { return lakgb::tc_status_take(); }
 
+extern "C" int lakgb_thread_device_status(void) { return lakgb::tc_status_take_stream(); }
+
+extern "C" void lakgb_debug_tc_pipeline(unsigned long long wait_limit_ns, int withhold) {
+  lakgb::tc_debug_set(wait_limit_ns ? wait_limit_ns : 2000000000ull, withhold);
+}
+
 namespace {
 
 bool params_from_args(const lakgb_gram_args *a, lakgb::GramParams *p) {

@@ -65,9 +65,13 @@ void launch_gram_tc(const GramParams &p, cudaStream_t s);
 // Read and clear the device status word of the tensor-core kernels
 // (0 = no pipeline error).
 int tc_status_take();
+int tc_status_take_stream();
 // Device address of that status word, for tensor-core kernels of other
 // translation units.
 int *tc_status_device_ptr();
+// Test hooks of the tensor-core pipelines: wall-time limit of a wait (ns) and
+// the withheld arrival (lakgb_debug_tc_pipeline).
+void tc_debug_set(unsigned long long wait_ns, int withhold);
 
 // Algorithmic bit-ops of one Gram launch: rows_A * rows_Z * retained columns
 // (the full square for the symmetric variant, as the reference counts it).

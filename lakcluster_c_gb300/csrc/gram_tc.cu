@@ -51,7 +51,10 @@
 
 namespace lakgb {
 
-__device__ int g_tc_status;  // first pipeline error code of any tensor-core kernel (0 = none)
+// Test hook: when set, producer warp 0 of CTA 0 withholds its arrival for
+// the first operand stage, so the MMA warp's wait for that stage runs out
+// (lakgb_debug_tc_withhold).
+static __device__ int g_withhold;
 
 namespace {
 
@@ -135,13 +138,19 @@ __device__ __forceinline__ double twice(double x) {
   return (e >= 1 && e <= 2045) ? __longlong_as_double(bits + (1ll << 52)) : __dmul_rn(2.0, x);
 }
 
-// (tile_m, tile_n) of tile r of one Gram's list: every (A tile row, Z tile
-// column) pair in row-major order, or, for a symmetric Gram with a square
-// tile grid, only the pairs on or above the diagonal.
-__device__ __forceinline__ void tile_coords(int ntn, bool tri, int r, int &tile_m, int &tile_n) {
+// (tile_m, tile_n) of tile r of one Gram's list.  A full grid is walked in
+// bands of kBand tile rows, each band column by column: the CTAs of a wave
+// (consecutive r) then share a few A row panels and a few Z row panels, a
+// working set that stays in L2 even when a whole side of the product does
+// not (32768-row bins: 2 MB per 128-row panel).  A symmetric Gram with a
+// square tile grid lists only the pairs on or above the diagonal, row by row.
+constexpr int kBand = 8;
+__device__ __forceinline__ void tile_coords(int ntm, int ntn, bool tri, int r, int &tile_m, int &tile_n) {
   if (!tri) {
-    tile_m = (r / ntn) * kBM;
-    tile_n = (r % ntn) * kBN;
+    const int band = r / (kBand * ntn), in = r - band * (kBand * ntn);
+    const int rows = min(kBand, ntm - band * kBand);
+    tile_m = (band * kBand + in % rows) * kBM;
+    tile_n = (in / rows) * kBN;
     return;
   }
   int i = 0;
@@ -172,16 +181,16 @@ __device__ __forceinline__ int find_instance(const I *start, int n, long long k)
 // grouped launch lists the tiles of its instances one instance after another.
 template <bool GRP>
 struct TileWalk {
-  int ntn, ntiles, k;
+  int ntm, ntn, ntiles, k;
   bool tri;
   __device__ TileWalk(const GramParams &p, const GramGroupDev &g) : k((int)blockIdx.x - (int)gridDim.x) {
     if (GRP) {
       ntiles = g.tile0[g.n];
-      ntn = 0;
+      ntm = ntn = 0;
       tri = false;
     } else {
       ntn = (p.nZ + kBN - 1) / kBN;
-      const int ntm = (p.nA + kBM - 1) / kBM;
+      ntm = (p.nA + kBM - 1) / kBM;
       tri = p.symmetric && ntm == ntn;
       ntiles = tri ? ntn * (ntn + 1) / 2 : ntm * ntn;
     }
@@ -193,14 +202,14 @@ struct TileWalk {
       inst = find_instance(g.tile0, g.n, k);
       const GramParams &q = g.ps[inst];
       const int n_z = (q.nZ + kBN - 1) / kBN, n_m = (q.nA + kBM - 1) / kBM;
-      tile_coords(n_z, q.symmetric && n_m == n_z, k - g.tile0[inst], tile_m, tile_n);
+      tile_coords(n_m, n_z, q.symmetric && n_m == n_z, k - g.tile0[inst], tile_m, tile_n);
       return true;
     }
     inst = 0;
     for (;;) {
       k += gridDim.x;
       if (k >= ntiles) return false;
-      tile_coords(ntn, tri, k, tile_m, tile_n);
+      tile_coords(ntm, ntn, tri, k, tile_m, tile_n);
       if (tri || !(p.symmetric && tile_m > tile_n + kBN - 1)) return true;
     }
   }
@@ -215,7 +224,7 @@ __device__ __forceinline__ const GramParams &params_of(const GramParams &p, cons
 
 template <int TYPE, bool GRP>
 __global__ void __launch_bounds__(kThreads, 1)
-    gram_tc_kernel(GramParams p, GramGroupDev grp, const double *__restrict__ T) {
+    gram_tc_kernel(GramParams p, GramGroupDev grp, const double *__restrict__ T, int *status) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ Smem sm;
   // stages first, on a 1024-byte boundary (swizzle atoms)
@@ -296,13 +305,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint4 x = side ? rx[u] : xm;
           load(g + kPrefetch, rm[u], rx[u]);
           if (TYPE == 1) cnt += popc4(xm);
-          if (wrap > 0 && ok) ok = tc::mbar_wait(&sm.empty[s], (uint32_t)((wrap - 1) & 1), abort, &g_tc_status, 1);
+          if (wrap > 0 && ok) ok = tc::mbar_wait(&sm.empty[s], (uint32_t)((wrap - 1) & 1), abort, status, 1);
           if (ok) {
             expand_row(my_row + s * kStageBytes, my_sw, x);
             tc::fence_proxy_async();
           }
           __syncwarp();
-          if (lane == 0) tc::mbar_arrive(&sm.full[s]);
+          if (lane == 0 && !(g_withhold && blockIdx.x == 0 && tid == 0 && wrap == 0 && s == 0))
+            tc::mbar_arrive(&sm.full[s]);
           if (++s == kStages) {
             s = 0;
             ++wrap;
@@ -311,7 +321,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // end of a block: publish the row counts
             const int t = gbb & 1;
             if (gbb >= 2 && ok)
-              ok = tc::mbar_wait(&sm.aux_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, &g_tc_status, 2);
+              ok = tc::mbar_wait(&sm.aux_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, status, 2);
             s_cnt[t * 256 + tid] = cnt;
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&sm.aux_full[t]);
@@ -334,11 +344,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int b = 0; b < P && ok; ++b, ++gbb) {
           const int t = gbb & 1;
           if (gbb >= 2)
-            ok = tc::mbar_wait(&sm.acc_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, &g_tc_status, 3);
+            ok = tc::mbar_wait(&sm.acc_empty[t], (uint32_t)(((gbb >> 1) - 1) & 1), abort, status, 3);
           tc::fence_after_sync();
           for (int ch = 0; ch < kChunks && ok; ++ch) {
             const int cs = s;
-            ok = tc::mbar_wait(&sm.full[cs], (uint32_t)(wrap & 1), abort, &g_tc_status, 4);
+            ok = tc::mbar_wait(&sm.full[cs], (uint32_t)(wrap & 1), abort, status, 4);
             if (++s == kStages) {
               s = 0;
               ++wrap;
@@ -362,8 +372,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc::mma_commit(&sm.done);
       const unsigned long long t0 = tc::globaltimer();
       while (!tc::mbar_try(&sm.done, 0)) {
-        if (tc::globaltimer() - t0 > tc::kWaitNs) {
-          atomicCAS(&g_tc_status, 0, 5);
+        if (tc::globaltimer() - t0 > tc::g_wait_ns) {
+          atomicCAS(status, 0, 5);
           break;
         }
       }
@@ -425,9 +435,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int b = 0; b < P; ++b) {
         const long long gbb = gb0 + b;
         const int t = (int)(gbb & 1);
-        bool w = ok && tc::mbar_wait(&sm.tab_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 8);
-        w = w && tc::mbar_wait(&sm.aux_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 6);
-        w = w && tc::mbar_wait(&sm.acc_full[t], (uint32_t)((gbb >> 1) & 1), abort, &g_tc_status, 7);
+        bool w = ok && tc::mbar_wait(&sm.tab_full[t], (uint32_t)((gbb >> 1) & 1), abort, status, 8);
+        w = w && tc::mbar_wait(&sm.aux_full[t], (uint32_t)((gbb >> 1) & 1), abort, status, 6);
+        w = w && tc::mbar_wait(&sm.acc_full[t], (uint32_t)((gbb >> 1) & 1), abort, status, 7);
         ok = __all_sync(0xffffffffu, w);
         tc::fence_after_sync();
         const double *Tb = sT + t * kTabStride;
@@ -463,12 +473,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&sm.acc_empty[t]);
           }
+          // the four columns' Z row counts in one 16-byte load (c0 is a
+          // multiple of kRound = 4)
+          static_assert(kRound == 4, "one int4 of Z row counts per round");
+          const int4 pz4 = *reinterpret_cast<const int4 *>(pzb + c0);
+          const int pzr[4] = {pz4.x, pz4.y, pz4.z, pz4.w};
 #pragma unroll
           for (int j = 0; j < kRound; ++j) {
             const int n = decode_count(cn[cur][j]);
-            int c = (TYPE == 1) ? pa + pzb[c0 + j] - 2 * n : n;
-            c = min(max(c, 0), kTabStride - 1);
-            const double x = Tb[c];
+            const int c = (TYPE == 1) ? pa + pzr[j] - 2 * n : n;
+            // 0 <= c <= 1920 for counts of a completed block; anything else
+            // (counts of an aborted pipeline) reads the NaN entry 1921
+            const double x = Tb[min((unsigned)c, (unsigned)(kTabStride - 1))];
             const double v =
                 (b > 0) ? __dadd_rn(__hiloint2double((int)a[cur][2 * j + 1], (int)a[cur][2 * j]), x) : x;
             a[cur][2 * j] = (uint32_t)__double2loint(v);
@@ -509,7 +525,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               if (tc::mbar_wait_landed(&sm.tab_full[t], (uint32_t)((gbb >> 1) & 1)))
                 issue_table(t, jt, b + 2);
               else
-                atomicCAS(&g_tc_status, 0, 9);
+                atomicCAS(status, 0, 9);
             }
           }
         }
@@ -527,7 +543,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (et == 0) {
       for (int t = 0; t < 2; ++t) {
         const unsigned n = *(volatile unsigned *)&sm.tab_issued[t];
-        if (n && !tc::mbar_wait_landed(&sm.tab_full[t], (n - 1) & 1)) atomicCAS(&g_tc_status, 0, 10);
+        if (n && !tc::mbar_wait_landed(&sm.tab_full[t], (n - 1) & 1)) atomicCAS(status, 0, 10);
       }
     }
   }
@@ -590,7 +606,7 @@ template <int TYPE>
 void launch_tc_type(const GramParams &p, const double *T, cudaStream_t s) {
   configure_tc<TYPE, false>();
   const int grid = std::max(1, std::min(active_tiles(p), sm_count()));
-  gram_tc_kernel<TYPE, false><<<grid, kThreads, kSmemBytes, s>>>(p, GramGroupDev{}, T);
+  gram_tc_kernel<TYPE, false><<<grid, kThreads, kSmemBytes, s>>>(p, GramGroupDev{}, T, tc_status_device_ptr());
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
 }
@@ -599,7 +615,7 @@ template <int TYPE>
 void launch_tc_group_type(const GramGroupDev &g, int total_tiles, const double *T, cudaStream_t s) {
   configure_tc<TYPE, true>();
   const int grid = std::max(1, std::min(total_tiles, sm_count()));
-  gram_tc_kernel<TYPE, true><<<grid, kThreads, kSmemBytes, s>>>(GramParams{}, g, T);
+  gram_tc_kernel<TYPE, true><<<grid, kThreads, kSmemBytes, s>>>(GramParams{}, g, T, tc_status_device_ptr());
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
 }
@@ -635,22 +651,55 @@ void launch_gram_tc_group(const GramGroupDev &g, int type, int total_tiles, long
     launch_tc_group_type<2>(g, total_tiles, T, s);
 }
 
-int *tc_status_device_ptr() {
-  static int *ptr = nullptr;
-  if (!ptr) LAKGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_tc_status));
-  return ptr;
+// The status word of the calling host thread's launches: every thread (a
+// solve, a server worker) has its own, so a pipeline timeout in one solve is
+// reported to that solve alone.  Zeroed on the thread's own stream (which
+// does not wait for the legacy default stream).
+namespace {
+thread_local int *t_status = nullptr;
 }
 
+int *tc_status_device_ptr() {
+  if (!t_status) {
+    LAKGB_CUDA(cudaMalloc(reinterpret_cast<void **>(&t_status), sizeof(int)));
+    LAKGB_CUDA(cudaMemsetAsync(t_status, 0, sizeof(int), stream()));
+  }
+  return t_status;
+}
+
+// Read and clear the calling thread's status word (after every launch made
+// so far has finished: the launches may be on a caller's stream).
 int tc_status_take() {
+  if (!t_status) return 0;
   int v = 0;
   LAKGB_CUDA(cudaDeviceSynchronize());
-  LAKGB_CUDA(cudaMemcpyFromSymbol(&v, g_tc_status, sizeof v));
+  LAKGB_CUDA(cudaMemcpy(&v, t_status, sizeof v, cudaMemcpyDeviceToHost));
   if (v) {
-    const int zero = 0;
-    LAKGB_CUDA(cudaMemcpyToSymbolAsync(g_tc_status, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, stream()));
+    LAKGB_CUDA(cudaMemsetAsync(t_status, 0, sizeof(int), stream()));
     LAKGB_CUDA(cudaStreamSynchronize(stream()));
   }
   return v;
+}
+
+// As tc_status_take, for launches on the calling thread's own stream only
+// (a whole solve): waits for that stream, not for the device.
+int tc_status_take_stream() {
+  if (!t_status) return 0;
+  int v = 0;
+  LAKGB_CUDA(cudaMemcpyAsync(&v, t_status, sizeof v, cudaMemcpyDeviceToHost, stream()));
+  LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  if (v) {
+    LAKGB_CUDA(cudaMemsetAsync(t_status, 0, sizeof(int), stream()));
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  }
+  return v;
+}
+
+void tc_debug_set(unsigned long long wait_ns, int withhold) {
+  LAKGB_CUDA(cudaDeviceSynchronize());
+  LAKGB_CUDA(cudaMemcpyToSymbol(tc::g_wait_ns, &wait_ns, sizeof wait_ns));
+  LAKGB_CUDA(cudaMemcpyToSymbol(g_withhold, &withhold, sizeof withhold));
+  LAKGB_CUDA(cudaDeviceSynchronize());
 }
 
 }  // namespace lakgb

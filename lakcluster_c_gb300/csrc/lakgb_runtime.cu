@@ -322,6 +322,23 @@ void gram_timer_end(cudaStream_t s) {
 
 using namespace lakgb;
 
+// High-water mark of the device memory the library's stream-ordered
+// allocations hold (the current device's default memory pool, from which
+// every working buffer, mirror and resident copy comes), optionally reset.
+extern "C" long long lakgb_pool_high_water(int reset) {
+  int dev = 0;
+  LAKGB_CUDA(cudaGetDevice(&dev));
+  cudaMemPool_t pool;
+  LAKGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  unsigned long long v = 0;
+  LAKGB_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &v));
+  if (reset) {
+    unsigned long long zero = 0;
+    LAKGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+  }
+  return (long long)v;
+}
+
 extern "C" int lakgb_last_error(char *msg, int msg_len) {
   std::lock_guard<std::mutex> lk(g_mu);
   int e = g_err;

@@ -15,8 +15,12 @@ namespace lakgb {
 namespace tc {
 
 // Wall-time limit of one wait (ns).  Legitimate waits in these kernels last
-// microseconds; the limit only ends a wait whose arrival never comes.
+// microseconds; the limit only ends a wait whose arrival never comes.  Each
+// translation unit that includes this header has its own copy; a test hook
+// (lakgb_debug_tc_wait_limit_ns) shortens it to make a withheld arrival run
+// out quickly.
 constexpr unsigned long long kWaitNs = 2000000000ull;
+static __device__ unsigned long long g_wait_ns = kWaitNs;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -47,6 +51,25 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 
+// As mbar_try, but the thread may be suspended for up to `hint_ns` while the
+// phase is still open (it resumes as soon as the phase completes), so a
+// waiting warp takes no issue slots from the warps doing the work.
+__device__ __forceinline__ bool mbar_try_suspend(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return done != 0;
+}
+
+// Suspend-time hint of the waits below (ns): long enough that a warp waiting
+// for the pipeline is not re-issued every few cycles, short against the
+// wall-time limit of a wait.
+constexpr uint32_t kSuspendNs = 100000;
+
 // Wait for the phase with the given parity to complete.  Returns false when
 // the CTA has aborted (or this wait ran out of time and aborted it).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort, int *status,
@@ -54,9 +77,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
   if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = globaltimer();
   for (;;) {
-    if (mbar_try(bar, parity)) return true;
+    if (mbar_try_suspend(bar, parity, kSuspendNs)) return true;
     if (*abort) return false;
-    if (globaltimer() - t0 > kWaitNs) {
+    if (globaltimer() - t0 > g_wait_ns) {
       *abort = 1;
       atomicCAS(status, 0, code);
       return false;
@@ -70,7 +93,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
 __device__ __forceinline__ bool mbar_wait_landed(uint64_t *bar, uint32_t parity) {
   const unsigned long long t0 = globaltimer();
   while (!mbar_try(bar, parity))
-    if (globaltimer() - t0 > kWaitNs) return false;
+    if (globaltimer() - t0 > g_wait_ns) return false;
   return true;
 }
 

@@ -283,6 +283,22 @@ class LargeGramPassHost:
             nbytes += 8 * n
         return nbytes
 
+    def run_timed(self) -> list:
+        """One pass as ``run``, returning each call's wall time (s)."""
+        import time
+        aj = self.lp.A_ajdk.ctypes.data_as(C.POINTER(C.c_double))
+        out_s = []
+        for key, ka, kz in self.calls():
+            out = self.outputs.get(key)
+            if out is None:
+                out = self.outputs[key] = C.POINTER(abi.L_handle)()
+            fn = self.lib.wrap_AnAt_vv__run if key[3] else self.lib.wrap_AnZt_vv__run
+            t0 = time.perf_counter()
+            fn(C.byref(C.c_int(0)), None, None, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_b,
+               self.M[ka].ptr, self.M[kz].ptr, aj, self.lf[ka].ptr, self.lf[kz].ptr, C.byref(out))
+            out_s.append(time.perf_counter() - t0)
+        return out_s
+
     def output(self, key) -> np.ndarray:
         L = self.outputs[key].contents
         return np.ctypeslib.as_array(C.cast(L.lf, C.POINTER(C.c_double)), shape=(int(L.length),))

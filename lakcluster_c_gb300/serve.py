@@ -25,8 +25,15 @@ def bind(lib):
     lib.lakgb_server_create.restype = C.c_void_p
     lib.lakgb_server_submit.argtypes = [C.c_void_p, C.POINTER(BccProblem)]
     lib.lakgb_server_submit.restype = C.c_longlong
+    lib.lakgb_server_submit_deadline.argtypes = [C.c_void_p, C.POINTER(BccProblem), C.c_double]
+    lib.lakgb_server_submit_deadline.restype = C.c_longlong
     lib.lakgb_server_wait.argtypes = [C.c_void_p, C.c_longlong, C.POINTER(BccResult), C.POINTER(C.c_double)]
     lib.lakgb_server_wait.restype = C.c_int
+    lib.lakgb_server_wait_msg.argtypes = [C.c_void_p, C.c_longlong, C.POINTER(BccResult), C.POINTER(C.c_double),
+                                          C.c_char_p, C.c_int]
+    lib.lakgb_server_wait_msg.restype = C.c_int
+    lib.lakgb_server_cancel.argtypes = [C.c_void_p, C.c_longlong]
+    lib.lakgb_server_cancel.restype = C.c_int
     lib.lakgb_server_peak_concurrency.argtypes = [C.c_void_p]
     lib.lakgb_server_peak_concurrency.restype = C.c_int
     lib.lakgb_server_destroy.argtypes = [C.c_void_p]
@@ -46,6 +53,17 @@ def _result_lines(lib, res):
     return format_outputs(tr, xa, xb)
 
 
+E_CANCELLED, E_DEADLINE = 6, 7  # LAKGB_E_CANCELLED, LAKGB_E_DEADLINE
+
+
+class SolveFailed(RuntimeError):
+    """A request that failed on the server (the others are unaffected)."""
+
+    def __init__(self, rid: int, rc: int, msg: str):
+        super().__init__("solve %d failed (%d): %s" % (rid, rc, msg))
+        self.rid, self.rc, self.msg = rid, rc, msg
+
+
 class Server:
     """Python handle on a native lakgb_server."""
 
@@ -53,16 +71,25 @@ class Server:
         self.lib = bind(lib or load())
         self.h = self.lib.lakgb_server_create(workers, hbm_budget_bytes)
 
-    def submit(self, p: Problem) -> int:
-        return self.lib.lakgb_server_submit(self.h, C.byref(p.prob))
+    def submit(self, p: Problem, deadline_s: float = 0.0) -> int:
+        """Queue a problem; with deadline_s > 0 it fails with E_DEADLINE if it
+        has not finished that many seconds after submission."""
+        return self.lib.lakgb_server_submit_deadline(self.h, C.byref(p.prob), float(deadline_s))
 
     def wait(self, rid: int):
+        """(output lines, (queueing, solving, total) seconds); raises
+        SolveFailed with the library's message if the request failed."""
         res = BccResult()
         t = (C.c_double * 3)()
-        rc = self.lib.lakgb_server_wait(self.h, rid, C.byref(res), t)
+        msg = C.create_string_buffer(512)
+        rc = self.lib.lakgb_server_wait_msg(self.h, rid, C.byref(res), t, msg, len(msg))
         if rc != 0:
-            raise RuntimeError("solve %d failed (%d)" % (rid, rc))
+            raise SolveFailed(rid, rc, msg.value.decode(errors="replace"))
         return _result_lines(self.lib, res), tuple(t)
+
+    def cancel(self, rid: int) -> bool:
+        """Cancel a queued or running request; False if it is unknown or done."""
+        return self.lib.lakgb_server_cancel(self.h, rid) == 0
 
     def peak_concurrency(self) -> int:
         return self.lib.lakgb_server_peak_concurrency(self.h)

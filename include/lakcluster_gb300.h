@@ -231,6 +231,8 @@ struct lakgb_bcc_problem {
   double gamma;      /* elimination fraction (GLOBAL_gamma) */
   int gamma_type;    /* GLOBAL_gamma_type (0 = log) */
   int test_sparse;   /* GLOBAL_TEST_sparse (1 = estimate allele frequencies) */
+  int Ireq;          /* GLOBAL_Ireq: > 0 scores each row / column by its Ireq-th
+                        highest per-bin score (bcc_sumscores_srt); <= 0 sums bins */
 };
 /* trace: 6 values per iteration (iteration, rows left, columns left, mean row
  * score, mean column score, bins with rows); xdrop_a / xdrop_b: 2 ints per

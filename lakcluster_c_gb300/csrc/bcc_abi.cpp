@@ -81,6 +81,7 @@ extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakg
   P.gamma = prob->gamma;
   P.gamma_type = prob->gamma_type;
   P.test_sparse = prob->test_sparse;
+  P.Ireq = prob->Ireq;
   lakbcc::Input I;
   I.ncols = prob->ncols;
   const long rb = lakbcc::bsize(prob->ncols), ch = row_bytes_min(prob->ncols);

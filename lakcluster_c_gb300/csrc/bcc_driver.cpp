@@ -11,9 +11,10 @@
 // FP contraction.
 //
 // Scope of this restatement: no extra column blocks (Y/W absent), one
-// covariate column of ones per bin (T = S = 1), GLOBAL_Ireq <= 0 -- the
-// configurations of the bcc case/control benchmark.  Other settings are
-// rejected with an error rather than computed differently.
+// covariate column of ones per bin (T = S = 1), any GLOBAL_Ireq (the per-bin
+// normalisation, sort and selection of bcc_sumscores_nrm/srt/xij when it is
+// positive).  Other settings are rejected with an error rather than
+// computed differently.
 #include "bcc_driver.h"
 
 #include <math.h>
@@ -272,6 +273,32 @@ void quicksort_xij(unsigned limit, double *d, int *i_, int *ib, int *ij, int *nb
         st.push_back({n.l, j - 1, n.nn + 1});
       }
     }
+  }
+}
+
+// dQuickSort / dPartition, dir_c/Quicksort.c:43-81: ascending sort of the
+// values d[stride*l] .. d[stride*r] with the first element as pivot (the
+// order of equal values follows this partition), recursion depth limited as
+// in the reference; an explicit stack instead of recursion.
+void dquicksort_strided(unsigned limit, double *d, long stride, int l, int r) {
+  struct Node { int l, r; unsigned nn; };
+  std::vector<Node> st;
+  st.push_back({l, r, 0});
+  while (!st.empty()) {
+    const Node n = st.back();
+    st.pop_back();
+    if (n.l >= n.r || n.nn >= limit) continue;
+    const double pivot = d[stride * n.l];
+    int i = n.l, j = n.r + 1;
+    while (true) {
+      do { i++; } while (i <= n.r && d[stride * i] <= pivot);
+      do { j--; } while (d[stride * j] > pivot);
+      if (i >= j) break;
+      std::swap(d[stride * i], d[stride * j]);
+    }
+    std::swap(d[stride * n.l], d[stride * j]);
+    st.push_back({j + 1, n.r, n.nn + 1});
+    st.push_back({n.l, j - 1, n.nn + 1});
   }
 }
 
@@ -1127,7 +1154,77 @@ void dra_sumx0(double *d, unsigned long long stride, unsigned long long length) 
   for (unsigned long long r = 1; r < length; ++r) d[0] += d[r * stride];
 }
 
-void sumscores_nrm(State &S) {  // bcc_sumscores_nrm (bcc_sumscores.c:550-779), GLOBAL_Ireq <= 0
+// bcc_sumscores_nrm with GLOBAL_Ireq > 0 (bcc_sumscores.c:583-628): each bin
+// pair normalised by its own number of summands, nothing summed over bins.
+void sumscores_nrm_per_bin(State &S) {
+  const int nb = S.nbins, T = S.T_ncols;
+  for (int nb1 = 0; nb1 < nb; ++nb1)
+    for (int nb2 = 0; nb2 < nb; ++nb2) {
+      const int nbx = nb1 + nb2 * nb, same = nb1 == nb2 ? 1 : 0;
+      Single *E = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      Double *F = S.f(nb1, nb2);
+      const unsigned long long AN = (unsigned long long)E->A_nrows;
+      if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
+        double *d = &E->QR_AnZtSZnAt_nrm[nb2 * AN * T];
+        memset(d, 0, AN * T * sizeof(double));
+        const long long lld = (long long)(E2->M_Zn->h.rpop_j - 0) * (long long)(E2->M_Zn->h.cpop_j) * (long long)(E2->M_Zn->h.cpop_j - 1);
+        plusdiv(S, d, AN, T, F->QR_AnZtSZnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
+      }
+      if (E->A_rbother && S.A_cbother && E2->A_rbother) {
+        double *d = &E->QR_AnAtTAnAt_nrm[nb2 * AN * T];
+        memset(d, 0, AN * T * sizeof(double));
+        const long long lld = (long long)(E2->M_An->h.rpop_j - same) * (long long)(E2->M_An->h.cpop_j) * (long long)(E2->M_An->h.cpop_j - 1);
+        plusdiv(S, d, AN, T, F->QR_AnAtTAnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
+      }
+      const unsigned long long AC = (unsigned long long)S.A_ncols;
+      if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
+        double *d = &S.QC_AtTAnZtSZn_nrm[nbx * AC * T];
+        memset(d, 0, AC * T * sizeof(double));
+        const long long lld = (long long)(E->M_An->h.rpop_j) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(E2->M_Zn->h.rpop_j);
+        plusdiv(S, d, AC, T, F->QC_AtTAnZtSZn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
+      }
+      if (E->A_rbother && S.A_cbother && E2->A_rbother) {
+        double *d = &S.QC_AtTAnAtTAn_nrm[nbx * AC * T];
+        memset(d, 0, AC * T * sizeof(double));
+        const long long lld = (long long)(E->M_An->h.rpop_j) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(E2->M_An->h.rpop_j - same);
+        plusdiv(S, d, AC, T, F->QC_AtTAnAtTAn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
+      }
+    }
+}
+
+// bcc_sumscores_srt (bcc_sumscores.c:358-482), GLOBAL_Ireq > 0: every
+// retained row's scores sorted across its bins, every retained column's
+// across the bin pairs, each ascending (dQuickSort on the strided values).
+void sumscores_srt(State &S) {
+  const int nb = S.nbins, T = S.T_ncols;
+  const unsigned lim = S.P.recursion_limit;
+  for (int nb1 = 0; nb1 < nb; ++nb1) {
+    Single *E = S.E[nb1].get();
+    const long stride = (long)E->A_nrows * T;
+    for (int which = 0; which < 2; ++which) {
+      if (!(E->A_rbother && S.A_cbother && (which == 0 ? E->Z_rbother : E->A_rbother))) continue;
+      double *v = which == 0 ? E->QR_AnZtSZnAt_nrm.data() : E->QR_AnAtTAnAt_nrm.data();
+      for (int ma_a = 0; ma_a < E->A_nrows; ++ma_a)
+        if (bget_on(E->A_bmr_b.data(), ma_a) && bget_on(E->A_bmr_j.data(), ma_a))
+          dquicksort_strided(lim, &v[ma_a], stride, 0, nb - 1);
+    }
+  }
+  const long stride = (long)S.A_ncols * T;
+  for (int which = 0; which < 2; ++which) {
+    if (which == 0 ? !(S.A_rpop_b_total && S.A_cbother && S.Z_rpop_b_total) : !(S.A_cbother && S.A_rpop_b_total))
+      continue;
+    double *v = which == 0 ? S.QC_AtTAnZtSZn_nrm.data() : S.QC_AtTAnAtTAn_nrm.data();
+    for (int na_a = 0; na_a < S.A_ncols; ++na_a)
+      if (bget_on(S.A_bmc_b.data(), na_a) && bget_on(S.A_bmc_j.data(), na_a))
+        dquicksort_strided(lim, &v[na_a], stride, 0, nb * nb - 1);
+  }
+}
+
+void sumscores_nrm(State &S) {  // bcc_sumscores_nrm (bcc_sumscores.c:550-779)
+  if (S.P.Ireq > 0) {
+    sumscores_nrm_per_bin(S);
+    return;
+  }
   const int nb = S.nbins, T = S.T_ncols;
   for (int nb1 = 0; nb1 < nb; ++nb1)
     for (int nb2 = 0; nb2 < nb; ++nb2) {
@@ -1208,8 +1305,11 @@ void sumscores_cmb(State &S) {  // bcc_sumscores_cmb (bcc_sumscores.c:324-356)
 void sumscores_xij(State &S) {  // bcc_sumscores_xij (bcc_sumscores.c:225-322)
   S.Irem = 0;
   for (auto &E : S.E) S.Irem += (E->A_rpop_j > 0 ? 1 : 0);
-  S.Ireq = 0;  // xcc_get_Ireq("empty low") with GLOBAL_Ireq <= 0
-  const int Irow = 0, Icol = 0;
+  // xcc_get_Ireq("empty low") (bcc_sumscores.c:207-223): the Ireq-th
+  // highest of the per-bin (per-bin-pair) scores sorted by sumscores_srt
+  S.Ireq = std::max(0, std::min(S.nbins, S.P.Ireq));
+  const int Irow = S.Ireq > 0 ? S.nbins - S.Ireq : 0;
+  const int Icol = S.Ireq > 0 ? S.nbins * S.nbins - S.Ireq * S.Ireq : 0;
   if (S.A_cbother && S.A_rpop_b_total) {
     int na_b = 0, na_j = 0;
     for (int na_a = 0; na_a < S.A_ncols; ++na_a) {
@@ -1694,7 +1794,6 @@ void set_stop_check(StopCheck fn, void *ctx) {
 }
 
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks) {
-  if (P.Ireq > 0) { err = "GLOBAL_Ireq > 0 is not supported by this build"; return 4; }
   if (P.QR_strategy.find("YnWt") == std::string::npos || P.QC_strategy.find("YnWt") == std::string::npos ||
       P.QR_strategy.find("condense") != std::string::npos || P.QC_strategy.find("store one") != std::string::npos ||
       P.QR_strategy.find("ZtSWn") != std::string::npos || P.QC_strategy.find("ZtSWn") != std::string::npos) {
@@ -1724,8 +1823,9 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
     if ((rc = stop_requested(err))) return rc;
     sumscores_nrm(S);
-    // bcc_sumscores_ifT: no MDS correction with a single covariate column;
-    // bcc_sumscores_srt: no per-bin sort with GLOBAL_Ireq <= 0.
+    // bcc_sumscores_ifT: no MDS correction with a single covariate column
+    // (its correction uses columns 2.. of T).
+    if (S.P.Ireq > 0) sumscores_srt(S);
     sumscores_cmb(S);
     sumscores_xij(S);
     sumscores_mxA(S);

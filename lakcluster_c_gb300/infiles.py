@@ -47,7 +47,7 @@ def read_b16(path: str) -> np.ndarray:
 
 
 def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.05, B_MLT=32,
-                     A_row_masks=None, Z_row_masks=None, col_mask=None, gamma_type=None,
+                     A_row_masks=None, Z_row_masks=None, col_mask=None, gamma_type=None, Ireq=None,
                      name="bcc.in") -> str:
     """Write the .b16 files of one bcc problem and the .in file that names them.
 
@@ -91,6 +91,8 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
     ]
     if gamma_type is not None:
         lines.append("GLOBAL_gamma_type= %d;" % gamma_type)
+    if Ireq is not None:
+        lines.append("GLOBAL_Ireq= %d;" % Ireq)
     lines += [
         "GLOBAL_DIR_XPRE= %s;" % os.path.abspath(in_dir),
         "GLOBAL_A_n_name_= %s;" % lst("A_%02d_n.b16"),

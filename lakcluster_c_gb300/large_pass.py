@@ -215,14 +215,17 @@ class LargeGramPassHost:
     them (every row and SNP retained), the full AJDK row-term handles from
     wrap_An_ajdk_v, and FP64 outputs in host L_handles the library allocates
     on the first call and refills on every later one (the reference's
-    zero-then-fill contract).
+    zero-then-fill contract) -- or, with ``pinned_outputs``, in caller-owned
+    output handles over page-locked host memory (the reference's callers
+    may pass pre-allocated outputs; the callee checks their length and fills
+    them).
 
     ``run`` makes one call per product.  With residency on, each packed bin
     is uploaded by the first call that reads it and reused by the others of
     the same pass; ``forget_inputs`` drops those copies so that the next pass
     uploads every bin again (the per-step host-to-device copy)."""
 
-    def __init__(self, lp: LargeGramPass):
+    def __init__(self, lp: LargeGramPass, pinned_outputs: bool = False):
         import torch
         self.lp = lp
         self.lib = lp.lib
@@ -248,6 +251,15 @@ class LargeGramPassHost:
             h.s.spacing_row, h.s.spacing_col = abi.SPACING_b, abi.SPACING_a
             self.lf[k] = h
         self.outputs = {}
+        self._out_bufs = []
+        if pinned_outputs:
+            for key, ka, kz in self.calls():
+                n = self.M[ka].rpop_b * self.M[kz].rpop_b
+                buf = torch.empty(n, dtype=torch.float64, pin_memory=True)
+                L = abi.L_handle()
+                L.length, L.lf = n, buf.data_ptr()
+                self._out_bufs.append((buf, L))
+                self.outputs[key] = C.pointer(L)
 
     def calls(self):
         for kind, nb1, nb2, sym in products(self.lp.nbins):

@@ -24,7 +24,8 @@ class BccBin(C.Structure):
 class BccProblem(C.Structure):
     _fields_ = [("ncols", C.c_int), ("row_bytes", C.c_longlong), ("mc_b", C.c_void_p),
                 ("nbins", C.c_int), ("bins", C.POINTER(BccBin)),
-                ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int)]
+                ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int),
+                ("Ireq", C.c_int)]
 
 
 class BccResult(C.Structure):
@@ -59,7 +60,7 @@ class Problem:
     rows already packed as pack_rows packs them (``packed_ncols`` SNPs)."""
 
     def __init__(self, A_bins, Z_bins=None, *, gamma=0.125, B_MLT=32, gamma_type=0, A_masks=None,
-                 Z_masks=None, col_mask=None, test_sparse=1, lib=None, packed_ncols=None):
+                 Z_masks=None, col_mask=None, test_sparse=1, Ireq=0, lib=None, packed_ncols=None):
         self.lib = bind(lib or load())
         self._keep = []
         nb = len(A_bins)
@@ -93,6 +94,7 @@ class Problem:
         self.prob.B_MLT = B_MLT
         self.prob.gamma_type = gamma_type
         self.prob.test_sparse = test_sparse
+        self.prob.Ireq = Ireq
         self.ncols = ncols
 
     def _hold(self, x):

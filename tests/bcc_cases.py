@@ -36,11 +36,13 @@ def _case_only(n, m, k, seed):
     return dict(A=inst.A_bins, Z=None, gamma=0.05)
 
 
-def _case_control(nA, nZ, m, kr, kc, nbins, seed, gamma=0.05, gamma_type=None):
+def _case_control(nA, nZ, m, kr, kc, nbins, seed, gamma=0.05, gamma_type=None, Ireq=None):
     inst = synth.case_control(nA, nZ, m, kr, kc, 0.05, nbins=nbins, seed=seed)
     d = dict(A=inst.A_bins, Z=inst.Z_bins, gamma=gamma)
     if gamma_type is not None:
         d["gamma_type"] = gamma_type
+    if Ireq is not None:
+        d["Ireq"] = Ireq
     return d
 
 
@@ -52,6 +54,10 @@ CASES = {
     "case_control_2bin_masked": (_masked_case_control, True),
     "case_control_1bin_gamma_lin": (lambda: _case_control(180, 160, 1500, 20, 40, 1, 11, 0.1, 2), True),
     "case_control_3bin_ragged": (lambda: _case_control(333, 271, 1931, 21, 33, 3, 13), True),
+    # GLOBAL_Ireq > 0: rows and columns scored by their Ireq-th highest bin
+    "case_control_3bin_Ireq1": (lambda: _case_control(300, 280, 2100, 24, 40, 3, 17, Ireq=1), True),
+    "case_control_3bin_Ireq2": (lambda: _case_control(330, 290, 1950, 24, 40, 3, 19, Ireq=2), True),
+    "case_control_2bin_Ireq2": (lambda: _case_control(260, 240, 2300, 22, 44, 2, 23, Ireq=2), True),
 }
 # Cases whose reference solve takes minutes even on every host thread (the
 # 4096 + 4096 x 16384 two-bin workload: 518 s on 8 cores): their golden
@@ -62,7 +68,8 @@ LARGE_CASES = {
     "case_control_4096x4096x16384": (lambda: _case_control(4096, 4096, 16384, 256, 512, 2, 2), True),
 }
 SMALL = ["case_only_200x300", "case_control_2bin_300x250x2100", "case_control_2bin_masked",
-         "case_control_1bin_gamma_lin", "case_control_3bin_ragged"]
+         "case_control_1bin_gamma_lin", "case_control_3bin_ragged", "case_control_3bin_Ireq1",
+         "case_control_3bin_Ireq2", "case_control_2bin_Ireq2"]
 
 
 def build(name):
@@ -73,7 +80,8 @@ def write_case(name, in_dir, out_dir, fname="bcc.in"):
     d = build(name)
     return infiles.write_bcc_inputs(in_dir, out_dir, d["A"], d.get("Z"), gamma=d["gamma"], B_MLT=32,
                                     A_row_masks=d.get("A_masks"), Z_row_masks=d.get("Z_masks"),
-                                    col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), name=fname)
+                                    col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), Ireq=d.get("Ireq"),
+                                    name=fname)
 
 
 def read_outputs(out_dir):
@@ -151,5 +159,6 @@ def solve_arrays(lib, d):
     """lakgb_bcc_solve on a problem given as 0/1 arrays (see the CASES builders)."""
     from lakcluster_c_gb300 import solve as sv
     p = sv.Problem(d["A"], d.get("Z"), gamma=d["gamma"], gamma_type=d.get("gamma_type") or 0,
-                   A_masks=d.get("A_masks"), Z_masks=d.get("Z_masks"), col_mask=d.get("col_mask"), lib=lib)
+                   A_masks=d.get("A_masks"), Z_masks=d.get("Z_masks"), col_mask=d.get("col_mask"),
+                   Ireq=d.get("Ireq") or 0, lib=lib)
     return p.solve()

@@ -267,6 +267,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t st0 = tc::smem_u32(stages);
     const uint32_t my_row = st0 + side * kStageA + (uint32_t)((rr >> 3) * kSBO + (rr & 7) * 128);
     const uint32_t my_sw = (uint32_t)(rr & 7);
+    // the test hook, read once: this thread withholds its first arrival
+    bool withhold = g_withhold && blockIdx.x == 0 && tid == 0;
     bool ok = true;
     // ring position of the next chunk: stage s, in pass `wrap` over the ring
     int s = 0, wrap = 0;
@@ -311,8 +313,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::fence_proxy_async();
           }
           __syncwarp();
-          if (lane == 0 && !(g_withhold && blockIdx.x == 0 && tid == 0 && wrap == 0 && s == 0))
-            tc::mbar_arrive(&sm.full[s]);
+          if (lane == 0 && !withhold) tc::mbar_arrive(&sm.full[s]);
+          withhold = false;
           if (++s == kStages) {
             s = 0;
             ++wrap;

@@ -223,6 +223,10 @@ int lakgb_bcc_run_in_file(const char *in_path);
 struct lakgb_bcc_bin {
   int A_nrows; const unsigned char *A_rows; const unsigned char *A_mr_b;
   int Z_nrows; const unsigned char *Z_rows; const unsigned char *Z_mr_b;
+  /* covariates (GLOBAL_T_t_name_ / GLOBAL_S_t_name_): one row of T_ncols bits
+   * per case row (T_rows) and per control row (S_rows), rup(T_ncols,16)/8
+   * bytes each; both NULL = one covariate column of ones (T_ncols 1) */
+  const unsigned char *T_rows; const unsigned char *S_rows;
 };
 struct lakgb_bcc_problem {
   int ncols; long long row_bytes; const unsigned char *mc_b;
@@ -233,6 +237,9 @@ struct lakgb_bcc_problem {
   int test_sparse;   /* GLOBAL_TEST_sparse (1 = estimate allele frequencies) */
   int Ireq;          /* GLOBAL_Ireq: > 0 scores each row / column by its Ireq-th
                         highest per-bin score (bcc_sumscores_srt); <= 0 sums bins */
+  int T_ncols;       /* covariate columns of the bins' T_rows / S_rows (GLOBAL_T_n_cols) */
+  double kappa_squared;  /* GLOBAL_kappa_squared: > 0 turns on the MDS correction
+                            of the covariate columns (bcc_sumscores_ifT) */
 };
 /* trace: 6 values per iteration (iteration, rows left, columns left, mean row
  * score, mean column score, bins with rows); xdrop_a / xdrop_b: 2 ints per

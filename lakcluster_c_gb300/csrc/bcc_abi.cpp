@@ -39,6 +39,7 @@ int pipeline_status() {
 
 extern "C" void lakgb_bcc_problem_init(struct lakgb_bcc_problem *p) {
   memset(p, 0, sizeof(*p));
+  p->T_ncols = 1;
   p->B_MLT = 32;
   p->gamma = 0.125;
   p->gamma_type = 0;
@@ -82,8 +83,10 @@ extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakg
   P.gamma_type = prob->gamma_type;
   P.test_sparse = prob->test_sparse;
   P.Ireq = prob->Ireq;
+  P.kappa_squared = prob->kappa_squared;
   lakbcc::Input I;
   I.ncols = prob->ncols;
+  I.T_ncols = prob->T_ncols > 0 ? prob->T_ncols : 1;  // 0: the default single column
   const long rb = lakbcc::bsize(prob->ncols), ch = row_bytes_min(prob->ncols);
   if (prob->mc_b) I.mc_b.assign(prob->mc_b, prob->mc_b + ch), I.mc_b.resize(rb, 0);
   I.bins.resize(prob->nbins);
@@ -109,6 +112,18 @@ extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakg
     if (b.Z_mr_b) {
       B.Z_mr_b.assign(b.Z_mr_b, b.Z_mr_b + row_bytes_min(b.Z_nrows));
       B.Z_mr_b.resize(lakbcc::bsize(b.Z_nrows), 0);
+    }
+    // covariate rows, repacked to bsize(T_ncols) bytes per row
+    if (!b.T_rows != !b.S_rows || (!b.T_rows && I.T_ncols > 1)) {
+      g_err = "covariate rows T_rows and S_rows must be given together (and for T_ncols > 1)";
+      return 2;
+    }
+    if (b.T_rows) {
+      const long tch = row_bytes_min(I.T_ncols), tb = lakbcc::bsize(I.T_ncols);
+      B.T_rows.assign((size_t)std::max(1, b.A_nrows) * (size_t)tb, 0);
+      for (int r = 0; r < b.A_nrows; ++r) memcpy(&B.T_rows[(size_t)r * tb], b.T_rows + (size_t)r * tch, tch);
+      B.S_rows.assign((size_t)std::max(1, b.Z_nrows) * (size_t)tb, 0);
+      for (int r = 0; r < b.Z_nrows; ++r) memcpy(&B.S_rows[(size_t)r * tb], b.S_rows + (size_t)r * tch, tch);
     }
   }
   lakgb_set_d_mlt(P.D_MLT);

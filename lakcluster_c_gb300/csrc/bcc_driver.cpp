@@ -10,11 +10,12 @@
 // elimination trace is bit-identical.  Host code must be compiled without
 // FP contraction.
 //
-// Scope of this restatement: no extra column blocks (Y/W absent), one
-// covariate column of ones per bin (T = S = 1), any GLOBAL_Ireq (the per-bin
-// normalisation, sort and selection of bcc_sumscores_nrm/srt/xij when it is
-// positive).  Other settings are rejected with an error rather than
-// computed differently.
+// Scope of this restatement: no extra column blocks (Y/W absent); covariate
+// matrices T / S of any width (one column of ones when absent) with every
+// covariate column retained, and the MDS correction of bcc_sumscores_ifT;
+// any GLOBAL_Ireq (the per-bin normalisation, sort and selection of
+// bcc_sumscores_nrm/srt/xij when it is positive).  Other settings are
+// rejected with an error rather than computed differently.
 #include "bcc_driver.h"
 
 #include <math.h>
@@ -382,7 +383,7 @@ int load(State &S, const Input &I, std::string &err) {
   S.A_umc_j_rmv.assign(std::max(1, S.A_ncols), 0);
   S.A_umc_j_rtn.assign(std::max(1, S.A_ncols), 0);
   ura_from_bits(S.A_umc_j, S.A_bmc_j, S.A_ncols);
-  S.T_ncols = 1;
+  S.T_ncols = I.T_ncols;
   S.T_mc_length = bsize(S.T_ncols);
   S.T_bmc_b.assign(S.T_mc_length, 0);
   for (int c = 0; c < S.T_ncols; ++c) bset_on(S.T_bmc_b.data(), c);
@@ -434,17 +435,30 @@ int load(State &S, const Input &I, std::string &err) {
     }
     E->M_Zn = S.keep(mh_make(E->Z_nrows, S.A_ncols, E->Zn_w.data(), E->Z_bmr_b.data(), S.A_bmc_b.data()));
     E->M_Zt = S.keep(mh_make(S.A_ncols, E->Z_nrows, E->Zt_w.data(), S.A_bmc_b.data(), E->Z_bmr_b.data()));
-    // T and S: one covariate column of ones (bcc.c:374-399)
-    E->Tn_w.assign((size_t)std::max(1, E->A_nrows) * (size_t)bsize(1), 0);
-    for (int r = 0; r < E->A_nrows; ++r) E->Tn_w[(size_t)r * bsize(1)] |= (1 << 7);
-    E->Tt_w.assign((size_t)bsize(E->A_nrows) + POPLENGTH / BIT8, 0);
-    for (int r = 0; r < E->A_nrows; ++r) bset_on(E->Tt_w.data(), r);
+    // T and S (bcc.c:360-399): the covariate matrices when given (rows
+    // compacted by the row mask, their transposes by the covariate mask),
+    // otherwise one covariate column of ones.
+    const long tb = bsize(S.T_ncols);
+    if (!B.T_rows.empty()) {
+      E->Tn_w = compact_rows(B.T_rows, E->A_nrows, tb, E->A_bmr_b);
+      E->Tt_w = compact_rows(transpose_rows(B.T_rows, E->A_nrows, S.T_ncols), S.T_ncols, bsize(E->A_nrows), S.T_bmc_b);
+    } else {
+      E->Tn_w.assign((size_t)std::max(1, E->A_nrows) * (size_t)bsize(1), 0);
+      for (int r = 0; r < E->A_nrows; ++r) E->Tn_w[(size_t)r * bsize(1)] |= (1 << 7);
+      E->Tt_w.assign((size_t)bsize(E->A_nrows) + POPLENGTH / BIT8, 0);
+      for (int r = 0; r < E->A_nrows; ++r) bset_on(E->Tt_w.data(), r);
+    }
     E->M_Tn = S.keep(mh_make(E->A_nrows, S.T_ncols, E->Tn_w.data(), E->A_bmr_b.data(), S.T_bmc_b.data()));
     E->M_Tt = S.keep(mh_make(S.T_ncols, E->A_nrows, E->Tt_w.data(), S.T_bmc_b.data(), E->A_bmr_b.data()));
-    E->Sn_w.assign((size_t)std::max(1, E->Z_nrows) * (size_t)bsize(1), 0);
-    for (int r = 0; r < E->Z_nrows; ++r) E->Sn_w[(size_t)r * bsize(1)] |= (1 << 7);
-    E->St_w.assign((size_t)bsize(E->Z_nrows) + POPLENGTH / BIT8, 0);
-    for (int r = 0; r < E->Z_nrows; ++r) bset_on(E->St_w.data(), r);
+    if (!B.S_rows.empty() && E->Z_nrows > 0) {
+      E->Sn_w = compact_rows(B.S_rows, E->Z_nrows, tb, E->Z_bmr_b);
+      E->St_w = compact_rows(transpose_rows(B.S_rows, E->Z_nrows, S.T_ncols), S.T_ncols, bsize(E->Z_nrows), S.T_bmc_b);
+    } else {
+      E->Sn_w.assign((size_t)std::max(1, E->Z_nrows) * (size_t)bsize(1), 0);
+      for (int r = 0; r < E->Z_nrows; ++r) E->Sn_w[(size_t)r * bsize(1)] |= (1 << 7);
+      E->St_w.assign((size_t)bsize(E->Z_nrows) * (size_t)std::max(1, S.T_ncols) + POPLENGTH / BIT8, 0);
+      for (int r = 0; r < E->Z_nrows; ++r) bset_on(E->St_w.data(), r);
+    }
     E->M_Sn = S.keep(mh_make(E->Z_nrows, S.T_ncols, E->Sn_w.data(), E->Z_bmr_b.data(), S.T_bmc_b.data()));
     E->M_St = S.keep(mh_make(S.T_ncols, E->Z_nrows, E->St_w.data(), S.T_bmc_b.data(), E->Z_bmr_b.data()));
     // low-rank-update views share the packed data with their base handles
@@ -1192,6 +1206,65 @@ void sumscores_nrm_per_bin(State &S) {
     }
 }
 
+// dra_mds_nrm_s___m_m (dir_c/ra_stats.c:77-85): column 0 of an nrows x
+// ncols column-major array loses sum_{c >= 1} d[:, c] / den, in column order.
+void dra_mds_nrm(double *d, unsigned long long nrows, unsigned long long ncols, double den,
+                 const unsigned char *bmr, const unsigned char *bmc) {
+  if (!(den > 0)) return;
+  for (unsigned long long r = 0; r < nrows; ++r) {
+    if (!bget_on(bmr, (long)r)) continue;
+    for (unsigned long long c = 1; c < ncols; ++c)
+      if (bget_on(bmc, (long)c)) d[r] -= d[r + c * nrows] / den;
+  }
+}
+
+// dra_mds_pow_s___m_m (dir_c/ra_stats.c:86-100): for rows whose column-0
+// value x >= 0, x becomes x^2 - sum_{c >= 1} d[:, c]^2 / den, then the signed
+// square root of that.
+void dra_mds_pow(double *d, unsigned long long nrows, unsigned long long ncols, double den,
+                 const unsigned char *bmr, const unsigned char *bmc) {
+  if (!(den > 0)) return;
+  for (unsigned long long r = 0; r < nrows; ++r) {
+    if (!bget_on(bmr, (long)r) || !(d[r] >= 0)) continue;
+    d[r] *= d[r];
+    for (unsigned long long c = 1; c < ncols; ++c)
+      if (bget_on(bmc, (long)c)) d[r] -= d[r + c * nrows] * d[r + c * nrows] / den;
+    d[r] = d[r] >= 0 ? sqrt(d[r]) : -sqrt(-d[r]);
+  }
+}
+
+// bcc_sumscores_ifT (bcc_sumscores.c:483-548): the MDS correction of the
+// row and column scores for covariate columns 2 and up, with n_mds =
+// min(6, T_cpop_j - 1).  The reference sets the scale factor with
+//   if (GLOBAL_kappa_squared>0);{ mds_scale_factor = GLOBAL_kappa_squared;}
+// -- the statement after the empty `if` always runs -- so the denominator
+// is n_mds * GLOBAL_kappa_squared, and the correction does nothing unless
+// GLOBAL_kappa_squared is positive.  Kept as is: the outputs must match.
+// Only bin pair nb2 = 0 of each nb1 is corrected when GLOBAL_Ireq <= 0.
+void sumscores_ifT(State &S) {
+  int n_mds = std::max(0, (int)S.T_cpop_j - 1);
+  if (n_mds > 6) n_mds = 6;
+  if (n_mds <= 0) return;
+  const double den = n_mds * S.P.kappa_squared;
+  const int nb = S.nbins, T = S.T_ncols;
+  const unsigned long long AC = (unsigned long long)S.A_ncols;
+  for (int nb1 = 0; nb1 < nb; ++nb1) {
+    Single *E = S.E[nb1].get();
+    const unsigned long long AN = (unsigned long long)E->A_nrows;
+    for (int nb2 = 0; nb2 < (S.P.Ireq > 0 ? nb : 1); ++nb2) {
+      const int nbx = nb1 + nb2 * nb;
+      if (E->A_rbother && S.A_cbother && E->Z_rbother)
+        dra_mds_pow(&E->QR_AnZtSZnAt_nrm[nb2 * AN * T], AN, T, den, E->A_bmr_j.data(), S.T_bmc_j.data());
+      if (E->A_rbother && S.A_cbother)
+        dra_mds_pow(&E->QR_AnAtTAnAt_nrm[nb2 * AN * T], AN, T, den, E->A_bmr_j.data(), S.T_bmc_j.data());
+      if (S.A_rpop_b_total && S.A_cbother && S.Z_rpop_b_total)
+        dra_mds_nrm(&S.QC_AtTAnZtSZn_nrm[nbx * AC * T], AC, T, den, S.A_bmc_j.data(), S.T_bmc_j.data());
+      if (S.A_cbother && S.A_rpop_b_total)
+        dra_mds_nrm(&S.QC_AtTAnAtTAn_nrm[nbx * AC * T], AC, T, den, S.A_bmc_j.data(), S.T_bmc_j.data());
+    }
+  }
+}
+
 // bcc_sumscores_srt (bcc_sumscores.c:358-482), GLOBAL_Ireq > 0: every
 // retained row's scores sorted across its bins, every retained column's
 // across the bin pairs, each ascending (dQuickSort on the strided values).
@@ -1823,8 +1896,7 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
     if ((rc = stop_requested(err))) return rc;
     sumscores_nrm(S);
-    // bcc_sumscores_ifT: no MDS correction with a single covariate column
-    // (its correction uses columns 2.. of T).
+    sumscores_ifT(S);
     if (S.P.Ireq > 0) sumscores_srt(S);
     sumscores_cmb(S);
     sumscores_xij(S);

@@ -31,10 +31,15 @@ struct BinInput {
   int A_nrows = 0, Z_nrows = 0;
   std::vector<unsigned char> A_rows, Z_rows;   // a-space rows, bsize(ncols) bytes each
   std::vector<unsigned char> A_mr_b, Z_mr_b;   // bsize(nrows) bytes; empty = all on
+  // covariates: T (cases x T_ncols) and S (controls x T_ncols), a-space rows of
+  // bsize(T_ncols) bytes; empty = the reference's default single column of
+  // ones (T_ncols must then be 1)
+  std::vector<unsigned char> T_rows, S_rows;
 };
 
 struct Input {
   int ncols = 0;
+  int T_ncols = 1;                             // covariate columns (GLOBAL_T_n_cols)
   std::vector<unsigned char> mc_b;             // bsize(ncols) bytes; empty = all on
   std::vector<BinInput> bins;
 };

@@ -110,8 +110,8 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
 
   std::string xpre, test_type, dir_base, out_name;
   int nbins = 0, Y_n_cols = 0, T_n_cols = 1;
-  std::vector<std::string> A_t, Z_t, A_rind, Z_rind, others;
-  std::string A_cind;
+  std::vector<std::string> A_t, Z_t, A_rind, Z_rind, T_t, S_t, others;
+  std::string A_cind, T_cind;
   std::vector<int> A_rows_decl, Z_rows_decl;
   int A_ncols_decl = -1;
   auto prefixed = [&](const std::string &f) { return xpre.empty() || f.empty() ? f : xpre + "/" + f; };
@@ -152,7 +152,11 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     else if (k == "GLOBAL_Z_n_rows_") { for (auto &s : split_list(v)) { int x = 0; rc |= parse_int(s, k, x, err); Z_rows_decl.push_back(x); } }
     else if (k == "GLOBAL_Y_n_cols") rc = parse_int(v, k, Y_n_cols, err);
     else if (k == "GLOBAL_T_n_cols") rc = parse_int(v, k, T_n_cols, err);
-    else if (k == "GLOBAL_A_p_name" || k == "GLOBAL_Y_p_name" || k == "GLOBAL_T_n_cind" || k == "GLOBAL_Y_n_cind") {
+    else if (k == "GLOBAL_T_t_name_") T_t = prefixed_list(v);
+    else if (k == "GLOBAL_S_t_name_") S_t = prefixed_list(v);
+    else if (k == "GLOBAL_T_n_name_" || k == "GLOBAL_S_n_name_") { /* transposes of T_t / S_t: rebuilt */ }
+    else if (k == "GLOBAL_T_n_cind") T_cind = prefixed(v);
+    else if (k == "GLOBAL_A_p_name" || k == "GLOBAL_Y_p_name" || k == "GLOBAL_Y_n_cind") {
       if (!v.empty()) others.push_back(k);
     } else if (k.rfind("GLOBAL_Y_", 0) == 0 || k.rfind("GLOBAL_W_", 0) == 0 || k.rfind("GLOBAL_T_", 0) == 0 ||
                k.rfind("GLOBAL_S_", 0) == 0) {
@@ -168,7 +172,16 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     err = "inputs not supported by this build: " + others[0] + " (extra Y/W/T/S matrices or preset allele frequencies)";
     return 4;
   }
-  if (Y_n_cols > 0 || T_n_cols > 1) { err = "Y_n_cols > 0 or T_n_cols > 1 is not supported by this build"; return 4; }
+  if (Y_n_cols > 0) { err = "Y_n_cols > 0 is not supported by this build"; return 4; }
+  auto any_named = [](const std::vector<std::string> &l) {
+    for (auto &x : l) if (!x.empty()) return true;
+    return false;
+  };
+  // Covariates: every bin names its T_t and S_t files, or none does (the
+  // reference's default for an absent S file with several covariate columns
+  // reads past its one-row buffer).
+  const bool has_T = any_named(T_t), has_S = any_named(S_t);
+  if (has_T != has_S) { err = "T_t and S_t covariate files must be given together"; return 4; }
   if (P.dir_name.empty() && !out_name.empty()) {
     std::string base = dir_base;
     if (base.empty()) base = ".";
@@ -213,6 +226,46 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     }
   }
   I.ncols = ncols;
+  I.T_ncols = 1;
+  if (has_T) {
+    // T_t: one chunk per case row holding its T_ncols covariate bits (the
+    // layout of the A_t files); S_t the same for the control rows.
+    int tc = -1;
+    for (int nb = 0; nb < nbins; ++nb) {
+      BinInput &B = I.bins[nb];
+      if (nb >= (int)T_t.size() || nb >= (int)S_t.size() || T_t[nb].empty() || S_t[nb].empty()) {
+        err = "every bin needs T_t and S_t covariate files";
+        return 4;
+      }
+      B16 t, u;
+      if (int rc = read_b16(T_t[nb], t, false, err)) return rc;
+      if (int rc = read_b16(S_t[nb], u, false, err)) return rc;
+      if (tc < 0) tc = t.nrows;
+      if (t.nrows != tc || u.nrows != tc || t.ncols != B.A_nrows || u.ncols != B.Z_nrows) {
+        err = "covariate files " + T_t[nb] + " / " + S_t[nb] + " do not match their bin";
+        return 2;
+      }
+      const long tb = bsize(tc);
+      B.T_rows.assign((size_t)std::max(1, B.A_nrows) * (size_t)tb, 0);
+      for (int r = 0; r < B.A_nrows; ++r) memcpy(&B.T_rows[(size_t)r * tb], &t.data[(size_t)r * t.chunk()], (size_t)t.chunk());
+      B.S_rows.assign((size_t)std::max(1, B.Z_nrows) * (size_t)tb, 0);
+      for (int r = 0; r < B.Z_nrows; ++r) memcpy(&B.S_rows[(size_t)r * tb], &u.data[(size_t)r * u.chunk()], (size_t)u.chunk());
+    }
+    I.T_ncols = tc;
+    if (T_n_cols != tc) { err = "GLOBAL_T_n_cols does not match the covariate files"; return 2; }
+  } else if (T_n_cols != 1) {
+    err = "GLOBAL_T_n_cols > 1 needs T_t and S_t covariate files";
+    return 4;
+  }
+  if (!T_cind.empty()) {
+    // a covariate mask is accepted when it retains every column (the
+    // restatement keeps every covariate column)
+    B16 m;
+    if (int rc = read_b16(T_cind, m, false, err)) return rc;
+    if (m.nrows < I.T_ncols) { err = "covariate mask " + T_cind + " is shorter than T_ncols"; return 2; }
+    for (int c = 0; c < I.T_ncols; ++c)
+      if (!((m.data[c / 8] >> (7 - c % 8)) & 1)) { err = "a covariate mask that drops columns is not supported"; return 4; }
+  }
   if (A_ncols_decl >= 0 && A_ncols_decl != ncols) { err = "GLOBAL_A_n_cols does not match the A_t files"; return 2; }
   if (!A_cind.empty()) {
     B16 m;

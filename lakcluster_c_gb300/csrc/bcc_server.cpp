@@ -52,12 +52,15 @@ struct OwnedProblem {
       store.emplace_back(ptr, ptr + n);
       return store.back().data();
     };
-    store.reserve((size_t)src.nbins * 4 + 1);
+    store.reserve((size_t)src.nbins * 6 + 1);
     for (auto &b : bins) {
       b.A_rows = keep(b.A_rows, (size_t)b.A_nrows * rb);
       b.Z_rows = keep(b.Z_rows, (size_t)b.Z_nrows * rb);
       b.A_mr_b = keep(b.A_mr_b, (size_t)(b.A_nrows + 15) / 16 * 2);
       b.Z_mr_b = keep(b.Z_mr_b, (size_t)(b.Z_nrows + 15) / 16 * 2);
+      const size_t tch = (size_t)((src.T_ncols > 0 ? src.T_ncols : 1) + 15) / 16 * 2;
+      b.T_rows = keep(b.T_rows, (size_t)b.A_nrows * tch);
+      b.S_rows = keep(b.S_rows, (size_t)b.Z_nrows * tch);
     }
     p.mc_b = keep(src.mc_b, (size_t)(src.ncols + 15) / 16 * 2);
     p.bins = bins.data();

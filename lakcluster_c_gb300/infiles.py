@@ -48,12 +48,15 @@ def read_b16(path: str) -> np.ndarray:
 
 def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.05, B_MLT=32,
                      A_row_masks=None, Z_row_masks=None, col_mask=None, gamma_type=None, Ireq=None,
-                     name="bcc.in") -> str:
+                     T_bins=None, S_bins=None, kappa_squared=None, name="bcc.in") -> str:
     """Write the .b16 files of one bcc problem and the .in file that names them.
 
     A_bins / Z_bins: per-bin 0/1 arrays (rows x SNPs).  Masks (0/1 vectors) are
-    optional; absent masks mean every row / column is used.  Returns the path
-    of the .in file.  Outputs of a solve go to ``out_dir``.
+    optional; absent masks mean every row / column is used.  T_bins / S_bins:
+    per-bin 0/1 covariate arrays (case rows x T_ncols, control rows x
+    T_ncols), written as T_t / T_n and S_t / S_n files like A; absent means
+    the reference's single column of ones.  Returns the path of the .in file.
+    Outputs of a solve go to ``out_dir``.
     """
     os.makedirs(in_dir, exist_ok=True)
     nbins = len(A_bins)
@@ -72,6 +75,16 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
             write_b16(os.path.join(in_dir, "Z_%02d_n.b16" % nb), Z.T)
             mz = np.ones(Z.shape[0], np.uint8) if Z_row_masks is None else np.asarray(Z_row_masks[nb], np.uint8)
             write_b16(os.path.join(in_dir, "mr_Z_%02d.b16" % nb), mz[None, :])
+    T_ncols = 1
+    if T_bins is not None:
+        T_ncols = np.asarray(T_bins[0]).shape[1]
+        for nb in range(nbins):
+            T = np.asarray(T_bins[nb], np.uint8)
+            S = np.asarray(S_bins[nb], np.uint8)
+            write_b16(os.path.join(in_dir, "T_%02d_t.b16" % nb), T)
+            write_b16(os.path.join(in_dir, "T_%02d_n.b16" % nb), T.T)
+            write_b16(os.path.join(in_dir, "S_%02d_t.b16" % nb), S)
+            write_b16(os.path.join(in_dir, "S_%02d_n.b16" % nb), S.T)
     mc = np.ones(ncols, np.uint8) if col_mask is None else np.asarray(col_mask, np.uint8)
     write_b16(os.path.join(in_dir, "mc_A.b16"), mc[None, :])
 
@@ -93,6 +106,8 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
         lines.append("GLOBAL_gamma_type= %d;" % gamma_type)
     if Ireq is not None:
         lines.append("GLOBAL_Ireq= %d;" % Ireq)
+    if kappa_squared is not None:
+        lines.append("GLOBAL_kappa_squared= %0.6f;" % kappa_squared)
     lines += [
         "GLOBAL_DIR_XPRE= %s;" % os.path.abspath(in_dir),
         "GLOBAL_A_n_name_= %s;" % lst("A_%02d_n.b16"),
@@ -109,9 +124,16 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
             "GLOBAL_Z_n_rows_= %s;" % ",".join(str(np.asarray(z).shape[0]) for z in Z_bins),
             "GLOBAL_Z_n_rind_= %s;" % lst("mr_Z_%02d.b16"),
         ]
+    if T_bins is not None:
+        lines += [
+            "GLOBAL_T_t_name_= %s;" % lst("T_%02d_t.b16"),
+            "GLOBAL_T_n_name_= %s;" % lst("T_%02d_n.b16"),
+            "GLOBAL_S_t_name_= %s;" % lst("S_%02d_t.b16"),
+            "GLOBAL_S_n_name_= %s;" % lst("S_%02d_n.b16"),
+        ]
     lines += [
         "GLOBAL_Y_n_cols= 0;",
-        "GLOBAL_T_n_cols= 1;",
+        "GLOBAL_T_n_cols= %d;" % T_ncols,
         "GLOBAL_DIR_NAME= %s;" % os.path.abspath(out_dir),
         "END= 0;",
     ]

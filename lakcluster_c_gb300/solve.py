@@ -18,14 +18,15 @@ from ._lib import load
 
 class BccBin(C.Structure):
     _fields_ = [("A_nrows", C.c_int), ("A_rows", C.c_void_p), ("A_mr_b", C.c_void_p),
-                ("Z_nrows", C.c_int), ("Z_rows", C.c_void_p), ("Z_mr_b", C.c_void_p)]
+                ("Z_nrows", C.c_int), ("Z_rows", C.c_void_p), ("Z_mr_b", C.c_void_p),
+                ("T_rows", C.c_void_p), ("S_rows", C.c_void_p)]
 
 
 class BccProblem(C.Structure):
     _fields_ = [("ncols", C.c_int), ("row_bytes", C.c_longlong), ("mc_b", C.c_void_p),
                 ("nbins", C.c_int), ("bins", C.POINTER(BccBin)),
                 ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int),
-                ("Ireq", C.c_int)]
+                ("Ireq", C.c_int), ("T_ncols", C.c_int), ("kappa_squared", C.c_double)]
 
 
 class BccResult(C.Structure):
@@ -60,7 +61,8 @@ class Problem:
     rows already packed as pack_rows packs them (``packed_ncols`` SNPs)."""
 
     def __init__(self, A_bins, Z_bins=None, *, gamma=0.125, B_MLT=32, gamma_type=0, A_masks=None,
-                 Z_masks=None, col_mask=None, test_sparse=1, Ireq=0, lib=None, packed_ncols=None):
+                 Z_masks=None, col_mask=None, test_sparse=1, Ireq=0, T_bins=None, S_bins=None,
+                 kappa_squared=0.0, lib=None, packed_ncols=None):
         self.lib = bind(lib or load())
         self._keep = []
         nb = len(A_bins)
@@ -82,8 +84,17 @@ class Problem:
                 self.bins[b].Z_rows = self._hold(pk(z)).ctypes.data
                 if Z_masks is not None:
                     self.bins[b].Z_mr_b = self._hold(pack_rows(Z_masks[b])).ctypes.data
+        # covariates: per-bin 0/1 arrays (case rows x T_ncols, control rows x T_ncols)
+        T_ncols = 1
+        if T_bins is not None:
+            T_ncols = np.asarray(T_bins[0]).shape[1]
+            for b in range(nb):
+                self.bins[b].T_rows = self._hold(pack_rows(T_bins[b])).ctypes.data
+                self.bins[b].S_rows = self._hold(pack_rows(S_bins[b])).ctypes.data
         self.prob = BccProblem()
         self.lib.lakgb_bcc_problem_init(C.byref(self.prob))
+        self.prob.T_ncols = T_ncols
+        self.prob.kappa_squared = kappa_squared
         self.prob.ncols = ncols
         self.prob.row_bytes = (ncols + (16 - ncols % 16) % 16) // 8
         if col_mask is not None:

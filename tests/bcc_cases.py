@@ -36,6 +36,21 @@ def _case_only(n, m, k, seed):
     return dict(A=inst.A_bins, Z=None, gamma=0.05)
 
 
+def _covariates(d, T_ncols, seed, kappa_squared):
+    """Covariate columns for every bin: column 0 all ones (the reference's
+    default covariate), the others Bernoulli(0.5) per row."""
+    rng = np.random.default_rng(seed)
+
+    def cols(n):
+        c = (rng.random((n, T_ncols)) < 0.5).astype(np.uint8)
+        c[:, 0] = 1
+        return c
+    d["T"] = [cols(a.shape[0]) for a in d["A"]]
+    d["S"] = [cols(z.shape[0]) for z in d["Z"]]
+    d["kappa_squared"] = kappa_squared
+    return d
+
+
 def _case_control(nA, nZ, m, kr, kc, nbins, seed, gamma=0.05, gamma_type=None, Ireq=None):
     inst = synth.case_control(nA, nZ, m, kr, kc, 0.05, nbins=nbins, seed=seed)
     d = dict(A=inst.A_bins, Z=inst.Z_bins, gamma=gamma)
@@ -58,6 +73,13 @@ CASES = {
     "case_control_3bin_Ireq1": (lambda: _case_control(300, 280, 2100, 24, 40, 3, 17, Ireq=1), True),
     "case_control_3bin_Ireq2": (lambda: _case_control(330, 290, 1950, 24, 40, 3, 19, Ireq=2), True),
     "case_control_2bin_Ireq2": (lambda: _case_control(260, 240, 2300, 22, 44, 2, 23, Ireq=2), True),
+    # covariate columns (T_n_cols > 1): products per covariate, and the MDS
+    # correction of bcc_sumscores_ifT when GLOBAL_kappa_squared > 0
+    "case_control_2bin_T3": (lambda: _covariates(_case_control(270, 250, 2000, 22, 40, 2, 29), 3, 31, None), True),
+    "case_control_2bin_T3_kappa": (lambda: _covariates(_case_control(270, 250, 2000, 22, 40, 2, 29), 3, 31, 0.3),
+                                   True),
+    "case_control_3bin_T2_kappa_Ireq1": (
+        lambda: dict(_covariates(_case_control(320, 300, 1940, 24, 40, 3, 37), 2, 41, 0.5), Ireq=1), True),
 }
 # Cases whose reference solve takes minutes even on every host thread (the
 # 4096 + 4096 x 16384 two-bin workload: 518 s on 8 cores): their golden
@@ -69,7 +91,8 @@ LARGE_CASES = {
 }
 SMALL = ["case_only_200x300", "case_control_2bin_300x250x2100", "case_control_2bin_masked",
          "case_control_1bin_gamma_lin", "case_control_3bin_ragged", "case_control_3bin_Ireq1",
-         "case_control_3bin_Ireq2", "case_control_2bin_Ireq2"]
+         "case_control_3bin_Ireq2", "case_control_2bin_Ireq2", "case_control_2bin_T3", "case_control_2bin_T3_kappa",
+         "case_control_3bin_T2_kappa_Ireq1"]
 
 
 def build(name):
@@ -81,6 +104,7 @@ def write_case(name, in_dir, out_dir, fname="bcc.in"):
     return infiles.write_bcc_inputs(in_dir, out_dir, d["A"], d.get("Z"), gamma=d["gamma"], B_MLT=32,
                                     A_row_masks=d.get("A_masks"), Z_row_masks=d.get("Z_masks"),
                                     col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), Ireq=d.get("Ireq"),
+                                    T_bins=d.get("T"), S_bins=d.get("S"), kappa_squared=d.get("kappa_squared"),
                                     name=fname)
 
 
@@ -160,5 +184,6 @@ def solve_arrays(lib, d):
     from lakcluster_c_gb300 import solve as sv
     p = sv.Problem(d["A"], d.get("Z"), gamma=d["gamma"], gamma_type=d.get("gamma_type") or 0,
                    A_masks=d.get("A_masks"), Z_masks=d.get("Z_masks"), col_mask=d.get("col_mask"),
-                   Ireq=d.get("Ireq") or 0, lib=lib)
+                   Ireq=d.get("Ireq") or 0, T_bins=d.get("T"), S_bins=d.get("S"),
+                   kappa_squared=d.get("kappa_squared") or 0.0, lib=lib)
     return p.solve()

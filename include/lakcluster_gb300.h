@@ -240,6 +240,7 @@ struct lakgb_bcc_problem {
   int T_ncols;       /* covariate columns of the bins' T_rows / S_rows (GLOBAL_T_n_cols) */
   double kappa_squared;  /* GLOBAL_kappa_squared: > 0 turns on the MDS correction
                             of the covariate columns (bcc_sumscores_ifT) */
+  const char *QC_strategy;  /* GLOBAL_QC_strategy: "YnWt" (NULL), "ZtSWn", or both */
 };
 /* trace: 6 values per iteration (iteration, rows left, columns left, mean row
  * score, mean column score, bins with rows); xdrop_a / xdrop_b: 2 ints per

@@ -84,6 +84,8 @@ struct Single {
   L_handle *lf_et_Tn, *lf_et_Sn, *lf_et_An, *lf_a1d1_At_en, *lf_a1d2_At_en, *lf_a3d2_At_en;
   L_handle *lf_et_An_a1d1, *lf_Tt_An_a1d1, *lf_T_AnAt_AnAt;
   L_handle *lf_An_a1d1 = nullptr, *lf_At_An_a1d1 = nullptr, *lf_a2d2_ZtSn = nullptr, *lf_a2d2_AtTn = nullptr;
+  // SNP x SNP x covariate products of the ZtSWn column strategy
+  L_handle *lf_AtTAn = nullptr, *lf_ZtSZn = nullptr, *lf_ktrkn = nullptr;
   std::vector<double> QR_AnZtSZnAt_nrm, QR_AnAtTAnAt_nrm;
   std::vector<int> QR_index_global_mr_a, QR_index_global_mr_b, QR_index_global_mr_j;
 };
@@ -101,6 +103,7 @@ struct Double {
   L_handle *lf_attjn____vtszn, *lf_attjn____jttan, *lf_attjn____htrkn, *lf_ktrhn____jttan, *lf_ktrhn____htrkn;
   L_handle *lf_AnZt_S_ZnAt, *lf_AnAt_T_AnAt;
   L_handle *lf_At_T_AnZt_S_Zn, *lf_At_T_AnAt_T_An;
+  L_handle *lf_AtTAn____ZtSZn = nullptr, *lf_AtTAn____AtTAn = nullptr;  // ZtSWn column strategy
   L_handle *lf_An_a2d2_Zt_Sn, *lf_An_a2d2_At_Tn;
   L_handle *QR_AnZtSZnAt, *QR_AnAtTAnAt, *QC_AtTAnZtSZn, *QC_AtTAnAtTAn;
 };
@@ -179,7 +182,7 @@ struct State {
       for (L_handle *L : {E->lf_An_ajdk, E->lf_Zn_ajdk, E->lf_AtTn, E->lf_ZtSn, E->lf_jn_ajdk, E->lf_vn_ajdk,
                           E->lf_kn_ajdk, E->lf_zn_ajdk, E->lf_hn_ajdk, E->lf_an_ajdk, E->lf_attn, E->lf_jttn,
                           E->lf_ktrn, E->lf_htrn, E->lf_ztsn, E->lf_vtsn, E->lf_ztsvn, E->lf_attjn, E->lf_ktrhn,
-                          E->lf_At_An_a1d1})
+                          E->lf_At_An_a1d1, E->lf_AtTAn, E->lf_ZtSZn, E->lf_ktrkn})
         release(L);
       for (auto *v : {&E->An_w, &E->At_w, &E->Zn_w, &E->Zt_w, &E->Tn_w, &E->Tt_w, &E->Sn_w, &E->St_w}) forget(*v);
     }
@@ -537,6 +540,7 @@ int load(State &S, const Input &I, std::string &err) {
       const unsigned long long NT = (unsigned long long)E1->M_An->h.nrows * S.T_ncols;
       F->lf_AnZt_S_ZnAt = S.L(NT); F->lf_AnAt_T_AnAt = S.L(NT);
       F->lf_At_T_AnZt_S_Zn = S.L(AT); F->lf_At_T_AnAt_T_An = S.L(AT);
+      F->lf_AtTAn____ZtSZn = S.L(AT); F->lf_AtTAn____AtTAn = S.L(AT);
       F->lf_An_a2d2_Zt_Sn = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
       F->lf_An_a2d2_At_Tn = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
       F->QR_AnZtSZnAt = S.L((unsigned long long)E1->A_nrows * S.T_ncols);
@@ -738,6 +742,68 @@ void lf_At_T_YnWt_S_Zn_all(State &S) {  // bcc_lf_At_T_YnWt_S_Zn (bcc_lf.c:649-7
       if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
         lh_duplicate(S.f(nb1, nb2)->lf_At_T_AnAt_T_An, S.f(nb2, nb1)->lf_At_T_AnAt_T_An);
     }
+}
+
+// The column strategies in use (GLOBAL_QC_strategy): YnWt (the bit-plane loop
+// product of the quantised Grams) and / or ZtSWn (SNP x SNP products); when
+// both are named the column scores come from ZtSWn (bcc_flattenloop.c:1458-1463).
+bool qc_ynwt(const State &S) { return S.P.QC_strategy.find("YnWt") != std::string::npos; }
+bool qc_ztswn(const State &S) { return S.P.QC_strategy.find("ZtSWn") != std::string::npos; }
+
+void lf_ZtSWn_all(State &S) {  // bcc_lf_ZtSWn (bcc_lf.c:105-153), the terms without Y/W blocks
+  if (!qc_ztswn(S)) return;
+  double *aj = S.A_ajdk.data();
+  for (auto &E : S.E) {
+    if (E->Z_rbother && S.A_cbother)
+      wrap_AtTAn_vv__run(TARGS, SP_b, SP_b, SP_b, E->M_Zt->p(), E->M_St->p(), E->M_Zt->p(), aj, aj, E->lf_ZtSn,
+                         E->lf_ZtSn, &E->lf_ZtSZn);
+    if (E->A_rbother && S.A_cbother)
+      wrap_AtTAn_vv__run(TARGS, SP_b, SP_b, SP_b, E->M_At->p(), E->M_Tt->p(), E->M_At->p(), aj, aj, E->lf_AtTn,
+                         E->lf_AtTn, &E->lf_AtTAn);
+  }
+}
+
+void lf_AtTYn____WtSZn_all(State &S) {  // bcc_lf_AtTYn____WtSZn (bcc_lf.c:566-632)
+  if (!qc_ztswn(S)) return;
+  double *aj = S.A_ajdk.data();
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_At->p(), E1->M_Tt->p(), E1->M_At->p(), E2->M_Zt->p(),
+                                    E2->M_St->p(), E2->M_Zt->p(), aj, E1->lf_AtTAn, E2->lf_ZtSZn,
+                                    &F->lf_AtTAn____ZtSZn);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 <= nb2)
+        wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_At->p(), E1->M_Tt->p(), E1->M_At->p(), E2->M_At->p(),
+                                    E2->M_Tt->p(), E2->M_At->p(), aj, E1->lf_AtTAn, E2->lf_AtTAn,
+                                    &F->lf_AtTAn____AtTAn);
+    }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 > nb2)
+        lh_duplicate(S.f(nb1, nb2)->lf_AtTAn____AtTAn, S.f(nb2, nb1)->lf_AtTAn____AtTAn);
+    }
+}
+
+// bcc_lrup_QC_ZtSWn_stage_0/1/2 (bcc_lrup.c:896-1006): the case rows just
+// removed leave lf_AtTAn through a low-rank product of theirs, subtracted
+// element by element (the control products never change: controls are not
+// eliminated).
+void lrup_QC_ZtSWn(State &S) {
+  if (!qc_ztswn(S)) return;
+  double *aj = S.A_ajdk.data();
+  for (auto &E : S.E)
+    if (E->A_rbother && S.A_cbother)
+      wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_kt->p(), E->M_rt->p(), nullptr, nullptr, nullptr, &E->lf_ktrn);
+  for (auto &E : S.E)
+    if (E->A_rbother && S.A_cbother)
+      wrap_AtTAn_vv__run(TARGS, SP_b, SP_b, SP_b, E->M_kt->p(), E->M_rt->p(), E->M_kt->p(), aj, aj, E->lf_ktrn,
+                         E->lf_ktrn, &E->lf_ktrkn);
+  for (auto &E : S.E)
+    if (E->A_rbother && S.A_cbother)
+      for (unsigned long long i = 0; i < E->lf_AtTAn->length; ++i) E->lf_AtTAn->lf[i] -= E->lf_ktrkn->lf[i];
 }
 
 void lf_AnZt_S_WnYt_all(State &S) {  // bcc_lf_AnZt_S_WnYt (bcc_lf.c:360-410)
@@ -980,6 +1046,10 @@ void flattenloop_pair(State &S, Double *F) {
   const int QR_AnZtSZnAt = E1->A_rbother && S.A_cbother && E2->Z_rbother;
   const int QR_AnAtTAnAt = E1->A_rbother && S.A_cbother && E2->A_rbother;
   const int QC_AtTAnZtSZn = QR_AnZtSZnAt, QC_AtTAnAtTAn = QR_AnAtTAnAt;
+  // the column loop products: ZtSWn's when that strategy is named
+  // (use_AtTXn____XtXXn_flag, bcc_flattenloop.c:1463), else the bit-plane ones
+  L_handle *qc_zs = qc_ztswn(S) ? F->lf_AtTAn____ZtSZn : F->lf_At_T_AnZt_S_Zn;
+  L_handle *qc_at = qc_ztswn(S) ? F->lf_AtTAn____AtTAn : F->lf_At_T_AnAt_T_An;
   for (L_handle *L : {F->QR_AnZtSZnAt, F->QR_AnAtTAnAt}) {
     L->row_stride = A_nrows1; L->spacing_row = SP_a; L->col_stride = T; L->spacing_col = SP_b; lh_zero(L);
   }
@@ -1070,8 +1140,8 @@ void flattenloop_pair(State &S, Double *F) {
       for (int na_j = 0; na_j < At1->rpop_j; ++na_j) {
         const unsigned na_a = At1->m_a_[na_j], na_b = At1->m_b_[na_j];
         const double D = aj[na_a / POPLENGTH + AJDK_0_1 * P];
-        if (QC_AtTAnZtSZn) *L2_get(F->QC_AtTAnZtSZn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = D * (*L2_get(F->lf_At_T_AnZt_S_Zn, na_j, na_b, na_a, ns_j, ns_b, ns_a));
-        if (QC_AtTAnAtTAn) *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = D * (*L2_get(F->lf_At_T_AnAt_T_An, na_j, na_b, na_a, ns_j, ns_b, ns_a));
+        if (QC_AtTAnZtSZn) *L2_get(F->QC_AtTAnZtSZn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = D * (*L2_get(qc_zs, na_j, na_b, na_a, ns_j, ns_b, ns_a));
+        if (QC_AtTAnAtTAn) *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = D * (*L2_get(qc_at, na_j, na_b, na_a, ns_j, ns_b, ns_a));
       }
     }
     for (int ns_j = 0; ns_j < Tt2->rpop_j; ++ns_j) {
@@ -1834,12 +1904,14 @@ void trace_stage(State &S, const char *stage) {
   fflush(f);
 }
 
-void initial_subscores(State &S) {
+void initial_subscores(State &S) {  // lakcluster_driver.c:70-100
   An_ajdk_all(S); trace_stage(S, "An_ajdk");
   lf_ZtSn_all(S); trace_stage(S, "lf_ZtSn");
+  lf_ZtSWn_all(S); trace_stage(S, "lf_ZtSWn");
   lf_YnWt_all(S); trace_stage(S, "lf_YnWt");
-  M_YnWt_all(S); trace_stage(S, "M_YnWt");
-  lf_At_T_YnWt_S_Zn_all(S); trace_stage(S, "lf_At_T_YnWt_S_Zn");
+  if (qc_ynwt(S)) { M_YnWt_all(S); trace_stage(S, "M_YnWt"); }
+  lf_AtTYn____WtSZn_all(S); trace_stage(S, "lf_AtTYn____WtSZn");
+  if (qc_ynwt(S)) { lf_At_T_YnWt_S_Zn_all(S); trace_stage(S, "lf_At_T_YnWt_S_Zn"); }
   lf_AnZt_S_WnYt_all(S); trace_stage(S, "lf_AnZt_S_WnYt");
   singlestudy_ww(S); trace_stage(S, "singlestudy");
   doublestudy_ww(S); trace_stage(S, "doublestudy");
@@ -1867,10 +1939,11 @@ void set_stop_check(StopCheck fn, void *ctx) {
 }
 
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks) {
-  if (P.QR_strategy.find("YnWt") == std::string::npos || P.QC_strategy.find("YnWt") == std::string::npos ||
-      P.QR_strategy.find("condense") != std::string::npos || P.QC_strategy.find("store one") != std::string::npos ||
-      P.QR_strategy.find("ZtSWn") != std::string::npos || P.QC_strategy.find("ZtSWn") != std::string::npos) {
-    err = "only the YnWt row and column strategies are supported by this build";
+  if (P.QR_strategy.find("YnWt") == std::string::npos || P.QR_strategy.find("condense") != std::string::npos ||
+      P.QR_strategy.find("ZtSWn") != std::string::npos ||
+      (P.QC_strategy.find("YnWt") == std::string::npos && P.QC_strategy.find("ZtSWn") == std::string::npos) ||
+      P.QC_strategy.find("store one") != std::string::npos) {
+    err = "supported strategies: rows YnWt; columns YnWt and / or ZtSWn (no condense / store one)";
     return 4;
   }
   if (P.B_MLT < 1 || P.B_MLT > 62) { err = "B_MLT out of range"; return 4; }
@@ -1903,12 +1976,14 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     sumscores_mxA(S);
     trace_stage(S, "sumscores");
     lrup_QR(S); trace_stage(S, "lrup_QR");
-    lrup_QC(S); trace_stage(S, "lrup_QC");
+    lrup_QC_ZtSWn(S); trace_stage(S, "lrup_QC_ZtSWn");
+    if (qc_ynwt(S)) { lrup_QC(S); trace_stage(S, "lrup_QC"); }
     lrup_mxdup(S);
     M_mxset_all(S);
     // bcc_M_YnWt here requantises the updated Grams, but nothing on the
     // YnWt path reads those planes before they are rebuilt, so it is skipped.
-    lrup_QC_stage_c(S); trace_stage(S, "lrup_QC_stage_c");
+    lf_AtTYn____WtSZn_all(S); trace_stage(S, "lf_AtTYn____WtSZn");
+    if (qc_ynwt(S)) { lrup_QC_stage_c(S); trace_stage(S, "lrup_QC_stage_c"); }
     lf_AnZt_S_WnYt_all(S); trace_stage(S, "lf_AnZt_S_WnYt");
     An_ajdk_all(S); trace_stage(S, "An_ajdk");
     lf_ZtSn_all(S); trace_stage(S, "lf_ZtSn");

@@ -42,6 +42,7 @@ struct OwnedProblem {
   lakgb_bcc_problem p{};
   std::vector<lakgb_bcc_bin> bins;
   std::vector<std::vector<unsigned char>> store;
+  std::string qc;
 
   explicit OwnedProblem(const lakgb_bcc_problem &src) {
     p = src;
@@ -63,6 +64,10 @@ struct OwnedProblem {
       b.S_rows = keep(b.S_rows, (size_t)b.Z_nrows * tch);
     }
     p.mc_b = keep(src.mc_b, (size_t)(src.ncols + 15) / 16 * 2);
+    if (src.QC_strategy) {
+      qc = src.QC_strategy;
+      p.QC_strategy = qc.c_str();
+    }
     p.bins = bins.data();
   }
 };

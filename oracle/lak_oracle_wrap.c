@@ -89,3 +89,11 @@ int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th, int sa, i
   (void)tidx; (void)vpra; (void)th;
   return lako_AtTYn____WtSZn_vv(sa, ss, M_At, M_Tt, M_Yt, M_Wt, M_St, M_Zt, Y_ajdk, lf_AtTYn, lf_ZtSWn, out);
 }
+
+int wrap_AtTAn_vv__run(int *tidx, void **vpra, pthread_t *th, int sa, int sy, int st, struct M_handle *M_At,
+                       struct M_handle *M_Tt, struct M_handle *M_Yt, double *A_ajdk, double *Y_ajdk,
+                       struct L_handle *lf_AtTn, struct L_handle *lf_YtTn, struct L_handle **out)
+{
+  (void)tidx; (void)vpra; (void)th;
+  return lako_AtTAn_vv(sa, sy, st, M_At, M_Tt, M_Yt, A_ajdk, Y_ajdk, lf_AtTn, lf_YtTn, out);
+}

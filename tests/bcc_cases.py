@@ -80,6 +80,10 @@ CASES = {
                                    True),
     "case_control_3bin_T2_kappa_Ireq1": (
         lambda: dict(_covariates(_case_control(320, 300, 1940, 24, 40, 3, 37), 2, 41, 0.5), Ireq=1), True),
+    # the ZtSWn column strategy: SNP x SNP products instead of the bit-plane product
+    "case_control_2bin_qc_ZtSWn": (lambda: dict(_case_control(280, 240, 1900, 22, 40, 2, 43), qc="ZtSWn"), True),
+    "case_control_2bin_T2_qc_ZtSWn": (
+        lambda: dict(_covariates(_case_control(250, 230, 1700, 20, 36, 2, 47), 2, 53, 0.4), qc="ZtSWn"), True),
 }
 # Cases whose reference solve takes minutes even on every host thread (the
 # 4096 + 4096 x 16384 two-bin workload: 518 s on 8 cores): their golden
@@ -92,7 +96,7 @@ LARGE_CASES = {
 SMALL = ["case_only_200x300", "case_control_2bin_300x250x2100", "case_control_2bin_masked",
          "case_control_1bin_gamma_lin", "case_control_3bin_ragged", "case_control_3bin_Ireq1",
          "case_control_3bin_Ireq2", "case_control_2bin_Ireq2", "case_control_2bin_T3", "case_control_2bin_T3_kappa",
-         "case_control_3bin_T2_kappa_Ireq1"]
+         "case_control_3bin_T2_kappa_Ireq1", "case_control_2bin_qc_ZtSWn", "case_control_2bin_T2_qc_ZtSWn"]
 
 
 def build(name):
@@ -105,7 +109,7 @@ def write_case(name, in_dir, out_dir, fname="bcc.in"):
                                     A_row_masks=d.get("A_masks"), Z_row_masks=d.get("Z_masks"),
                                     col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), Ireq=d.get("Ireq"),
                                     T_bins=d.get("T"), S_bins=d.get("S"), kappa_squared=d.get("kappa_squared"),
-                                    name=fname)
+                                    qc_strategy=d.get("qc", "YnWt"), name=fname)
 
 
 def read_outputs(out_dir):
@@ -185,5 +189,5 @@ def solve_arrays(lib, d):
     p = sv.Problem(d["A"], d.get("Z"), gamma=d["gamma"], gamma_type=d.get("gamma_type") or 0,
                    A_masks=d.get("A_masks"), Z_masks=d.get("Z_masks"), col_mask=d.get("col_mask"),
                    Ireq=d.get("Ireq") or 0, T_bins=d.get("T"), S_bins=d.get("S"),
-                   kappa_squared=d.get("kappa_squared") or 0.0, lib=lib)
+                   kappa_squared=d.get("kappa_squared") or 0.0, qc_strategy=d.get("qc", "YnWt"), lib=lib)
     return p.solve()

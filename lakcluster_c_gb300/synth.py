@@ -131,3 +131,68 @@ def served_request(seed, rows=(512, 16384), cols=(2048, 65536), maf=(0.05, 0.5),
         inst.A_bins.append(np.ascontiguousarray(a))
         inst.Z_bins.append(np.ascontiguousarray(z))
     return inst
+
+
+def _packed_bernoulli_rows(rng, nrows, f, planted=None, chunk=1024):
+    """Rows of Bernoulli(f) bits packed as solve.pack_rows packs them (MSB
+    first, rows padded to 16 bits), drawn `chunk` rows at a time from float32
+    uniforms so that host memory stays at a few chunks whatever the size.
+    `planted` = (row indices, column indices, 0/1 pattern, flip) overwrites
+    those entries of the listed rows with the pattern, each bit flipped with
+    probability flip."""
+    c = f.size
+    rb = (c + 15) // 16 * 2
+    out = np.zeros((nrows, rb), np.uint8)
+    f32 = f.astype(np.float32)[None, :]
+    if planted is not None:
+        prow, pcol, pat, flip = planted
+        in_plant = np.zeros(nrows, bool)
+        in_plant[prow] = True
+    for r0 in range(0, nrows, chunk):
+        r1 = min(nrows, r0 + chunk)
+        bits = (rng.random((r1 - r0, c), dtype=np.float32) < f32).astype(np.uint8)
+        if planted is not None:
+            rows = np.nonzero(in_plant[r0:r1])[0]
+            if rows.size:
+                flips = (rng.random((rows.size, pcol.size)) < flip).astype(np.uint8)
+                bits[np.ix_(rows, pcol)] = pat[None, :] ^ flips
+        pad = rb * 8 - c
+        if pad:
+            bits = np.concatenate([bits, np.zeros((r1 - r0, pad), np.uint8)], axis=1)
+        out[r0:r1] = np.packbits(bits, axis=1, bitorder="big")
+    return out
+
+
+def served_request_packed(seed, rows=(512, 16384), cols=(2048, 65536), maf=(0.05, 0.5), case_fraction=0.5,
+                          max_categories=3, flip=0.05):
+    """A served-stream request drawn like served_request (r ~ logU[rows] rows,
+    case fraction 0.5, c ~ logU[cols] SNPs, MAF U[maf], k ~ U{0..3} covariate
+    categories with NBINS = max(1, k) and rows assigned uniformly, a planted
+    bicluster of r_case/16 rows x c/32 SNPs in the cases), with the rows
+    generated and packed in chunks so that requests at the top of the size
+    range (16384 x 65536) need no unpacked copy.  Returns a BccInstance whose
+    A_bins / Z_bins hold packed rows (solve.Problem's packed_ncols form)."""
+    rng = np.random.default_rng(seed)
+    r = log_uniform_int(rng, *rows)
+    c = log_uniform_int(rng, *cols)
+    k = int(rng.integers(0, max_categories + 1))
+    nb = max(1, k)
+    n_case = max(2, int(round(r * case_fraction)))
+    n_ctrl = max(2, r - n_case)
+    f = maf[0] + (maf[1] - maf[0]) * rng.random(c)
+    kr, kc = max(2, n_case // 16), max(2, c // 32)
+    prow = rng.permutation(n_case)[:kr]
+    pcol = np.sort(rng.permutation(c)[:kc])
+    pat = (rng.random(kc) < 0.5).astype(np.uint8)
+    A = _packed_bernoulli_rows(rng, n_case, f, (prow, pcol, pat, flip))
+    Z = _packed_bernoulli_rows(rng, n_ctrl, f)
+    bA = (rng.random(n_case) * nb).astype(np.int64)
+    bZ = (rng.random(n_ctrl) * nb).astype(np.int64)
+    inst = BccInstance("req_packed_%d" % seed, c, planted_rows=prow, planted_cols=pcol)
+    for b in range(nb):
+        a, z = A[bA == b], Z[bZ == b]
+        if a.shape[0] == 0 or z.shape[0] == 0:   # keep every bin populated
+            a, z = A[:2], Z[:2]
+        inst.A_bins.append(np.ascontiguousarray(a))
+        inst.Z_bins.append(np.ascontiguousarray(z))
+    return inst

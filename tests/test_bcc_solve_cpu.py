@@ -52,6 +52,18 @@ def test_driver_on_reference_kernels_matches_golden(tmp_path, golden, name):
 
 
 @needs_ref
+@pytest.mark.parametrize("name", ["case_only_200x300", "case_control_2bin_masked"])
+def test_stage_digest_golden_is_current(tmp_path, golden, name):
+    """The committed per-stage digests (what the GPU solve's LAKBCC_TRACE is
+    compared with) are those of the current driver on the reference's kernels,
+    so a driver change that adds or reorders a stage shows up here first."""
+    p = bc.write_case(name, str(tmp_path / "in"), str(tmp_path / "out"))
+    tpath = str(tmp_path / "stages.trace")
+    bc.run_refkernels(p, env=dict(os.environ, LAKBCC_TRACE=tpath))
+    assert bc.trace_digest(tpath) == golden[name]["stages"]
+
+
+@needs_ref
 def test_driver_reproduces_reference_program_on_case_control(tmp_path):
     name = "case_control_1bin_gamma_lin"
     p = bc.write_case(name, str(tmp_path / "in"), str(tmp_path / "ref"), "ref.in")

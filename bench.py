@@ -819,38 +819,57 @@ def solve_measurements(args, with_cpu: bool):
 def many_solves_measurements(args):
     """Batched label-shuffled nulls and a served Poisson stream, each against
     the plain one-solve-at-a-time path on the same problems (results must be
-    identical)."""
+    identical).
+
+    Batched nulls: 256 instances with rows logU[1024, 8192] (split case /
+    control by a label permutation) and SNPs logU[4096, 32768], drawn on the
+    GPU; all submitted at once.  The plain path is timed on every 8th instance
+    (32 solves, the same size distribution) and its throughput compared with
+    the batched one; those 32 results must equal their batched results.
+
+    Served stream: 24 requests with rows logU[512, 16384] and SNPs
+    logU[2048, 65536], 0-3 covariate categories, MAF U[0.05, 0.5]; the plain
+    path solves them one at a time; the server takes Poisson arrivals at 2x
+    and 4x the plain throughput and all 24 at once (saturation), reporting
+    solves/s and p50 / p99 latency at each rate."""
     from lakcluster_c_gb300 import serve, solve as sv, synth
     workers = max(2, min(16, os.cpu_count() or 2))
     out = {}
-    # Batched nulls: label-shuffled case/control instances of uneven sizes.
-    n_null = 24
+    n_null, stride = 256, 8
     probs = []
     for i in range(n_null):
-        inst = synth.null_instance(1000 + i, rows=(1024, 8192), cols=(4096, 32768))
-        probs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05))
-    plain, t_plain = serve.solve_plain(probs)
+        inst = synth.null_instance_packed(1000 + i)
+        probs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05, packed_ncols=inst.ncols))
+    sample = probs[::stride]
+    plain, t_plain = serve.solve_plain(sample)
     batched, t_batch, peak = serve.solve_batched(probs, workers=workers)
+    plain_rate, batch_rate = len(sample) / t_plain, n_null / t_batch
     out["batched_nulls"] = {
         "instances": n_null, "rows": "logU[1024,8192]", "cols": "logU[4096,32768]", "workers": workers,
-        "plain_solves_per_s": n_null / t_plain, "batched_solves_per_s": n_null / t_batch,
-        "speedup": t_plain / t_batch, "peak_concurrency": peak, "identical_to_plain": batched == plain}
-    # Served stream: Poisson arrivals at twice the plain path's throughput.
-    n_req = 16
+        "plain_sample": "every %dth instance (%d solves)" % (stride, len(sample)),
+        "plain_solves_per_s": plain_rate, "batched_solves_per_s": batch_rate,
+        "speedup": batch_rate / plain_rate, "peak_concurrency": peak,
+        "identical_to_plain": batched[::stride] == plain}
+    n_req = 24
     reqs = []
     for i in range(n_req):
-        inst = synth.served_request(5000 + i, rows=(512, 4096), cols=(2048, 16384))
-        reqs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05))
+        inst = synth.served_request_packed(5000 + i)
+        reqs.append(sv.Problem(inst.A_bins, inst.Z_bins, gamma=0.05, packed_ncols=inst.ncols))
     solo, t_solo = serve.solve_plain(reqs)
-    rate = 2.0 * n_req / t_solo
-    r1, lat1, wall1, _ = serve.serve_stream(reqs, rate, workers=1, seed=7)
-    rw, latw, wallw, peakw = serve.serve_stream(reqs, rate, workers=workers, seed=7)
-    out["served"] = {
-        "requests": n_req, "rows": "logU[512,4096]", "cols": "logU[2048,16384]", "categories": "U{0..3}",
-        "arrival_rate_per_s": rate, "workers": workers,
-        "plain": dict(serve.latency_stats(lat1), solves_per_s=n_req / wall1),
-        "continuous_batching": dict(serve.latency_stats(latw), solves_per_s=n_req / wallw, peak_concurrency=peakw),
-        "identical_to_solo": (r1 == solo) and (rw == solo)}
+    plain_rate = n_req / t_solo
+    served = {"requests": n_req, "rows": "logU[512,16384]", "cols": "logU[2048,65536]", "categories": "U{0..3}",
+              "workers": workers, "plain_solves_per_s": plain_rate, "rates": []}
+    same = True
+    for mult in (2.0, 4.0, float("inf")):
+        rate = mult * plain_rate
+        r, lat, wall, peak = serve.serve_stream(reqs, rate, workers=workers, seed=7)
+        same = same and r == solo
+        served["rates"].append(dict(serve.latency_stats(lat), arrival_rate_per_s=(rate if mult != float("inf") else
+                                                                                  "all at once"),
+                                    solves_per_s=n_req / wall, speedup=(n_req / wall) / plain_rate,
+                                    peak_concurrency=peak))
+    served["identical_to_solo"] = same
+    out["served"] = served
     return out
 
 

@@ -93,6 +93,10 @@ inline DBuf upload_vec(const std::vector<T> &v) {
 }
 
 inline void copy_back(double *host, const DBuf &dev, unsigned long long length, HostOutputFill *fill = nullptr) {
+  if (profile_calls_on()) {  // time the wait for the producing kernels apart from the copy
+    LAKGB_PROFILE_CALL("(kernel wait)");
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  }
   LAKGB_PROFILE_CALL("(copy back + sync)");
   if (fill) fill->copied = true;
   if (length) LAKGB_CUDA(cudaMemcpyAsync(host, dev.p, length * sizeof(double), cudaMemcpyDeviceToHost, stream()));

@@ -230,7 +230,6 @@ ResidencyScope::~ResidencyScope() {
   t_scope_keys.clear();
 }
 
-namespace {
 bool profile_calls_on() {
   static const bool on = [] {
     const char *e = getenv("LAKGB_PROFILE_CALLS");
@@ -238,6 +237,8 @@ bool profile_calls_on() {
   }();
   return on;
 }
+
+namespace {
 long long now_ns() {
   return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
       .count();

@@ -144,6 +144,9 @@ struct CallTimer {
 };
 #define LAKGB_PROFILE_CALL(name) ::lakgb::CallTimer lakgb_call_timer_(name)
 
+// True when LAKGB_PROFILE_CALLS is set: the call timers above are collecting.
+bool profile_calls_on();
+
 // True while stream s is being captured into a CUDA graph.
 bool capturing(cudaStream_t s);
 

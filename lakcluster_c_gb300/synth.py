@@ -196,3 +196,52 @@ def served_request_packed(seed, rows=(512, 16384), cols=(2048, 65536), maf=(0.05
         inst.A_bins.append(np.ascontiguousarray(a))
         inst.Z_bins.append(np.ascontiguousarray(z))
     return inst
+
+
+def _pack_bits_torch(bits):
+    """(n, c) bool tensor -> (n, rup(c,16)/8) uint8 tensor, MSB first (the
+    layout of solve.pack_rows)."""
+    import torch
+    n, c = bits.shape
+    pad = (16 - c % 16) % 16
+    if pad:
+        bits = torch.cat([bits, torch.zeros((n, pad), dtype=torch.bool, device=bits.device)], dim=1)
+    w = torch.tensor([128, 64, 32, 16, 8, 4, 2, 1], dtype=torch.int32, device=bits.device)
+    return (bits.view(n, -1, 8).to(torch.int32) * w).sum(dim=2).to(torch.uint8)
+
+
+def null_instance_packed(seed, rows=(1024, 8192), cols=(4096, 32768), maf=(0.05, 0.5), flip=0.05,
+                         device="cuda"):
+    """A label-shuffled null instance drawn like null_instance (r ~ logU[rows]
+    pooled rows, c ~ logU[cols] SNPs, MAF U[maf], an r/16 x c/32 bicluster
+    planted in the first half of the pooled rows with the given flip rate,
+    then case/control labels from a random permutation of the pooled rows,
+    one covariate bin), with the Bernoulli draws made on `device` by a torch
+    Philox generator seeded with `seed` and the rows packed there, so that
+    hundreds of instances are drawn in seconds.  Sizes, frequencies, the
+    bicluster and the permutation come from the numpy stream of `seed`.
+    Returns a BccInstance of packed rows (solve.Problem's packed_ncols form)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    r = log_uniform_int(rng, *rows)
+    c = log_uniform_int(rng, *cols)
+    f = maf[0] + (maf[1] - maf[0]) * rng.random(c)
+    kr, kc = max(2, r // 16), max(2, c // 32)
+    rr = rng.permutation(r // 2)[:kr]
+    cc = rng.permutation(c)[:kc]
+    pat = (rng.random(kc) < 0.5).astype(np.uint8)
+    flips = rng.random((kr, kc)) < flip
+    perm = rng.permutation(r)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    fd = torch.from_numpy(f.astype(np.float32)).to(device)
+    X = torch.rand((r, c), generator=g, device=device) < fd[None, :]
+    blk = torch.from_numpy((pat[None, :].astype(bool) ^ flips)).to(device)
+    X[torch.from_numpy(rr).to(device)[:, None], torch.from_numpy(cc).to(device)[None, :]] = blk
+    P = _pack_bits_torch(X[torch.from_numpy(perm).to(device)])
+    del X
+    host = P.cpu().numpy()
+    inst = BccInstance("null_packed_%d" % seed, c, planted_rows=rr, planted_cols=cc)
+    inst.A_bins.append(np.ascontiguousarray(host[: r // 2]))
+    inst.Z_bins.append(np.ascontiguousarray(host[r // 2:]))
+    return inst

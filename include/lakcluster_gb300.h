@@ -207,12 +207,18 @@ int wrap_An_ZtSWn_Yt_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int s
  * Whole solves.
  * ------------------------------------------------------------------------- */
 
-/* Run the bcc solve described by a reference .in file (YnWt row and column
- * strategies, no Y/W/T/S matrices) and write out_trace.txt, out_xdrop_a.txt
- * and out_xdrop_b.txt into its GLOBAL_DIR_NAME, exactly as the reference
- * program does.  Replaces the reference's main -> read_input ->
- * lakcluster_driver path (dir_c/lakcluster_ver18.c:238-330,
- * dir_c/updateglobals.c:188-198, dir_c/lakcluster_driver.c:14-251).
+/* Run the bcc solve described by a reference .in file (YnWt row strategy,
+ * YnWt and / or ZtSWn column strategy, covariate T/S files, no Y/W matrices)
+ * and write out_trace.txt, out_xdrop_a.txt and out_xdrop_b.txt into its
+ * GLOBAL_DIR_NAME, exactly as the reference program does.  Replaces the
+ * reference's main -> read_input -> lakcluster_driver path
+ * (dir_c/lakcluster_ver18.c:238-330, dir_c/updateglobals.c:188-198,
+ * dir_c/lakcluster_driver.c:14-251), including the scrambles named by
+ * GLOBAL_scramble_num / GLOBAL_scramble_out_xdrop_ / GLOBAL_scramble_rseed_
+ * (wrap_bcc_scramble, dir_c/R_init.c:165-290).  With GLOBAL_TEST_TYPE=
+ * lakcluster_scorebox it runs the scorebox instead (lakcluster_scorebox,
+ * dir_c/lakcluster_scorebox.c:103-271) over GLOBAL_scorebox_out_xdrop and
+ * writes its five scorebox_r*n*_c*n*_*.mda arrays (dir_c/S_init.c:79-89).
  * Returns 0 on success; lakgb_bcc_last_error() describes a failure. */
 int lakgb_bcc_run_in_file(const char *in_path);
 

@@ -160,6 +160,17 @@ extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
   int rc = lakbcc::read_in_file(in_path, P, I, g_err);
   if (rc) return rc;
   lakgb_set_d_mlt(P.D_MLT);
+  if (P.test_type == "lakcluster_scorebox") {  // lakcluster_ver18.c:338
+    lakbcc::ScoreboxOutput SO;
+    rc = lakbcc::scorebox(P, I, SO, g_err, &kHooks);
+    if (rc) return rc;
+    if ((rc = pipeline_status())) return rc;
+    if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_scorebox(P.dir_name, SO)) {
+      g_err = "cannot write outputs into " + P.dir_name;
+      return 2;
+    }
+    return 0;
+  }
   lakbcc::Output O;
   rc = lakbcc::solve(P, I, O, g_err, &kHooks);
   if (rc) return rc;

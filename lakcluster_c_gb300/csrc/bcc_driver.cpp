@@ -20,6 +20,7 @@
 
 #include <math.h>
 #include <stdio.h>
+#include <string.h>
 
 #include <algorithm>
 #include <chrono>
@@ -357,11 +358,16 @@ std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows
   return t;
 }
 
-MH *xcalc_out(State &S, int n1a, int n1b, int n2a, int n2b, int *trm) {
+// n1b_cap / n2b_cap (default n1b / n2b): the largest counts the planes must
+// hold, when more rows can be removed in one step than the transposition
+// flag was chosen for.
+MH *xcalc_out(State &S, int n1a, int n1b, int n2a, int n2b, int *trm, int n1b_cap = -1, int n2b_cap = -1) {
   // bcc_double_init_lf_excerpt / M_handle_w_make (bcc.c:992-1003, M_init.c:418-430)
+  if (n1b_cap < 0) n1b_cap = n1b;
+  if (n2b_cap < 0) n2b_cap = n2b;
   int nrows_bZ, ncols_tmp;
-  if (n2b <= n1b) { *trm = 0; nrows_bZ = n1a; ncols_tmp = n2b; }
-  else { *trm = 1; nrows_bZ = n2a; ncols_tmp = n1b; }
+  if (n2b <= n1b) { *trm = 0; nrows_bZ = n1a; ncols_tmp = n2b_cap; }
+  else { *trm = 1; nrows_bZ = n2a; ncols_tmp = n1b_cap; }
   const int ncols_bZ = (1 + S.P.B_MLT) * ncols_tmp;
   return S.keep(mh_make_owned(ncols_bZ, nrows_bZ));
 }
@@ -502,10 +508,35 @@ int load(State &S, const Input &I, std::string &err) {
     E->lf_a2d2_AtTn = S.L((unsigned long long)S.A_cpop_b * S.T_cpop_b);
     E->M_a2d2_AtTn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_ncols));
   }
+  // bcc_single_init_lf (bcc.c:762-792, "store all"): the SNP x SNP x covariate
+  // products of the column low-rank update, sized for ckeep retained x cdrop
+  // removed columns (a scorebox removes up to ceil(col_max / (col_num - 1))
+  // columns per step)
+  if (P.QC_strategy.find("YnWt") != std::string::npos) {
+    int cdrop = 0;
+    get_xdrop(P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, nullptr, &cdrop);
+    if (P.test_type.find("scorebox") != std::string::npos && P.scorebox_col_num > 1 && P.scorebox_col_max > 0)
+      cdrop = (int)ceil((double)P.scorebox_col_max / (double)(P.scorebox_col_num - 1));
+    const unsigned long long ckeep = (unsigned long long)std::max(0, (int)S.A_cpop_j - cdrop);
+    const unsigned long long n = ckeep * (unsigned long long)cdrop * (unsigned long long)S.T_ncols;
+    for (auto &E : S.E) {  // released with the entry points' outputs (~State)
+      E->lf_ztsvn = lh_make(E->Z_rbother ? n : 0);
+      E->lf_attjn = lh_make(E->A_rbother ? n : 0);
+      E->lf_ktrhn = lh_make(E->A_rbother ? n : 0);
+    }
+  }
   // bcc_double_init_lf (bcc.c:1005-1150)
   int rdrop = 0;
   get_xdrop(P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, &rdrop, nullptr);
+  // The transposition flags of the removed-row products follow rdrop2 from
+  // the gamma schedule (bcc.c:1027).  A scorebox removes up to
+  // ceil(row_max / (row_num - 1)) rows per step; the reference sets that
+  // count after rdrop2 (bcc.c:1028), so its buffers do not grow with it and a
+  // larger step writes past them.  Here the buffers hold the larger step.
   const int rdrop2 = std::max(2, rdrop);
+  int rcap = rdrop2;
+  if (P.test_type.find("scorebox") != std::string::npos && P.scorebox_row_num > 1 && P.scorebox_row_max > 0)
+    rcap = std::max(rcap, (int)ceil((double)P.scorebox_row_max / (double)(P.scorebox_row_num - 1)));
   S.F.resize((size_t)S.nbins * S.nbins);
   for (int nb1 = 0; nb1 < S.nbins; ++nb1) {
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
@@ -522,16 +553,17 @@ int load(State &S, const Input &I, std::string &err) {
       F->lf_jnvt = S.L((unsigned long long)A1b * Z2b);
       F->lf_jnjt = S.L((unsigned long long)A1b * A2b);
       const int c = S.A_cbother;
-      int n1b = c * std::min(rdrop2, A1b);
-      F->lf_knzt = S.L((unsigned long long)n1b * (c * Z2b));
-      F->M_knzt = xcalc_out(S, c * A1a, n1b, c * Z2a, c * Z2b, &F->M_knzt_trm);
-      F->lf_hnvt = S.L((unsigned long long)n1b * (c * Z2b));
-      F->M_hnvt = xcalc_out(S, c * A1a, n1b, c * Z2a, c * Z2b, &F->M_hnvt_trm);
-      F->lf_ankt = S.L((unsigned long long)(c * A1b) * (c * std::min(rdrop2, A2b)));
-      F->M_ankt = xcalc_out(S, c * A1a, c * A1b, c * A2a, c * std::min(rdrop2, A2b), &F->M_ankt_trm);
-      F->lf_knat = S.L((unsigned long long)n1b * (c * A2b));
-      F->lf_knkt = S.L((unsigned long long)n1b * (c * std::min(rdrop2, A2b)));
-      F->M_knkt = xcalc_out(S, c * A1a, n1b, c * A2a, c * std::min(rdrop2, A2b), &F->M_knkt_trm);
+      const int n1b = c * std::min(rdrop2, A1b), n1c = c * std::min(rcap, A1b);
+      const int n2k = c * std::min(rdrop2, A2b), n2c = c * std::min(rcap, A2b);
+      F->lf_knzt = S.L((unsigned long long)n1c * (c * Z2b));
+      F->M_knzt = xcalc_out(S, c * A1a, n1b, c * Z2a, c * Z2b, &F->M_knzt_trm, n1c);
+      F->lf_hnvt = S.L((unsigned long long)n1c * (c * Z2b));
+      F->M_hnvt = xcalc_out(S, c * A1a, n1b, c * Z2a, c * Z2b, &F->M_hnvt_trm, n1c);
+      F->lf_ankt = S.L((unsigned long long)(c * A1b) * n2c);
+      F->M_ankt = xcalc_out(S, c * A1a, c * A1b, c * A2a, n2k, &F->M_ankt_trm, -1, n2c);
+      F->lf_knat = S.L((unsigned long long)n1c * (c * A2b));
+      F->lf_knkt = S.L((unsigned long long)n1c * n2c);
+      F->M_knkt = xcalc_out(S, c * A1a, n1b, c * A2a, n2k, &F->M_knkt_trm, n1c, n2c);
       const unsigned long long AT = (unsigned long long)S.A_ncols * S.T_ncols;
       F->lf_kt_r_knzt_s_zn = S.L(AT); F->lf_kt_r_hnvt_s_zn = S.L(AT); F->lf_at_t_ankt_r_kn = S.L(AT);
       F->lf_kt_r_knat_t_an = S.L(AT); F->lf_kt_r_knkt_r_kn = S.L(AT);
@@ -1445,14 +1477,20 @@ void sumscores_cmb(State &S) {  // bcc_sumscores_cmb (bcc_sumscores.c:324-356)
   }
 }
 
-void sumscores_xij(State &S) {  // bcc_sumscores_xij (bcc_sumscores.c:225-322)
+// The bins still holding rows (Irem) and xcc_get_Ireq("empty low")
+// (bcc_sumscores.c:207-223): the Ireq-th highest of the per-bin (per-bin-pair)
+// scores sorted by sumscores_srt, as row / column-pair offsets.
+void get_Ireq(State &S, int &Irow, int &Icol) {
   S.Irem = 0;
   for (auto &E : S.E) S.Irem += (E->A_rpop_j > 0 ? 1 : 0);
-  // xcc_get_Ireq("empty low") (bcc_sumscores.c:207-223): the Ireq-th
-  // highest of the per-bin (per-bin-pair) scores sorted by sumscores_srt
   S.Ireq = std::max(0, std::min(S.nbins, S.P.Ireq));
-  const int Irow = S.Ireq > 0 ? S.nbins - S.Ireq : 0;
-  const int Icol = S.Ireq > 0 ? S.nbins * S.nbins - S.Ireq * S.Ireq : 0;
+  Irow = S.Ireq > 0 ? S.nbins - S.Ireq : 0;
+  Icol = S.Ireq > 0 ? S.nbins * S.nbins - S.Ireq * S.Ireq : 0;
+}
+
+void sumscores_xij(State &S) {  // bcc_sumscores_xij (bcc_sumscores.c:225-322)
+  int Irow = 0, Icol = 0;
+  get_Ireq(S, Irow, Icol);
   if (S.A_cbother && S.A_rpop_b_total) {
     int na_b = 0, na_j = 0;
     for (int na_a = 0; na_a < S.A_ncols; ++na_a) {
@@ -1502,9 +1540,11 @@ double ra_mean(const double *v, unsigned long long n) {  // ra_stats "double" me
   return mean;
 }
 
-void sumscores_mxA(State &S) {  // bcc_sumscores_mxA / mxB / mxC (bcc_sumscores.c:37-205)
-  int rdrop = 0, cdrop = 0;
-  get_xdrop(S.P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, &rdrop, &cdrop);
+// The elimination choice shared by bcc_sumscores_mxA (bcc_sumscores.c:115-160)
+// and bcc_scorebox_mxA (bcc_scorebox.c:5-20): the first cdrop columns of
+// QC_index_local_mc_a and the first rdrop rows of QR_index_local_mr_a /
+// QR_index_local_nb move from the retained to the removed masks.
+void mx_select(State &S, int rdrop, int cdrop) {
   for (int nc = 0; nc < S.A_ncols; ++nc) S.A_umc_j[nc] = (unsigned char)bget_on(S.A_bmc_j.data(), nc);
   for (int nc = 0; nc < S.A_ncols; ++nc) { S.A_umc_j_rtn[nc] = S.A_umc_j[nc]; S.A_umc_j_rmv[nc] = 0; }
   for (int nc = 0; nc < std::min(cdrop, (int)S.A_cpop_j); ++nc) {
@@ -1518,7 +1558,9 @@ void sumscores_mxA(State &S) {  // bcc_sumscores_mxA / mxB / mxC (bcc_sumscores.
     Single *E = S.E[S.QR_index_local_nb[nr]].get();
     E->A_umr_j_rmv[S.QR_index_local_mr_a[nr]] = 1; E->A_umr_j_rtn[S.QR_index_local_mr_a[nr]] = 0;
   }
-  // mxB
+}
+
+void sumscores_mxB(State &S) {  // bcc_sumscores_mxB (bcc_sumscores.c:37-91)
   bits_from_ura(S.A_bmc_j, S.A_umc_j, S.A_ncols);
   bits_from_ura(S.A_bmc_j_rmv, S.A_umc_j_rmv, S.A_ncols);
   bits_from_ura(S.A_bmc_j_rtn, S.A_umc_j_rtn, S.A_ncols);
@@ -1536,6 +1578,13 @@ void sumscores_mxA(State &S) {  // bcc_sumscores_mxA / mxB / mxC (bcc_sumscores.
     E->A_rpop_j_rtn = popcount_bytes(E->A_bmr_j_rtn.data(), E->A_mr_length);
   }
   lrup_mxset(S);
+}
+
+void sumscores_mxA(State &S) {  // bcc_sumscores_mxA / mxB / mxC (bcc_sumscores.c:37-205)
+  int rdrop = 0, cdrop = 0;
+  get_xdrop(S.P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, &rdrop, &cdrop);
+  mx_select(S, rdrop, cdrop);
+  sumscores_mxB(S);
   // mxC: trace
   Output &O = *S.out;
   double m = ra_mean(S.QR_svalue.data(), S.A_rpop_j_total);
@@ -1918,6 +1967,234 @@ void initial_subscores(State &S) {  // lakcluster_driver.c:70-100
   flattenloop(S); trace_stage(S, "flattenloop");
 }
 
+// ---------------------------------------------------------------------------
+// out_xdrop lists (dir_c/bcc_scorebox.c:125-180, dir_c/R_init.c:216-262)
+
+// xcc_out_xdrop_sort: the row indices (first entries >= 0) and the column
+// indices (second entries >= 0) of out_xdrop lines, in line order.
+void xdrop_lists(const std::vector<int> &pairs, std::vector<int> &rows, std::vector<int> &cols) {
+  rows.clear(); cols.clear();
+  for (size_t l = 0; l + 1 < pairs.size(); l += 2) {
+    if (pairs[l] >= 0) rows.push_back(pairs[l]);
+    if (pairs[l + 1] >= 0) cols.push_back(pairs[l + 1]);
+  }
+}
+
+// bcc_out_xdrop_lkp: global row indices (bins concatenated) to (bin, row).
+int xdrop_lookup(const State &S, const std::vector<int> &rows, std::vector<int> &lnb, std::vector<int> &lmr,
+                 std::string &err) {
+  lnb.assign(rows.size(), 0); lmr.assign(rows.size(), 0);
+  for (size_t l = 0; l < rows.size(); ++l) {
+    int r = rows[l], nb = 0;
+    while (nb < S.nbins && r >= S.E[nb]->A_nrows) { r -= S.E[nb]->A_nrows; ++nb; }
+    if (nb >= S.nbins || r < 0) { err = "out_xdrop row index " + std::to_string(rows[l]) + " out of range"; return 2; }
+    lnb[l] = nb; lmr[l] = r;
+  }
+  return 0;
+}
+
+// R01GET (dir_c/boxmuller.c:57-65): seed <- seed*35 mod (2^31-1), drawn as
+// (double)((long double)seed / (long double)(2^31-1)).  The reference runs on
+// x86-64, whose long double has a 64-bit significand, so the quotient is
+// rounded to 64 significant bits and then to 53.  The same two roundings are
+// done here in integer arithmetic, so that every host draws the same doubles.
+// The quotient s/M never terminates in binary (M is an odd prime, 0 < s < M),
+// so the first rounding meets no ties.
+double r01_next(unsigned long long *seed) {
+  const unsigned long long M = 2147483647ULL;
+  *seed = (*seed * 35ULL) % M;
+  const unsigned long long s = *seed;
+  if (s == 0) return 0.0;
+  int k = 0;  // 2^-k <= s/M < 2^(1-k)
+  while (((unsigned __int128)s << k) < M) ++k;
+  const unsigned __int128 q = ((unsigned __int128)s << (k + 64)) / M;  // in [2^64, 2^65)
+  unsigned __int128 m64 = (q + 1) >> 1;                                 // 64-bit significand
+  if (m64 >> 64) { m64 >>= 1; --k; }
+  unsigned long long m = (unsigned long long)m64;
+  const unsigned long long low = m & 0x7FFULL;
+  unsigned long long m53 = m >> 11;
+  if (low > 0x400ULL || (low == 0x400ULL && (m53 & 1ULL))) ++m53;
+  if (m53 >> 53) { m53 >>= 1; --k; }
+  return ldexp((double)m53, -k - 52);
+}
+
+// bcc_scramble (dir_c/R_init.c:165-207) after bcc_out_xdrop_prune /
+// bcc_out_xdrop_lkp (R_init.c:216-262, bcc_scorebox.c:100-123): every case
+// entry in a row and a column listed by out_xdrop (rows and columns each in
+// ascending order, those outside the row / column masks dropped) is redrawn,
+// set when an R01GET draw falls below that column's frequency among the
+// controls (Zt row sums over the control count), in row-major order.  Both
+// the case rows (An) and their transpose (At) are changed.  Where a listed
+// row or column is outside the retained masks the reference's index walk
+// runs past its arrays; here that row / the remaining columns are skipped.
+int scramble(State &S, const Input::Scramble &sc, std::string &err) {
+  for (auto &E : S.E) {
+    memset(E->lf_Zt_rsum->lf, 0, sizeof(double) * E->lf_Zt_rsum->length);
+    wrap_An_v__run(TARGS, LAKGB_TYPE_00, SP_a, E->M_Zt->p(), &E->lf_Zt_rsum);
+  }
+  std::vector<int> rows, cols;
+  xdrop_lists(sc.xdrop, rows, cols);
+  std::sort(rows.begin(), rows.end());
+  std::sort(cols.begin(), cols.end());
+  std::vector<int> keep_c, keep_r;
+  for (int c : cols)
+    if (c >= 0 && c < S.A_ncols && bget_on(S.A_bmc_b.data(), c)) keep_c.push_back(c);
+  for (int r : rows) {
+    if (r < 0 || r >= S.A_nrows_total) continue;
+    int x = r, nb = 0;
+    while (x >= S.E[nb]->A_nrows) { x -= S.E[nb]->A_nrows; ++nb; }
+    if (bget_on(S.E[nb]->A_bmr_b.data(), x)) keep_r.push_back(r);
+  }
+  std::vector<int> lnb, lmr;
+  int rc = xdrop_lookup(S, keep_r, lnb, lmr, err);
+  if (rc) return rc;
+  unsigned long long seed = sc.rseed;
+  std::vector<int> ma_j(S.nbins, 0);
+  int nb = 0;
+  for (size_t mx = 0; mx < keep_r.size(); ++mx) {
+    while (nb < lnb[mx]) ++nb;
+    Single *E = S.E[nb].get();
+    M_handle &An = E->M_An->h, &At = E->M_At->h;
+    while (ma_j[nb] < (int)An.rpop_j && (int)An.m_a_[ma_j[nb]] < lmr[mx]) ++ma_j[nb];
+    if (ma_j[nb] >= (int)An.rpop_j) continue;
+    const unsigned ma_a = An.m_a_[ma_j[nb]], ma_b = An.m_b_[ma_j[nb]];
+    unsigned char *An_tag = An.wX + (size_t)ma_b * An.mc_length;
+    int na_j = 0;
+    const double zr = (double)E->M_Zn->h.rpop_b;
+    for (size_t nx = 0; nx < keep_c.size(); ++nx) {
+      while (na_j < (int)An.cpop_j && (int)An.n_a_[na_j] < keep_c[nx]) ++na_j;
+      if (na_j >= (int)An.cpop_j) break;
+      const unsigned na_a = An.n_a_[na_j], na_b = An.n_b_[na_j];
+      unsigned char *At_tag = At.wX + (size_t)na_b * At.mc_length;
+      const bool on = r01_next(&seed) < E->lf_Zt_rsum->lf[na_a] / zr;
+      if (on) { bset_on(An_tag, na_a); bset_on(At_tag, ma_a); }
+      else { bset_off(An_tag, na_a); bset_off(At_tag, ma_a); }
+    }
+  }
+  // the device copies of the case rows are stale now
+  for (auto &E : S.E) { S.forget(E->An_w); S.forget(E->At_w); }
+  return 0;
+}
+
+// The packed case rows as wrap_bcc_scramble writes them around the scrambles
+// (R_init.c:268-289 with binary_write, binary_read.c:57-81): a header of
+// three ints (16, bits per record, records) and each record's bits rounded
+// up to 16; At_<bin>_scramble_* holds the rows of An, An_<bin>_* those of At.
+void scramble_snapshot(State &S, const char *when) {
+  auto b16 = [](const M_handle &M) {
+    const int bitj = BITJ, nrows = M.ncols, ncols = (int)M.rpop_b;
+    const long wp = (long)(nrows + (bitj - nrows % bitj) % bitj) / 8;
+    std::vector<unsigned char> f(12 + (size_t)wp * ncols);
+    memcpy(&f[0], &bitj, 4); memcpy(&f[4], &nrows, 4); memcpy(&f[8], &ncols, 4);
+    for (int c = 0; c < ncols; ++c) memcpy(&f[12 + (size_t)c * wp], M.wX + (size_t)c * bsize(nrows), wp);
+    return f;
+  };
+  for (auto &E : S.E) {
+    char name[64];
+    snprintf(name, sizeof name, "At_%.2d_scramble_%s.b16", E->nb, when);
+    S.out->files.emplace_back(name, b16(E->M_An->h));
+    snprintf(name, sizeof name, "An_%.2d_scramble_%s.b16", E->nb, when);
+    S.out->files.emplace_back(name, b16(E->M_At->h));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// scorebox (dir_c/lakcluster_scorebox.c, dir_c/bcc_scorebox.c)
+
+// xcc_scorebox_xdrop_array (bcc_scorebox.c:283-308): x_num values from x_max
+// down to 0 and the number of indices removed to reach each.
+void scorebox_xdrop_array(int nxols, int x_max, int x_num, std::vector<int> &xval, std::vector<int> &xdrop) {
+  xval.assign(std::max(0, x_num), 0);
+  xdrop.assign(std::max(0, x_num), 0);
+  if (x_num <= 0) return;
+  const double d = (double)(x_max - 0) / (double)std::max(1, x_num - 1);
+  for (int nx = 0; nx < x_num; ++nx) xval[nx] = (int)round(x_max - nx * d);
+  xdrop[0] = std::max(0, nxols - (x_max + 1));
+  for (int nx = 1; nx < x_num; ++nx) xdrop[nx] = xval[nx - 1] - xval[nx];
+}
+
+struct ScoreboxLists {
+  std::vector<int> rows, cols, lnb, lmr;
+};
+
+// bcc_scorebox_srt (bcc_scorebox.c:82-98): the elimination order of the rows
+// and columns still retained is the tail of the out_xdrop lists.
+void scorebox_srt(State &S, const ScoreboxLists &L) {
+  const int ncols = (int)L.cols.size(), nrows = (int)L.rows.size();
+  if (ncols >= (int)S.A_cpop_j)
+    for (int j = 0; j < (int)S.A_cpop_j; ++j) S.QC_index_local_mc_a[j] = L.cols[ncols - S.A_cpop_j + j];
+  if (nrows >= (int)S.A_rpop_j_total)
+    for (int r = 0; r < (int)S.A_rpop_j_total; ++r) {
+      S.QR_index_local_mr_a[r] = L.lmr[nrows - S.A_rpop_j_total + r];
+      S.QR_index_local_nb[r] = L.lnb[nrows - S.A_rpop_j_total + r];
+    }
+}
+
+void scorebox_mxA(State &S, int rdrop, int cdrop) {  // bcc_scorebox_mxA (bcc_scorebox.c:5-49)
+  mx_select(S, rdrop, cdrop);
+  sumscores_mxB(S);
+}
+
+// bcc_scorebox_svalue (bcc_scorebox.c:51-80): the selection scores of
+// sumscores_xij without the sort.
+void scorebox_svalue(State &S) {
+  int Irow = 0, Icol = 0;
+  get_Ireq(S, Irow, Icol);
+  if (S.A_cbother && S.A_rpop_b_total) {
+    int na_j = 0;
+    for (int na_a = 0; na_a < S.A_ncols; ++na_a)
+      if (bget_on(S.A_bmc_b.data(), na_a) && bget_on(S.A_bmc_j.data(), na_a))
+        S.QC_svalue[na_j++] = S.QC_AtTAnAtTAn_nrm[na_a + 0 * S.A_ncols + (size_t)Icol * S.A_ncols * S.T_ncols];
+  }
+  if (S.A_rpop_b_total && S.A_cbother) {
+    S.A_nrows_total = 0; S.A_rpop_b_total = 0; S.A_rpop_j_total = 0;
+    for (auto &E : S.E) {
+      for (int ma_a = 0; ma_a < E->A_nrows; ++ma_a) {
+        if (bget_on(E->A_bmr_b.data(), ma_a)) {
+          if (bget_on(E->A_bmr_j.data(), ma_a))
+            S.QR_svalue[S.A_rpop_j_total++] = E->QR_AnAtTAnAt_nrm[ma_a + 0 * E->A_nrows + (size_t)Irow * E->A_nrows * S.T_ncols];
+          S.A_rpop_b_total++;
+        }
+        S.A_nrows_total++;
+      }
+    }
+  }
+}
+
+void scorebox_scores(State &S) {  // the scoring tail of lakcluster_scorebox_excerpt_1/2
+  sumscores_nrm(S);
+  sumscores_ifT(S);
+  if (S.P.Ireq > 0) sumscores_srt(S);
+  sumscores_cmb(S);
+  scorebox_svalue(S);
+}
+
+// lakcluster_scorebox_excerpt_1 (lakcluster_scorebox.c:22-52): the loop
+// subscores computed directly.
+void scorebox_full(State &S) {
+  initial_subscores(S);
+  scorebox_scores(S);
+}
+
+// lakcluster_scorebox_excerpt_2 (lakcluster_scorebox.c:54-101): the loop
+// subscores after a removal, by the low-rank update of the elimination loop.
+void scorebox_update(State &S) {
+  lrup_QR(S);
+  lrup_QC_ZtSWn(S);
+  if (qc_ynwt(S)) lrup_QC(S);
+  lrup_mxdup(S);
+  M_mxset_all(S);
+  lf_AtTYn____WtSZn_all(S);
+  if (qc_ynwt(S)) lrup_QC_stage_c(S);
+  lf_AnZt_S_WnYt_all(S);
+  An_ajdk_all(S);
+  lf_ZtSn_all(S);
+  singlestudy_ww(S);
+  doublestudy_ww(S);
+  flattenloop(S);
+  scorebox_scores(S);
+}
+
 }  // namespace
 
 namespace {
@@ -1964,6 +2241,12 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   if (rc) return rc;
   if ((rc = stop_requested(err))) return rc;
   M_mxset_all(S);
+  if (!I.scramble.empty()) {  // wrap_bcc_scramble (R_init.c:264-290), lakcluster_driver.c:58-62
+    scramble_snapshot(S, "pre");
+    for (const auto &sc : I.scramble)
+      if ((rc = scramble(S, sc, err))) return rc;
+    scramble_snapshot(S, "pos");
+  }
   trace_stage(S, "load");
   initial_subscores(S);
   while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
@@ -2005,6 +2288,130 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
   return 0;
 }
 
+// lakcluster_scorebox (lakcluster_scorebox.c:103-271): rows and columns are
+// removed in the order of a previous run's out_xdrop, and the mean row and
+// column scores are recorded on a row_num x col_num grid of retained counts
+// (row_max ... 0 rows and col_max ... 0 columns past the initial removal).
+// The first grid point is computed directly, every other one by one
+// low-rank update from its neighbour: the longer dimension is stepped in the
+// inner loop from a copy of the state reached by the outer one.  The copy
+// (bcc_copy, bcc.c:1440-1480) is made here by replaying the outer steps on
+// a second state loaded from the same inputs, which reaches the same values
+// bit for bit.
+int scorebox(const Params &P, const Input &I, ScoreboxOutput &SO, std::string &err, const Hooks *hooks) {
+  if (P.QR_strategy.find("YnWt") == std::string::npos || P.QR_strategy.find("condense") != std::string::npos ||
+      P.QR_strategy.find("ZtSWn") != std::string::npos ||
+      (P.QC_strategy.find("YnWt") == std::string::npos && P.QC_strategy.find("ZtSWn") == std::string::npos) ||
+      P.QC_strategy.find("store one") != std::string::npos) {
+    err = "supported strategies: rows YnWt; columns YnWt and / or ZtSWn (no condense / store one)";
+    return 4;
+  }
+  const int row_num = std::max(0, P.scorebox_row_num), col_num = std::max(0, P.scorebox_col_num);
+  SO = ScoreboxOutput();
+  SO.row_max = P.scorebox_row_max; SO.row_num = row_num;
+  SO.col_max = P.scorebox_col_max; SO.col_num = col_num;
+  const size_t cells = (size_t)row_num * col_num;
+  SO.A_rpop_j_total.assign(cells, 0); SO.A_cpop_j.assign(cells, 0); SO.Irem.assign(cells, 0);
+  SO.QR_avg.assign(cells, 0.0); SO.QC_avg.assign(cells, 0.0);
+  g_clock = StageClock();
+  Output O_ori, O_sub;
+  auto prepare = [&](State &S, Output &O) -> int {
+    S.P = P; S.hooks = hooks; S.out = &O;
+    const int rc = load(S, I, err);
+    if (rc) return rc;
+    M_mxset_all(S);
+    return 0;
+  };
+  std::unique_ptr<State> D(new State);
+  int rc = prepare(*D, O_ori);
+  if (rc) return rc;
+  ScoreboxLists L;
+  xdrop_lists(I.scorebox_xdrop, L.rows, L.cols);
+  if ((rc = xdrop_lookup(*D, L.rows, L.lnb, L.lmr, err))) return rc;
+  std::vector<int> ckeep, cdrop, rkeep, rdrop;
+  scorebox_xdrop_array((int)D->A_cpop_j, P.scorebox_col_max, col_num, ckeep, cdrop);
+  scorebox_xdrop_array((int)D->A_rpop_j_total, P.scorebox_row_max, row_num, rkeep, rdrop);
+  auto record = [&](State &S, int nr, int nc) {  // lakcluster_scorebox_excerpt_0 (:5-20)
+    const size_t t = (size_t)nr + (size_t)nc * row_num;
+    SO.A_rpop_j_total[t] = (int)S.A_rpop_j_total;
+    SO.A_cpop_j[t] = (int)S.A_cpop_j;
+    SO.Irem[t] = S.Irem;
+    double m = ra_mean(S.QR_svalue.data(), S.A_rpop_j_total);
+    SO.QR_avg[t] = std::isfinite(m) ? m : 1.0;
+    m = ra_mean(S.QC_svalue.data(), S.A_cpop_j);
+    SO.QC_avg[t] = std::isfinite(m) ? m : 1.0;
+  };
+  // rows outer when row_max > col_max is false (lakcluster_scorebox:
+  // _rc steps columns outside, rows inside; _cr the reverse)
+  const bool rows_inner = P.scorebox_row_max > P.scorebox_col_max;
+  const int outer_num = rows_inner ? col_num : row_num, inner_num = rows_inner ? row_num : col_num;
+  auto outer_step = [&](State &S, int k) {
+    scorebox_srt(S, L);
+    if (k == 0) {
+      scorebox_mxA(S, rdrop.empty() ? 0 : rdrop[0], cdrop.empty() ? 0 : cdrop[0]);
+      lrup_mxdup(S);
+      M_mxset_all(S);
+      scorebox_full(S);
+    } else {
+      scorebox_mxA(S, rows_inner ? 0 : rdrop[k], rows_inner ? cdrop[k] : 0);
+      scorebox_update(S);
+    }
+  };
+  if (row_num > 0 && col_num > 0) {
+    for (int k = 0; k < outer_num; ++k) {
+      if ((rc = stop_requested(err))) return rc;
+      outer_step(*D, k);
+      record(*D, rows_inner ? 0 : k, rows_inner ? k : 0);
+      if (inner_num <= 1) continue;
+      std::unique_ptr<State> Sub(new State);
+      if ((rc = prepare(*Sub, O_sub))) return rc;
+      for (int r = 0; r <= k; ++r) outer_step(*Sub, r);
+      for (int j = 1; j < inner_num; ++j) {
+        if ((rc = stop_requested(err))) return rc;
+        scorebox_srt(*Sub, L);
+        scorebox_mxA(*Sub, rows_inner ? rdrop[j] : 0, rows_inner ? 0 : cdrop[j]);
+        scorebox_update(*Sub);
+        record(*Sub, rows_inner ? j : k, rows_inner ? k : j);
+      }
+    }
+  }
+  return 0;
+}
+
+namespace {
+int write_mda_i4(const std::string &path, int nrows, int ncols, const std::vector<int> &v) {
+  FILE *fp = fopen(path.c_str(), "wb");
+  if (!fp) return 1;
+  const int hdr[3] = {2, nrows, ncols};
+  fwrite(hdr, sizeof(int), 3, fp);
+  if (!v.empty()) fwrite(v.data(), sizeof(int), v.size(), fp);
+  return fclose(fp) != 0;
+}
+int write_mda_r8(const std::string &path, int nrows, int ncols, const std::vector<double> &v) {
+  FILE *fp = fopen(path.c_str(), "wb");
+  if (!fp) return 1;
+  const int hdr[3] = {2, nrows, ncols};
+  fwrite(hdr, sizeof(int), 3, fp);
+  if (!v.empty()) fwrite(v.data(), sizeof(double), v.size(), fp);
+  return fclose(fp) != 0;
+}
+}  // namespace
+
+// S_handle_dmp (dir_c/S_init.c:79-89): five row_num x col_num arrays in the
+// mda format of mda_write_d2_i4 / mda_write_d2_r8 (dir_c/mda_io.c:5-31).
+int write_scorebox(const std::string &dir, const ScoreboxOutput &SO) {
+  char prefix[160];
+  snprintf(prefix, sizeof prefix, "%s/scorebox_r%dn%d_c%dn%d", dir.c_str(), SO.row_max, SO.row_num, SO.col_max,
+           SO.col_num);
+  const std::string p = prefix;
+  int rc = write_mda_i4(p + "_A_rpop_j_total.mda", SO.row_num, SO.col_num, SO.A_rpop_j_total);
+  rc |= write_mda_i4(p + "_A_cpop_j.mda", SO.row_num, SO.col_num, SO.A_cpop_j);
+  rc |= write_mda_i4(p + "_Irem.mda", SO.row_num, SO.col_num, SO.Irem);
+  rc |= write_mda_r8(p + "_QR_avg.mda", SO.row_num, SO.col_num, SO.QR_avg);
+  rc |= write_mda_r8(p + "_QC_avg.mda", SO.row_num, SO.col_num, SO.QC_avg);
+  return rc;
+}
+
 int write_outputs(const std::string &dir, const Output &O) {
   std::string p = dir + "/out_trace.txt";
   FILE *fp = fopen(p.c_str(), "w");
@@ -2023,6 +2430,13 @@ int write_outputs(const std::string &dir, const Output &O) {
   }
   fclose(fa);
   fclose(fb);
+  for (const auto &f : O.files) {
+    FILE *fo = fopen((dir + "/" + f.first).c_str(), "wb");
+    if (!fo) return 2;
+    const size_t n = f.second.size();
+    const bool ok = (n == 0 || fwrite(f.second.data(), 1, n, fo) == n);
+    if (fclose(fo) != 0 || !ok) return 2;
+  }
   return 0;
 }
 

@@ -23,6 +23,10 @@ struct Params {
   unsigned recursion_limit = 1024 * 32;
   std::string QR_strategy = "YnWt", QC_strategy = "YnWt";
   std::string dir_name;        // output directory (GLOBAL_DIR_NAME); empty: no files
+  // GLOBAL_TEST_TYPE: lakcluster_driver (the solve) or lakcluster_scorebox
+  std::string test_type = "lakcluster_driver";
+  // scorebox grid (GLOBAL_scorebox_row_max / _row_num / _col_max / _col_num)
+  int scorebox_row_max = 0, scorebox_row_num = 0, scorebox_col_max = 0, scorebox_col_num = 0;
 };
 
 // One bin's inputs: packed rows of A (patients x SNPs, bsize(ncols) bytes per
@@ -38,6 +42,15 @@ struct BinInput {
 };
 
 struct Input {
+  // out_xdrop lines of earlier runs as (row, column) pairs, -1 where absent:
+  // the scorebox order (GLOBAL_scorebox_out_xdrop) and the scrambles applied
+  // after loading (GLOBAL_scramble_out_xdrop_ / GLOBAL_scramble_rseed_)
+  std::vector<int> scorebox_xdrop;
+  struct Scramble {
+    std::vector<int> xdrop;
+    unsigned long long rseed = 1;
+  };
+  std::vector<Scramble> scramble;
   int ncols = 0;
   int T_ncols = 1;                             // covariate columns (GLOBAL_T_n_cols)
   std::vector<unsigned char> mc_b;             // bsize(ncols) bytes; empty = all on
@@ -48,6 +61,10 @@ struct Output {
   std::vector<int> xdrop_a, xdrop_b;          // pairs (row, col)
   std::vector<double> trace;                  // 6 values per iteration
   int iterations = 0;
+  // further files the reference writes into the output directory: the case
+  // rows before and after a scramble (*_scramble_pre.b16 / _pos.b16), as
+  // (file name, contents)
+  std::vector<std::pair<std::string, std::vector<unsigned char>>> files;
 };
 
 // Callbacks into the kernel library that owns the entry points the solve
@@ -72,6 +89,14 @@ struct Hooks {
   void (*L_mirror_zero)(L_handle *L) = nullptr;
 };
 
+// The scorebox grid (S_handle outputs, dir_c/S_init.c): row_num x col_num
+// arrays, row index fastest.
+struct ScoreboxOutput {
+  int row_max = 0, row_num = 0, col_max = 0, col_num = 0;
+  std::vector<int> A_rpop_j_total, A_cpop_j, Irem;
+  std::vector<double> QR_avg, QC_avg;
+};
+
 // Parse a reference .in file (updateglobals.c syntax) and load its .b16 files.
 int read_in_file(const char *path, Params &P, Input &I, std::string &err);
 // Create the output directory when it does not exist (set_globals,
@@ -79,6 +104,10 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err);
 int make_output_dir(const std::string &dir);
 // Run the solve.  Returns 0 on success.
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks = nullptr);
+// Run the scorebox (GLOBAL_TEST_TYPE lakcluster_scorebox) over I.scorebox_xdrop.
+int scorebox(const Params &P, const Input &I, ScoreboxOutput &SO, std::string &err, const Hooks *hooks = nullptr);
+// Write its five .mda arrays into dir (names as S_handle_dmp writes them).
+int write_scorebox(const std::string &dir, const ScoreboxOutput &SO);
 // A check the solves of the calling thread run before the initial pass and
 // before every elimination iteration: a non-zero return ends the solve with
 // that code (its buffers released as on any return) and `why` as the error.

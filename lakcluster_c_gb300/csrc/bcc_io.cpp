@@ -83,6 +83,30 @@ int parse_double(const std::string &v, const std::string &name, double &out, std
   return 0;
 }
 
+// xcc_out_xdrop_load (dir_c/bcc_scorebox.c:182-200): one (row, column) pair
+// per line; the number of lines is the number of newline characters.
+int read_xdrop(const std::string &path, std::vector<int> &pairs, std::string &err) {
+  FILE *fp = fopen(path.c_str(), "rb");
+  if (!fp) { err = "cannot open out_xdrop file " + path; return 2; }
+  std::string text;
+  char buf[65536];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), fp)) > 0) text.append(buf, n);
+  fclose(fp);
+  size_t nlines = 0;
+  for (char c : text) nlines += (c == '\n');
+  pairs.assign(2 * nlines, 0);
+  const char *p = text.c_str();
+  for (size_t i = 0; i < 2 * nlines; ++i) {
+    char *end = nullptr;
+    const long x = strtol(p, &end, 10);
+    if (end == p) { err = "bad out_xdrop line in " + path; return 2; }
+    pairs[i] = (int)x;
+    p = end;
+  }
+  return 0;
+}
+
 }  // namespace
 
 int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
@@ -111,7 +135,9 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
   std::string xpre, test_type, dir_base, out_name;
   int nbins = 0, Y_n_cols = 0, T_n_cols = 1;
   std::vector<std::string> A_t, Z_t, A_rind, Z_rind, T_t, S_t, others;
-  std::string A_cind, T_cind;
+  std::string A_cind, T_cind, scorebox_xdrop;
+  int scramble_num = 0;
+  std::vector<std::string> scramble_xdrop, scramble_rseed;
   std::vector<int> A_rows_decl, Z_rows_decl;
   int A_ncols_decl = -1;
   auto prefixed = [&](const std::string &f) { return xpre.empty() || f.empty() ? f : xpre + "/" + f; };
@@ -126,6 +152,14 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     if (k == "END") break;
     else if (k == "GLOBAL_verbose" || k == "GLOBAL_thread_count" || k == "GLOBAL_omp_type" || k == "GLOBAL_LBITS") { /* host threading and logging: not used */ }
     else if (k == "GLOBAL_TEST_TYPE") test_type = v;
+    else if (k == "GLOBAL_scorebox_out_xdrop") scorebox_xdrop = v;
+    else if (k == "GLOBAL_scorebox_row_max") rc = parse_int(v, k, P.scorebox_row_max, err);
+    else if (k == "GLOBAL_scorebox_row_num") rc = parse_int(v, k, P.scorebox_row_num, err);
+    else if (k == "GLOBAL_scorebox_col_max") rc = parse_int(v, k, P.scorebox_col_max, err);
+    else if (k == "GLOBAL_scorebox_col_num") rc = parse_int(v, k, P.scorebox_col_num, err);
+    else if (k == "GLOBAL_scramble_num") rc = parse_int(v, k, scramble_num, err);
+    else if (k == "GLOBAL_scramble_out_xdrop_") scramble_xdrop = split_list(v);
+    else if (k == "GLOBAL_scramble_rseed_") scramble_rseed = split_list(v);
     else if (k == "GLOBAL_QR_strategy") P.QR_strategy = v;
     else if (k == "GLOBAL_QC_strategy") P.QC_strategy = v;
     else if (k == "GLOBAL_NBINS") rc = parse_int(v, k, nbins, err);
@@ -164,10 +198,11 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     }
     if (rc) return rc;
   }
-  if (!test_type.empty() && test_type != "lakcluster_driver") {
-    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc driver";
+  if (!test_type.empty() && test_type != "lakcluster_driver" && test_type != "lakcluster_scorebox") {
+    err = "GLOBAL_TEST_TYPE " + test_type + " is neither the bcc driver nor its scorebox";
     return 3;
   }
+  P.test_type = test_type.empty() ? "lakcluster_driver" : test_type;
   if (!others.empty()) {
     err = "inputs not supported by this build: " + others[0] + " (extra Y/W/T/S matrices or preset allele frequencies)";
     return 4;
@@ -190,6 +225,24 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
   if (nbins <= 0 || (int)A_t.size() < nbins) { err = "GLOBAL_NBINS and GLOBAL_A_t_name_ must name one file per bin"; return 2; }
   P.nbins = nbins;
   I = Input();
+  if (P.test_type == "lakcluster_scorebox") {
+    if (scorebox_xdrop.empty()) { err = "GLOBAL_scorebox_out_xdrop is not set"; return 2; }
+    if (int rc = read_xdrop(scorebox_xdrop, I.scorebox_xdrop, err)) return rc;
+  } else if (scramble_num > 0) {
+    // updateglobals.c:122-135: one out_xdrop file and seed per scramble, seeds 1, 2, ... by default
+    if ((int)scramble_xdrop.size() < scramble_num) { err = "GLOBAL_scramble_out_xdrop_ names fewer files than GLOBAL_scramble_num"; return 2; }
+    for (int i = 0; i < scramble_num; ++i) {
+      Input::Scramble sc;
+      sc.rseed = (unsigned long long)(i + 1);
+      if (i < (int)scramble_rseed.size() && !scramble_rseed[i].empty()) {
+        int x = 0;
+        if (int rc = parse_int(scramble_rseed[i], "GLOBAL_scramble_rseed_", x, err)) return rc;
+        sc.rseed = (unsigned long long)(unsigned long)(long)x;
+      }
+      if (int rc = read_xdrop(scramble_xdrop[i], sc.xdrop, err)) return rc;
+      I.scramble.push_back(std::move(sc));
+    }
+  }
   I.bins.resize(nbins);
   int ncols = -1;
   for (int nb = 0; nb < nbins; ++nb) {

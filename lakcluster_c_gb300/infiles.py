@@ -48,7 +48,8 @@ def read_b16(path: str) -> np.ndarray:
 
 def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.05, B_MLT=32,
                      A_row_masks=None, Z_row_masks=None, col_mask=None, gamma_type=None, Ireq=None,
-                     T_bins=None, S_bins=None, kappa_squared=None, qc_strategy="YnWt", name="bcc.in") -> str:
+                     T_bins=None, S_bins=None, kappa_squared=None, qc_strategy="YnWt", name="bcc.in",
+                     extra_statements=()) -> str:
     """Write the .b16 files of one bcc problem and the .in file that names them.
 
     A_bins / Z_bins: per-bin 0/1 arrays (rows x SNPs).  Masks (0/1 vectors) are
@@ -56,7 +57,9 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
     per-bin 0/1 covariate arrays (case rows x T_ncols, control rows x
     T_ncols), written as T_t / T_n and S_t / S_n files like A; absent means
     the reference's single column of ones.  Returns the path of the .in file.
-    Outputs of a solve go to ``out_dir``.
+    Outputs of a solve go to ``out_dir``.  ``extra_statements`` (name, value)
+    pairs are written before END, e.g. ("GLOBAL_TEST_TYPE", ...) to replace
+    the solve by the scorebox, or the GLOBAL_scramble_* statements.
     """
     os.makedirs(in_dir, exist_ok=True)
     nbins = len(A_bins)
@@ -135,8 +138,9 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
         "GLOBAL_Y_n_cols= 0;",
         "GLOBAL_T_n_cols= %d;" % T_ncols,
         "GLOBAL_DIR_NAME= %s;" % os.path.abspath(out_dir),
-        "END= 0;",
     ]
+    lines += ["%s= %s;" % (k, v) for k, v in extra_statements]
+    lines += ["END= 0;"]
     path = os.path.join(in_dir, name)
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")

@@ -23,6 +23,16 @@ int main(int argc, char **argv) {
   if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
   if (argc > 2) lako_set_threads(atoi(argv[2]));
   lako_set_d_mlt(P.D_MLT);
+  if (P.test_type == "lakcluster_scorebox") {
+    lakbcc::ScoreboxOutput SO;
+    rc = lakbcc::scorebox(P, I, SO, err);
+    if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
+    if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_scorebox(P.dir_name, SO)) {
+      fprintf(stderr, "error: cannot write outputs into %s\n", P.dir_name.c_str());
+      return 2;
+    }
+    return 0;
+  }
   rc = lakbcc::solve(P, I, O, err);
   if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
   if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_outputs(P.dir_name, O)) {

@@ -55,6 +55,16 @@ int main(int argc, char **argv) {
   if (lakref_init(mb ? atoll(mb) : 4096, 1, 0)) { fprintf(stderr, "error: arena\n"); return 1; }
   GLOBAL_D_MLT = P.D_MLT;
   GLOBAL_B_MLT = P.B_MLT;
+  if (P.test_type == "lakcluster_scorebox") {
+    lakbcc::ScoreboxOutput SO;
+    rc = lakbcc::scorebox(P, I, SO, err);
+    if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
+    if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_scorebox(P.dir_name, SO)) {
+      fprintf(stderr, "error: cannot write outputs into %s\n", P.dir_name.c_str());
+      return 2;
+    }
+    return 0;
+  }
   rc = lakbcc::solve(P, I, O, err);
   if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
   if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_outputs(P.dir_name, O)) {

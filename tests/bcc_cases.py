@@ -103,13 +103,113 @@ def build(name):
     return (CASES.get(name) or LARGE_CASES[name])[0]()
 
 
-def write_case(name, in_dir, out_dir, fname="bcc.in"):
+def write_case(name, in_dir, out_dir, fname="bcc.in", extra_statements=()):
     d = build(name)
     return infiles.write_bcc_inputs(in_dir, out_dir, d["A"], d.get("Z"), gamma=d["gamma"], B_MLT=32,
                                     A_row_masks=d.get("A_masks"), Z_row_masks=d.get("Z_masks"),
                                     col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), Ireq=d.get("Ireq"),
                                     T_bins=d.get("T"), S_bins=d.get("S"), kappa_squared=d.get("kappa_squared"),
-                                    qc_strategy=d.get("qc", "YnWt"), name=fname)
+                                    qc_strategy=d.get("qc", "YnWt"), name=fname, extra_statements=extra_statements)
+
+
+# --- scorebox and scramble cases -------------------------------------------------
+#
+# Scorebox (GLOBAL_TEST_TYPE lakcluster_scorebox): (case, (row_max, row_num,
+# col_max, col_num)) over the case's own solve order (its golden out_xdrop_a
+# lines).  The per-step row count stays within the lrup row buffers the
+# reference sizes from its gamma schedule (2 * ceil(0.05 * rows) here); larger
+# steps write past them in the reference (see lakcluster_c_gb300/csrc/
+# bcc_driver.cpp, load).  row_max > col_max steps rows in the inner loop
+# (lakcluster_scorebox_rc), otherwise columns (_cr).
+SCOREBOX = {
+    "sb_2bin_cr": ("case_control_2bin_300x250x2100", (20, 3, 200, 3)),
+    "sb_2bin_rc": ("case_control_2bin_300x250x2100", (45, 4, 40, 3)),
+    "sb_3bin_ragged_cr": ("case_control_3bin_ragged", (20, 3, 200, 4)),
+    "sb_3bin_Ireq1_rc": ("case_control_3bin_Ireq1", (24, 3, 10, 3)),
+    "sb_2bin_T3_kappa_cr": ("case_control_2bin_T3_kappa", (20, 3, 200, 3)),
+    "sb_2bin_qc_ZtSWn_rc": ("case_control_2bin_qc_ZtSWn", (24, 3, 10, 3)),
+}
+SCOREBOX_ARRAYS = ("A_rpop_j_total", "A_cpop_j", "Irem", "QR_avg", "QC_avg")
+
+# Scramble (GLOBAL_scramble_num): (case, [(rows, cols, seed), ...]); each
+# scramble redraws the case entries of the last `rows` rows and `cols`
+# columns of the case's solve order (the planted block), with that seed.
+SCRAMBLE = {
+    "scr_2bin": ("case_control_2bin_300x250x2100", [(40, 200, 7)]),
+    "scr_3bin_ragged": ("case_control_3bin_ragged", [(30, 150, 3)]),
+    "scr_2bin_masked_two": ("case_control_2bin_masked", [(25, 300, 11), (10, 60, 2)]),
+    "scr_2bin_T3": ("case_control_2bin_T3", [(40, 200, 5)]),
+}
+
+
+def scramble_xdrop_lines(xdrop_a, rows, cols):
+    """The out_xdrop lines a scramble reads: the last `rows` row lines and the
+    last `cols` column lines of a solve's out_xdrop_a."""
+    r = [ln for ln in xdrop_a if not ln.startswith("-1")]
+    c = [ln for ln in xdrop_a if ln.startswith("-1")]
+    return r[len(r) - rows:] + c[len(c) - cols:]
+
+
+def write_scorebox_case(key, xdrop_a, in_dir, out_dir, fname="bcc.in"):
+    """The .in of scorebox `key` over the solve order xdrop_a (text lines);
+    the order is written to in_dir/scorebox_xdrop.txt."""
+    name, (rmax, rnum, cmax, cnum) = SCOREBOX[key]
+    os.makedirs(in_dir, exist_ok=True)
+    xp = os.path.abspath(os.path.join(in_dir, "scorebox_xdrop.txt"))
+    with open(xp, "w") as f:
+        f.write("\n".join(xdrop_a) + "\n")
+    return write_case(name, in_dir, out_dir, fname, extra_statements=(
+        ("GLOBAL_TEST_TYPE", "lakcluster_scorebox"), ("GLOBAL_scorebox_out_xdrop", xp),
+        ("GLOBAL_scorebox_row_max", rmax), ("GLOBAL_scorebox_row_num", rnum),
+        ("GLOBAL_scorebox_col_max", cmax), ("GLOBAL_scorebox_col_num", cnum)))
+
+
+def write_scramble_case(key, xdrop_a, in_dir, out_dir, fname="bcc.in"):
+    """The .in of scramble `key`, its out_xdrop files cut from xdrop_a."""
+    name, specs = SCRAMBLE[key]
+    os.makedirs(in_dir, exist_ok=True)
+    files, seeds = [], []
+    for i, (rows, cols, seed) in enumerate(specs):
+        xp = os.path.abspath(os.path.join(in_dir, "scramble_xdrop_%d.txt" % i))
+        with open(xp, "w") as f:
+            f.write("\n".join(scramble_xdrop_lines(xdrop_a, rows, cols)) + "\n")
+        files.append(xp)
+        seeds.append(str(seed))
+    return write_case(name, in_dir, out_dir, fname, extra_statements=(
+        ("GLOBAL_scramble_num", len(specs)), ("GLOBAL_scramble_out_xdrop_", ",".join(files)),
+        ("GLOBAL_scramble_rseed_", ",".join(seeds))))
+
+
+def read_scorebox(out_dir, grid):
+    """The five scorebox arrays (row_num x col_num) a scorebox run wrote."""
+    rmax, rnum, cmax, cnum = grid
+    out = {}
+    for a in SCOREBOX_ARRAYS:
+        path = os.path.join(out_dir, "scorebox_r%dn%d_c%dn%d_%s.mda" % (rmax, rnum, cmax, cnum, a))
+        raw = open(path, "rb").read()
+        hdr = np.frombuffer(raw[:12], np.int32)
+        dt = np.float64 if a.endswith("avg") else np.int32
+        assert list(hdr) == [2, rnum, cnum], (path, hdr)
+        out[a] = np.frombuffer(raw[12:], dt).reshape(cnum, rnum).T.copy()
+    return out
+
+
+SCOREBOX_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bcc_scorebox.npz")
+
+
+def load_scorebox_golden():
+    z = np.load(SCOREBOX_GOLDEN, allow_pickle=False)
+    sb = {k: {a: z["%s/%s" % (k, a)] for a in SCOREBOX_ARRAYS} for k in SCOREBOX}
+    scr = {k: {key: [str(s) for s in z["%s/%s" % (k, key)]] for key in ("trace", "xdrop_a", "xdrop_b", "b16_sha1")}
+           for k in SCRAMBLE}
+    return sb, scr
+
+
+def b16_digests(out_dir):
+    """sha1 of each *_scramble_*.b16 file a scrambled solve wrote, by name."""
+    import hashlib
+    return sorted("%s %s" % (f, hashlib.sha1(open(os.path.join(out_dir, f), "rb").read()).hexdigest())
+                  for f in os.listdir(out_dir) if f.endswith(".b16") and "_scramble_" in f)
 
 
 def read_outputs(out_dir):

@@ -428,6 +428,12 @@ int lakgb_xcalc_noalloc(const struct lakgb_xcalc_noalloc_args *args);
 /* Last error recorded by any entry point (0 = none) and its message; reading
  * it clears it. */
 int lakgb_last_error(char *msg, int msg_len);
+/* The first error recorded by entry points called on this thread since the
+ * previous call (0: none), with its message; clears it.  Each thread keeps its
+ * own, so concurrent callers (one solve per thread) see only theirs; the
+ * whole-solve entry points check it and fail with code 9 when a kernel entry
+ * point they called reported an error. */
+int lakgb_thread_error_take(char *msg, int msg_len);
 /* Keep uploaded wX bit matrices resident on the device between calls, keyed
  * by their host address and size (1), or upload them afresh on every call (0,
  * default).  With 1, a caller that rewrites a wX buffer in place, or frees one

@@ -30,9 +30,23 @@ long row_bytes_min(int ncols) { return (long)(ncols + (16 - ncols % 16) % 16) / 
 // invalidates the solve's products: report it as the solve's error.
 int pipeline_status() {
   const int st = lakgb_thread_device_status();
-  if (!st) return 0;
-  g_err = "a tensor-core pipeline wait ran out of time (code " + std::to_string(st) + "); results invalid";
-  return 8;
+  char msg[256];
+  const int e = lakgb_thread_error_take(msg, sizeof msg);
+  if (st) {
+    g_err = "a tensor-core pipeline wait ran out of time (code " + std::to_string(st) + "); results invalid";
+    return 8;
+  }
+  if (e) {
+    g_err = std::string("a kernel entry point failed: ") + msg;
+    return 9;
+  }
+  return 0;
+}
+
+// Forget this thread's leftovers from earlier calls before a solve starts.
+void pipeline_reset() {
+  lakgb_thread_device_status();
+  lakgb_thread_error_take(nullptr, 0);
 }
 
 }  // namespace
@@ -71,6 +85,7 @@ struct SolveResidency {
 extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakgb_bcc_result *res) {
   SolveResidency residency;
   g_err.clear();
+  pipeline_reset();
   if (!prob || !res) { g_err = "null argument"; return 2; }
   memset(res, 0, sizeof(*res));
   if (prob->nbins <= 0 || !prob->bins || prob->ncols < 0) { g_err = "bad problem description"; return 2; }
@@ -155,6 +170,7 @@ extern "C" void lakgb_bcc_result_free(struct lakgb_bcc_result *res) {
 extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
   SolveResidency residency;
   g_err.clear();
+  pipeline_reset();
   lakbcc::Params P;
   lakbcc::Input I;
   int rc = lakbcc::read_in_file(in_path, P, I, g_err);

@@ -26,14 +26,26 @@ cudaEvent_t g_ev0 = nullptr, g_ev1 = nullptr;
 bool g_ev_pending = false;
 }  // namespace
 
+// The first error of the calling thread since lakgb_thread_error_take read it
+// (a solve checks its own thread's entry points; another thread's errors are
+// not its own).
+thread_local int t_err = 0;
+thread_local char t_msg[256];
+
 void set_error(int code, const char *fmt, ...) {
+  char msg[256];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, sizeof(msg), fmt, ap);
+  va_end(ap);
+  if (!t_err) {
+    t_err = code;
+    memcpy(t_msg, msg, sizeof(t_msg));
+  }
   std::lock_guard<std::mutex> lk(g_mu);
   if (g_err) return;
   g_err = code;
-  va_list ap;
-  va_start(ap, fmt);
-  vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
-  va_end(ap);
+  memcpy(g_msg, msg, sizeof(g_msg));
 }
 
 void check_cuda(cudaError_t e, const char *what, const char *file, int line) {
@@ -338,6 +350,17 @@ extern "C" long long lakgb_pool_high_water(int reset) {
     LAKGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
   }
   return (long long)v;
+}
+
+extern "C" int lakgb_thread_error_take(char *msg, int msg_len) {
+  const int e = lakgb::t_err;
+  if (msg && msg_len > 0) {
+    strncpy(msg, lakgb::t_msg, (size_t)msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  lakgb::t_err = 0;
+  lakgb::t_msg[0] = 0;
+  return e;
 }
 
 extern "C" int lakgb_last_error(char *msg, int msg_len) {

@@ -283,7 +283,8 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
   const int npairs = (int)std::min(M_At->rpop_j, M_Zt->rpop_j);
   const int ninner = (int)std::min(M_Yt->rpop_j, M_Wt->rpop_j);
   const int nS = (int)M_St->rpop_j;
-  if (npairs == 0 || nS == 0) return (int)length;
+  // no pairs, covariates or inner rows: every sum is empty (the zeros written above)
+  if (npairs == 0 || nS == 0 || ninner == 0) return (int)length;
   const int Y_pcols = (int)lakbcc::psize(M_Yt->nrows);
   const double *D_Yn = Y_ajdk + (size_t)lakbcc::AJDK_0_1 * Y_pcols;
   const L_handle *LA = lf_AtTYn, *LZ = lf_ZtSWn;
@@ -305,8 +306,8 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
     zw_s[s] = pick_u(LZ->spacing_lyr, s, M_St->m_b_[s], M_St->m_a_[s]) * LZ->row_stride * LZ->col_stride;
     s_off[s] = pick_u(output_spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * length_a;
   }
-  if (max_index(ay_a) + (ninner ? max_index(ay_y) : 0) + max_index(ay_s) >= populated(LA, true) ||
-      max_index(zw_z) + (ninner ? max_index(zw_w) : 0) + max_index(zw_s) >= populated(LZ, true)) {
+  if (max_index(ay_a) + max_index(ay_y) + max_index(ay_s) >= populated(LA, true) ||
+      max_index(zw_z) + max_index(zw_w) + max_index(zw_s) >= populated(LZ, true)) {
     set_error(4, "wrap_AtTYn____WtSZn_vv__run: L_handle smaller than the rows and columns it is indexed by");
     return (int)length;
   }

@@ -175,6 +175,7 @@ def test_noalloc_rejects_oversize(gpu_lib):
     out = (C.c_double * 3)()
     p = dummy.data_ptr()
     a = NoAllocArgs(p, p, 16, p, 1, p, MAXC + 1, p, 32, 1 << 32, 240, p, C.cast(out, C.POINTER(C.c_double)), None)
+    lib.lakgb_last_error(None, 0)   # the library-wide status keeps the first error until read
     assert lib.lakgb_xcalc_noalloc(C.byref(a)) != 0
     buf = C.create_string_buffer(256)
     lib.lakgb_last_error(buf, 256)

@@ -204,6 +204,51 @@ int wrap_An_ZtSWn_Yt_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int s
                              struct L_handle **output_An_ZtSWn_Yt_ww_p);
 
 /* ---------------------------------------------------------------------------
+ * Input pipeline: PLINK .bed to .b16 (bed_to_b16, dir_c/bed_to_b16.c:711-1355).
+ * ------------------------------------------------------------------------- */
+
+/* The conversion's thresholds (GLOBAL_snp_mss_threshold, _snp_maf_threshold,
+ * _snp_I_opt_threshold, _pat_mss_threshold); _init sets the reference's
+ * defaults 0.01, 0.25, 0.01, 0.04 (dir_c/lakcluster_ver18.c:158-161). */
+struct lakgb_bed_params {
+  double snp_mss_threshold, snp_maf_threshold, snp_I_opt_threshold, pat_mss_threshold;
+};
+void lakgb_bed_params_init(struct lakgb_bed_params *p);
+
+/* A conversion's result: the kept SNPs (.bim indices) and patients (.fam
+ * indices), three alleles per kept SNP (allele 3k+0 / 3k+1 / 3k+2 = nor / xor
+ * / and of kept SNP k) with their frequency, maf, missing fraction and
+ * relative entropy, the sorted allele order (row r of A_n is allele
+ * allele_orig_from_sort[r]) and A_n itself: n_allele rows of row_bytes =
+ * rup(n_pat_retain, 16) / 8 bytes, patients MSB first (the .b16 payload).
+ * Arrays are malloc'ed; free with lakgb_bed_result_free. */
+struct lakgb_bed_result {
+  int n_snp, n_fam;
+  int n_snp_retain, n_pat_retain, n_allele;
+  long long row_bytes;
+  int *snp_from_retain, *pat_from_retain, *allele_orig_from_sort;
+  double *allele_frequency, *allele_maf, *allele_mss, *allele_I_opt;
+  unsigned char *A_n;
+};
+void lakgb_bed_result_free(struct lakgb_bed_result *r);
+
+/* bed_records: the .bed body (after its three magic bytes), n_snp records of
+ * ceil(n_fam / 4) bytes.  params may be null (defaults).  Returns 0 on
+ * success. */
+int lakgb_bed_to_b16_mem(const unsigned char *bed_records, int n_snp, int n_fam,
+                         const struct lakgb_bed_params *params, struct lakgb_bed_result *out);
+
+/* The file form, replacing bed_to_b16 (GLOBAL_TEST_TYPE= bed_to_b16 with
+ * GLOBAL_fname_{bed,bim,fam}_0in and GLOBAL_fname_{b16,bim,fam}_out; the same
+ * .in statements work through lakgb_bcc_run_in_file): reads the .bed / .bim /
+ * .fam, writes the .b16, one .bim line per allele in sorted order and the
+ * kept patients' .fam lines, as the reference writes them.  Returns 0 on
+ * success; lakgb_bed_last_error describes a failure. */
+int lakgb_bed_to_b16(const char *bed, const char *bim, const char *fam, const char *b16_out,
+                     const char *bim_out, const char *fam_out, const struct lakgb_bed_params *params);
+int lakgb_bed_last_error(char *msg, int msg_len);
+
+/* ---------------------------------------------------------------------------
  * Whole solves.
  * ------------------------------------------------------------------------- */
 

@@ -175,6 +175,20 @@ extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
   lakbcc::Input I;
   int rc = lakbcc::read_in_file(in_path, P, I, g_err);
   if (rc) return rc;
+  if (P.test_type == "bed_to_b16") {  // lakcluster_ver18.c:361
+    struct lakgb_bed_params bp;
+    bp.snp_mss_threshold = P.bed.snp_mss; bp.snp_maf_threshold = P.bed.snp_maf;
+    bp.snp_I_opt_threshold = P.bed.snp_I_opt; bp.pat_mss_threshold = P.bed.pat_mss;
+    rc = lakgb_bed_to_b16(P.bed.bed.c_str(), P.bed.bim.c_str(), P.bed.fam.c_str(), P.bed.b16_out.c_str(),
+                          P.bed.bim_out.c_str(), P.bed.fam_out.c_str(), &bp);
+    if (rc) {
+      char msg[256];
+      lakgb_bed_last_error(msg, sizeof msg);
+      g_err = msg;
+      return rc;
+    }
+    return pipeline_status();
+  }
   lakgb_set_d_mlt(P.D_MLT);
   if (P.test_type == "lakcluster_scorebox") {  // lakcluster_ver18.c:338
     lakbcc::ScoreboxOutput SO;

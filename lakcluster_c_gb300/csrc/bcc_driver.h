@@ -27,6 +27,12 @@ struct Params {
   std::string test_type = "lakcluster_driver";
   // scorebox grid (GLOBAL_scorebox_row_max / _row_num / _col_max / _col_num)
   int scorebox_row_max = 0, scorebox_row_num = 0, scorebox_col_max = 0, scorebox_col_num = 0;
+  // bed_to_b16 (GLOBAL_fname_{bed,bim,fam}_0in, GLOBAL_fname_{b16,bim,fam}_out
+  // and the four thresholds, defaults as dir_c/lakcluster_ver18.c:150-163)
+  struct BedFiles {
+    std::string bed, bim, fam, b16_out, bim_out, fam_out;
+    double snp_mss = 0.01, snp_maf = 0.25, snp_I_opt = 0.01, pat_mss = 0.04;
+  } bed;
 };
 
 // One bin's inputs: packed rows of A (patients x SNPs, bsize(ncols) bytes per

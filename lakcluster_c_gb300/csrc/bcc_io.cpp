@@ -160,6 +160,19 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     else if (k == "GLOBAL_scramble_num") rc = parse_int(v, k, scramble_num, err);
     else if (k == "GLOBAL_scramble_out_xdrop_") scramble_xdrop = split_list(v);
     else if (k == "GLOBAL_scramble_rseed_") scramble_rseed = split_list(v);
+    else if (k == "GLOBAL_fname_bed_0in") P.bed.bed = v;
+    else if (k == "GLOBAL_fname_bim_0in") P.bed.bim = v;
+    else if (k == "GLOBAL_fname_fam_0in") P.bed.fam = v;
+    else if (k == "GLOBAL_fname_b16_out") P.bed.b16_out = v;
+    else if (k == "GLOBAL_fname_bim_out") P.bed.bim_out = v;
+    else if (k == "GLOBAL_fname_fam_out") P.bed.fam_out = v;
+    else if (k == "GLOBAL_snp_mss_threshold") rc = parse_double(v, k, P.bed.snp_mss, err);
+    else if (k == "GLOBAL_snp_maf_threshold") rc = parse_double(v, k, P.bed.snp_maf, err);
+    else if (k == "GLOBAL_snp_I_opt_threshold") rc = parse_double(v, k, P.bed.snp_I_opt, err);
+    else if (k == "GLOBAL_pat_mss_threshold") rc = parse_double(v, k, P.bed.pat_mss, err);
+    else if (k == "GLOBAL_fname_flip_flag" || k == "GLOBAL_n_fam_char_max" || k == "GLOBAL_n_bim_char_max") {
+      /* the flip file is not read by the reference either; field widths are unbounded here */
+    }
     else if (k == "GLOBAL_QR_strategy") P.QR_strategy = v;
     else if (k == "GLOBAL_QC_strategy") P.QC_strategy = v;
     else if (k == "GLOBAL_NBINS") rc = parse_int(v, k, nbins, err);
@@ -198,8 +211,12 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     }
     if (rc) return rc;
   }
+  if (test_type == "bed_to_b16") {  // lakcluster_ver18.c:361: the conversion only, no bcc inputs
+    P.test_type = test_type;
+    return 0;
+  }
   if (!test_type.empty() && test_type != "lakcluster_driver" && test_type != "lakcluster_scorebox") {
-    err = "GLOBAL_TEST_TYPE " + test_type + " is neither the bcc driver nor its scorebox";
+    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc driver, its scorebox or bed_to_b16";
     return 3;
   }
   P.test_type = test_type.empty() ? "lakcluster_driver" : test_type;

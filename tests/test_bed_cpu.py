@@ -1,0 +1,37 @@
+"""bed_to_b16 without a GPU: the numpy restatement in tests/bed_cases.py (the
+checker of the GPU conversion) writes exactly the .b16, .bim and .fam files
+the reference program wrote for the same synthetic PLINK inputs
+(tests/golden/bed_to_b16.npz), and the input generator is reproducible."""
+import numpy as np
+import pytest
+
+import bed_cases as bd
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return bd.load_golden()
+
+
+@pytest.mark.parametrize("name", list(bd.BED_CASES))
+def test_oracle_equals_reference_outputs(golden, tmp_path, name):
+    bd.write_case(name, str(tmp_path))
+    got = bd.oracle_files(name, str(tmp_path))
+    for k in ("b16", "bim", "fam"):
+        assert got[k] == golden[name][k], (name, k)
+
+
+def test_filters_remove_snps_and_patients(golden):
+    n_snp, n_fam, _, _ = bd.BED_CASES["bed_1000x512"]
+    hdr = np.frombuffer(golden["bed_1000x512"]["b16"][:12], np.int32)
+    assert hdr[0] == 16 and 0 < hdr[1] < n_fam and 0 < hdr[2] < 3 * n_snp and hdr[2] % 3 == 0
+
+
+def test_generator_is_reproducible():
+    a = bd.genotypes(50, 33, 7)
+    b = bd.genotypes(50, 33, 7)
+    assert np.array_equal(a, b) and set(np.unique(a)) <= {0, 1, 2, 3}
+    rec = bd.pack_bed(a)
+    assert rec.shape == (50, 9)
+    for p in range(33):
+        assert np.array_equal((rec[:, p // 4] >> (2 * (p % 4))) & 3, a[:, p])

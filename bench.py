@@ -584,6 +584,7 @@ def run_gpu(args):
             extras["grouped_null_gram_passes"] = grouped_gram_measurement(stream, sh, flush)
         if not args.no_transpose:
             extras["b16_transpose"] = transpose_measurement(stream, sh, with_cpu=not args.no_cpu_baseline)
+            extras["bed_to_b16"] = bed_measurement(with_cpu=not args.no_cpu_baseline)
         if not args.no_ww:
             extras["an_ztswn_yt_ww"] = ztswn_ww_measurement(with_cpu=not args.no_cpu_baseline)
         del flush
@@ -768,6 +769,77 @@ def transpose_measurement(stream, sh, with_cpu: bool):
         cs = time.perf_counter() - t0
         out["cpu_baseline"] = {"gbs": 2.0 * a.size / cs / 1e9, "seconds": cs, "cores": os.cpu_count(),
                                "kind": "port", "sample": "8192 records of 8192 bits (8 MB) on the C oracle"}
+    return out
+
+
+def bed_measurement(with_cpu: bool):
+    """PLINK .bed to .b16 (bed_to_b16, dir_c/bed_to_b16.c:711-1355) through
+    lakgb_bed_to_b16_mem: 200000 SNPs x 16384 patients (819 MB of .bed
+    records in page-locked host memory; MAF U[0.05,0.5], Hardy-Weinberg
+    genotypes, 0.4 % missing calls, drawn on the GPU), both passes over the
+    records (upload, code counts, allele expansion), the host statistics and
+    sort, and the allele matrix's download inside the call.  The numpy
+    restatement of the conversion (tests/bed_cases.py) is timed on the first
+    2000 SNPs."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from lakcluster_c_gb300._lib import load
+
+    class Prm(C.Structure):
+        _fields_ = [("a", C.c_double), ("b", C.c_double), ("c", C.c_double), ("d", C.c_double)]
+
+    class Res(C.Structure):
+        _fields_ = [("n_snp", C.c_int), ("n_fam", C.c_int), ("n_snp_retain", C.c_int), ("n_pat_retain", C.c_int),
+                    ("n_allele", C.c_int), ("row_bytes", C.c_longlong)] + [(n, C.c_void_p) for n in (
+                        "snp", "pat", "order", "freq", "maf", "mss", "I", "A_n")]
+
+    lib = load()
+    lib.lakgb_bed_to_b16_mem.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(Prm), C.POINTER(Res)]
+    lib.lakgb_bed_result_free.argtypes = [C.POINTER(Res)]
+    n_snp, n_fam = 200000, 16384
+    n_bam = n_fam // 4
+    thr = (0.01, 0.05, 0.01, 0.04)
+    host = torch.empty((n_snp, n_bam), dtype=torch.uint8, pin_memory=True)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(31)
+    w = torch.tensor([1, 4, 16, 64], dtype=torch.int32, device="cuda")
+    for r0 in range(0, n_snp, 20000):
+        n = min(20000, n_snp - r0)
+        q = 0.05 + 0.45 * torch.rand((n, 1), generator=g, device="cuda")
+        u = torch.rand((n, n_fam), generator=g, device="cuda")
+        c = torch.where(u < q * q, 0, torch.where(u < q * q + 2 * q * (1 - q), 2, 3))
+        c = torch.where(torch.rand((n, n_fam), generator=g, device="cuda") < 0.004, 1, c)
+        host[r0:r0 + n] = (c.view(n, n_bam, 4).to(torch.int32) * w).sum(2).to(torch.uint8).cpu()
+        del q, u, c
+    torch.cuda.synchronize()
+    prm = Prm(*thr)
+    t = []
+    res = Res()
+    for rep in range(4):
+        t0 = time.perf_counter()
+        rc = lib.lakgb_bed_to_b16_mem(host.data_ptr(), n_snp, n_fam, C.byref(prm), C.byref(res))
+        dt = time.perf_counter() - t0
+        assert rc == 0
+        if rep:
+            t.append(dt)
+        kept = (res.n_snp_retain, res.n_pat_retain, res.n_allele, res.row_bytes)
+        lib.lakgb_bed_result_free(C.byref(res))
+    s = statistics.median(t)
+    out = {"snps": n_snp, "patients": n_fam, "bed_bytes": n_snp * n_bam, "seconds": s, "seconds_all": t,
+           "bed_gbs": n_snp * n_bam / s / 1e9, "genotypes_per_s": n_snp * n_fam / s,
+           "kept_snps": kept[0], "kept_patients": kept[1], "alleles": kept[2],
+           "allele_matrix_bytes": kept[2] * kept[3],
+           "note": "whole conversion from page-locked host records: two uploads of the records, both GPU passes, "
+                   "host statistics and allele sort, the allele matrix's download"}
+    if with_cpu:
+        import bed_cases as bd
+        rec = host[:2000].numpy()
+        t0 = time.perf_counter()
+        bd.oracle(rec, n_fam, thr)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"genotypes_per_s": 2000 * n_fam / cs, "seconds": cs, "cores": 1, "kind": "port",
+                               "sample": "the numpy restatement on the first 2000 SNPs"}
+    del host
     return out
 
 

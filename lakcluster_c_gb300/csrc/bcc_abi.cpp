@@ -202,7 +202,8 @@ extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
     return 0;
   }
   lakbcc::Output O;
-  rc = lakbcc::solve(P, I, O, g_err, &kHooks);
+  rc = P.test_type == "dexcluster_driver" ? lakbcc::dcc_solve(P, I, O, g_err, &kHooks)  // lakcluster_ver18.c:345
+                                          : lakbcc::solve(P, I, O, g_err, &kHooks);
   if (rc) return rc;
   if ((rc = pipeline_status())) return rc;
   if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_outputs(P.dir_name, O)) {

@@ -87,12 +87,19 @@ struct Single {
   L_handle *lf_An_a1d1 = nullptr, *lf_At_An_a1d1 = nullptr, *lf_a2d2_ZtSn = nullptr, *lf_a2d2_AtTn = nullptr;
   // SNP x SNP x covariate products of the ZtSWn column strategy
   L_handle *lf_AtTAn = nullptr, *lf_ZtSZn = nullptr, *lf_ktrkn = nullptr;
+  // dexcluster single-study terms (dcc_single_init_lf, dir_c/dcc.c:667-725)
+  L_handle *lf_A_a0d1 = nullptr, *lf_A_a2d1 = nullptr, *lf_a1d1_ZtSn = nullptr, *lf_a1d1_AtTn = nullptr;
+  L_handle *lf_a0d1_ZtSn = nullptr, *lf_a0d1_AtTn = nullptr;
+  MH *M_a0d1_ZtSn = nullptr, *M_a0d1_AtTn = nullptr;
   std::vector<double> QR_AnZtSZnAt_nrm, QR_AnAtTAnAt_nrm;
   std::vector<int> QR_index_global_mr_a, QR_index_global_mr_b, QR_index_global_mr_j;
 };
 
 struct Double {
   int nb1 = 0, nb2 = 0;
+  // dexcluster bin-pair terms (dcc_double_init_lf, dir_c/dcc.c:775-828)
+  L_handle *lf_An_a0d1_ZtSn = nullptr, *lf_An_a0d1_AtTn = nullptr, *lf_TAnZtS_ww = nullptr, *lf_TAnAtT_ww = nullptr;
+  L_handle *lf_D_AtTn_ZtSn_vv = nullptr, *lf_D_AtTn_AtTn_vv = nullptr;
   L_handle *lf_AnZt = nullptr, *lf_AnAt = nullptr;
   MH *M_AnZt = nullptr, *M_AnAt = nullptr;
   int M_AnZt_trm = 0, M_AnAt_trm = 0;
@@ -358,6 +365,10 @@ std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows
   return t;
 }
 
+// GLOBAL_TEST_TYPE dexcluster_driver: the dcc method (dir_c/dexcluster_driver.c)
+// on the same state.
+bool dcc_mode(const Params &P) { return P.test_type == "dexcluster_driver"; }
+
 // n1b_cap / n2b_cap (default n1b / n2b): the largest counts the planes must
 // hold, when more rows can be removed in one step than the transposition
 // flag was chosen for.
@@ -507,6 +518,14 @@ int load(State &S, const Input &I, std::string &err) {
     E->M_a2d2_ZtSn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_ncols));
     E->lf_a2d2_AtTn = S.L((unsigned long long)S.A_cpop_b * S.T_cpop_b);
     E->M_a2d2_AtTn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_ncols));
+    if (dcc_mode(P)) {
+      E->lf_A_a0d1 = S.L(1); E->lf_A_a2d1 = S.L(1);
+      E->lf_a1d1_ZtSn = S.L(T); E->lf_a1d1_AtTn = S.L(T);
+      E->lf_a0d1_ZtSn = S.L((unsigned long long)S.A_cbother * S.A_cpop_b * S.T_cpop_b);
+      E->lf_a0d1_AtTn = S.L((unsigned long long)S.A_cbother * S.A_cpop_b * S.T_cpop_b);
+      E->M_a0d1_ZtSn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_cbother * S.A_ncols));
+      E->M_a0d1_AtTn = S.keep(mh_make_owned((1 + P.B_MLT) * (int)S.T_cpop_b, S.A_cbother * S.A_ncols));
+    }
   }
   // bcc_single_init_lf (bcc.c:762-792, "store all"): the SNP x SNP x covariate
   // products of the column low-rank update, sized for ckeep retained x cdrop
@@ -546,6 +565,17 @@ int load(State &S, const Input &I, std::string &err) {
       const int A1a = E1->M_An->h.nrows, A1b = (int)E1->M_An->h.rpop_b;
       const int A2a = E2->M_An->h.nrows, A2b = (int)E2->M_An->h.rpop_b;
       const int Z2a = E2->M_Zn->h.nrows, Z2b = (int)E2->M_Zn->h.rpop_b;
+      if (dcc_mode(P)) {  // the half loop needs no row x row products
+        const unsigned long long NT = (unsigned long long)E1->A_nrows * S.T_ncols;
+        const unsigned long long AT = (unsigned long long)S.A_ncols * S.T_ncols;
+        F->lf_An_a0d1_ZtSn = S.L(NT); F->lf_An_a0d1_AtTn = S.L(NT);
+        F->lf_TAnZtS_ww = S.L(NT); F->lf_TAnAtT_ww = S.L(NT);
+        F->lf_D_AtTn_ZtSn_vv = S.L(AT); F->lf_D_AtTn_AtTn_vv = S.L(AT);
+        F->QR_AnZtSZnAt = S.L(NT); F->QR_AnAtTAnAt = S.L(NT);
+        F->QC_AtTAnZtSZn = S.L(AT); F->QC_AtTAnAtTAn = S.L(AT);
+        S.F[nb1 + nb2 * S.nbins] = std::move(F);
+        continue;
+      }
       F->lf_AnZt = S.L((unsigned long long)A1b * Z2b);
       F->M_AnZt = xcalc_out(S, A1a, A1b, Z2a, Z2b, &F->M_AnZt_trm);
       F->lf_AnAt = S.L((unsigned long long)A1b * A2b);
@@ -1274,6 +1304,7 @@ void dra_sumx0(double *d, unsigned long long stride, unsigned long long length) 
 // pair normalised by its own number of summands, nothing summed over bins.
 void sumscores_nrm_per_bin(State &S) {
   const int nb = S.nbins, T = S.T_ncols;
+  const bool dcc = dcc_mode(S.P);  // dcc_sumscores_nrm (dcc_sumscores.c:478-532): one fewer column factor
   for (int nb1 = 0; nb1 < nb; ++nb1)
     for (int nb2 = 0; nb2 < nb; ++nb2) {
       const int nbx = nb1 + nb2 * nb, same = nb1 == nb2 ? 1 : 0;
@@ -1283,26 +1314,30 @@ void sumscores_nrm_per_bin(State &S) {
       if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
         double *d = &E->QR_AnZtSZnAt_nrm[nb2 * AN * T];
         memset(d, 0, AN * T * sizeof(double));
-        const long long lld = (long long)(E2->M_Zn->h.rpop_j - 0) * (long long)(E2->M_Zn->h.cpop_j) * (long long)(E2->M_Zn->h.cpop_j - 1);
+        const long long lld = dcc ? (long long)(E2->M_Zn->h.rpop_j - 0) * (long long)(E2->M_Zn->h.cpop_j)
+                                  : (long long)(E2->M_Zn->h.rpop_j - 0) * (long long)(E2->M_Zn->h.cpop_j) * (long long)(E2->M_Zn->h.cpop_j - 1);
         plusdiv(S, d, AN, T, F->QR_AnZtSZnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
       }
       if (E->A_rbother && S.A_cbother && E2->A_rbother) {
         double *d = &E->QR_AnAtTAnAt_nrm[nb2 * AN * T];
         memset(d, 0, AN * T * sizeof(double));
-        const long long lld = (long long)(E2->M_An->h.rpop_j - same) * (long long)(E2->M_An->h.cpop_j) * (long long)(E2->M_An->h.cpop_j - 1);
+        const long long lld = dcc ? (long long)(E2->M_An->h.rpop_j - same) * (long long)(E2->M_An->h.cpop_j)
+                                  : (long long)(E2->M_An->h.rpop_j - same) * (long long)(E2->M_An->h.cpop_j) * (long long)(E2->M_An->h.cpop_j - 1);
         plusdiv(S, d, AN, T, F->QR_AnAtTAnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
       }
       const unsigned long long AC = (unsigned long long)S.A_ncols;
       if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
         double *d = &S.QC_AtTAnZtSZn_nrm[nbx * AC * T];
         memset(d, 0, AC * T * sizeof(double));
-        const long long lld = (long long)(E->M_An->h.rpop_j) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(E2->M_Zn->h.rpop_j);
+        const long long lld = dcc ? (long long)(E->M_An->h.rpop_j) * (long long)(E2->M_Zn->h.rpop_j)
+                                  : (long long)(E->M_An->h.rpop_j) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(E2->M_Zn->h.rpop_j);
         plusdiv(S, d, AC, T, F->QC_AtTAnZtSZn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
       }
       if (E->A_rbother && S.A_cbother && E2->A_rbother) {
         double *d = &S.QC_AtTAnAtTAn_nrm[nbx * AC * T];
         memset(d, 0, AC * T * sizeof(double));
-        const long long lld = (long long)(E->M_An->h.rpop_j) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(E2->M_An->h.rpop_j - same);
+        const long long lld = dcc ? (long long)(E->M_An->h.rpop_j) * (long long)(E2->M_An->h.rpop_j - same)
+                                  : (long long)(E->M_An->h.rpop_j) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(E2->M_An->h.rpop_j - same);
         plusdiv(S, d, AC, T, F->QC_AtTAnAtTAn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
       }
     }
@@ -1401,6 +1436,7 @@ void sumscores_nrm(State &S) {  // bcc_sumscores_nrm (bcc_sumscores.c:550-779)
     return;
   }
   const int nb = S.nbins, T = S.T_ncols;
+  const bool dcc = dcc_mode(S.P);  // dcc_sumscores_nrm (dcc_sumscores.c:533-573): one fewer column factor
   for (int nb1 = 0; nb1 < nb; ++nb1)
     for (int nb2 = 0; nb2 < nb; ++nb2) {
       const int nbx = nb1 + nb2 * nb;
@@ -1410,26 +1446,30 @@ void sumscores_nrm(State &S) {  // bcc_sumscores_nrm (bcc_sumscores.c:550-779)
       if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
         double *d = &E->QR_AnZtSZnAt_nrm[nb2 * AN * T];
         memset(d, 0, AN * T * sizeof(double));
-        const long long lld = (long long)(S.Z_rpop_j_total - 0) * (long long)(E2->M_Zn->h.cpop_j) * (long long)(E2->M_Zn->h.cpop_j - 1);
+        const long long lld = dcc ? (long long)(S.Z_rpop_j_total - 0) * (long long)(E2->M_Zn->h.cpop_j)
+                                  : (long long)(S.Z_rpop_j_total - 0) * (long long)(E2->M_Zn->h.cpop_j) * (long long)(E2->M_Zn->h.cpop_j - 1);
         plusdiv(S, d, AN, T, F->QR_AnZtSZnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
       }
       if (E->A_rbother && S.A_cbother && E2->A_rbother) {
         double *d = &E->QR_AnAtTAnAt_nrm[nb2 * AN * T];
         memset(d, 0, AN * T * sizeof(double));
-        const long long lld = (long long)(S.A_rpop_j_total - 1) * (long long)(E2->M_An->h.cpop_j) * (long long)(E2->M_An->h.cpop_j - 1);
+        const long long lld = dcc ? (long long)(S.A_rpop_j_total - 1) * (long long)(E2->M_An->h.cpop_j)
+                                  : (long long)(S.A_rpop_j_total - 1) * (long long)(E2->M_An->h.cpop_j) * (long long)(E2->M_An->h.cpop_j - 1);
         plusdiv(S, d, AN, T, F->QR_AnAtTAnAt->lf, (double)lld, E->A_bmr_j.data(), S.T_bmc_j.data());
       }
       const unsigned long long AC = (unsigned long long)S.A_ncols;
       if (E->A_rbother && S.A_cbother && E2->Z_rbother) {
         double *d = &S.QC_AtTAnZtSZn_nrm[nbx * AC * T];
         memset(d, 0, AC * T * sizeof(double));
-        const long long lld = (long long)(S.A_rpop_j_total) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(S.Z_rpop_j_total);
+        const long long lld = dcc ? (long long)(S.A_rpop_j_total) * (long long)(S.Z_rpop_j_total)
+                                  : (long long)(S.A_rpop_j_total) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(S.Z_rpop_j_total);
         plusdiv(S, d, AC, T, F->QC_AtTAnZtSZn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
       }
       if (E->A_rbother && S.A_cbother && E2->A_rbother) {
         double *d = &S.QC_AtTAnAtTAn_nrm[nbx * AC * T];
         memset(d, 0, AC * T * sizeof(double));
-        const long long lld = (long long)(S.A_rpop_j_total) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(S.A_rpop_j_total - 1);
+        const long long lld = dcc ? (long long)(S.A_rpop_j_total) * (long long)(S.A_rpop_j_total - 1)
+                                  : (long long)(S.A_rpop_j_total) * (long long)(E->M_An->h.cpop_j - 1) * (long long)(S.A_rpop_j_total - 1);
         plusdiv(S, d, AC, T, F->QC_AtTAnAtTAn->lf, (double)lld, S.A_bmc_j.data(), S.T_bmc_j.data());
       }
     }
@@ -1894,6 +1934,7 @@ void trace_L(FILE *f, const char *stage, int it, const char *name, int a, int b,
 }
 
 void trace_M(FILE *f, const char *stage, int it, const char *name, int a, int b, const MH *M) {
+  if (!M) return;
   const M_handle &h = M->h;
   unsigned long long x = fnv(h.wX, (size_t)h.nrows * h.mc_length);
   x = fnv(&h.min_d, sizeof(double), x);
@@ -2195,6 +2236,238 @@ void scorebox_update(State &S) {
   scorebox_scores(S);
 }
 
+// ---------------------------------------------------------------------------
+// dexcluster (dcc): the half-loop method of dir_c/dexcluster_driver.c on the
+// same state -- one pass of row and column sub-scores per elimination step,
+// recomputed each step (no low-rank update).  The dcc score arrays reuse the
+// bcc ones of the same shape and role: QR_AnZtSZnAt(_nrm) holds QR_TAnZtS,
+// QR_AnAtTAnAt QR_TAnAtT, QC_AtTAnZtSZn QC_TAnZtS, QC_AtTAnAtTAn QC_TAnAtT.
+
+// get_D_AtTn_ZtSn_vv / get_D_AtTn_AtTn_vv (dir_c/D_AtTn_ZtSn.c:5-110,
+// :152-270), output spacing a x a: for every retained covariate ns and row
+// na of At, ((AtTn - etT a) D (ZtSn - a etS)), less the repeated-index term
+// D (cpop - 2 etA a + cpop a^2) when repeated (At == Zt).
+void D_AtTn_ZtSn(State &S, MH *At_, MH *Tt_, MH *Zt_, MH *St_, L_handle *lf_AtTn, L_handle *lf_ZtSn,
+                 L_handle *out, bool repeated) {
+  M_handle *At = At_->p(), *Tt = Tt_->p(), *St = St_->p();
+  (void)Zt_;
+  const int P = (int)psize(At->nrows);
+  const double *D_An = &S.A_ajdk[AJDK_0_1 * P], *a_An = &S.A_ajdk[AJDK_1_0 * P];
+  out->spacing_row = SP_a; out->row_stride = At->nrows;
+  out->spacing_col = SP_a; out->col_stride = Tt->nrows;
+  lh_zero(out);
+  for (int ns_j = 0; ns_j < (int)St->rpop_j; ++ns_j) {
+    const unsigned ns_a = St->m_a_[ns_j], ns_b = St->m_b_[ns_j];
+    const double etS = -(double)St->cpop_j + 2.0 * popcount_masked_row(St->wX + (long)ns_b * St->mc_length, St->mc_j, (long)St->mc_length);
+    const double etT = -(double)Tt->cpop_j + 2.0 * popcount_masked_row(Tt->wX + (long)ns_b * Tt->mc_length, Tt->mc_j, (long)Tt->mc_length);
+    for (int na_j = 0; na_j < (int)At->rpop_j; ++na_j) {
+      const unsigned na_a = At->m_a_[na_j], na_b = At->m_b_[na_j];
+      const double a = a_An[na_a / POPLENGTH], D = D_An[na_a / POPLENGTH];
+      double v = (*L2_get(lf_AtTn, na_j, na_b, na_a, ns_j, ns_b, ns_a) - etT * a) * D *
+                 (*L2_get(lf_ZtSn, na_j, na_b, na_a, ns_j, ns_b, ns_a) - a * etS);
+      if (repeated) {
+        const double etA = -(double)At->cpop_j +
+                           2.0 * popcount_masked_row(At->wX + (long)na_b * At->mc_length, At->mc_j, (long)At->mc_length);
+        v -= D * (At->cpop_j - 2 * etA * a + At->cpop_j * a * a);
+      }
+      out->lf[na_a + (size_t)ns_a * out->row_stride] = v;
+    }
+  }
+}
+
+void dcc_D_AtTn_ZtSn_all(State &S) {  // dcc_lf_D_AtTn_ZtSn_vv (dir_c/dcc_lf.c:102-163), no Y blocks
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (E1->A_rbother && S.A_cbother && E2->Z_rbother)
+        D_AtTn_ZtSn(S, E1->M_At, E1->M_Tt, E2->M_Zt, E2->M_St, E1->lf_AtTn, E2->lf_ZtSn, F->lf_D_AtTn_ZtSn_vv, false);
+      if (E1->A_rbother && S.A_cbother && E2->A_rbother)
+        D_AtTn_ZtSn(S, E1->M_At, E1->M_Tt, E2->M_At, E2->M_Tt, E1->lf_AtTn, E2->lf_AtTn, F->lf_D_AtTn_AtTn_vv,
+                    nb1 == nb2);
+    }
+}
+
+// get_dcc_TAnZtS_ww_stage_0 (dir_c/TAnZtS.c:5-209): per bin, the masked
+// column weight sums, the covariate-weighted a1d1 row sums and et_Tn / et_Sn.
+void dcc_stage_0(State &S) {
+  for (auto &Ep : S.E) {
+    Single *E = Ep.get();
+    M_handle *An = E->M_An->p(), *At = E->M_At->p(), *Tt = E->M_Tt->p(), *St = E->M_St->p(), *Zt = E->M_Zt->p();
+    const int T = Tt->nrows;
+    set_l1(E->lf_A_a0d1, 1); set_l1(E->lf_A_a2d1, 1);
+    set_l1(E->lf_a1d1_ZtSn, T); set_l1(E->lf_a1d1_AtTn, T);
+    set_l1(E->lf_et_Tn, T); set_l1(E->lf_et_Sn, T);
+    E->lf_A_a0d1->lf[0] = mask_sum(S, An, AJDK_0_1);
+    E->lf_A_a2d1->lf[0] = mask_sum(S, An, AJDK_2_1);
+    const int QR_TAnZtS = E->A_rbother && S.A_cbother && E->Z_rbother;
+    const int QR_TAnAtT = E->A_rbother && S.A_cbother;
+    if (QR_TAnZtS || QR_TAnAtT) {
+      for (int ns_j = 0; ns_j < (int)Tt->rpop_j; ++ns_j) {
+        const unsigned ns_a = St->m_a_[ns_j], ns_b = St->m_b_[ns_j];
+        const unsigned char *Tt_tag = Tt->wX + (long)ns_b * Tt->mc_length;
+        if (QR_TAnAtT)
+          for (int ma_j = 0; ma_j < (int)At->cpop_j; ++ma_j) {
+            const unsigned ma_a = An->m_a_[ma_j], ma_b = An->m_b_[ma_j];
+            *L1_get(E->lf_a1d1_AtTn, ns_j, ns_b, ns_a) += bget_pm(Tt_tag, ma_a) * (*L2_get(E->lf_An_ajdk, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1));
+          }
+        const unsigned char *St_tag = St->wX + (long)ns_b * St->mc_length;
+        if (QR_TAnZtS)
+          for (int mz_j = 0; mz_j < (int)Zt->cpop_j; ++mz_j) {
+            const unsigned mz_a = Zt->n_a_[mz_j], mz_b = Zt->n_b_[mz_j];
+            *L1_get(E->lf_a1d1_ZtSn, ns_j, ns_b, ns_a) += bget_pm(St_tag, mz_a) * (*L2_get(E->lf_Zn_ajdk, mz_j, mz_b, mz_a, 0, 0, AJDK_1_1));
+          }
+      }
+      for (int ns_j = 0; ns_j < (int)Tt->rpop_j; ++ns_j) {
+        const unsigned ns_a = St->m_a_[ns_j], ns_b = St->m_b_[ns_j];
+        if (QR_TAnAtT)
+          *L1_get(E->lf_et_Tn, ns_j, ns_b, ns_a) = (double)(-(long long)Tt->cpop_j + 2 * (long long)popcount_masked_row(Tt->wX + (long)ns_b * Tt->mc_length, Tt->mc_j, (long)Tt->mc_length));
+        if (QR_TAnZtS)
+          *L1_get(E->lf_et_Sn, ns_j, ns_b, ns_a) = (double)(-(long long)St->cpop_j + 2 * (long long)popcount_masked_row(St->wX + (long)ns_b * St->mc_length, St->mc_j, (long)St->mc_length));
+      }
+    }
+  }
+}
+
+// An_a0d1_ZtSn_excerpt (dir_c/An_ZtSn_ww.c:243-265): lf_ZtSn scaled by the
+// column weights D (AJDK_0_1), spacing b x b.
+void a0d1_excerpt(State &S, M_handle *Zt, M_handle *St, L_handle *lf_ZtSn, L_handle *out) {
+  out->spacing_row = SP_b; out->spacing_col = SP_b;
+  out->row_stride = Zt->rpop_b; out->col_stride = St->rpop_b;
+  lh_zero(out);
+  const int P = (int)psize(Zt->nrows);
+  for (int nz_j = 0; nz_j < (int)Zt->rpop_j; ++nz_j) {
+    const unsigned nz_a = Zt->m_a_[nz_j], nz_b = Zt->m_b_[nz_j];
+    for (int ns_j = 0; ns_j < (int)St->rpop_j; ++ns_j) {
+      const unsigned ns_a = St->m_a_[ns_j], ns_b = St->m_b_[ns_j];
+      *L2_get(out, nz_j, nz_b, nz_a, ns_j, ns_b, ns_a) =
+          S.A_ajdk[nz_a / POPLENGTH + AJDK_0_1 * P] * (*L2_get(lf_ZtSn, nz_j, nz_b, nz_a, ns_j, ns_b, ns_a));
+    }
+  }
+}
+
+void dcc_stage_1(State &S) {  // dcc_TAnZtS_ww_stage_1 (dir_c/TAnZtS.c:254-326)
+  for (auto &E : S.E) {
+    if (E->Z_rbother && S.A_cbother) a0d1_excerpt(S, E->M_Zt->p(), E->M_St->p(), E->lf_ZtSn, E->lf_a0d1_ZtSn);
+    if (E->A_rbother && S.A_cbother) a0d1_excerpt(S, E->M_At->p(), E->M_Tt->p(), E->lf_AtTn, E->lf_a0d1_AtTn);
+  }
+  int b_mlt = S.P.B_MLT;
+  for (auto &E : S.E) {
+    if (E->Z_rbother && S.A_cbother) {
+      M_handle *out = E->M_a0d1_ZtSn->p();
+      wrap_xcalc(TARGS, E->M_Zt->h.mr_j, E->M_Zt->h.mr_b, E->M_St->h.mr_j, E->M_St->h.mr_b, E->lf_a0d1_ZtSn,
+                 E->lf_a0d1_ZtSn->lf, &E->M_Zt->h.nrows, &E->M_St->h.nrows, &out, &b_mlt, 0);
+    }
+    if (E->A_rbother && S.A_cbother) {
+      M_handle *out = E->M_a0d1_AtTn->p();
+      wrap_xcalc(TARGS, E->M_At->h.mr_j, E->M_At->h.mr_b, E->M_Tt->h.mr_j, E->M_Tt->h.mr_b, E->lf_a0d1_AtTn,
+                 E->lf_a0d1_AtTn->lf, &E->M_At->h.nrows, &E->M_Tt->h.nrows, &out, &b_mlt, 0);
+    }
+  }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      for (L_handle *L : {F->lf_An_a0d1_ZtSn, F->lf_An_a0d1_AtTn}) {
+        L->row_stride = E1->A_nrows; L->spacing_row = SP_a; L->col_stride = S.T_ncols; L->spacing_col = SP_a; lh_zero(L);
+      }
+      if (E1->A_rbother && S.A_cbother && E2->Z_rbother)
+        wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->lf_a0d1_ZtSn, E2->M_a0d1_ZtSn->p(), E2->M_St->p(), &F->lf_An_a0d1_ZtSn);
+      if (E1->A_rbother && S.A_cbother && E2->A_rbother)
+        wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->lf_a0d1_AtTn, E2->M_a0d1_AtTn->p(), E2->M_Tt->p(), &F->lf_An_a0d1_AtTn);
+    }
+}
+
+void dcc_stage_2(State &S) {  // get_dcc_TAnZtS_ww_stage_2 (dir_c/TAnZtS.c:380-495), no Y blocks
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      for (L_handle *L : {F->lf_TAnZtS_ww, F->lf_TAnAtT_ww}) {
+        L->row_stride = E1->A_nrows; L->spacing_row = SP_a; L->col_stride = S.T_ncols; L->spacing_col = SP_a; lh_zero(L);
+      }
+      M_handle *An = E1->M_An->p(), *Tt = E1->M_Tt->p();
+      const int QR_TAnZtS = E1->A_rbother && S.A_cbother && E2->Z_rbother;
+      const int QR_TAnAtT = E1->A_rbother && S.A_cbother && E2->A_rbother;
+      const double A_a2d1 = E1->lf_A_a2d1->lf[0], A_a0d1 = E1->lf_A_a0d1->lf[0];
+      if (QR_TAnZtS || QR_TAnAtT)
+        for (int ns_j = 0; ns_j < (int)Tt->rpop_j; ++ns_j) {
+          const unsigned ns_a = Tt->m_a_[ns_j], ns_b = Tt->m_b_[ns_j];
+          if (QR_TAnZtS)
+            for (int ma_j = 0; ma_j < (int)An->rpop_j; ++ma_j) {
+              const unsigned ma_a = An->m_a_[ma_j], ma_b = An->m_b_[ma_j];
+              const double et = *L1_get(E2->lf_et_Sn, ns_j, ns_b, ns_a);
+              const double v = (*L2_get(F->lf_An_a0d1_ZtSn, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a)) -
+                               (*L1_get(E2->lf_a1d1_ZtSn, ns_j, ns_b, ns_a)) -
+                               (*L2_get(E1->lf_An_ajdk, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1)) * et + A_a2d1 * et;
+              *L2_get(F->lf_TAnZtS_ww, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += +v;
+            }
+          if (QR_TAnAtT)
+            for (int ma_j = 0; ma_j < (int)An->rpop_j; ++ma_j) {
+              const unsigned ma_a = An->m_a_[ma_j], ma_b = An->m_b_[ma_j];
+              const double et = *L1_get(E2->lf_et_Tn, ns_j, ns_b, ns_a);
+              const double v = (*L2_get(F->lf_An_a0d1_AtTn, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a)) -
+                               (*L1_get(E2->lf_a1d1_AtTn, ns_j, ns_b, ns_a)) -
+                               (*L2_get(E1->lf_An_ajdk, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1)) * et + A_a2d1 * et;
+              *L2_get(F->lf_TAnAtT_ww, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += +v;
+            }
+        }
+      if (QR_TAnAtT && nb1 == nb2)
+        for (int ns_j = 0; ns_j < (int)Tt->rpop_j; ++ns_j) {
+          const unsigned ns_a = Tt->m_a_[ns_j], ns_b = Tt->m_b_[ns_j];
+          const unsigned char *Tt_tag = Tt->wX + (long)ns_b * Tt->mc_length;
+          for (int ma_j = 0; ma_j < (int)An->rpop_j; ++ma_j) {
+            const unsigned ma_a = An->m_a_[ma_j], ma_b = An->m_b_[ma_j];
+            const double v = bget_pm(Tt_tag, ma_a) *
+                             (A_a0d1 - 2 * (*L2_get(E1->lf_An_ajdk, ma_j, ma_b, ma_a, 0, 0, AJDK_1_1)) + A_a2d1);
+            *L2_get(F->lf_TAnAtT_ww, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) += -v;
+          }
+        }
+    }
+}
+
+// get_dcc_halfloop (dir_c/dcc_lf.c:379-488): the row and column loop scores,
+// covariates turned from spacing a to spacing b.
+void dcc_halfloop(State &S) {
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      M_handle *An = E1->M_An->p(), *At = E1->M_At->p(), *Tt2 = E2->M_Tt->p();
+      for (L_handle *L : {F->QR_AnZtSZnAt, F->QR_AnAtTAnAt}) {
+        L->row_stride = At->ncols; L->spacing_row = SP_a; L->col_stride = S.T_ncols; L->spacing_col = SP_b; lh_zero(L);
+      }
+      for (L_handle *L : {F->QC_AtTAnZtSZn, F->QC_AtTAnAtTAn}) {
+        L->row_stride = At->nrows; L->spacing_row = SP_a; L->col_stride = S.T_ncols; L->spacing_col = SP_b; lh_zero(L);
+      }
+      const int ZS = E1->A_rbother && S.A_cbother && E2->Z_rbother;
+      const int AT = E1->A_rbother && S.A_cbother && E2->A_rbother;
+      if (ZS || AT)
+        for (int ns_j = 0; ns_j < (int)Tt2->rpop_j; ++ns_j) {
+          const unsigned ns_a = Tt2->m_a_[ns_j], ns_b = Tt2->m_b_[ns_j];
+          for (int ma_j = 0; ma_j < (int)An->rpop_j; ++ma_j) {
+            const unsigned ma_a = An->m_a_[ma_j], ma_b = An->m_b_[ma_j];
+            if (ZS) *L2_get(F->QR_AnZtSZnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) = *L2_get(F->lf_TAnZtS_ww, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a);
+            if (AT) *L2_get(F->QR_AnAtTAnAt, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a) = *L2_get(F->lf_TAnAtT_ww, ma_j, ma_b, ma_a, ns_j, ns_b, ns_a);
+          }
+          for (int na_j = 0; na_j < (int)At->rpop_j; ++na_j) {
+            const unsigned na_a = At->m_a_[na_j], na_b = At->m_b_[na_j];
+            if (ZS) *L2_get(F->QC_AtTAnZtSZn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = *L2_get(F->lf_D_AtTn_ZtSn_vv, na_j, na_b, na_a, ns_j, ns_b, ns_a);
+            if (AT) *L2_get(F->QC_AtTAnAtTAn, na_j, na_b, na_a, ns_j, ns_b, ns_a) = *L2_get(F->lf_D_AtTn_AtTn_vv, na_j, na_b, na_a, ns_j, ns_b, ns_a);
+          }
+        }
+    }
+}
+
+// dexcluster_driver.c:22-28 / :43-47: every step's sub-scores.
+void dcc_subscores(State &S) {
+  An_ajdk_all(S); trace_stage(S, "An_ajdk");
+  lf_ZtSn_all(S); trace_stage(S, "lf_ZtSn");
+  dcc_D_AtTn_ZtSn_all(S); trace_stage(S, "D_AtTn_ZtSn");
+  dcc_stage_0(S); dcc_stage_1(S); dcc_stage_2(S); trace_stage(S, "TAnZtS");
+  dcc_halfloop(S); trace_stage(S, "halfloop");
+}
+
 }  // namespace
 
 namespace {
@@ -2374,6 +2647,39 @@ int scorebox(const Params &P, const Input &I, ScoreboxOutput &SO, std::string &e
         record(*Sub, rows_inner ? j : k, rows_inner ? k : j);
       }
     }
+  }
+  return 0;
+}
+
+// dexcluster_driver (dir_c/dexcluster_driver.c:5-57): the dcc method on the
+// same inputs and outputs as the bcc solve.
+int dcc_solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks) {
+  if (P.B_MLT < 1 || P.B_MLT > 62) { err = "B_MLT out of range"; return 4; }
+  State S;
+  S.P = P;
+  S.hooks = hooks;
+  S.out = &O;
+  g_clock = StageClock();
+  O = Output();
+  int rc = load(S, I, err);
+  if (rc) return rc;
+  if ((rc = stop_requested(err))) return rc;
+  M_mxset_all(S);
+  trace_stage(S, "load");
+  dcc_subscores(S);
+  while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {
+    if ((rc = stop_requested(err))) return rc;
+    sumscores_nrm(S);
+    sumscores_ifT(S);
+    if (S.P.Ireq > 0) sumscores_srt(S);
+    sumscores_cmb(S);
+    sumscores_xij(S);
+    sumscores_mxA(S);
+    trace_stage(S, "sumscores");
+    lrup_mxdup(S);
+    M_mxset_all(S);
+    dcc_subscores(S);
+    if (O.iterations > 10000000) { err = "iteration limit"; return 5; }
   }
   return 0;
 }

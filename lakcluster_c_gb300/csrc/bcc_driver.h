@@ -110,6 +110,8 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err);
 int make_output_dir(const std::string &dir);
 // Run the solve.  Returns 0 on success.
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks = nullptr);
+// Run the dexcluster method (GLOBAL_TEST_TYPE dexcluster_driver) instead.
+int dcc_solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks = nullptr);
 // Run the scorebox (GLOBAL_TEST_TYPE lakcluster_scorebox) over I.scorebox_xdrop.
 int scorebox(const Params &P, const Input &I, ScoreboxOutput &SO, std::string &err, const Hooks *hooks = nullptr);
 // Write its five .mda arrays into dir (names as S_handle_dmp writes them).

@@ -215,8 +215,9 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     P.test_type = test_type;
     return 0;
   }
-  if (!test_type.empty() && test_type != "lakcluster_driver" && test_type != "lakcluster_scorebox") {
-    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc driver, its scorebox or bed_to_b16";
+  if (!test_type.empty() && test_type != "lakcluster_driver" && test_type != "lakcluster_scorebox" &&
+      test_type != "dexcluster_driver") {
+    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc driver, its scorebox, dexcluster_driver or bed_to_b16";
     return 3;
   }
   P.test_type = test_type.empty() ? "lakcluster_driver" : test_type;

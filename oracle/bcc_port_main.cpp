@@ -33,7 +33,7 @@ int main(int argc, char **argv) {
     }
     return 0;
   }
-  rc = lakbcc::solve(P, I, O, err);
+  rc = P.test_type == "dexcluster_driver" ? lakbcc::dcc_solve(P, I, O, err) : lakbcc::solve(P, I, O, err);
   if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
   if (lakbcc::make_output_dir(P.dir_name) || lakbcc::write_outputs(P.dir_name, O)) {
     fprintf(stderr, "error: cannot write outputs into %s\n", P.dir_name.c_str());

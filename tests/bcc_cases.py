@@ -291,3 +291,21 @@ def solve_arrays(lib, d):
                    Ireq=d.get("Ireq") or 0, T_bins=d.get("T"), S_bins=d.get("S"),
                    kappa_squared=d.get("kappa_squared") or 0.0, qc_strategy=d.get("qc", "YnWt"), lib=lib)
     return p.solve()
+
+
+# --- dexcluster (GLOBAL_TEST_TYPE dexcluster_driver) -------------------------------
+# The dcc method on case/control inputs of the bcc cases (the case-only input
+# is left out: without controls the reference reads past an empty buffer).
+DCC_CASES = ["case_control_2bin_300x250x2100", "case_control_1bin_gamma_lin", "case_control_2bin_masked",
+             "case_control_3bin_ragged", "case_control_3bin_Ireq1", "case_control_2bin_Ireq2",
+             "case_control_2bin_T3_kappa", "case_control_3bin_T2_kappa_Ireq1"]
+DCC_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dcc_traces.npz")
+
+
+def write_dcc_case(name, in_dir, out_dir, fname="bcc.in"):
+    return write_case(name, in_dir, out_dir, fname, extra_statements=(("GLOBAL_TEST_TYPE", "dexcluster_driver"),))
+
+
+def load_dcc_golden():
+    z = np.load(DCC_GOLDEN, allow_pickle=False)
+    return {n: {k: [str(s) for s in z[n + "/" + k]] for k in ("trace", "xdrop_a", "xdrop_b")} for n in DCC_CASES}

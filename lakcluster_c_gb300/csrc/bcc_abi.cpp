@@ -190,7 +190,7 @@ extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
     return pipeline_status();
   }
   lakgb_set_d_mlt(P.D_MLT);
-  if (P.test_type == "lakcluster_scorebox") {  // lakcluster_ver18.c:338
+  if (P.test_type == "lakcluster_scorebox" || P.test_type == "dexcluster_scorebox") {  // lakcluster_ver18.c:338
     lakbcc::ScoreboxOutput SO;
     rc = lakbcc::scorebox(P, I, SO, g_err, &kHooks);
     if (rc) return rc;

@@ -367,7 +367,7 @@ std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows
 
 // GLOBAL_TEST_TYPE dexcluster_driver: the dcc method (dir_c/dexcluster_driver.c)
 // on the same state.
-bool dcc_mode(const Params &P) { return P.test_type == "dexcluster_driver"; }
+bool dcc_mode(const Params &P) { return P.test_type.rfind("dexcluster", 0) == 0; }
 
 // n1b_cap / n2b_cap (default n1b / n2b): the largest counts the planes must
 // hold, when more rows can be removed in one step than the transposition
@@ -2210,16 +2210,27 @@ void scorebox_scores(State &S) {  // the scoring tail of lakcluster_scorebox_exc
   scorebox_svalue(S);
 }
 
+void dcc_subscores(State &S);
+
 // lakcluster_scorebox_excerpt_1 (lakcluster_scorebox.c:22-52): the loop
-// subscores computed directly.
+// subscores computed directly; for dexcluster its sub-scores
+// (dexcluster_scorebox_excerpt_1, dir_c/dexcluster_scorebox.c:21-43).
 void scorebox_full(State &S) {
-  initial_subscores(S);
+  if (dcc_mode(S.P)) dcc_subscores(S);
+  else initial_subscores(S);
   scorebox_scores(S);
 }
 
 // lakcluster_scorebox_excerpt_2 (lakcluster_scorebox.c:54-101): the loop
 // subscores after a removal, by the low-rank update of the elimination loop.
 void scorebox_update(State &S) {
+  if (dcc_mode(S.P)) {  // dexcluster_scorebox_excerpt_2 (dir_c/dexcluster_scorebox.c:45-65): recomputed
+    lrup_mxdup(S);
+    M_mxset_all(S);
+    dcc_subscores(S);
+    scorebox_scores(S);
+    return;
+  }
   lrup_QR(S);
   lrup_QC_ZtSWn(S);
   if (qc_ynwt(S)) lrup_QC(S);
@@ -2572,10 +2583,10 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
 // a second state loaded from the same inputs, which reaches the same values
 // bit for bit.
 int scorebox(const Params &P, const Input &I, ScoreboxOutput &SO, std::string &err, const Hooks *hooks) {
-  if (P.QR_strategy.find("YnWt") == std::string::npos || P.QR_strategy.find("condense") != std::string::npos ||
+  if (!dcc_mode(P) && (P.QR_strategy.find("YnWt") == std::string::npos || P.QR_strategy.find("condense") != std::string::npos ||
       P.QR_strategy.find("ZtSWn") != std::string::npos ||
       (P.QC_strategy.find("YnWt") == std::string::npos && P.QC_strategy.find("ZtSWn") == std::string::npos) ||
-      P.QC_strategy.find("store one") != std::string::npos) {
+      P.QC_strategy.find("store one") != std::string::npos)) {
     err = "supported strategies: rows YnWt; columns YnWt and / or ZtSWn (no condense / store one)";
     return 4;
   }
@@ -2665,6 +2676,11 @@ int dcc_solve(const Params &P, const Input &I, Output &O, std::string &err, cons
   if (rc) return rc;
   if ((rc = stop_requested(err))) return rc;
   M_mxset_all(S);
+  // wrap_dcc_scramble (dir_c/R_init.c:134-160): bcc_scramble on the dcc
+  // state; its .b16 snapshots are written only when its (fixed-off) verbose
+  // flag is set, so none are written here
+  for (const auto &sc : I.scramble)
+    if ((rc = scramble(S, sc, err))) return rc;
   trace_stage(S, "load");
   dcc_subscores(S);
   while (S.A_rpop_j_total > 0 || S.A_cpop_j > 0) {

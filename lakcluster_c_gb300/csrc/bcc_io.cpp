@@ -216,8 +216,8 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     return 0;
   }
   if (!test_type.empty() && test_type != "lakcluster_driver" && test_type != "lakcluster_scorebox" &&
-      test_type != "dexcluster_driver") {
-    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc driver, its scorebox, dexcluster_driver or bed_to_b16";
+      test_type != "dexcluster_driver" && test_type != "dexcluster_scorebox") {
+    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc or dexcluster driver or scorebox, or bed_to_b16";
     return 3;
   }
   P.test_type = test_type.empty() ? "lakcluster_driver" : test_type;
@@ -243,7 +243,7 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
   if (nbins <= 0 || (int)A_t.size() < nbins) { err = "GLOBAL_NBINS and GLOBAL_A_t_name_ must name one file per bin"; return 2; }
   P.nbins = nbins;
   I = Input();
-  if (P.test_type == "lakcluster_scorebox") {
+  if (P.test_type == "lakcluster_scorebox" || P.test_type == "dexcluster_scorebox") {
     if (scorebox_xdrop.empty()) { err = "GLOBAL_scorebox_out_xdrop is not set"; return 2; }
     if (int rc = read_xdrop(scorebox_xdrop, I.scorebox_xdrop, err)) return rc;
   } else if (scramble_num > 0) {

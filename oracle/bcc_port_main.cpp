@@ -23,7 +23,7 @@ int main(int argc, char **argv) {
   if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }
   if (argc > 2) lako_set_threads(atoi(argv[2]));
   lako_set_d_mlt(P.D_MLT);
-  if (P.test_type == "lakcluster_scorebox") {
+  if (P.test_type == "lakcluster_scorebox" || P.test_type == "dexcluster_scorebox") {
     lakbcc::ScoreboxOutput SO;
     rc = lakbcc::scorebox(P, I, SO, err);
     if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }

@@ -55,7 +55,7 @@ int main(int argc, char **argv) {
   if (lakref_init(mb ? atoll(mb) : 4096, 1, 0)) { fprintf(stderr, "error: arena\n"); return 1; }
   GLOBAL_D_MLT = P.D_MLT;
   GLOBAL_B_MLT = P.B_MLT;
-  if (P.test_type == "lakcluster_scorebox") {
+  if (P.test_type == "lakcluster_scorebox" || P.test_type == "dexcluster_scorebox") {
     lakbcc::ScoreboxOutput SO;
     rc = lakbcc::scorebox(P, I, SO, err);
     if (rc) { fprintf(stderr, "error: %s\n", err.c_str()); return rc; }

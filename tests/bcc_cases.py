@@ -151,22 +151,26 @@ def scramble_xdrop_lines(xdrop_a, rows, cols):
 
 
 def write_scorebox_case(key, xdrop_a, in_dir, out_dir, fname="bcc.in"):
-    """The .in of scorebox `key` over the solve order xdrop_a (text lines);
-    the order is written to in_dir/scorebox_xdrop.txt."""
-    name, (rmax, rnum, cmax, cnum) = SCOREBOX[key]
+    """The .in of scorebox `key` (of SCOREBOX or DCC_SCOREBOX) over the solve
+    order xdrop_a (text lines); the order is written to
+    in_dir/scorebox_xdrop.txt."""
+    dcc = key in DCC_SCOREBOX
+    name, (rmax, rnum, cmax, cnum) = (DCC_SCOREBOX if dcc else SCOREBOX)[key]
     os.makedirs(in_dir, exist_ok=True)
     xp = os.path.abspath(os.path.join(in_dir, "scorebox_xdrop.txt"))
     with open(xp, "w") as f:
         f.write("\n".join(xdrop_a) + "\n")
     return write_case(name, in_dir, out_dir, fname, extra_statements=(
-        ("GLOBAL_TEST_TYPE", "lakcluster_scorebox"), ("GLOBAL_scorebox_out_xdrop", xp),
+        ("GLOBAL_TEST_TYPE", "dexcluster_scorebox" if dcc else "lakcluster_scorebox"), ("GLOBAL_scorebox_out_xdrop", xp),
         ("GLOBAL_scorebox_row_max", rmax), ("GLOBAL_scorebox_row_num", rnum),
         ("GLOBAL_scorebox_col_max", cmax), ("GLOBAL_scorebox_col_num", cnum)))
 
 
 def write_scramble_case(key, xdrop_a, in_dir, out_dir, fname="bcc.in"):
-    """The .in of scramble `key`, its out_xdrop files cut from xdrop_a."""
-    name, specs = SCRAMBLE[key]
+    """The .in of scramble `key` (of SCRAMBLE or DCC_SCRAMBLE), its out_xdrop
+    files cut from xdrop_a."""
+    dcc = key in DCC_SCRAMBLE
+    name, specs = (DCC_SCRAMBLE if dcc else SCRAMBLE)[key]
     os.makedirs(in_dir, exist_ok=True)
     files, seeds = [], []
     for i, (rows, cols, seed) in enumerate(specs):
@@ -176,7 +180,7 @@ def write_scramble_case(key, xdrop_a, in_dir, out_dir, fname="bcc.in"):
         files.append(xp)
         seeds.append(str(seed))
     return write_case(name, in_dir, out_dir, fname, extra_statements=(
-        ("GLOBAL_scramble_num", len(specs)), ("GLOBAL_scramble_out_xdrop_", ",".join(files)),
+        ("GLOBAL_TEST_TYPE", "dexcluster_driver" if dcc else "lakcluster_driver"), ("GLOBAL_scramble_num", len(specs)), ("GLOBAL_scramble_out_xdrop_", ",".join(files)),
         ("GLOBAL_scramble_rseed_", ",".join(seeds))))
 
 
@@ -309,3 +313,23 @@ def write_dcc_case(name, in_dir, out_dir, fname="bcc.in"):
 def load_dcc_golden():
     z = np.load(DCC_GOLDEN, allow_pickle=False)
     return {n: {k: [str(s) for s in z[n + "/" + k]] for k in ("trace", "xdrop_a", "xdrop_b")} for n in DCC_CASES}
+
+# dexcluster scorebox (dexcluster_scorebox, dir_c/dexcluster_scorebox.c) and
+# scramble (wrap_dcc_scramble), over the dexcluster solve orders
+DCC_SCOREBOX = {
+    "dsb_2bin_cr": ("case_control_2bin_300x250x2100", (20, 3, 200, 3)),
+    "dsb_3bin_Ireq1_rc": ("case_control_3bin_Ireq1", (45, 4, 40, 3)),
+    "dsb_2bin_T3_kappa_cr": ("case_control_2bin_T3_kappa", (30, 4, 300, 3)),
+}
+DCC_SCRAMBLE = {
+    "dscr_2bin": ("case_control_2bin_300x250x2100", [(40, 200, 5)]),
+    "dscr_3bin_ragged": ("case_control_3bin_ragged", [(30, 150, 3), (12, 40, 8)]),
+}
+
+
+def load_dcc_extra_golden():
+    z = np.load(DCC_GOLDEN, allow_pickle=False)
+    sb = {k: {a: z["%s/%s" % (k, a)] for a in SCOREBOX_ARRAYS} for k in DCC_SCOREBOX}
+    scr = {k: {key: [str(s) for s in z["%s/%s" % (k, key)]] for key in ("trace", "xdrop_a", "xdrop_b", "b16_sha1")}
+           for k in DCC_SCRAMBLE}
+    return sb, scr

@@ -1829,87 +1829,89 @@ void lrup_mxdup(State &S) {  // bcc_lrup_mxdup (bcc_lrup.c:1128-1138)
   }
 }
 
-// L2_clean (L_init.c:287-326)
-void L2_clean(L_handle *L, unsigned long long nrows, const unsigned char *mr_b, const unsigned char *mr_j,
-              unsigned long long ncols, const unsigned char *mc_b, const unsigned char *mc_j) {
-  unsigned long long nc_j = 0, nc_b = 0;
-  for (unsigned long long nc_a = 0; nc_a < ncols; ++nc_a) {
-    if (bget_on(mc_b, (long)nc_a)) {
-      if (bget_on(mc_j, (long)nc_a)) {
-        const unsigned long long tab_c = pick(L->spacing_col, nc_j, nc_b, nc_a);
-        unsigned long long nr_j = 0, nr_b = 0;
-        for (unsigned long long nr_a = 0; nr_a < nrows; ++nr_a) {
-          if (bget_on(mr_b, (long)nr_a)) {
-            if (bget_on(mr_j, (long)nr_a)) {
-              nr_j++;
-            } else {
-              const unsigned long long tab_r = pick(L->spacing_row, nr_j, nr_b, nr_a);
-              if (L->spacing_row == SP_b || L->spacing_row == SP_a) L->lf[tab_r + tab_c * L->row_stride] = 0;
-            }
-            nr_b++;
-          } else {
-            const unsigned long long tab_r = pick(L->spacing_row, nr_j, nr_b, nr_a);
-            if (L->spacing_row == SP_a) L->lf[tab_r + tab_c * L->row_stride] = 0;
-          }
-        }
-        nc_j++;
+// The indices of a mask pair as L2_clean / LL2_plustimes walk them: for each
+// index a in [0, n), in order, its j / b / a positions, split into those in
+// both masks (kept), in mc_b only (b_not_j) and outside mc_b (not_b).
+struct MaskWalk {
+  std::vector<unsigned long long> kj, kb, ka, bj, bb, ba, nj, nb_, na;
+  MaskWalk(unsigned long long n, const unsigned char *mb, const unsigned char *mj) {
+    unsigned long long j = 0, b = 0;
+    for (unsigned long long a = 0; a < n; ++a) {
+      if (bget_on(mb, (long)a)) {
+        if (bget_on(mj, (long)a)) { kj.push_back(j); kb.push_back(b); ka.push_back(a); ++j; }
+        else { bj.push_back(j); bb.push_back(b); ba.push_back(a); }
+        ++b;
       } else {
-        const unsigned long long tab_c = pick(L->spacing_col, nc_j, nc_b, nc_a);
-        if (L->spacing_col == SP_b || L->spacing_col == SP_a)
-          for (unsigned long long r = 0; r < L->row_stride; ++r) L->lf[r + tab_c * L->row_stride] = 0;
+        nj.push_back(j); nb_.push_back(b); na.push_back(a);
       }
-      nc_b++;
-    } else {
-      const unsigned long long tab_c = pick(L->spacing_col, nc_j, nc_b, nc_a);
-      if (L->spacing_col == SP_a)
-        for (unsigned long long r = 0; r < L->row_stride; ++r) L->lf[r + tab_c * L->row_stride] = 0;
     }
   }
-}
+  // the kept indices in the given spacing
+  const unsigned long long *kept(int spacing) const {
+    return spacing == SP_j ? kj.data() : spacing == SP_b ? kb.data() : ka.data();
+  }
+};
 
-// LL2_plustimesequals (L_init.c:328-358)
-void LL2_plustimes(L_handle *LA, L_handle *LB, double dtmp, unsigned long long nrows, const unsigned char *mr_b,
-                   const unsigned char *mr_j, unsigned long long ncols, const unsigned char *mc_b,
-                   const unsigned char *mc_j) {
-  unsigned long long nc_j = 0, nc_b = 0;
-  for (unsigned long long nc_a = 0; nc_a < ncols; ++nc_a) {
-    if (bget_on(mc_b, (long)nc_a)) {
-      if (bget_on(mc_j, (long)nc_a)) {
-        unsigned long long nr_j = 0, nr_b = 0;
-        for (unsigned long long nr_a = 0; nr_a < nrows; ++nr_a) {
-          if (bget_on(mr_b, (long)nr_a)) {
-            if (bget_on(mr_j, (long)nr_a)) {
-              *L2_get(LA, nr_j, nr_b, nr_a, nc_j, nc_b, nc_a) += dtmp * (*L2_get(LB, nr_j, nr_b, nr_a, nc_j, nc_b, nc_a));
-              nr_j++;
-            }
-            nr_b++;
-          }
-        }
-        nc_j++;
-      }
-      nc_b++;
+// bcc_lrup_QC_YnWt_stage_c (bcc_lrup.c:592-655): L2_clean and the
+// LL2_plustimes subtractions of each column product, on index lists built
+// once per call from the masks.  Each element sees the same operations in
+// the same order as the element-by-element walk (its clearing, then the
+// subtractions in list order), so the results are identical.
+void stage_c_update(L_handle *LA, std::initializer_list<L_handle *> LBs, const MaskWalk &R, const MaskWalk &Cw) {
+  const unsigned long long rs = LA->row_stride;
+  // L2_clean (L_init.c:287-326)
+  const int sr = LA->spacing_row, sc = LA->spacing_col;
+  for (size_t c = 0; c < Cw.ka.size(); ++c) {
+    const unsigned long long tc = pick(sc, Cw.kj[c], Cw.kb[c], Cw.ka[c]) * rs;
+    if (sr == SP_b || sr == SP_a)
+      for (size_t r = 0; r < R.ba.size(); ++r) LA->lf[pick(sr, R.bj[r], R.bb[r], R.ba[r]) + tc] = 0;
+    if (sr == SP_a)
+      for (size_t r = 0; r < R.na.size(); ++r) LA->lf[R.na[r] + tc] = 0;
+  }
+  if (sc == SP_b || sc == SP_a)
+    for (size_t c = 0; c < Cw.ba.size(); ++c) {
+      const unsigned long long tc = pick(sc, Cw.bj[c], Cw.bb[c], Cw.ba[c]) * rs;
+      for (unsigned long long r = 0; r < rs; ++r) LA->lf[r + tc] = 0;
+    }
+  if (sc == SP_a)
+    for (size_t c = 0; c < Cw.na.size(); ++c)
+      for (unsigned long long r = 0; r < rs; ++r) LA->lf[r + Cw.na[c] * rs] = 0;
+  // LL2_plustimesequals with multiplier -1 (L_init.c:328-358), all sources
+  // of one element in turn
+  const size_t nlb = LBs.size();
+  std::vector<const double *> base(nlb);
+  std::vector<const unsigned long long *> rsel(nlb);
+  std::vector<unsigned long long> lrs(nlb);
+  const unsigned long long *rA = R.kept(sr);
+  for (size_t c = 0; c < Cw.ka.size(); ++c) {
+    double *colA = LA->lf + pick(sc, Cw.kj[c], Cw.kb[c], Cw.ka[c]) * rs;
+    size_t k = 0;
+    for (L_handle *LB : LBs) {
+      base[k] = LB->lf + pick(LB->spacing_col, Cw.kj[c], Cw.kb[c], Cw.ka[c]) * LB->row_stride;
+      rsel[k] = R.kept(LB->spacing_row);
+      ++k;
+    }
+    for (size_t r = 0; r < R.ka.size(); ++r) {
+      double v = colA[rA[r]];
+      for (size_t q = 0; q < nlb; ++q) v += -1.0 * base[q][rsel[q][r]];
+      colA[rA[r]] = v;
     }
   }
 }
 
 void lrup_QC_stage_c(State &S) {  // bcc_lrup_QC_YnWt_stage_c (bcc_lrup.c:592-655)
-  const unsigned char *Ab = S.A_bmc_b.data(), *Ar = S.A_bmc_j_rtn.data(), *Tb = S.T_bmc_b.data(), *Tj = S.T_bmc_j.data();
-  const unsigned long long AC = S.A_ncols, T = S.T_ncols;
+  const MaskWalk R(S.A_ncols, S.A_bmc_b.data(), S.A_bmc_j_rtn.data()), Cw(S.T_ncols, S.T_bmc_b.data(), S.T_bmc_j.data());
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
       Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
-      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) {
-        L2_clean(F->lf_At_T_AnZt_S_Zn, AC, Ab, Ar, T, Tb, Tj);
-        for (L_handle *LB : {F->lf_attjn____vtszn, F->lf_kt_r_knzt_s_zn, F->lf_kt_r_hnvt_s_zn})
-          LL2_plustimes(F->lf_At_T_AnZt_S_Zn, LB, -1.0, AC, Ab, Ar, T, Tb, Tj);
-      }
-      if (S.A_cbother && E1->A_rbother && E2->A_rbother) {
-        L2_clean(F->lf_At_T_AnAt_T_An, AC, Ab, Ar, T, Tb, Tj);
-        for (L_handle *LB : {F->lf_attjn____jttan, F->lf_attjn____htrkn, F->lf_ktrhn____jttan, F->lf_ktrhn____htrkn,
-                             F->lf_at_t_ankt_r_kn, F->lf_kt_r_knat_t_an, F->lf_kt_r_knkt_r_kn})
-          LL2_plustimes(F->lf_At_T_AnAt_T_An, LB, -1.0, AC, Ab, Ar, T, Tb, Tj);
-      }
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother)
+        stage_c_update(F->lf_At_T_AnZt_S_Zn, {F->lf_attjn____vtszn, F->lf_kt_r_knzt_s_zn, F->lf_kt_r_hnvt_s_zn}, R, Cw);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother)
+        stage_c_update(F->lf_At_T_AnAt_T_An,
+                       {F->lf_attjn____jttan, F->lf_attjn____htrkn, F->lf_ktrhn____jttan, F->lf_ktrhn____htrkn,
+                        F->lf_at_t_ankt_r_kn, F->lf_kt_r_knat_t_an, F->lf_kt_r_knkt_r_kn},
+                       R, Cw);
     }
 }
 

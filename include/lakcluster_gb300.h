@@ -203,6 +203,28 @@ int wrap_An_ZtSWn_Yt_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int s
                              struct M_handle *M_Wt, struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk,
                              struct L_handle **output_An_ZtSWn_Yt_ww_p);
 
+/* Dense FP64 copy of the retained entries of a bit matrix whose rows are SNPs
+ * (At): (b - a_k) * sqrt(d_k), b = +1/-1 (TYPE_pm) or 1/0 (TYPE_00) and a_k,
+ * d_k the A_ajdk terms of row k's SNP, or b alone when A_ajdk is NULL; rows
+ * at output_spacing_r, columns at output_spacing_c; the whole output handle
+ * is zeroed first.  Replaces wrap_M_At_to_L2_run, dir_c/M_Ax_to_L2.c:282
+ * (kernel :137-280); used by the condense row strategy. */
+int wrap_M_At_to_L2_run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag, int output_spacing_r,
+                        int output_spacing_c, struct M_handle *M_At, double *A_ajdk, struct L_handle **output_L_p);
+
+/* The same with SNPs as columns (An; a_k, d_k of column k's SNP).  Replaces
+ * wrap_M_An_to_L2_run, dir_c/M_Ax_to_L2.c:102 (kernel :5-100). */
+int wrap_M_An_to_L2_run(int *tidx, void **vpra, pthread_t *thread_in, int type_flag, int output_spacing_r,
+                        int output_spacing_c, struct M_handle *M_An, double *A_ajdk, struct L_handle **output_L_p);
+
+/* FP64 product of two dense L_handles, C(i,j) = sum_k At(k,i) * Zt(k,j) over
+ * At's row_stride values of k, each element one sum from +0 in ascending k
+ * with the product and the sum rounded once (the order of the GSL CBLAS dgemm
+ * the reference links).  Output rows follow At's column spacing, columns Zt's.
+ * Replaces wrap_AnZt_mm__run, dir_c/AnZt_mm.c:86 (kernel :6-84). */
+int wrap_AnZt_mm__run(int *tidx, void **vpra, pthread_t *thread_in, struct L_handle *lf_At, struct L_handle *lf_Zt,
+                      struct L_handle **output_AnZt_p);
+
 /* ---------------------------------------------------------------------------
  * Input pipeline: PLINK .bed to .b16 (bed_to_b16, dir_c/bed_to_b16.c:711-1355).
  * ------------------------------------------------------------------------- */
@@ -291,7 +313,9 @@ struct lakgb_bcc_problem {
   int T_ncols;       /* covariate columns of the bins' T_rows / S_rows (GLOBAL_T_n_cols) */
   double kappa_squared;  /* GLOBAL_kappa_squared: > 0 turns on the MDS correction
                             of the covariate columns (bcc_sumscores_ifT) */
-  const char *QC_strategy;  /* GLOBAL_QC_strategy: "YnWt" (NULL), "ZtSWn", or both */
+  const char *QC_strategy;  /* GLOBAL_QC_strategy: "YnWt" (NULL), "ZtSWn", or both;
+                               "YnWt store one" is accepted (same results as "YnWt") */
+  const char *QR_strategy;  /* GLOBAL_QR_strategy: "YnWt" (NULL) or "YnWt condense" */
 };
 /* trace: 6 values per iteration (iteration, rows left, columns left, mean row
  * score, mean column score, bins with rows); xdrop_a / xdrop_b: 2 ints per

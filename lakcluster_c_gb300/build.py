@@ -22,7 +22,7 @@ LIB = os.path.join(HERE, "liblakgb300.so")
 
 CU_SOURCES = ["lakgb_runtime.cu", "gram.cu", "gram_tc.cu", "rowvec.cu", "abi_kernels.cu", "xcalc.cu", "bitplane.cu",
               "bitplane_tc.cu", "loopsum.cu", "lmirror.cu",
-              "vv_kernels.cu", "transpose.cu", "bed.cu"]
+              "vv_kernels.cu", "transpose.cu", "bed.cu", "condense.cu"]
 # Host-only translation units (the solve driver and its input reader).
 CPP_SOURCES = ["bcc_model.cpp", "bcc_driver.cpp", "bcc_io.cpp", "bcc_abi.cpp", "bcc_server.cpp"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-pthread", "-I" + os.path.join(ROOT, "include")]

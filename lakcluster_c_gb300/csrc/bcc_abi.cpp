@@ -100,6 +100,7 @@ extern "C" int lakgb_bcc_solve(const struct lakgb_bcc_problem *prob, struct lakg
   P.Ireq = prob->Ireq;
   P.kappa_squared = prob->kappa_squared;
   if (prob->QC_strategy) P.QC_strategy = prob->QC_strategy;
+  if (prob->QR_strategy) P.QR_strategy = prob->QR_strategy;
   lakbcc::Input I;
   I.ncols = prob->ncols;
   I.T_ncols = prob->T_ncols > 0 ? prob->T_ncols : 1;  // 0: the default single column

@@ -78,6 +78,8 @@ struct Single {
   L_handle *lf_At_rsum = nullptr, *lf_Zt_rsum = nullptr;
   L_handle *lf_An_ajdk = nullptr, *lf_Zn_ajdk = nullptr, *lf_AtTn = nullptr, *lf_ZtSn = nullptr;
   L_handle *lf_jn_ajdk = nullptr, *lf_vn_ajdk = nullptr, *lf_kn_ajdk = nullptr, *lf_zn_ajdk = nullptr;
+  // dense removed columns of the condense row strategy (SNPs x rows)
+  L_handle *lf_jn = nullptr, *lf_vn = nullptr;
   L_handle *lf_hn_ajdk = nullptr, *lf_an_ajdk = nullptr;
   L_handle *lf_attn = nullptr, *lf_jttn = nullptr, *lf_ktrn = nullptr, *lf_htrn = nullptr;
   L_handle *lf_ztsn = nullptr, *lf_vtsn = nullptr, *lf_ztsvn = nullptr, *lf_attjn = nullptr, *lf_ktrhn = nullptr;
@@ -369,6 +371,21 @@ std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows
 // on the same state.
 bool dcc_mode(const Params &P) { return P.test_type.rfind("dexcluster", 0) == 0; }
 
+// GLOBAL_QR_strategy / GLOBAL_QC_strategy (substrings, as the reference tests
+// them with strstr).  Rows: "YnWt", optionally "condense" (lrup_QR_condense).
+// Columns: "YnWt" and / or "ZtSWn"; "store one" loops the covariates one at a
+// time through one-covariate forms of the same products (AttYn_vv,
+// AttYn____WtsZn_vv, bcc_lrup.c:483-590) to save host memory: each product
+// element is the same sum in the same order as in "store all", so the
+// store-all stages give its results and it needs nothing else here.
+bool qr_condense(const Params &P) { return P.QR_strategy.find("condense") != std::string::npos; }
+bool strategies_supported(const Params &P) {
+  return P.QR_strategy.find("YnWt") != std::string::npos && P.QR_strategy.find("ZtSWn") == std::string::npos &&
+         (P.QC_strategy.find("YnWt") != std::string::npos || P.QC_strategy.find("ZtSWn") != std::string::npos);
+}
+const char *const kStrategyError =
+    "supported strategies: rows YnWt (optionally condense); columns YnWt and / or ZtSWn";
+
 // n1b_cap / n2b_cap (default n1b / n2b): the largest counts the planes must
 // hold, when more rows can be removed in one step than the transposition
 // flag was chosen for.
@@ -542,6 +559,20 @@ int load(State &S, const Input &I, std::string &err) {
       E->lf_ztsvn = lh_make(E->Z_rbother ? n : 0);
       E->lf_attjn = lh_make(E->A_rbother ? n : 0);
       E->lf_ktrhn = lh_make(E->A_rbother ? n : 0);
+    }
+  }
+  // bcc_single_init_lf (bcc.c:750-761, "condense"): the removed columns as
+  // dense matrices, up to cdrop SNPs x the bin's rows
+  if (qr_condense(P)) {
+    int cdrop = 0;
+    get_xdrop(P, (double)S.A_rpop_j_total, (double)S.A_cpop_j, nullptr, &cdrop);
+    if (P.test_type.find("scorebox") != std::string::npos && P.scorebox_col_num > 1 && P.scorebox_col_max > 0)
+      cdrop = (int)ceil((double)P.scorebox_col_max / (double)(P.scorebox_col_num - 1));
+    for (auto &E : S.E) {
+      E->lf_jn = S.L((unsigned long long)E->A_rbother * E->A_nrows * cdrop);
+      E->lf_vn = S.L((unsigned long long)E->Z_rbother * E->Z_nrows * cdrop);
+      S.mirror_zero(E->lf_jn);
+      S.mirror_zero(E->lf_vn);
     }
   }
   // bcc_double_init_lf (bcc.c:1005-1150)
@@ -1650,8 +1681,30 @@ void sumscores_mxA(State &S) {  // bcc_sumscores_mxA / mxB / mxC (bcc_sumscores.
 
 // --- low-rank update ------------------------------------------------------------
 
+// bcc_lrup_QR_YnWt_stage_2 (bcc_lrup.c:772-861), the condense form of
+// stages 0 and 1: the removed columns of every bin as dense centred FP64
+// matrices (SNPs x rows), then their FP64 products.
+void lrup_QR_condense(State &S) {
+  double *aj = S.A_ajdk.data();
+  for (auto &E : S.E) {
+    if (S.A_cbother && E->A_rbother) wrap_M_At_to_L2_run(TARGS, T_pm, SP_j, SP_b, E->M_jt->p(), aj, &E->lf_jn);
+    if (S.A_cbother && E->Z_rbother) wrap_M_At_to_L2_run(TARGS, T_pm, SP_j, SP_b, E->M_vt->p(), aj, &E->lf_vn);
+  }
+  for (int nb1 = 0; nb1 < S.nbins; ++nb1)
+    for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
+      Double *F = S.f(nb1, nb2);
+      Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
+      if (S.A_cbother && E1->A_rbother && E2->Z_rbother) wrap_AnZt_mm__run(TARGS, E1->lf_jn, E2->lf_vn, &F->lf_jnvt);
+      if (S.A_cbother && E1->A_rbother && E2->A_rbother && nb1 <= nb2)
+        wrap_AnZt_mm__run(TARGS, E1->lf_jn, E2->lf_jn, &F->lf_jnjt);
+    }
+}
+
 void lrup_QR(State &S) {  // bcc_lrup_QR_YnWt_stage_0/1/3 (bcc_lrup.c:659-892)
   double *aj = S.A_ajdk.data();
+  if (qr_condense(S.P)) {
+    lrup_QR_condense(S);
+  } else {
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_jn->p(), aj, &E->lf_jn_ajdk);
     if (E->Z_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_vn->p(), aj, &E->lf_vn_ajdk);
@@ -1669,6 +1722,7 @@ void lrup_QR(State &S) {  // bcc_lrup_QR_YnWt_stage_0/1/3 (bcc_lrup.c:659-892)
           wrap_AnZt_vv__run(TARGS, T_pm, SP_b, SP_b, E1->M_jn->p(), E2->M_jn->p(), aj, E1->lf_jn_ajdk, E2->lf_jn_ajdk, &F->lf_jnjt);
       }
     }
+  }
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Single *E1 = S.E[nb1].get(), *E2 = S.E[nb2].get();
@@ -2502,11 +2556,8 @@ void set_stop_check(StopCheck fn, void *ctx) {
 }
 
 int solve(const Params &P, const Input &I, Output &O, std::string &err, const Hooks *hooks) {
-  if (P.QR_strategy.find("YnWt") == std::string::npos || P.QR_strategy.find("condense") != std::string::npos ||
-      P.QR_strategy.find("ZtSWn") != std::string::npos ||
-      (P.QC_strategy.find("YnWt") == std::string::npos && P.QC_strategy.find("ZtSWn") == std::string::npos) ||
-      P.QC_strategy.find("store one") != std::string::npos) {
-    err = "supported strategies: rows YnWt; columns YnWt and / or ZtSWn (no condense / store one)";
+  if (!strategies_supported(P)) {
+    err = kStrategyError;
     return 4;
   }
   if (P.B_MLT < 1 || P.B_MLT > 62) { err = "B_MLT out of range"; return 4; }
@@ -2585,11 +2636,8 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
 // a second state loaded from the same inputs, which reaches the same values
 // bit for bit.
 int scorebox(const Params &P, const Input &I, ScoreboxOutput &SO, std::string &err, const Hooks *hooks) {
-  if (!dcc_mode(P) && (P.QR_strategy.find("YnWt") == std::string::npos || P.QR_strategy.find("condense") != std::string::npos ||
-      P.QR_strategy.find("ZtSWn") != std::string::npos ||
-      (P.QC_strategy.find("YnWt") == std::string::npos && P.QC_strategy.find("ZtSWn") == std::string::npos) ||
-      P.QC_strategy.find("store one") != std::string::npos)) {
-    err = "supported strategies: rows YnWt; columns YnWt and / or ZtSWn (no condense / store one)";
+  if (!dcc_mode(P) && !strategies_supported(P)) {
+    err = kStrategyError;
     return 4;
   }
   const int row_num = std::max(0, P.scorebox_row_num), col_num = std::max(0, P.scorebox_col_num);

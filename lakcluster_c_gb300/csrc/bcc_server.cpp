@@ -42,7 +42,7 @@ struct OwnedProblem {
   lakgb_bcc_problem p{};
   std::vector<lakgb_bcc_bin> bins;
   std::vector<std::vector<unsigned char>> store;
-  std::string qc;
+  std::string qc, qr;
 
   explicit OwnedProblem(const lakgb_bcc_problem &src) {
     p = src;
@@ -68,6 +68,10 @@ struct OwnedProblem {
       qc = src.QC_strategy;
       p.QC_strategy = qc.c_str();
     }
+    if (src.QR_strategy) {
+      qr = src.QR_strategy;
+      p.QR_strategy = qr.c_str();
+    }
     p.bins = bins.data();
   }
 };
@@ -90,7 +94,9 @@ long long footprint(const lakgb_bcc_problem &p) {
     }
   const long long cdrop = p.ncols / 8 + 1;
   bytes += 8 * 3 * (long long)p.ncols * cdrop * p.nbins;        // SNP x SNP blocks
-  return bytes + (64ll << 20);                                  // staging arena, scratch
+  if (p.QR_strategy && strstr(p.QR_strategy, "condense"))
+    bytes += 8 * (rows_total + rows_total) * cdrop;             // dense removed columns, their uploads
+  return bytes + (64ll << 20);                                // staging arena, scratch
 }
 
 struct Job {

@@ -56,58 +56,88 @@ struct XcalcParams {
   int *bad;                  // set when an index would leave its buffer (access skipped)
 };
 
-// Grid: blockIdx.y strides the retained columns, blockIdx.x * blockDim.x +
-// threadIdx.x the retained rows, about four rows per thread and column (the
-// launch sizes gridDim.x so), loaded together; one partial (min, max, any)
-// per block.
+// The masked min / max compare order keys instead of doubles: GB300's FP64
+// pipe issues about two compares per clock per SM, which held a min/max scan
+// to a quarter of HBM bandwidth, while the integer pipe compares 64-bit keys
+// at memory speed.  The key of x is its bit pattern with the sign bit flipped
+// for x >= 0 and every bit flipped for x < 0, so unsigned key order is the
+// order of the values, with -0 below +0.  The reference keeps the first of
+// equal extremes (xcalc.c:25), so a min or max of zero may differ from it in
+// sign only; min, max and mlt (xcalc.c:130) come out the same either way:
+// a zero extreme enters them only through differences with the other extreme
+// or, when both are zero, through min_data + 1 (xcalc.c:34).
+__device__ __forceinline__ unsigned long long order_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double key_value(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// Grid: blockIdx.x * blockDim.x + threadIdx.x strides the retained rows, each
+// thread holding kMinMaxRows row offsets in registers for all its columns;
+// blockIdx.y strides the retained columns, kMinMaxCols per pass, so that
+// kMinMaxRows * kMinMaxCols loads are in flight per thread.  One partial
+// (min, max, any) per block.
+constexpr int kMinMaxRows = 4, kMinMaxCols = 2, kMinMaxThreads = 256;
+
 __global__ void xcalc_minmax_kernel(const double *lf, const long long *rows_j, int nr,
                                     const long long *cols_j, int nc, double *pmin, double *pmax,
                                     int *pany) {
-  double mn = 0.0, mx = 0.0;
-  int any = 0;
+  unsigned long long kmn = ~0ull, kmx = 0ull;  // empty: kmn > kmx
   const int stride = gridDim.x * blockDim.x;
-  for (int c = blockIdx.y; c < nc; c += gridDim.y) {
-    const long long co = cols_j[c];
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += 4 * stride) {
-      double x[4];
-      int n = 0;
+  for (int rb = blockIdx.x * blockDim.x + threadIdx.x; rb < nr; rb += kMinMaxRows * stride) {
+    long long ro[kMinMaxRows];
+    bool rok[kMinMaxRows];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int ru = r + u * stride;
-        if (ru < nr) { x[u] = lf[rows_j[ru] + co]; n = u + 1; }
+    for (int u = 0; u < kMinMaxRows; ++u) {
+      const int r = rb + u * stride;
+      rok[u] = r < nr;
+      ro[u] = rok[u] ? rows_j[r] : 0;
+    }
+    for (int c = blockIdx.y; c < nc; c += kMinMaxCols * gridDim.y) {
+      double x[kMinMaxCols][kMinMaxRows];
+      bool cok[kMinMaxCols];
+#pragma unroll
+      for (int k = 0; k < kMinMaxCols; ++k) {
+        const int ck = c + k * gridDim.y;
+        cok[k] = ck < nc;
+        const long long co = cok[k] ? cols_j[ck] : 0;
+#pragma unroll
+        for (int u = 0; u < kMinMaxRows; ++u) x[k][u] = (cok[k] && rok[u]) ? __ldg(lf + ro[u] + co) : 0.0;
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (u >= n) break;
-        if (!any) { mn = x[u]; mx = x[u]; any = 1; }
-        else { mn = x[u] < mn ? x[u] : mn; mx = x[u] > mx ? x[u] : mx; }
-      }
+      for (int k = 0; k < kMinMaxCols; ++k)
+#pragma unroll
+        for (int u = 0; u < kMinMaxRows; ++u)
+          if (cok[k] && rok[u]) {
+            const unsigned long long q = order_key(x[k][u]);
+            kmn = q < kmn ? q : kmn;
+            kmx = q > kmx ? q : kmx;
+          }
     }
   }
-  __shared__ double smn[32], smx[32];
-  __shared__ int sany[32];
+  __shared__ unsigned long long smn[32], smx[32];
   for (int o = 16; o > 0; o >>= 1) {
-    const double omn = __shfl_xor_sync(0xffffffffu, mn, o);
-    const double omx = __shfl_xor_sync(0xffffffffu, mx, o);
-    const int oany = __shfl_xor_sync(0xffffffffu, any, o);
-    if (oany) {
-      if (!any) { mn = omn; mx = omx; any = 1; }
-      else { mn = omn < mn ? omn : mn; mx = omx > mx ? omx : mx; }
-    }
+    const unsigned long long omn = __shfl_xor_sync(0xffffffffu, kmn, o);
+    const unsigned long long omx = __shfl_xor_sync(0xffffffffu, kmx, o);
+    kmn = omn < kmn ? omn : kmn;
+    kmx = omx > kmx ? omx : kmx;
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) { smn[warp] = mn; smx[warp] = mx; sany[warp] = any; }
+  if (lane == 0) { smn[warp] = kmn; smx[warp] = kmx; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    int a = 0;
-    double bmn = 0.0, bmx = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      if (!sany[w]) continue;
-      if (!a) { bmn = smn[w]; bmx = smx[w]; a = 1; }
-      else { bmn = smn[w] < bmn ? smn[w] : bmn; bmx = smx[w] > bmx ? smx[w] : bmx; }
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      kmn = smn[w] < kmn ? smn[w] : kmn;
+      kmx = smx[w] > kmx ? smx[w] : kmx;
     }
     const int b = blockIdx.x + gridDim.x * blockIdx.y;
-    pmin[b] = bmn; pmax[b] = bmx; pany[b] = a;
+    const int any = kmn <= kmx;
+    pmin[b] = any ? key_value(kmn) : 0.0;
+    pmax[b] = any ? key_value(kmx) : 0.0;
+    pany[b] = any;
   }
 }
 
@@ -403,13 +433,13 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
     d_cols = upload_vec(cols_j);
     d_roff_all = upload_vec(row_off_a);
     st->flush();
-    // About 8 resident blocks per SM: rows across blockIdx.x (about four per
+    // About 16 blocks per SM: rows across blockIdx.x (kMinMaxRows per
     // thread), columns across blockIdx.y.
-    const int gx = std::min((nr + 1023) / 1024, 1216);
-    const int gy = std::max(1, std::min(nc, 1216 / gx));
+    const int gx = std::min((nr + kMinMaxRows * kMinMaxThreads - 1) / (kMinMaxRows * kMinMaxThreads), 2432);
+    const int gy = std::max(1, std::min(nc, 2432 / gx));
     const int blocks = gx * gy;
     DBuf d_min(blocks * sizeof(double)), d_max(blocks * sizeof(double)), d_any(blocks * sizeof(int));
-    xcalc_minmax_kernel<<<dim3(gx, gy), 256, 0, stream()>>>(plf, d_rows.as<long long>(), nr,
+    xcalc_minmax_kernel<<<dim3(gx, gy), kMinMaxThreads, 0, stream()>>>(plf, d_rows.as<long long>(), nr,
                                                        d_cols.as<long long>(), nc, d_min.as<double>(),
                                                        d_max.as<double>(), d_any.as<int>());
     LAKGB_CUDA(cudaGetLastError());

@@ -48,8 +48,8 @@ def read_b16(path: str) -> np.ndarray:
 
 def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.05, B_MLT=32,
                      A_row_masks=None, Z_row_masks=None, col_mask=None, gamma_type=None, Ireq=None,
-                     T_bins=None, S_bins=None, kappa_squared=None, qc_strategy="YnWt", name="bcc.in",
-                     extra_statements=()) -> str:
+                     T_bins=None, S_bins=None, kappa_squared=None, qc_strategy="YnWt", qr_strategy="YnWt",
+                     name="bcc.in", extra_statements=()) -> str:
     """Write the .b16 files of one bcc problem and the .in file that names them.
 
     A_bins / Z_bins: per-bin 0/1 arrays (rows x SNPs).  Masks (0/1 vectors) are
@@ -99,7 +99,7 @@ def write_bcc_inputs(in_dir: str, out_dir: str, A_bins, Z_bins=None, *, gamma=0.
         "GLOBAL_thread_count= 1;",
         "GLOBAL_omp_type= 0;",
         "GLOBAL_TEST_TYPE= lakcluster_driver;",
-        "GLOBAL_QR_strategy= YnWt;",
+        "GLOBAL_QR_strategy= %s;" % qr_strategy,
         "GLOBAL_QC_strategy= %s;" % qc_strategy,
         "GLOBAL_NBINS= %d;" % nbins,
         "GLOBAL_B_MLT= %d;" % B_MLT,

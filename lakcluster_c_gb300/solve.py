@@ -27,7 +27,7 @@ class BccProblem(C.Structure):
                 ("nbins", C.c_int), ("bins", C.POINTER(BccBin)),
                 ("B_MLT", C.c_int), ("gamma", C.c_double), ("gamma_type", C.c_int), ("test_sparse", C.c_int),
                 ("Ireq", C.c_int), ("T_ncols", C.c_int), ("kappa_squared", C.c_double),
-                ("QC_strategy", C.c_char_p)]
+                ("QC_strategy", C.c_char_p), ("QR_strategy", C.c_char_p)]
 
 
 class BccResult(C.Structure):
@@ -63,7 +63,7 @@ class Problem:
 
     def __init__(self, A_bins, Z_bins=None, *, gamma=0.125, B_MLT=32, gamma_type=0, A_masks=None,
                  Z_masks=None, col_mask=None, test_sparse=1, Ireq=0, T_bins=None, S_bins=None,
-                 kappa_squared=0.0, qc_strategy="YnWt", lib=None, packed_ncols=None):
+                 kappa_squared=0.0, qc_strategy="YnWt", qr_strategy="YnWt", lib=None, packed_ncols=None):
         self.lib = bind(lib or load())
         self._keep = []
         nb = len(A_bins)
@@ -98,6 +98,8 @@ class Problem:
         self.prob.kappa_squared = kappa_squared
         self._qc = qc_strategy.encode()
         self.prob.QC_strategy = self._qc
+        self._qr = qr_strategy.encode()
+        self.prob.QR_strategy = self._qr
         self.prob.ncols = ncols
         self.prob.row_bytes = (ncols + (16 - ncols % 16) % 16) // 8
         if col_mask is not None:

@@ -785,3 +785,71 @@ void lako_bits_transpose(const unsigned char *in, long long in_rec_bytes, int n_
     }
   }
 }
+
+/* dir_c/M_Ax_to_L2.c:5-100 (at = 0, SNPs are the columns of M) and :137-280
+ * (at = 1, SNPs are the rows): each retained entry becomes (b - a) * sqrt(d),
+ * b = +1/-1 (TYPE_pm) or 1/0 (TYPE_00), a and d the A_ajdk terms of the
+ * entry's SNP (b alone without A_ajdk); the whole output handle is zeroed
+ * first (L_zero).  TYPE_p0 leaves it zero. */
+int lako_M_to_L2(int at, int type_flag, int spacing_r, int spacing_c, struct M_handle *M, double *A_ajdk,
+                 struct L_handle **out_p)
+{
+  unsigned long long lr = spacing_len(spacing_r, M), lc = 0;
+  switch (spacing_c) {
+    case LAKGB_SPACING_j: lc = (unsigned long long)M->cpop_j; break;
+    case LAKGB_SPACING_b: lc = (unsigned long long)M->cpop_b; break;
+    case LAKGB_SPACING_a: lc = (unsigned long long)M->ncols; break;
+    default: break;
+  }
+  struct L_handle *out = ensure(out_p, lr * lc);
+  if (!out) return (int)(lr * lc);
+  memset(out->lf, 0, out->length * sizeof(double));
+  out->spacing_row = spacing_r; out->row_stride = lr;
+  out->spacing_col = spacing_c; out->col_stride = lc;
+  out->spacing_lyr = LAKGB_SPACING_b; out->lyr_stride = 0;
+  if (type_flag != LAKGB_TYPE_pm && type_flag != LAKGB_TYPE_00) return (int)(lr * lc);
+  const long long P = psize_c(at ? M->nrows : M->ncols);
+  for (long long ma = 0; ma < M->rpop_j; ma++) {
+    const unsigned char *row = M->wX + (long long)M->m_b_[ma] * M->mc_length;
+    for (long long na = 0; na < M->cpop_j; na++) {
+      const unsigned int ca = M->n_a_[na];
+      double v = (type_flag == LAKGB_TYPE_pm) ? (double)bit_pm(row, ca) : (double)bit_on(row, ca);
+      if (A_ajdk) {
+        const unsigned int snp = at ? M->m_a_[ma] : ca;
+        const double a = A_ajdk[snp / 1920 + 1 * P], d = A_ajdk[snp / 1920 + AJDK_0_1 * P];
+        v = (v - a) * sqrt(d);
+      }
+      unsigned long long tc = 0;
+      switch (spacing_c) {
+        case LAKGB_SPACING_j: tc = (unsigned long long)na; break;
+        case LAKGB_SPACING_b: tc = M->n_b_[na]; break;
+        case LAKGB_SPACING_a: tc = ca; break;
+        default: break;
+      }
+      out->lf[tab(spacing_r, M, ma) + tc * lr] = v;
+    }
+  }
+  return (int)(lr * lc);
+}
+
+/* dir_c/AnZt_mm.c:6-109 with the GSL CBLAS dgemm the reference links: every
+ * element one running sum from +0 over k ascending, product and sum each
+ * rounded once (this file is compiled without FP contraction). */
+int lako_AnZt_mm(struct L_handle *lf_At, struct L_handle *lf_Zt, struct L_handle **out_p)
+{
+  const unsigned long long m = lf_At->col_stride, n = lf_Zt->col_stride, K = lf_At->row_stride;
+  struct L_handle *out = ensure(out_p, m * n);
+  if (!out) return (int)(m * n);
+  out->spacing_row = lf_At->spacing_col; out->row_stride = m;
+  out->spacing_col = lf_Zt->spacing_col; out->col_stride = n;
+  if (K == 0 || lf_Zt->row_stride < K) return (int)(m * n);
+  const unsigned long long ldb = lf_Zt->row_stride;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (long long j = 0; j < (long long)n; j++)
+    for (unsigned long long i = 0; i < m; i++) {
+      double s = 0.0;
+      for (unsigned long long k = 0; k < K; k++) s += lf_At->lf[k + i * K] * lf_Zt->lf[k + j * ldb];
+      out->lf[i + j * m] = s;
+    }
+  return (int)(m * n);
+}

@@ -79,6 +79,12 @@ int lako_An_ZtSWn_Yt_vv(int spacing_a, int spacing_s, struct M_handle *M_An, str
                         struct M_handle *M_Yn, double *A_ajdk, double *Y_ajdk, struct L_handle *lf_ZtSWn,
                         struct L_handle **out_p);
 
+/* dir_c/M_Ax_to_L2.c:5-100 (at = 0) and :137-280 (at = 1) */
+int lako_M_to_L2(int at, int type_flag, int spacing_r, int spacing_c, struct M_handle *M, double *A_ajdk,
+                 struct L_handle **out_p);
+/* dir_c/AnZt_mm.c:6-109 (GSL CBLAS dgemm order: ascending k from +0) */
+int lako_AnZt_mm(struct L_handle *lf_At, struct L_handle *lf_Zt, struct L_handle **out_p);
+
 /* dir_c/binary_read.c:174-269 (wrap_transpose), on memory: n_in_rec records
  * of in_rec_bytes bytes (bits MSB first) into n_out_rec records of
  * out_rec_bytes bytes, out record r bit c = in record c bit r; bits of out

@@ -97,3 +97,24 @@ int wrap_AtTAn_vv__run(int *tidx, void **vpra, pthread_t *th, int sa, int sy, in
   (void)tidx; (void)vpra; (void)th;
   return lako_AtTAn_vv(sa, sy, st, M_At, M_Tt, M_Yt, A_ajdk, Y_ajdk, lf_AtTn, lf_YtTn, out);
 }
+
+int wrap_M_At_to_L2_run(int *tidx, void **vpra, pthread_t *th, int type_flag, int sr, int sc, struct M_handle *M_At,
+                        double *A_ajdk, struct L_handle **out)
+{
+  (void)tidx; (void)vpra; (void)th;
+  return lako_M_to_L2(1, type_flag, sr, sc, M_At, A_ajdk, out);
+}
+
+int wrap_M_An_to_L2_run(int *tidx, void **vpra, pthread_t *th, int type_flag, int sr, int sc, struct M_handle *M_An,
+                        double *A_ajdk, struct L_handle **out)
+{
+  (void)tidx; (void)vpra; (void)th;
+  return lako_M_to_L2(0, type_flag, sr, sc, M_An, A_ajdk, out);
+}
+
+int wrap_AnZt_mm__run(int *tidx, void **vpra, pthread_t *th, struct L_handle *lf_At, struct L_handle *lf_Zt,
+                      struct L_handle **out)
+{
+  (void)tidx; (void)vpra; (void)th;
+  return lako_AnZt_mm(lf_At, lf_Zt, out);
+}

@@ -84,6 +84,16 @@ CASES = {
     "case_control_2bin_qc_ZtSWn": (lambda: dict(_case_control(280, 240, 1900, 22, 40, 2, 43), qc="ZtSWn"), True),
     "case_control_2bin_T2_qc_ZtSWn": (
         lambda: dict(_covariates(_case_control(250, 230, 1700, 20, 36, 2, 47), 2, 53, 0.4), qc="ZtSWn"), True),
+    # the condense row strategy (dense FP64 removed columns and their products)
+    # and the store-one column strategy (one covariate at a time)
+    "case_control_2bin_qr_condense": (lambda: dict(_case_control(280, 250, 2050, 22, 40, 2, 59), qr="YnWt condense"),
+                                      True),
+    "case_control_2bin_masked_qr_condense": (lambda: dict(_masked_case_control(), qr="YnWt condense"), True),
+    "case_control_2bin_T2_qc_store_one": (
+        lambda: dict(_covariates(_case_control(260, 240, 1900, 22, 40, 2, 61), 2, 67, 0.3), qc="YnWt store one"),
+        True),
+    "case_control_3bin_qr_condense_qc_store_one": (
+        lambda: dict(_case_control(300, 270, 1800, 22, 36, 3, 71), qr="YnWt condense", qc="YnWt store one"), True),
 }
 # Cases whose reference solve takes minutes even on every host thread (the
 # 4096 + 4096 x 16384 two-bin workload: 518 s on 8 cores): their golden
@@ -96,7 +106,9 @@ LARGE_CASES = {
 SMALL = ["case_only_200x300", "case_control_2bin_300x250x2100", "case_control_2bin_masked",
          "case_control_1bin_gamma_lin", "case_control_3bin_ragged", "case_control_3bin_Ireq1",
          "case_control_3bin_Ireq2", "case_control_2bin_Ireq2", "case_control_2bin_T3", "case_control_2bin_T3_kappa",
-         "case_control_3bin_T2_kappa_Ireq1", "case_control_2bin_qc_ZtSWn", "case_control_2bin_T2_qc_ZtSWn"]
+         "case_control_3bin_T2_kappa_Ireq1", "case_control_2bin_qc_ZtSWn", "case_control_2bin_T2_qc_ZtSWn",
+         "case_control_2bin_qr_condense", "case_control_2bin_masked_qr_condense", "case_control_2bin_T2_qc_store_one",
+         "case_control_3bin_qr_condense_qc_store_one"]
 
 
 def build(name):
@@ -109,7 +121,8 @@ def write_case(name, in_dir, out_dir, fname="bcc.in", extra_statements=()):
                                     A_row_masks=d.get("A_masks"), Z_row_masks=d.get("Z_masks"),
                                     col_mask=d.get("col_mask"), gamma_type=d.get("gamma_type"), Ireq=d.get("Ireq"),
                                     T_bins=d.get("T"), S_bins=d.get("S"), kappa_squared=d.get("kappa_squared"),
-                                    qc_strategy=d.get("qc", "YnWt"), name=fname, extra_statements=extra_statements)
+                                    qc_strategy=d.get("qc", "YnWt"), qr_strategy=d.get("qr", "YnWt"), name=fname,
+                                    extra_statements=extra_statements)
 
 
 # --- scorebox and scramble cases -------------------------------------------------
@@ -293,7 +306,8 @@ def solve_arrays(lib, d):
     p = sv.Problem(d["A"], d.get("Z"), gamma=d["gamma"], gamma_type=d.get("gamma_type") or 0,
                    A_masks=d.get("A_masks"), Z_masks=d.get("Z_masks"), col_mask=d.get("col_mask"),
                    Ireq=d.get("Ireq") or 0, T_bins=d.get("T"), S_bins=d.get("S"),
-                   kappa_squared=d.get("kappa_squared") or 0.0, qc_strategy=d.get("qc", "YnWt"), lib=lib)
+                   kappa_squared=d.get("kappa_squared") or 0.0, qc_strategy=d.get("qc", "YnWt"),
+                   qr_strategy=d.get("qr", "YnWt"), lib=lib)
     return p.solve()
 
 

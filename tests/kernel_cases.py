@@ -162,3 +162,90 @@ def build_gram_inputs(spec):
     P = abi.psize(m)
     A_p = 0.02 + 0.96 * rng.random(P) if spec["ajdk"] else None
     return dict(A=A, ar_b=ar_b, ar_j=ar_j, Z=Z, zr_b=zr_b, zr_j=zr_j, mc_b=mc_b, mc_j=mc_j, A_p=A_p)
+
+
+# ---------------------------------------------------------------------------
+# the condense row strategy's entry points (M_Ax_to_L2.c, AnZt_mm.c)
+
+
+def call_m_to_l2(backend: str, at: bool, type_flag: int, spr: int, spc: int, M: MHandle,
+                 A_ajdk: np.ndarray | None, out_length: int | None = None) -> tuple[np.ndarray, LHandle | None]:
+    """wrap_M_At_to_L2_run (at) / wrap_M_An_to_L2_run; returns the output's
+    first rows x columns values and, with ``out_length``, the caller-owned
+    handle it was written into (longer than the product: the whole handle is
+    zeroed)."""
+    lib = load_backend(backend)
+    aj = None if A_ajdk is None else A_ajdk.ctypes.data_as(C.POINTER(C.c_double))
+    own = LHandle(out_length) if out_length else None
+    if own is not None:
+        own.buf[:] = 7.0
+    out = C.pointer(own.s) if own is not None else C.POINTER(L_handle)()
+    if backend == "oracle":
+        n = lib.lako_M_to_L2(int(at), type_flag, spr, spc, M.ptr, aj, C.byref(out))
+    else:
+        fn = lib.wrap_M_At_to_L2_run if at else lib.wrap_M_An_to_L2_run
+        n = fn(*_thread_args(), type_flag, spr, spc, M.ptr, aj, C.byref(out))
+    if own is not None:
+        return own.buf.copy(), own
+    return _take(out, n), None
+
+
+def call_anzt_mm(backend: str, lfA: LHandle, lfZ: LHandle) -> np.ndarray:
+    lib = load_backend(backend)
+    out = C.POINTER(L_handle)()
+    if backend == "oracle":
+        n = lib.lako_AnZt_mm(lfA.ptr, lfZ.ptr, C.byref(out))
+    else:
+        n = lib.wrap_AnZt_mm__run(*_thread_args(), lfA.ptr, lfZ.ptr, C.byref(out))
+    return _take(out, n)
+
+
+def to_l2_specs():
+    """(name, nrows (SNPs for At), ncols, masked, type, spacings, ajdk) covering
+    ragged sizes, partial masks, both value types and every spacing."""
+    out = []
+    shapes = [(1, 1), (17, 33), (40, 1921), (129, 300)]
+    spac = [(abi.SPACING_j, abi.SPACING_b), (abi.SPACING_a, abi.SPACING_a), (abi.SPACING_b, abi.SPACING_j)]
+    for i, (nr, nc) in enumerate(shapes):
+        for t, tf in enumerate((abi.TYPE_pm, abi.TYPE_00)):
+            for s, (sr, sc) in enumerate(spac):
+                out.append(dict(name=f"l{i}{t}{s}", nr=nr, nc=nc, masked=bool((i + s) % 2), type=tf, sr=sr, sc=sc,
+                                ajdk=(t + s) % 3 != 2, seed=3000 + 31 * i + 7 * t + s))
+    return out
+
+
+def build_to_l2(spec, at=True):
+    """M with SNPs as rows (at) or columns, and the A_ajdk of those SNPs."""
+    rng = np.random.default_rng(spec["seed"])
+    frac = 0.7 if spec["masked"] else 1.0
+    rows, mr_b, mr_j = make_matrix_case(rng, spec["nr"], spec["nc"], frac, frac)
+    mc_b = (rng.random(spec["nc"]) < frac).astype(np.uint8)
+    mc_j = mc_b & (rng.random(spec["nc"]) < frac).astype(np.uint8)
+    M = mhandle(rows, mr_b, mr_j, mc_b, mc_j)
+    snps = spec["nr"] if at else spec["nc"]
+    A_ajdk = abi.calc_A_ajdk(0.02 + 0.96 * rng.random(abi.psize(snps))) if spec["ajdk"] else None
+    return M, A_ajdk
+
+
+def mm_specs():
+    """(K, m, n, extra rows per Zt column) for AnZt_mm: single elements, tile
+    edges (16 in k, 64 in i and j), and a Zt with more rows per column than K."""
+    return [(1, 1, 1, 0), (16, 64, 64, 0), (17, 65, 63, 0), (5, 130, 200, 3), (300, 97, 129, 0), (0, 4, 5, 0)]
+
+
+def build_mm(K, m, n, extra, seed):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((K, m)) * rng.choice([1e-3, 1.0, 1e3], size=(K, m))
+    B = rng.standard_normal((K + extra, n))
+    lfA = LHandle.from_matrix(A, abi.SPACING_j, abi.SPACING_b)
+    lfZ = LHandle.from_matrix(B, abi.SPACING_j, abi.SPACING_a)
+    return A, B, lfA, lfZ
+
+
+def mm_numpy(A, B):
+    """The GSL dgemm order: one running sum from +0 over k ascending."""
+    K, m = A.shape
+    S = np.zeros((m, B.shape[1]))
+    for k in range(K):
+        S = S + np.multiply.outer(A[k], B[k])
+    return S

@@ -54,7 +54,7 @@ def test_in_file_solve_matches_reference(solve_lib, golden, tmp_path, name):
         assert got[key] == golden[name][key], key
 
 
-@pytest.mark.parametrize("name", ["case_only_200x300", "case_control_2bin_masked"])
+@pytest.mark.parametrize("name", ["case_only_200x300", "case_control_2bin_masked", "case_control_2bin_masked_qr_condense"])
 def test_stage_digests_match_reference_kernels(gpu_lib, golden, tmp_path, name):
     p = bc.write_case(name, str(tmp_path / "in"), str(tmp_path / "out"))
     tpath = str(tmp_path / "stages.trace")

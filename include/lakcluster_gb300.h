@@ -270,6 +270,18 @@ int lakgb_bed_to_b16(const char *bed, const char *bim, const char *fam, const ch
                      const char *bim_out, const char *fam_out, const struct lakgb_bed_params *params);
 int lakgb_bed_last_error(char *msg, int msg_len);
 
+/* Merge n_file converted studies into one, replacing b16_merge
+ * (dir_c/bed_to_b16.c:1659-1985; GLOBAL_TEST_TYPE= b16_merge with
+ * GLOBAL_n_file, the GLOBAL_fname_{b16,bim,fam}_0in_ lists and
+ * GLOBAL_fname_{b16,bim,fam}_out, also through lakgb_bcc_run_in_file): the
+ * patients found in every study (FID and IID of the .fam lines, in sorted
+ * order; the .fam lines of the first study), every study's allele rows
+ * interleaved by the allele frequency of their .bim lines (ties to the lower
+ * study), each row holding the common patients' bits.  Returns 0 on success;
+ * lakgb_bed_last_error describes a failure. */
+int lakgb_b16_merge(int n_file, const char *const *b16_in, const char *const *bim_in, const char *const *fam_in,
+                    const char *b16_out, const char *bim_out, const char *fam_out);
+
 /* ---------------------------------------------------------------------------
  * Whole solves.
  * ------------------------------------------------------------------------- */

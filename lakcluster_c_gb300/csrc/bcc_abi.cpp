@@ -190,6 +190,23 @@ extern "C" int lakgb_bcc_run_in_file(const char *in_path) {
     }
     return pipeline_status();
   }
+  if (P.test_type == "b16_merge") {  // lakcluster_ver18.c:364
+    std::vector<const char *> b16, bim, fam;
+    for (int f = 0; f < P.bed.n_file; ++f) {
+      b16.push_back(P.bed.b16_in[f].c_str());
+      bim.push_back(P.bed.bim_in[f].c_str());
+      fam.push_back(P.bed.fam_in[f].c_str());
+    }
+    rc = lakgb_b16_merge(P.bed.n_file, b16.data(), bim.data(), fam.data(), P.bed.b16_out.c_str(),
+                         P.bed.bim_out.c_str(), P.bed.fam_out.c_str());
+    if (rc) {
+      char msg[256];
+      lakgb_bed_last_error(msg, sizeof msg);
+      g_err = msg;
+      return rc;
+    }
+    return pipeline_status();
+  }
   lakgb_set_d_mlt(P.D_MLT);
   if (P.test_type == "lakcluster_scorebox" || P.test_type == "dexcluster_scorebox") {  // lakcluster_ver18.c:338
     lakbcc::ScoreboxOutput SO;

@@ -32,6 +32,9 @@ struct Params {
   struct BedFiles {
     std::string bed, bim, fam, b16_out, bim_out, fam_out;
     double snp_mss = 0.01, snp_maf = 0.25, snp_I_opt = 0.01, pat_mss = 0.04;
+    // b16_merge: GLOBAL_n_file studies GLOBAL_fname_{b16,bim,fam}_0in_
+    int n_file = 0;
+    std::vector<std::string> b16_in, bim_in, fam_in;
   } bed;
 };
 

@@ -166,6 +166,10 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     else if (k == "GLOBAL_fname_b16_out") P.bed.b16_out = v;
     else if (k == "GLOBAL_fname_bim_out") P.bed.bim_out = v;
     else if (k == "GLOBAL_fname_fam_out") P.bed.fam_out = v;
+    else if (k == "GLOBAL_n_file") rc = parse_int(v, k, P.bed.n_file, err);
+    else if (k == "GLOBAL_fname_b16_0in_") P.bed.b16_in = prefixed_list(v);
+    else if (k == "GLOBAL_fname_bim_0in_") P.bed.bim_in = prefixed_list(v);
+    else if (k == "GLOBAL_fname_fam_0in_") P.bed.fam_in = prefixed_list(v);
     else if (k == "GLOBAL_snp_mss_threshold") rc = parse_double(v, k, P.bed.snp_mss, err);
     else if (k == "GLOBAL_snp_maf_threshold") rc = parse_double(v, k, P.bed.snp_maf, err);
     else if (k == "GLOBAL_snp_I_opt_threshold") rc = parse_double(v, k, P.bed.snp_I_opt, err);
@@ -211,13 +215,19 @@ int read_in_file(const char *path, Params &P, Input &I, std::string &err) {
     }
     if (rc) return rc;
   }
-  if (test_type == "bed_to_b16") {  // lakcluster_ver18.c:361: the conversion only, no bcc inputs
+  if (test_type == "bed_to_b16" || test_type == "b16_merge") {  // lakcluster_ver18.c:361-364: no bcc inputs
     P.test_type = test_type;
+    if (test_type == "b16_merge" &&
+        (P.bed.n_file < 1 || (int)P.bed.b16_in.size() < P.bed.n_file || (int)P.bed.bim_in.size() < P.bed.n_file ||
+         (int)P.bed.fam_in.size() < P.bed.n_file)) {
+      err = "b16_merge: GLOBAL_n_file and the GLOBAL_fname_{b16,bim,fam}_0in_ lists do not agree";
+      return 3;
+    }
     return 0;
   }
   if (!test_type.empty() && test_type != "lakcluster_driver" && test_type != "lakcluster_scorebox" &&
       test_type != "dexcluster_driver" && test_type != "dexcluster_scorebox") {
-    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc or dexcluster driver or scorebox, or bed_to_b16";
+    err = "GLOBAL_TEST_TYPE " + test_type + " is not the bcc or dexcluster driver or scorebox, bed_to_b16 or b16_merge";
     return 3;
   }
   P.test_type = test_type.empty() ? "lakcluster_driver" : test_type;

@@ -156,12 +156,14 @@ struct BedRecords {
   }
 };
 
-// dQuickSort_index (dir_c/Quicksort.c:216-248): first-element pivot,
-// "<= pivot" from the left and "> pivot" from the right, the index array
-// permuted alongside; subranges past the recursion limit stay unsorted.
-// Written with an explicit stack: the subranges are disjoint, so the order
-// they are done in does not change the result.
-void quicksort_index(std::vector<double> &d, std::vector<int> &idx, unsigned limit) {
+// dQuickSort_index (dir_c/Quicksort.c:216-248) and charpQuickSort_index
+// (:364-414, strcmp order): first-element pivot, "<= pivot" from the left and
+// "> pivot" from the right, the index array permuted alongside; subranges
+// past the recursion limit stay unsorted.  Written with an explicit stack:
+// the subranges are disjoint, so the order they are done in does not change
+// the result.
+template <typename K>
+void quicksort_index(std::vector<K> &d, std::vector<int> &idx, unsigned limit) {
   struct Range { int l, r; unsigned depth; };
   std::vector<Range> st;
   if (!d.empty()) st.push_back({0, (int)d.size() - 1, 0});
@@ -169,7 +171,7 @@ void quicksort_index(std::vector<double> &d, std::vector<int> &idx, unsigned lim
     const Range g = st.back();
     st.pop_back();
     if (g.l >= g.r) continue;
-    const double pivot = d[g.l];
+    const K pivot = d[g.l];
     int i = g.l, j = g.r + 1;
     for (;;) {
       do { ++i; } while (i <= g.r && d[i] <= pivot);
@@ -382,6 +384,199 @@ int read_fields(const char *path, std::vector<std::string> &out) {
   return 0;
 }
 
+// The lines of a text file as getline reads them, without their newlines.
+int read_lines(const char *path, std::vector<std::string> &out) {
+  FILE *fp = fopen(path, "rb");
+  if (!fp) return 2;
+  std::string cur;
+  int c;
+  bool any = false;
+  while ((c = fgetc(fp)) != EOF) {
+    any = true;
+    if (c == '\n') { out.push_back(cur); cur.clear(); any = false; }
+    else cur.push_back((char)c);
+  }
+  if (any) out.push_back(cur);
+  fclose(fp);
+  return 0;
+}
+
+// b16_merge's bit gather: output row r (one allele) holds, at bit k, the bit
+// of common patient k in the source row (idx: per study, the patient's
+// position in that study).  One thread per output byte, grid-stride; bytes
+// past the last patient stay zero.
+__global__ void b16_gather_kernel(const uint8_t *__restrict__ in, const long long *__restrict__ row_off,
+                                  const int *__restrict__ row_study, const int *__restrict__ idx, int n_int,
+                                  long long out_bytes, long long n_rows, uint8_t *__restrict__ out) {
+  const long long total = n_rows * out_bytes;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long r = t / out_bytes, j = t - r * out_bytes;
+    const uint8_t *row = in + row_off[r];
+    const int *ix = idx + (long long)row_study[r] * n_int;
+    unsigned v = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const long long k = 8 * j + q;
+      if (k < n_int) {
+        const int p = ix[k];
+        v |= (unsigned)((row[p >> 3] >> (7 - (p & 7))) & 1) << (7 - q);
+      }
+    }
+    out[t] = (uint8_t)v;
+  }
+}
+
+// b16_merge (dir_c/bed_to_b16.c:1659-1985):
+//   1. per study: the .fam keys FID + IID (the first two fields of each line,
+//      concatenated), sorted with the reference's string quicksort;
+//   2. the intersection (charpIntersectall_index_index_driver,
+//      dir_c/Quicksort.c:624-690): step the sorted lists together, advance
+//      the list holding the smallest key, and when all current keys are
+//      equal take them as the next common patient -- sorted key order, each
+//      study's patient at that key;
+//   3. the .fam lines of the common patients from the first study;
+//   4. the alleles of every study interleaved by the allele frequency of
+//      their .bim lines (field 9): repeatedly the study whose next allele has
+//      the smallest frequency, ties to the lower study; its .bim line (11
+//      fields, tab-joined) and its row with the common patients' bits (the
+//      GPU gather above);
+//   5. the .b16: header 16, common patients, alleles of all studies; rows of
+//      rup(patients, 16) / 8 bytes.
+int b16_merge_files(int n_file, const char *const *b16_in, const char *const *bim_in, const char *const *fam_in,
+                    const char *b16_out, const char *bim_out, const char *fam_out, std::string &err) {
+  if (n_file < 1) { err = "no studies"; return 2; }
+  std::vector<long long> n_bim(n_file), n_fam(n_file), l_fam(n_file), base(n_file + 1, 0);
+  std::vector<std::vector<std::string>> keys(n_file), bim_tok(n_file);
+  std::vector<std::string> fam0;
+  std::vector<uint8_t> all;
+  for (int f = 0; f < n_file; ++f) {
+    n_bim[f] = count_lines(bim_in[f]);
+    n_fam[f] = count_lines(fam_in[f]);
+    if (n_bim[f] < 0) { err = std::string("cannot open ") + bim_in[f]; return 2; }
+    if (n_fam[f] < 0) { err = std::string("cannot open ") + fam_in[f]; return 2; }
+    FILE *fp = fopen(b16_in[f], "rb");
+    if (!fp) { err = std::string("cannot open ") + b16_in[f]; return 2; }
+    int hdr[3] = {0, 0, 0};
+    if (fread(hdr, sizeof(int), 3, fp) != 3) { fclose(fp); err = std::string("short .b16 file ") + b16_in[f]; return 2; }
+    if (hdr[2] != n_bim[f]) printf(" %% Warning, n_bim_[%d] %lld vs %d\n", f, n_bim[f], hdr[2]);
+    if (hdr[1] != n_fam[f]) printf(" %% Warning, n_fam_[%d] %lld vs %d\n", f, n_fam[f], hdr[1]);
+    l_fam[f] = (n_fam[f] + (16 - n_fam[f] % 16) % 16) / 8;
+    base[f + 1] = base[f] + n_bim[f] * l_fam[f];
+    all.resize((size_t)base[f + 1]);
+    const size_t want = (size_t)(n_bim[f] * l_fam[f]);
+    const bool short_rows = want && fread(all.data() + base[f], 1, want, fp) != want;
+    fclose(fp);
+    if (short_rows) { err = std::string("short .b16 file ") + b16_in[f]; return 2; }
+    std::vector<std::string> lines;
+    if (read_lines(fam_in[f], lines)) { err = std::string("cannot open ") + fam_in[f]; return 2; }
+    for (long long i = 0; i < n_fam[f]; ++i) {
+      char a[4096], b[4096];
+      if ((size_t)i >= lines.size() || lines[i].size() >= sizeof(a) || sscanf(lines[i].c_str(), "%s %s", a, b) != 2) {
+        err = std::string("bad .fam line in ") + fam_in[f];
+        return 2;
+      }
+      keys[f].push_back(std::string(a) + b);
+    }
+    if (read_fields(bim_in[f], bim_tok[f]) || (long long)bim_tok[f].size() < 11 * n_bim[f]) {
+      err = std::string("bad .bim file ") + bim_in[f];
+      return 2;
+    }
+  }
+  if (read_fields(fam_in[0], fam0) || (long long)fam0.size() < 6 * n_fam[0]) { err = "bad .fam file"; return 2; }
+  // 1-2: sorted keys and their intersection
+  std::vector<std::vector<int>> order(n_file);
+  for (int f = 0; f < n_file; ++f) {
+    order[f].resize(keys[f].size());
+    for (size_t i = 0; i < order[f].size(); ++i) order[f][i] = (int)i;
+    quicksort_index(keys[f], order[f], 1024u * 32u);
+  }
+  std::vector<size_t> pos(n_file, 0);
+  std::vector<int> common;  // n_int x n_file: each study's patient
+  long long n_int = 0;
+  auto all_left = [&] {
+    for (int f = 0; f < n_file; ++f) if (pos[f] >= keys[f].size()) return false;
+    return true;
+  };
+  while (all_left()) {
+    int fmin = 0;
+    bool found = false;
+    for (int f = 0; f < n_file; ++f) {
+      const int c = keys[fmin][pos[fmin]].compare(keys[f][pos[f]]);
+      if (c > 0) { found = true; fmin = f; }
+      if (c < 0) found = true;
+    }
+    if (found) {
+      ++pos[fmin];
+      continue;
+    }
+    for (int f = 0; f < n_file; ++f) common.push_back(order[f][pos[f]++]);
+    ++n_int;
+  }
+  // 3: .fam of the common patients (first study's lines)
+  FILE *fo = fopen(fam_out, "wb");
+  if (!fo) { err = std::string("cannot write ") + fam_out; return 2; }
+  for (long long k = 0; k < n_int; ++k) {
+    const size_t p = (size_t)common[(size_t)k * n_file] * 6;
+    fprintf(fo, "%s %s %s %s %s %s\n", fam0[p].c_str(), fam0[p + 1].c_str(), fam0[p + 2].c_str(), fam0[p + 3].c_str(),
+            fam0[p + 4].c_str(), fam0[p + 5].c_str());
+  }
+  fclose(fo);
+  // 4: alleles interleaved by frequency
+  long long n_rows = 0;
+  for (int f = 0; f < n_file; ++f) n_rows += n_bim[f];
+  std::vector<long long> row_off;
+  std::vector<int> row_study;
+  row_off.reserve((size_t)n_rows);
+  row_study.reserve((size_t)n_rows);
+  FILE *bo = fopen(bim_out, "wb");
+  if (!bo) { err = std::string("cannot write ") + bim_out; return 2; }
+  std::vector<long long> nb(n_file, 0);
+  for (;;) {
+    int fmin = -1;
+    double fr_min = 0.0;
+    for (int f = 0; f < n_file; ++f) {
+      if (nb[f] >= n_bim[f]) continue;
+      const double fr = atof(bim_tok[f][(size_t)(11 * nb[f] + 8)].c_str());
+      if (fmin < 0 || fr < fr_min) { fmin = f; fr_min = fr; }
+    }
+    if (fmin < 0) break;
+    const std::string *t = &bim_tok[fmin][(size_t)(11 * nb[fmin])];
+    for (int q = 0; q < 11; ++q) fprintf(bo, q < 10 ? "%s\t" : "%s\n", t[q].c_str());
+    row_off.push_back(base[fmin] + nb[fmin] * l_fam[fmin]);
+    row_study.push_back(fmin);
+    ++nb[fmin];
+  }
+  fclose(bo);
+  // 5: the merged rows, gathered on the device
+  const long long l_int = (n_int + (16 - n_int % 16) % 16) / 8;
+  std::vector<uint8_t> out((size_t)(n_rows * l_int), 0);
+  if (n_rows > 0 && l_int > 0) {
+    std::vector<int> idx((size_t)(n_int * n_file));
+    for (long long k = 0; k < n_int; ++k)
+      for (int f = 0; f < n_file; ++f) idx[(size_t)(f * n_int + k)] = common[(size_t)(k * n_file + f)];
+    DBuf d_in = upload_bytes(all.data(), all.size());
+    DBuf d_off = upload_vec(row_off), d_study = upload_vec(row_study), d_idx = upload_vec(idx);
+    DBuf d_out(out.size());
+    const long long total = n_rows * l_int;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 32);
+    b16_gather_kernel<<<blocks, 256, 0, stream()>>>(d_in.as<uint8_t>(), d_off.as<long long>(), d_study.as<int>(),
+                                                    d_idx.as<int>(), (int)n_int, l_int, n_rows, d_out.as<uint8_t>());
+    LAKGB_CUDA(cudaGetLastError());
+    count_launch();
+    LAKGB_CUDA(cudaMemcpyAsync(out.data(), d_out.p, out.size(), cudaMemcpyDeviceToHost, stream()));
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  }
+  FILE *b16 = fopen(b16_out, "wb");
+  if (!b16) { err = std::string("cannot write ") + b16_out; return 2; }
+  const int hdr[3] = {16, (int)n_int, (int)n_rows};
+  fwrite(hdr, sizeof(int), 3, b16);
+  const bool ok = out.empty() || fwrite(out.data(), 1, out.size(), b16) == out.size();
+  const bool closed = fclose(b16) == 0;
+  if (!ok || !closed) { err = std::string("cannot write ") + b16_out; return 2; }
+  return 0;
+}
+
 thread_local std::string t_bed_err;
 
 }  // namespace
@@ -497,4 +692,17 @@ extern "C" int lakgb_bed_last_error(char *msg, int msg_len) {
     msg[msg_len - 1] = 0;
   }
   return t_bed_err.empty() ? 0 : 1;
+}
+
+extern "C" int lakgb_b16_merge(int n_file, const char *const *b16_in, const char *const *bim_in,
+                               const char *const *fam_in, const char *b16_out, const char *bim_out,
+                               const char *fam_out) {
+  LAKGB_PROFILE_CALL("lakgb_b16_merge");
+  t_bed_err.clear();
+  bool null_name = !b16_in || !bim_in || !fam_in || !b16_out || !bim_out || !fam_out;
+  for (int f = 0; !null_name && f < n_file; ++f) null_name = !b16_in[f] || !bim_in[f] || !fam_in[f];
+  const int rc = null_name ? 2 : b16_merge_files(n_file, b16_in, bim_in, fam_in, b16_out, bim_out, fam_out, t_bed_err);
+  if (null_name) t_bed_err = "null file name";
+  if (rc) set_error(rc, "lakgb_b16_merge: %s", t_bed_err.c_str());
+  return rc;
 }

@@ -193,3 +193,168 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bed
 def load_golden():
     z = np.load(GOLDEN, allow_pickle=False)
     return {n: {k: z["%s/%s" % (n, k)].tobytes() for k in ("b16", "bim", "fam")} for n in BED_CASES}
+
+
+# --- b16_merge --------------------------------------------------------------------
+# Several converted studies (.b16 / .bim / .fam triples as bed_to_b16 writes
+# them) merged into one (dir_c/bed_to_b16.c:1659-1985): the patients common to
+# every study (by FID + IID), the SNP alleles of all studies interleaved by
+# allele frequency.  Each study draws its patients from a shared pool in its
+# own order, and its allele frequencies from a coarse grid so that studies tie.
+#
+# name: (seed, [(patients, alleles), ...])
+MERGE_CASES = {
+    "merge_2x": (21, [(90, 40), (75, 33)]),
+    "merge_3x_ragged": (22, [(301, 97), (257, 130), (280, 61)]),
+    "merge_4x_small": (23, [(20, 9), (17, 12), (25, 7), (19, 15)]),
+}
+
+
+def merge_inputs(name):
+    """Per study: (fam lines, bim lines, b16 bytes)."""
+    seed, studies = MERGE_CASES[name]
+    rng = np.random.default_rng(seed)
+    pool = max(n for n, _ in studies) + 40
+    out = []
+    for n_pat, n_all in studies:
+        pats = rng.permutation(pool)[:n_pat]
+        fam = ["F%d I%d 0 0 %d %d" % (p // 4, p, 1 + p % 2, 1 + (p % 3 == 0)) for p in pats]
+        freq = np.sort(rng.integers(1, 40, n_all) / 40.0)
+        bim = ["%d\trs%d\t0\t%d\tA\tG\tand(orig)\t%f\t%f\t%f\t%f" % (1 + a % 22, int(rng.integers(1, 10 ** 6)),
+                                                                    100 * a, rng.random() * 0.01, f,
+                                                                    rng.random() * 0.02, min(f, 1 - f))
+               for a, f in enumerate(freq)]
+        row_bytes = (n_pat + 15) // 16 * 2
+        bits = np.zeros((n_all, 8 * row_bytes), np.uint8)
+        bits[:, :n_pat] = rng.random((n_all, n_pat)) < 0.4
+        b16 = np.array([16, n_pat, n_all], np.int32).tobytes() + np.packbits(bits, 1, bitorder="big").tobytes()
+        out.append((fam, bim, b16))
+    return out
+
+
+def write_merge_case(name, d):
+    """Write the studies as <d>/<name>_<k>.{b16,bim,fam}; returns the file lists."""
+    os.makedirs(d, exist_ok=True)
+    files = []
+    for k, (fam, bim, b16) in enumerate(merge_inputs(name)):
+        base = os.path.join(d, "%s_%d" % (name, k))
+        with open(base + ".fam", "w") as f:
+            f.write("".join(x + "\n" for x in fam))
+        with open(base + ".bim", "w") as f:
+            f.write("".join(x + "\n" for x in bim))
+        with open(base + ".b16", "wb") as f:
+            f.write(b16)
+        files.append((base + ".b16", base + ".bim", base + ".fam"))
+    return files
+
+
+def merge_in_text(name, d, out_dir):
+    files = [tuple(os.path.join(d, "%s_%d.%s" % (name, k, x)) for x in ("b16", "bim", "fam"))
+             for k in range(len(MERGE_CASES[name][1]))]
+    out = os.path.join(out_dir, name)
+    return "\n".join([
+        "GLOBAL_verbose= 0;", "GLOBAL_thread_count= 1;", "GLOBAL_omp_type= 0;",
+        "GLOBAL_TEST_TYPE= b16_merge;", "GLOBAL_n_file= %d;" % len(files),
+        "GLOBAL_fname_b16_0in_= %s;" % ",".join(f[0] for f in files),
+        "GLOBAL_fname_bim_0in_= %s;" % ",".join(f[1] for f in files),
+        "GLOBAL_fname_fam_0in_= %s;" % ",".join(f[2] for f in files),
+        "GLOBAL_fname_b16_out= %s_out.b16;" % out, "GLOBAL_fname_bim_out= %s_out.bim;" % out,
+        "GLOBAL_fname_fam_out= %s_out.fam;" % out, "END= 0;", ""])
+
+
+def _quicksort_str(keys, idx, limit=1024 * 32):
+    """charpQuickSort_index (dir_c/Quicksort.c:364-414): the partition of
+    dQuickSort_index with strcmp order (byte order of the strings)."""
+    st = [(0, len(keys) - 1, 0)] if keys else []
+    while st:
+        l, r, depth = st.pop()
+        if l >= r:
+            continue
+        pivot = keys[l]
+        i, j = l, r + 1
+        while True:
+            i += 1
+            while i <= r and keys[i] <= pivot:
+                i += 1
+            j -= 1
+            while keys[j] > pivot:
+                j -= 1
+            if i >= j:
+                break
+            keys[i], keys[j] = keys[j], keys[i]
+            idx[i], idx[j] = idx[j], idx[i]
+        keys[l], keys[j] = keys[j], keys[l]
+        idx[l], idx[j] = idx[j], idx[l]
+        if depth < limit:
+            st.append((l, j - 1, depth + 1))
+            st.append((j + 1, r, depth + 1))
+
+
+def merge_oracle(studies):
+    """TEST INFRASTRUCTURE ONLY: b16_merge (dir_c/bed_to_b16.c:1659-1985) in
+    Python.  studies: [(fam lines, bim lines, b16 bytes)].  Returns the three
+    output files' bytes."""
+    n_file = len(studies)
+    keys, order = [], []
+    for fam, _, _ in studies:
+        k = [(ln.split()[0] + ln.split()[1]).encode() for ln in fam]
+        idx = list(range(len(k)))
+        kk = list(k)
+        _quicksort_str(kk, idx)
+        keys.append(kk)
+        order.append(idx)
+    # charpIntersectall_index_index_driver (dir_c/Quicksort.c:624-690)
+    pos = [0] * n_file
+    inter = []  # per intersected patient: original index in each study
+    while all(pos[f] < len(keys[f]) for f in range(n_file)):
+        fmin, found = 0, False
+        for f in range(n_file):
+            if keys[fmin][pos[fmin]] > keys[f][pos[f]]:
+                fmin, found = f, True
+            elif keys[fmin][pos[fmin]] < keys[f][pos[f]]:
+                found = True
+        if found:
+            pos[fmin] += 1
+        else:
+            inter.append([order[f][pos[f]] for f in range(n_file)])
+            for f in range(n_file):
+                pos[f] += 1
+    n_int = len(inter)
+    fam0 = studies[0][0]
+    fam_txt = "".join(" ".join(fam0[p[0]].split()[:6]) + "\n" for p in inter)
+    # SNPs interleaved by allele frequency, ties to the lower study
+    rows = []
+    nb = [0] * n_file
+    bim_txt = []
+    heads = []
+    for fam, bim, b16 in studies:
+        n_pat = len(fam)
+        rb = (n_pat + 15) // 16 * 2
+        heads.append(np.frombuffer(b16[12:], np.uint8).reshape(-1, rb))
+    while True:
+        fmin = -1
+        for f in range(n_file):
+            if nb[f] < len(studies[f][1]):
+                if fmin < 0 or float(studies[f][1][nb[f]].split()[8]) < float(studies[fmin][1][nb[fmin]].split()[8]):
+                    fmin = f
+        if fmin < 0:
+            break
+        bim_txt.append("\t".join(studies[fmin][1][nb[fmin]].split()[:11]) + "\n")
+        src = np.unpackbits(heads[fmin][nb[fmin]], bitorder="big")
+        rows.append(src[[p[fmin] for p in inter]])
+        nb[fmin] += 1
+    rb = (n_int + 15) // 16 * 2
+    out = np.zeros((len(rows), 8 * rb), np.uint8)
+    for r, v in enumerate(rows):
+        out[r, :n_int] = v
+    n_bim = sum(len(s[1]) for s in studies)
+    b16 = np.array([16, n_int, n_bim], np.int32).tobytes() + np.packbits(out, 1, bitorder="big").tobytes()
+    return {"b16": b16, "bim": "".join(bim_txt).encode(), "fam": fam_txt.encode()}
+
+
+MERGE_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "b16_merge.npz")
+
+
+def load_merge_golden():
+    z = np.load(MERGE_GOLDEN, allow_pickle=False)
+    return {n: {k: z["%s/%s" % (n, k)].tobytes() for k in ("b16", "bim", "fam")} for n in MERGE_CASES}

@@ -35,3 +35,21 @@ def test_generator_is_reproducible():
     assert rec.shape == (50, 9)
     for p in range(33):
         assert np.array_equal((rec[:, p // 4] >> (2 * (p % 4))) & 3, a[:, p])
+
+
+@pytest.mark.parametrize("name", list(bd.MERGE_CASES))
+def test_merge_oracle_equals_reference_outputs(name):
+    """b16_merge: the Python restatement writes exactly the files the
+    reference program wrote for the same studies (tests/golden/b16_merge.npz)."""
+    g = bd.load_merge_golden()[name]
+    got = bd.merge_oracle(bd.merge_inputs(name))
+    for k in ("b16", "bim", "fam"):
+        assert got[k] == g[k], (name, k)
+
+
+def test_merge_keeps_only_common_patients():
+    g = bd.load_merge_golden()["merge_3x_ragged"]
+    hdr = np.frombuffer(g["b16"][:12], np.int32)
+    studies = bd.merge_inputs("merge_3x_ragged")
+    common = set.intersection(*[set(tuple(x.split()[:2]) for x in fam) for fam, _, _ in studies])
+    assert hdr[1] == len(common) and hdr[2] == sum(len(b) for _, b, _ in studies)

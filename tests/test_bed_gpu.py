@@ -85,3 +85,53 @@ def test_gpu_bed_mem_equals_oracle_on_a_larger_case(gpu_lib):
         assert not np.any(rows[:, res.n_pat_retain:])
     finally:
         lib.lakgb_bed_result_free(C.byref(res))
+
+
+@pytest.mark.parametrize("name", list(bd.MERGE_CASES))
+def test_gpu_b16_merge_equals_reference(gpu_lib, tmp_path, name):
+    """b16_merge through the reference's .in interface: the merged .b16, .bim
+    and .fam byte for byte equal to the reference program's."""
+    lib = bc.bind_solve(gpu_lib)
+    g = bd.load_merge_golden()[name]
+    bd.write_merge_case(name, str(tmp_path / "in"))
+    (tmp_path / "out").mkdir()
+    p = tmp_path / "merge.in"
+    p.write_text(bd.merge_in_text(name, str(tmp_path / "in"), str(tmp_path / "out")))
+    assert lib.lakgb_bcc_run_in_file(str(p).encode()) == 0
+    got = bd.read_outputs(name, str(tmp_path / "out"))
+    for k in ("b16", "bim", "fam"):
+        assert got[k] == g[k], (name, k)
+
+
+def test_gpu_b16_merge_larger_equals_oracle(gpu_lib, tmp_path):
+    """Three studies of 3000-4100 patients and 700-1200 alleles against the
+    Python restatement (pinned to the reference program above)."""
+    rng = np.random.default_rng(77)
+    studies = []
+    for n_pat, n_all in [(4100, 1200), (3000, 700), (3650, 950)]:
+        pats = rng.permutation(5000)[:n_pat]
+        fam = ["F%d I%d 0 0 1 2" % (p // 7, p) for p in pats]
+        freq = np.sort(rng.integers(1, 200, n_all) / 200.0)
+        bim = ["1\trs%d\t0\t%d\tA\tG\tand(orig)\t0.001\t%f\t0.002\t%f" % (a, a, f, min(f, 1 - f))
+               for a, f in enumerate(freq)]
+        rb = (n_pat + 15) // 16 * 2
+        bits = np.zeros((n_all, 8 * rb), np.uint8)
+        bits[:, :n_pat] = rng.random((n_all, n_pat)) < 0.3
+        studies.append((fam, bim, np.array([16, n_pat, n_all], np.int32).tobytes()
+                        + np.packbits(bits, 1, bitorder="big").tobytes()))
+    files = []
+    for k, (fam, bim, b16) in enumerate(studies):
+        base = tmp_path / ("s%d" % k)
+        (tmp_path / ("s%d.fam" % k)).write_text("".join(x + "\n" for x in fam))
+        (tmp_path / ("s%d.bim" % k)).write_text("".join(x + "\n" for x in bim))
+        (tmp_path / ("s%d.b16" % k)).write_bytes(b16)
+        files.append(str(base))
+    lib = gpu_lib
+    arr = lambda ext: (C.c_char_p * 3)(*[(f + ext).encode() for f in files])  # noqa: E731
+    out = str(tmp_path / "m")
+    lib.lakgb_b16_merge.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p]
+    assert lib.lakgb_b16_merge(3, arr(".b16"), arr(".bim"), arr(".fam"), (out + ".b16").encode(),
+                               (out + ".bim").encode(), (out + ".fam").encode()) == 0
+    want = bd.merge_oracle(studies)
+    for k in ("b16", "bim", "fam"):
+        assert open(out + "." + k, "rb").read() == want[k], k

@@ -34,6 +34,7 @@
 #include "abi_common.cuh"
 #include "bcc_model.h"
 #include "bitplane.cuh"
+#include "gram.cuh"
 
 namespace lakgb {
 
@@ -253,51 +254,49 @@ bitplane_main_kernel(BitplaneParams p) {
   if (tid < kBP_M && pair0 + tid < p.npairs) p.out[p.out_off[pair0 + tid] + p.t_off[t]] = acc;
 }
 
-// An_ZtSn_ww: warp per An row.
-struct AnZtSnParams {
-  const uint8_t *An; const uint32_t *rowb; int n; long long row_bytes;
-  const uint8_t *mask; int nwords;
-  const uint8_t *planes; long long plane_bytes;
-  int nS; int ncols_per;
+// An_ZtSn_ww (dir_c/An_ZtSn_ww.c:5-108).  With pm0(a, y) = 2 pos - all,
+// pos = popcount(a & y & mask) and all = popcount(y & mask) over the whole
+// row, each output is
+//   (pm0(a, plane 0) * min * mlt + sum_{mx = B..1} 2^(B-mx) pm0(a, plane(s, mx))) / mlt
+// in that order.  The pos counts of every (row, plane) pair are one
+// masked-AND Gram of the An rows against the plane rows (launch_gram with
+// unit block weights: its FP64 sums of integer block counts are exact), the
+// all counts one warp per plane, and the FP64 combination a thread per
+// (row, s).
+struct AnZtSnFinish {
+  const double *pos;              // n x nplanes, pos[i + k*n]
+  const long long *all;           // per plane
+  int n, nS, ncols_per;
   double min_d, mlt_d;
   const unsigned long long *out_r; const unsigned long long *s_off;
   double *out;
 };
 
-__device__ __forceinline__ long long pm0_row(const uint32_t *a, const uint32_t *y, const uint32_t *m,
-                                             int nwords, int lane) {
-  int pos = 0, all = 0;
-  for (int i = lane; i < nwords; i += 32) {
-    const uint32_t ym = __ldg(y + i) & __ldg(m + i);
-    pos += __popc(__ldg(a + i) & ym);
-    all += __popc(ym);
-  }
+__global__ void plane_counts_kernel(const uint8_t *planes, long long plane_bytes, const uint8_t *mask, int nwords,
+                                    int nplanes, long long *all) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nplanes) return;
+  const uint32_t *y = reinterpret_cast<const uint32_t *>(planes + (long long)warp * plane_bytes);
+  const uint32_t *m = reinterpret_cast<const uint32_t *>(mask);
+  int c = 0;
+  for (int i = lane; i < nwords; i += 32) c += __popc(__ldg(y + i) & __ldg(m + i));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    pos += __shfl_xor_sync(0xffffffffu, pos, o);
-    all += __shfl_xor_sync(0xffffffffu, all, o);
-  }
-  return 2ll * pos - all;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0) all[warp] = c;
 }
 
-__global__ void an_ztsn_kernel(AnZtSnParams p) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= p.n) return;
-  const uint32_t *a = reinterpret_cast<const uint32_t *>(p.An + (long long)p.rowb[warp] * p.row_bytes);
-  const uint32_t *m = reinterpret_cast<const uint32_t *>(p.mask);
-  const long long b0 = pm0_row(a, reinterpret_cast<const uint32_t *>(p.planes), m, p.nwords, lane);
-  const double base = __dmul_rn(__dmul_rn((double)b0, p.min_d), p.mlt_d);
-  for (int s = 0; s < p.nS; ++s) {
-    double tmp = 0.0, n2 = 1.0;
-    for (int mx = p.ncols_per - 1; mx > 0; --mx) {
-      const uint32_t *y = reinterpret_cast<const uint32_t *>(p.planes + (long long)(p.ncols_per * s + mx) * p.plane_bytes);
-      const long long v = pm0_row(a, y, m, p.nwords, lane);
-      tmp = __dadd_rn(tmp, __dmul_rn(n2, (double)v));
-      n2 *= 2.0;
-    }
-    if (lane == 0) p.out[p.out_r[warp] + p.s_off[s]] = __ddiv_rn(__dadd_rn(base, tmp), p.mlt_d);
+__global__ void an_ztsn_finish_kernel(AnZtSnFinish p) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)p.n * p.nS) return;
+  const int i = (int)(t % p.n), s = (int)(t / p.n);
+  auto pm0 = [&](int k) { return 2ll * (long long)p.pos[i + (long long)k * p.n] - p.all[k]; };
+  const double base = __dmul_rn(__dmul_rn((double)pm0(0), p.min_d), p.mlt_d);
+  double tmp = 0.0, n2 = 1.0;
+  for (int mx = p.ncols_per - 1; mx > 0; --mx) {
+    tmp = __dadd_rn(tmp, __dmul_rn(n2, (double)pm0(p.ncols_per * s + mx)));
+    n2 *= 2.0;
   }
+  p.out[p.out_r[i] + p.s_off[s]] = __ddiv_rn(__dadd_rn(base, tmp), p.mlt_d);
 }
 
 inline unsigned long long pick_u(int s, unsigned long long j, unsigned long long b, unsigned long long a) {
@@ -679,24 +678,40 @@ extern "C" int wrap_An_ZtSn_ww__run(int *tidx, void **vpra, pthread_t *thread_in
   std::vector<unsigned long long> out_r(n), s_off(nS);
   for (int i = 0; i < n; ++i) out_r[i] = pick_u(spacing_a, i, M_An->m_b_[i], M_An->m_a_[i]);
   for (int s = 0; s < nS; ++s) s_off[s] = pick_u(spacing_s, s, M_St->m_b_[s], M_St->m_a_[s]) * length_a;
-  AnZtSnParams p{};
+  const int nplanes = nS * M_ZtSn->ncols_per_z;
   Stager st;
-  p.An = (const uint8_t *)resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
-  p.row_bytes = (long long)M_An->mc_length;
+  const uint8_t *An = (const uint8_t *)resident(M_An->wX, (size_t)M_An->rpop_b * M_An->mc_length);
+  const uint8_t *planes = (const uint8_t *)resident(M_ZtSn->wX, (size_t)M_ZtSn->nrows * M_ZtSn->mc_length);
+  std::vector<uint32_t> zrow(nplanes), orow(n), ocol(nplanes);
+  for (int k = 0; k < nplanes; ++k) zrow[k] = ocol[k] = (uint32_t)k;
+  for (int i = 0; i < n; ++i) orow[i] = (uint32_t)i;
   DBuf d_rowb = upload_vec(rowb), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
-  p.rowb = d_rowb.as<uint32_t>(); p.n = n;
+  DBuf d_zrow = upload_vec(zrow), d_orow = upload_vec(orow), d_ocol = upload_vec(ocol);
   DBuf mask = upload_bytes(M_An->mc_j, M_An->mc_length);
-  p.mask = mask.as<uint8_t>(); p.nwords = (int)(M_An->mc_length / 4);
-  p.planes = (const uint8_t *)resident(M_ZtSn->wX, (size_t)M_ZtSn->nrows * M_ZtSn->mc_length);
-  p.plane_bytes = (long long)M_ZtSn->mc_length;
-  p.nS = nS; p.ncols_per = M_ZtSn->ncols_per_z;
-  p.min_d = M_ZtSn->min_d; p.mlt_d = M_ZtSn->mlt_d;
-  p.out_r = d_or.as<unsigned long long>(); p.s_off = d_so.as<unsigned long long>();
+  DBuf d_pos((size_t)n * nplanes * sizeof(double)), d_all((size_t)nplanes * sizeof(long long));
   DBuf d_out(length * sizeof(double));
   d_out.zero();
-  p.out = d_out.as<double>();
   st.flush();
-  an_ztsn_kernel<<<(n * 32 + 255) / 256, 256, 0, stream()>>>(p);
+  GramParams g{};
+  g.wA = An; g.a_rowb = d_rowb.as<uint32_t>(); g.nA = n; g.a_row_bytes = (long long)M_An->mc_length;
+  g.wZ = planes; g.z_rowb = d_zrow.as<uint32_t>(); g.nZ = nplanes; g.z_row_bytes = (long long)M_ZtSn->mc_length;
+  g.mask = mask.as<uint8_t>(); g.P = (int)(M_An->mc_length / kBlockBytes);
+  g.D = nullptr; g.type = 2;  // masked AND counts
+  g.out_r = d_orow.as<uint32_t>(); g.out_c = d_ocol.as<uint32_t>(); g.out_stride = n; g.out = d_pos.as<double>();
+  launch_gram(g);
+  const int nwords = (int)(M_An->mc_length / 4);
+  plane_counts_kernel<<<(nplanes * 32 + 255) / 256, 256, 0, stream()>>>(planes, (long long)M_ZtSn->mc_length,
+                                                                     mask.as<uint8_t>(), nwords, nplanes,
+                                                                     d_all.as<long long>());
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+  AnZtSnFinish p{};
+  p.pos = d_pos.as<double>(); p.all = d_all.as<long long>();
+  p.n = n; p.nS = nS; p.ncols_per = M_ZtSn->ncols_per_z;
+  p.min_d = M_ZtSn->min_d; p.mlt_d = M_ZtSn->mlt_d;
+  p.out_r = d_or.as<unsigned long long>(); p.s_off = d_so.as<unsigned long long>();
+  p.out = d_out.as<double>();
+  an_ztsn_finish_kernel<<<(unsigned)(((long long)n * nS + 255) / 256), 256, 0, stream()>>>(p);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
   copy_back(out->lf, d_out, length);

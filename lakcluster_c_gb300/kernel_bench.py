@@ -134,7 +134,8 @@ def bench_an_ztsn(lib, rng, reps):
                                  C.byref(out))
     s = _time(call, reps)
     return {"seconds": s, "bitops": float(n) * (B + 1) * An.s.mc_length * 8, "bytes": An.s.rpop_b * An.s.mc_length,
-            "kernel": "an_ztsn_kernel", "bound": "hbm (each An row read once, 33 plane rows from L2)"}
+            "kernel": "the masked-AND Gram of the An rows against the 33 planes (gram kernels), an_ztsn_finish_kernel",
+            "bound": "integer or tensor pipe (the Gram)"}
 
 
 def bench_anzt_s_wnyt(lib, rng, reps):

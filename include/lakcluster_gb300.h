@@ -466,6 +466,20 @@ void lakgb_L_to_host(struct L_handle *L);
 void lakgb_L_sub(struct L_handle *dst, const struct L_handle *src);
 void lakgb_L_transpose(struct L_handle *dst, const struct L_handle *src);
 
+/* Joined groups of calls (the reference runs a stage's calls on thread slots
+ * and joins them with GLOBAL_pthread_tuc): between lakgb_defer_begin and the
+ * matching lakgb_defer_end, this host thread's calls write their host
+ * outputs only when the outermost scope ends -- the kernels are enqueued and
+ * the copies into the L_handles made then, with one wait for all of them.
+ * wrap_AnZt_S_WnYt_vv__run, wrap_AtTYn____WtSZn_vv__run and (with residency
+ * on and the tensor-core bit-plane kernel, B_MLT 8 / 16 / 32)
+ * wrap_At_T_YnWt_S_Zn_ww__run calls are also held back and run as one
+ * launch per entry point then (their FP64 sums are long dependent chains).
+ * Read the outputs only after lakgb_defer_end; every output equals the one
+ * the call makes alone. */
+void lakgb_defer_begin(void);
+void lakgb_defer_end(void);
+
 /* Allocation-free quantisation (no counterpart in the reference): the
  * arithmetic of wrap_xcalc on caller-owned device buffers, for callers that
  * must not allocate device memory -- e.g. a process whose device memory is

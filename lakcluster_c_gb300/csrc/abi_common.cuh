@@ -92,7 +92,24 @@ inline DBuf upload_vec(const std::vector<T> &v) {
   return upload_bytes(v.data(), v.size() * sizeof(T));
 }
 
-inline void copy_back(double *host, const DBuf &dev, unsigned long long length, HostOutputFill *fill = nullptr) {
+// Deferral scopes (lakgb_defer_begin / lakgb_defer_end, loopsum.cu): whether
+// this host thread is inside one, and a group of held-back calls that another
+// translation unit keeps -- `enqueue` launches them and their copies back to
+// the host on the library stream when the outermost scope ends, `clear`
+// releases them after the stream has drained.
+bool defer_active();
+void defer_register(void (*enqueue)(), void (*clear)());
+// A copy of `length` doubles of `dev` into `host`, made when the scope ends.
+void defer_copy(double *host, DBuf &&dev, unsigned long long length);
+
+// The call's device output into its host L_handle -- inside a deferral scope
+// when the scope ends (the device buffer is kept until then).
+inline void copy_back(double *host, DBuf &dev, unsigned long long length, HostOutputFill *fill = nullptr) {
+  if (defer_active()) {
+    if (fill) fill->copied = true;
+    defer_copy(host, std::move(dev), length);
+    return;
+  }
   if (profile_calls_on()) {  // time the wait for the producing kernels apart from the copy
     LAKGB_PROFILE_CALL("(kernel wait)");
     LAKGB_CUDA(cudaStreamSynchronize(stream()));

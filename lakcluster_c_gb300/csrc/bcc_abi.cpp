@@ -22,7 +22,8 @@ void release_L(L_handle *L) {
 }
 
 const lakbcc::Hooks kHooks = {release_L,       lakgb_forget_host_buffer, lakgb_L_mirror,      lakgb_L_release_mirror,
-                               lakgb_L_to_host, lakgb_L_sub,              lakgb_L_transpose, lakgb_L_mirror_zero};
+                               lakgb_L_to_host, lakgb_L_sub,              lakgb_L_transpose, lakgb_L_mirror_zero,
+                               lakgb_defer_begin, lakgb_defer_end};
 
 long row_bytes_min(int ncols) { return (long)(ncols + (16 - ncols % 16) % 16) / 8; }
 

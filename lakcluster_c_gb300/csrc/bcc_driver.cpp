@@ -180,6 +180,12 @@ struct State {
     if (hooks && hooks->L_sub) { hooks->L_sub(dst, src); return; }
     for (unsigned long long i = 0; i < dst->length; ++i) dst->lf[i] -= src->lf[i];
   }
+  void defer_begin() {
+    if (hooks && hooks->defer_begin) hooks->defer_begin();
+  }
+  void defer_end() {
+    if (hooks && hooks->defer_end) hooks->defer_end();
+  }
   void transpose(L_handle *dst, const L_handle *src) {
     if (hooks && hooks->L_transpose) { hooks->L_transpose(dst, src); return; }
     lh_transpose(dst, src);
@@ -750,20 +756,26 @@ void lrup_mxset(State &S) {
 // ---------------------------------------------------------------------------
 // stages
 
+// The stages below run their independent calls as one joined group (a
+// deferral scope): no call reads another's output before the stage ends.
 void An_ajdk_all(State &S) {  // bcc_An_ajdk (bcc_lf.c:7-51)
+  S.defer_begin();
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_An->p(), S.A_ajdk.data(), &E->lf_An_ajdk);
     if (E->Z_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_Zn->p(), S.A_ajdk.data(), &E->lf_Zn_ajdk);
   }
+  S.defer_end();
 }
 
 void lf_ZtSn_all(State &S) {  // bcc_lf_ZtSn (bcc_lf.c:53-100)
+  S.defer_begin();
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother)
       wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_At->p(), E->M_Tt->p(), nullptr, nullptr, nullptr, &E->lf_AtTn);
     if (E->Z_rbother && S.A_cbother)
       wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_Zt->p(), E->M_St->p(), nullptr, nullptr, nullptr, &E->lf_ZtSn);
   }
+  S.defer_end();
 }
 
 void lf_YnWt_all(State &S) {  // bcc_lf_YnWt (bcc_lf.c:223-290)
@@ -900,6 +912,8 @@ void lrup_QC_ZtSWn(State &S) {
 }
 
 void lf_AnZt_S_WnYt_all(State &S) {  // bcc_lf_AnZt_S_WnYt (bcc_lf.c:360-410)
+  // the bin pairs' products are independent: one joined group
+  S.defer_begin();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
@@ -909,6 +923,7 @@ void lf_AnZt_S_WnYt_all(State &S) {  // bcc_lf_AnZt_S_WnYt (bcc_lf.c:360-410)
       if (S.A_cbother && E1->A_rbother && E2->A_rbother)
         wrap_AnZt_S_WnYt_vv__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->M_Tt->p(), E2->M_An->p(), F->lf_AnAt, F->lf_AnAt, &F->lf_AnAt_T_AnAt);
     }
+  S.defer_end();
 }
 
 void set_l1(L_handle *L, unsigned long long length) {
@@ -1065,11 +1080,13 @@ void singlestudy_ww(State &S) {  // bcc_singlestudy_ww (bcc_flattenloop.c:773-83
                  E->lf_An_a1d1->lf, &E->M_An->h.nrows, &one, &out, &b_mlt, 0);
     }
   }
+  S.defer_begin();
   for (auto &Ep : S.E) {
     Single *E = Ep.get();
     if (E->A_rbother && S.A_cbother)
       wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E->M_At->p(), E->lf_An_a1d1, E->M_An_a1d1->p(), E->M_1->p(), &E->lf_At_An_a1d1);
   }
+  S.defer_end();
   for (auto &Ep : S.E) singlestudy_vv(S, Ep.get());
 }
 
@@ -1107,6 +1124,7 @@ void doublestudy_ww(State &S) {  // bcc_doublestudy_ww (bcc_flattenloop.c:977-10
                  E->lf_a2d2_AtTn->lf, &E->M_At->h.nrows, &E->M_Tt->h.nrows, &out, &b_mlt, 0);
     }
   }
+  S.defer_begin();  // the bin pairs' products, read from flattenloop on
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
@@ -1119,6 +1137,7 @@ void doublestudy_ww(State &S) {  // bcc_doublestudy_ww (bcc_flattenloop.c:977-10
       if (E1->A_rbother && S.A_cbother && E2->A_rbother)
         wrap_An_ZtSn_ww__run(TARGS, SP_a, SP_a, E1->M_An->p(), E2->lf_a2d2_AtTn, E2->M_a2d2_AtTn->p(), E2->M_Tt->p(), &F->lf_An_a2d2_At_Tn);
     }
+  S.defer_end();
 }
 
 double mask_sum(State &S, M_handle *An, int k) {
@@ -1705,10 +1724,12 @@ void lrup_QR(State &S) {  // bcc_lrup_QR_YnWt_stage_0/1/3 (bcc_lrup.c:659-892)
   if (qr_condense(S.P)) {
     lrup_QR_condense(S);
   } else {
+  S.defer_begin();
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_jn->p(), aj, &E->lf_jn_ajdk);
     if (E->Z_rbother && S.A_cbother) wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_vn->p(), aj, &E->lf_vn_ajdk);
   }
+  S.defer_end();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
@@ -1740,7 +1761,8 @@ void lrup_QR(State &S) {  // bcc_lrup_QR_YnWt_stage_0/1/3 (bcc_lrup.c:659-892)
 
 void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5-481)
   double *aj = S.A_ajdk.data();
-  // a0
+  // a0 (its outputs are read from a1 on: one joined group)
+  S.defer_begin();
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother) {
       wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_kn->p(), aj, &E->lf_kn_ajdk);
@@ -1752,6 +1774,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       wrap_An_ajdk_v(TARGS, T_pm, SP_a, E->M_vn->p(), aj, &E->lf_vn_ajdk);
     }
   }
+  S.defer_end();
   g_clock.tick("lrup_QC_a0");
   // a1
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
@@ -1795,7 +1818,8 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       }
     }
   g_clock.tick("lrup_QC_a2");
-  // a3
+  // a3: independent bit-plane products of every bin pair, one joined group
+  S.defer_begin();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
@@ -1810,6 +1834,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
           bitplane_excerpt(S, F->M_knkt_trm, E1->M_kt, E1->M_rt, E1->M_kn, E2->M_kn, E2->M_rt, E2->M_kt, F->M_knkt, &F->lf_kt_r_knkt_r_kn);
       }
     }
+  S.defer_end();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2), *Ft = S.f(nb2, nb1);
@@ -1820,7 +1845,8 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       }
     }
   g_clock.tick("lrup_QC_a3");
-  // b0
+  // b0 (its outputs are read from b1 on: one joined group)
+  S.defer_begin();
   for (auto &E : S.E) {
     if (E->A_rbother && S.A_cbother) {
       wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_at->p(), E->M_tt->p(), nullptr, nullptr, nullptr, &E->lf_attn);
@@ -1833,6 +1859,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       wrap_AnZt_vv__run(TARGS, T_pm, SP_a, SP_a, E->M_vt->p(), E->M_St->p(), nullptr, nullptr, nullptr, &E->lf_vtsn);
     }
   }
+  S.defer_end();
   g_clock.tick("lrup_QC_b0");
   // b1
   for (auto &E : S.E) {
@@ -1847,7 +1874,8 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
     S.mirror(E->lf_ztsvn); S.mirror(E->lf_attjn); S.mirror(E->lf_ktrhn);
   }
   g_clock.tick("lrup_QC_b1");
-  // b2
+  // b2: independent products of every bin pair, one joined group
+  S.defer_begin();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
@@ -1862,6 +1890,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
           wrap_AtTYn____WtSZn_vv__run(TARGS, SP_a, SP_a, E1->M_kt->p(), E1->M_rt->p(), E1->M_ht->p(), E2->M_ht->p(), E2->M_rt->p(), E2->M_kt->p(), aj, E1->lf_ktrhn, E2->lf_ktrhn, &F->lf_ktrhn____htrkn);
       }
     }
+  S.defer_end();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2), *Ft = S.f(nb2, nb1);

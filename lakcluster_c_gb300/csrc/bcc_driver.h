@@ -96,6 +96,11 @@ struct Hooks {
   // As L_mirror for an L whose values are all zero (freshly allocated): the
   // device copy is zero-filled, nothing is uploaded.  Null: L_mirror is used.
   void (*L_mirror_zero)(L_handle *L) = nullptr;
+  // A scope whose kernel calls may run together when it ends (the reference
+  // runs them on thread slots and joins them, GLOBAL_pthread_tuc): outputs
+  // are read only after defer_end.  Null: every call completes at once.
+  void (*defer_begin)() = nullptr;
+  void (*defer_end)() = nullptr;
 };
 
 // The scorebox grid (S_handle outputs, dir_c/S_init.c): row_num x col_num

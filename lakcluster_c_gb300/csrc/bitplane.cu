@@ -30,6 +30,7 @@
 // SNP) then run the FP64 recurrence over the chunk's Wn rows in order.
 #include <atomic>
 #include <mutex>
+#include <optional>
 
 #include "abi_common.cuh"
 #include "bcc_model.h"
@@ -550,6 +551,52 @@ extern "C" void lakgb_set_bitplane_impl(int impl) {
 
 extern "C" int lakgb_bitplane_impl(void) { return g_bitplane_impl.load(); }
 
+namespace lakgb {
+namespace {
+
+// Bit-plane products held back by a deferral scope (tensor-core path): the
+// prep kernels of each call run when it is made; the main kernels of all
+// calls with the same B run as one grouped launch when the scope ends.
+struct BitplaneDeferred {
+  BitplaneParams p{};
+  int nT = 0;
+  std::vector<DBuf> keep;
+  double *host_out = nullptr;
+  unsigned long long length = 0;
+};
+thread_local std::vector<BitplaneDeferred> t_bp;
+thread_local std::vector<DBuf> t_bp_groups;
+
+void bitplane_deferred_enqueue() {
+  for (int B : {8, 16, 32}) {
+    std::vector<BitplaneParams> ps;
+    std::vector<int> tile0;
+    int tiles = 0;
+    for (const auto &d : t_bp)
+      if (d.p.B == B) {
+        ps.push_back(d.p);
+        tile0.push_back(tiles);
+        tiles += bitplane_tc_tiles(d.p, d.nT);
+      }
+    if (ps.empty()) continue;
+    t_bp_groups.push_back(upload_vec(ps));
+    t_bp_groups.push_back(upload_vec(tile0));
+    launch_bitplane_tc_group(B, t_bp_groups[t_bp_groups.size() - 2].as<BitplaneParams>(),
+                             t_bp_groups.back().as<int>(), (int)ps.size(), tiles, stream());
+  }
+  for (const auto &d : t_bp)
+    if (d.length)
+      LAKGB_CUDA(cudaMemcpyAsync(d.host_out, d.p.out, d.length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+}
+
+void bitplane_deferred_clear() {
+  t_bp.clear();
+  t_bp_groups.clear();
+}
+
+}  // namespace
+}  // namespace lakgb
+
 extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *thread_in, int spacing_a,
                                            int spacing_t, M_handle *M_At, M_handle *M_Tt, M_handle *M_Yn,
                                            M_handle *M_Wn, M_handle *M_St, M_handle *M_Zt, double *A_ajdk,
@@ -600,8 +647,17 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   }
   for (int mw = 0; mw < nW; ++mw) mw_a[mw] = M_Wn->m_a_[mw];
 
+  // Inside a deferral scope the tensor-core main kernel waits for the scope's
+  // end (its uploads are then owned buffers, not staging views).  Only with
+  // residency on: the matrices' device copies must stay where they are until
+  // the scope ends, which an upload of the same host buffer without residency
+  // would not guarantee.
+  const bool defer = defer_active() && residency_enabled() &&
+                     g_bitplane_impl.load(std::memory_order_relaxed) == LAKGB_IMPL_TENSOR &&
+                     (B == 8 || B == 16 || B == 32);
   BitplaneParams p{};
-  Stager st;
+  std::optional<Stager> st;
+  if (!defer) st.emplace();
   p.At = (const uint8_t *)resident(M_At->wX, (size_t)M_At->rpop_b * M_At->mc_length);
   p.at_row_bytes = (long long)M_At->mc_length;
   p.Tt = (const uint8_t *)resident(M_Tt->wX, (size_t)M_Tt->rpop_b * M_Tt->mc_length);
@@ -626,7 +682,7 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   DBuf d_Tb((size_t)nT * sizeof(double)), d_Tt((size_t)nT * nW * sizeof(double));
   {
     const long long warps = (long long)nq * nT;
-    st.flush();
+    if (st) st->flush();
     bitplane_prep_kernel<<<(int)((warps * 32 + 255) / 256), 256, 0, stream()>>>(p, nT, d_pm.as<int>(), d_ycnt.as<int>());
     LAKGB_CUDA(cudaGetLastError());
     const int n = nT * (nW + 1);
@@ -638,6 +694,19 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   p.out = d_out.as<double>();
+  if (defer) {
+    BitplaneDeferred d;
+    d.p = p;
+    d.nT = nT;
+    d.host_out = out->lf;
+    d.length = length;
+    for (DBuf *b : {&mask, &d_at, &d_zt, &d_tt, &d_mw, &d_vS, &d_aA, &d_aZ, &d_oo, &d_to, &d_pm, &d_ycnt, &d_Tb, &d_Tt,
+                    &d_out})
+      d.keep.push_back(std::move(*b));
+    t_bp.push_back(std::move(d));
+    defer_register(bitplane_deferred_enqueue, bitplane_deferred_clear);
+    return (int)length;
+  }
   const size_t smem = std::max((size_t)(kBP_M + kBP_N) * kLd * sizeof(uint32_t),
                                (size_t)kBP_M * (kBP_N + 1) * sizeof(int) + (size_t)kBP_M * kBP_N * sizeof(double));
   static std::once_flag attr;

@@ -31,5 +31,10 @@ struct BitplaneParams {
 // The tensor-core main kernel (bitplane_tc.cu), in place of
 // bitplane_main_kernel; requires B in {8, 16, 32}.
 void launch_bitplane_tc(const BitplaneParams &p, int nT, cudaStream_t s);
+// CTAs of one call (pair tiles x covariate columns), and many calls of the
+// same B in one launch: ps / tile0 in device memory, tile0 the prefix sums
+// of the calls' CTA counts, `tiles` their total.
+int bitplane_tc_tiles(const BitplaneParams &p, int nT);
+void launch_bitplane_tc_group(int B, const BitplaneParams *ps, const int *tile0, int n, int tiles, cudaStream_t s);
 
 }  // namespace lakgb

@@ -24,6 +24,8 @@
 //   warps 13-16 fold: thread = SNP pair = TMEM lane.
 // Every wait is bounded (tc_ptx.cuh); a pipeline error is recorded in the
 // tensor-core status word read by lakgb_device_status.
+#include <mutex>
+
 #include "bitplane.cuh"
 #include "gram.cuh"
 #include "lakgb_runtime.cuh"
@@ -73,15 +75,14 @@ __device__ __forceinline__ int plane_row(int mw, int k, int ncols_per) {
   return mw * ncols_per + ncols_per - 1 - k;
 }
 
+// One CTA's work: SNP pairs pair0 .. pair0 + 127 of covariate column t.
 template <int B>
-__global__ void __launch_bounds__(kThreads, 1) bitplane_tc_kernel(BitplaneParams p, int *status) {
+__device__ __forceinline__ void bitplane_tc_cta(const BitplaneParams &p, int t, int pair0, int *status) {
   constexpr int CW = kN / B;  // Wn rows per N tile
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ Smem sm;
   uint8_t *stages = dsm + ((1024 - (tc::smem_u32(dsm) & 1023)) & 1023);
 
-  const int t = blockIdx.y;
-  const int pair0 = blockIdx.x * kM;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   volatile int *abort = &sm.abort;
   const int NT = (p.nW + CW - 1) / CW;   // N tiles
@@ -286,15 +287,49 @@ __global__ void __launch_bounds__(kThreads, 1) bitplane_tc_kernel(BitplaneParams
 }
 
 template <int B>
+__global__ void __launch_bounds__(kThreads, 1) bitplane_tc_kernel(BitplaneParams p, int *status) {
+  bitplane_tc_cta<B>(p, blockIdx.y, blockIdx.x * kM, status);
+}
+
+// Several calls in one launch (a deferral scope's group): CTA k belongs to
+// the last call whose tile0 <= k; within it, pair tile (k - tile0) % pair
+// tiles, covariate column (k - tile0) / pair tiles.
+template <int B>
+__global__ void __launch_bounds__(kThreads, 1) bitplane_tc_group_kernel(const BitplaneParams *ps, const int *tile0,
+                                                                       int n, int *status) {
+  const int k = blockIdx.x;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile0[mid] <= k) lo = mid; else hi = mid - 1;
+  }
+  const BitplaneParams &p = ps[lo];
+  const int ptiles = (p.npairs + kM - 1) / kM;
+  const int j = k - tile0[lo];
+  bitplane_tc_cta<B>(p, j / ptiles, (j % ptiles) * kM, status);
+}
+
+template <int B>
 void launch_b(const BitplaneParams &p, int nT, cudaStream_t s) {
-  static bool configured = false;
-  if (!configured) {
+  static std::once_flag configured;
+  std::call_once(configured, [] {
     LAKGB_CUDA(cudaFuncSetAttribute(bitplane_tc_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kSmemBytes));
-    configured = true;
-  }
+  });
   dim3 grid((p.npairs + kM - 1) / kM, nT);
   bitplane_tc_kernel<B><<<grid, kThreads, kSmemBytes, s>>>(p, tc_status_device_ptr());
+  LAKGB_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+template <int B>
+void launch_group_b(const BitplaneParams *ps, const int *tile0, int n, int tiles, cudaStream_t s) {
+  static std::once_flag configured;
+  std::call_once(configured, [] {
+    LAKGB_CUDA(cudaFuncSetAttribute(bitplane_tc_group_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmemBytes));
+  });
+  bitplane_tc_group_kernel<B><<<tiles, kThreads, kSmemBytes, s>>>(ps, tile0, n, tc_status_device_ptr());
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
 }
@@ -308,6 +343,17 @@ void launch_bitplane_tc(const BitplaneParams &p, int nT, cudaStream_t s) {
     launch_b<16>(p, nT, s);
   else
     launch_b<8>(p, nT, s);
+}
+
+int bitplane_tc_tiles(const BitplaneParams &p, int nT) { return ((p.npairs + kM - 1) / kM) * nT; }
+
+void launch_bitplane_tc_group(int B, const BitplaneParams *ps, const int *tile0, int n, int tiles, cudaStream_t s) {
+  if (B == 32)
+    launch_group_b<32>(ps, tile0, n, tiles, s);
+  else if (B == 16)
+    launch_group_b<16>(ps, tile0, n, tiles, s);
+  else
+    launch_group_b<8>(ps, tile0, n, tiles, s);
 }
 
 }  // namespace lakgb

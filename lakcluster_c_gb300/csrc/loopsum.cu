@@ -19,6 +19,8 @@
 // The popcount is a tiled XOR Gram: per 1920-bit block the CTA stages
 // (At ^ Tt) & mask for 64 At rows and Yt & mask for 64 Yt rows, and each
 // thread accumulates a 4 x 4 tile of integer counts over all blocks.
+#include <optional>
+
 #include "abi_common.cuh"
 #include "lmirror.cuh"
 #include "bcc_model.h"
@@ -57,26 +59,32 @@ DBuf upload_L(const L_handle *L, bool three_d) {
 // products in mz order.  The additions stay sequential per row; the loads
 // and multiplies run 256 wide.
 constexpr int kSW_R = 16, kSW_Z = 128, kSW_T = 256;
-__global__ void __launch_bounds__(kSW_T) anzt_s_wnyt_kernel(
-    const double *A, const unsigned long long *a_r, const unsigned long long *a_c, const double *Y,
-    const unsigned long long *y_r, const unsigned long long *y_c, const int8_t *vS, int nA, int nZ, int nS,
-    const unsigned long long *out_r, const unsigned long long *s_off, double *out) {
+struct SwnytCall {
+  const double *A; const unsigned long long *a_r, *a_c;
+  const double *Y; const unsigned long long *y_r, *y_c;
+  const int8_t *vS; int nA, nZ, nS;
+  const unsigned long long *out_r, *s_off;
+  double *out;
+  int tile0;  // grouped launch: first CTA of this call
+};
+
+// CTA (row tile rt, covariate s) of one call.
+__device__ __forceinline__ void anzt_s_wnyt_tile(const SwnytCall &c, int rt, int s) {
   __shared__ double prod[kSW_Z][kSW_R + 1];
-  const int r0 = blockIdx.x * kSW_R;
-  const int s = blockIdx.y;
-  const int8_t *vs = vS + (long long)s * nZ;
+  const int r0 = rt * kSW_R;
+  const int8_t *vs = c.vS + (long long)s * c.nZ;
   const int lr = threadIdx.x % kSW_R, lz = threadIdx.x / kSW_R;   // 16 rows x 16 columns per pass
   const int ma = r0 + lr;
-  const unsigned long long ar = ma < nA ? a_r[ma] : 0, yr = ma < nA ? y_r[ma] : 0;
+  const unsigned long long ar = ma < c.nA ? c.a_r[ma] : 0, yr = ma < c.nA ? c.y_r[ma] : 0;
   double acc = 0.0;
-  for (int z0 = 0; z0 < nZ; z0 += kSW_Z) {
-    const int zn = min(kSW_Z, nZ - z0);
+  for (int z0 = 0; z0 < c.nZ; z0 += kSW_Z) {
+    const int zn = min(kSW_Z, c.nZ - z0);
     __syncthreads();
     for (int z = lz; z < zn; z += kSW_T / kSW_R) {
       double v = 0.0;
-      if (ma < nA) {
+      if (ma < c.nA) {
         const int mz = z0 + z;
-        v = __dmul_rn(__dmul_rn(A[ar + a_c[mz]], (double)vs[mz]), Y[yr + y_c[mz]]);
+        v = __dmul_rn(__dmul_rn(c.A[ar + c.a_c[mz]], (double)vs[mz]), c.Y[yr + c.y_c[mz]]);
       }
       prod[z][lr] = v;
     }
@@ -84,23 +92,88 @@ __global__ void __launch_bounds__(kSW_T) anzt_s_wnyt_kernel(
     if (threadIdx.x < kSW_R)
       for (int z = 0; z < zn; ++z) acc = __dadd_rn(acc, prod[z][threadIdx.x]);
   }
-  if (threadIdx.x < kSW_R && r0 + threadIdx.x < nA) out[out_r[r0 + threadIdx.x] + s_off[s]] = acc;
+  if (threadIdx.x < kSW_R && r0 + threadIdx.x < c.nA) c.out[c.out_r[r0 + threadIdx.x] + c.s_off[s]] = acc;
 }
 
-__global__ void attyn_wtszn_kernel(const double *AY, const unsigned long long *ay_a, const unsigned long long *ay_y,
-                                   const unsigned long long *ay_s, const double *ZW, const unsigned long long *zw_z,
-                                   const unsigned long long *zw_w, const unsigned long long *zw_s, const double *Dy,
-                                   int npairs, int ninner, int nS, const unsigned long long *out_r,
-                                   const unsigned long long *s_off, double *out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = blockIdx.y;
-  if (i >= npairs || s >= nS) return;
-  const unsigned long long a0 = ay_a[i] + ay_s[s], z0 = zw_z[i] + zw_s[s];
-  double acc = 0.0;
-  for (int k = 0; k < ninner; ++k)
-    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(AY[a0 + ay_y[k]], Dy[k]), ZW[z0 + zw_w[k]]));
-  out[out_r[i] + s_off[s]] = acc;
+__global__ void __launch_bounds__(kSW_T) anzt_s_wnyt_kernel(SwnytCall c) {
+  anzt_s_wnyt_tile(c, blockIdx.x, blockIdx.y);
 }
+
+// Several calls in one launch (a deferred group, lakgb_defer_end): CTA k
+// belongs to the last call whose tile0 <= k; within it, row tile (k - tile0)
+// % row tiles, covariate (k - tile0) / row tiles.
+__global__ void __launch_bounds__(kSW_T) anzt_s_wnyt_group_kernel(const SwnytCall *calls, int n) {
+  const int k = blockIdx.x;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (calls[mid].tile0 <= k) lo = mid; else hi = mid - 1;
+  }
+  const SwnytCall &c = calls[lo];
+  const int rtiles = (c.nA + kSW_R - 1) / kSW_R;
+  const int j = k - c.tile0;
+  anzt_s_wnyt_tile(c, j % rtiles, j / rtiles);
+}
+
+// The calls a deferral scope holds back (this host thread): their device
+// inputs and outputs, and where each output goes on the host.
+struct SwnytDeferred {
+  SwnytCall c{};
+  std::vector<DBuf> keep;   // uploads and the device output
+  double *host_out = nullptr;
+  unsigned long long length = 0;
+};
+
+struct WtszCall {
+  const double *AY; const unsigned long long *ay_a, *ay_y, *ay_s;
+  const double *ZW; const unsigned long long *zw_z, *zw_w, *zw_s;
+  const double *Dy; int npairs, ninner, nS;
+  const unsigned long long *out_r, *s_off;
+  double *out;
+  int tile0;  // grouped launch: first CTA of this call
+};
+constexpr int kWZ_T = 128;
+
+// Thread = (pair i, covariate s): the sum over the inner rows in order.
+__device__ __forceinline__ void attyn_wtszn_one(const WtszCall &c, int i, int s) {
+  if (i >= c.npairs || s >= c.nS) return;
+  const unsigned long long a0 = c.ay_a[i] + c.ay_s[s], z0 = c.zw_z[i] + c.zw_s[s];
+  double acc = 0.0;
+  for (int k = 0; k < c.ninner; ++k)
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(c.AY[a0 + c.ay_y[k]], c.Dy[k]), c.ZW[z0 + c.zw_w[k]]));
+  c.out[c.out_r[i] + c.s_off[s]] = acc;
+}
+
+__global__ void attyn_wtszn_kernel(WtszCall c) {
+  attyn_wtszn_one(c, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+__global__ void attyn_wtszn_group_kernel(const WtszCall *calls, int n) {
+  const int k = blockIdx.x;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (calls[mid].tile0 <= k) lo = mid; else hi = mid - 1;
+  }
+  const WtszCall &c = calls[lo];
+  const int ptiles = (c.npairs + kWZ_T - 1) / kWZ_T;
+  const int j = k - c.tile0;
+  attyn_wtszn_one(c, (j % ptiles) * kWZ_T + threadIdx.x, j / ptiles);
+}
+
+struct WtszDeferred {
+  WtszCall c{};
+  std::vector<DBuf> keep;
+  double *host_out = nullptr;
+  unsigned long long length = 0;
+};
+thread_local int t_defer_depth = 0;
+thread_local std::vector<SwnytDeferred> t_swnyt;
+thread_local std::vector<WtszDeferred> t_wtsz;
+struct DeferKind { void (*enqueue)(); void (*clear)(); };
+thread_local std::vector<DeferKind> t_kinds;  // groups of other translation units
+struct DeferCopy { double *host; DBuf dev; unsigned long long length; };
+thread_local std::vector<DeferCopy> t_copies;  // other calls' outputs
 
 constexpr int kLd = kBlockWords + 1;
 constexpr int kTY_M = 64, kTY_N = 64, kTY_TM = 4, kTY_TN = 4, kTY_T = 256;
@@ -201,6 +274,18 @@ __global__ void __launch_bounds__(kTY_T, 2) attyn_kernel(AtTYnParams p) {
 
 }  // namespace
 
+bool defer_active() { return t_defer_depth > 0; }
+
+void defer_copy(double *host, DBuf &&dev, unsigned long long length) {
+  t_copies.push_back(DeferCopy{host, std::move(dev), length});
+}
+
+void defer_register(void (*enqueue)(), void (*clear)()) {
+  for (const DeferKind &k : t_kinds)
+    if (k.enqueue == enqueue) return;
+  t_kinds.push_back({enqueue, clear});
+}
+
 }  // namespace lakgb
 
 using namespace lakgb;
@@ -246,7 +331,11 @@ extern "C" int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *threa
   }
   // Mirrored matrices (lmirror.cu) are read in place.
   Mirror *mA = find_mirror(lf_AnZt), *mY = find_mirror(lf_YnWt);
-  Stager st;
+  // Inside a deferral scope the uploads are owned buffers (they must outlive
+  // the call), and the kernel runs at the end of the scope.
+  const bool defer = t_defer_depth > 0;
+  std::optional<Stager> st;
+  if (!defer) st.emplace();
   DBuf dA = mA ? DBuf() : upload_L(lf_AnZt, false);
   DBuf dY = (mY || lf_YnWt == lf_AnZt) ? DBuf() : upload_L(lf_YnWt, false);
   const double *pA = mA ? mA->d : dA.as<double>();
@@ -255,16 +344,88 @@ extern "C" int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *threa
   DBuf d_vS = upload_vec(vS), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
   DBuf d_out(length * sizeof(double));
   d_out.zero();
-  dim3 grid((nA + kSW_R - 1) / kSW_R, nS);
-  st.flush();
-  anzt_s_wnyt_kernel<<<grid, kSW_T, 0, stream()>>>(pA, d_ar.as<unsigned long long>(), d_ac.as<unsigned long long>(),
-                                                 pY, d_yr.as<unsigned long long>(), d_yc.as<unsigned long long>(),
-                                                 d_vS.as<int8_t>(), nA, nZ, nS, d_or.as<unsigned long long>(),
-                                                 d_so.as<unsigned long long>(), d_out.as<double>());
+  SwnytCall c{};
+  c.A = pA; c.a_r = d_ar.as<unsigned long long>(); c.a_c = d_ac.as<unsigned long long>();
+  c.Y = pY; c.y_r = d_yr.as<unsigned long long>(); c.y_c = d_yc.as<unsigned long long>();
+  c.vS = d_vS.as<int8_t>(); c.nA = nA; c.nZ = nZ; c.nS = nS;
+  c.out_r = d_or.as<unsigned long long>(); c.s_off = d_so.as<unsigned long long>(); c.out = d_out.as<double>();
+  if (defer) {
+    SwnytDeferred d;
+    d.c = c;
+    d.host_out = out->lf;
+    d.length = length;
+    for (DBuf *b : {&dA, &dY, &d_ar, &d_yr, &d_ac, &d_yc, &d_vS, &d_or, &d_so, &d_out}) d.keep.push_back(std::move(*b));
+    t_swnyt.push_back(std::move(d));
+    return (int)length;
+  }
+  st->flush();
+  anzt_s_wnyt_kernel<<<dim3((nA + kSW_R - 1) / kSW_R, nS), kSW_T, 0, stream()>>>(c);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
   copy_back(out->lf, d_out, length);
   return (int)length;
+}
+
+// Deferral scope: AnZt_S_WnYt and AtTYn____WtSZn calls made inside it (the
+// reference runs them on thread slots and joins them afterwards,
+// GLOBAL_pthread_tuc) are held back and run together when the outermost scope
+// ends -- one grouped launch per kind, then every output copied into its host
+// L_handle.  Outputs are not to be read before the scope ends.
+extern "C" void lakgb_defer_begin(void) { ++t_defer_depth; }
+
+extern "C" void lakgb_defer_end(void) {
+  if (t_defer_depth <= 0 || --t_defer_depth > 0) return;
+  if (t_swnyt.empty() && t_wtsz.empty() && t_kinds.empty() && t_copies.empty()) return;
+  LAKGB_PROFILE_CALL("lakgb_defer_end");
+  std::vector<SwnytCall> c1;
+  std::vector<WtszCall> c2;
+  int tiles1 = 0, tiles2 = 0;
+  for (auto &d : t_swnyt) {
+    d.c.tile0 = tiles1;
+    tiles1 += ((d.c.nA + kSW_R - 1) / kSW_R) * d.c.nS;
+    c1.push_back(d.c);
+  }
+  for (auto &d : t_wtsz) {
+    d.c.tile0 = tiles2;
+    tiles2 += ((d.c.npairs + kWZ_T - 1) / kWZ_T) * d.c.nS;
+    c2.push_back(d.c);
+  }
+  {
+    DBuf d_c1, d_c2;
+    if (!c1.empty()) {
+      d_c1 = upload_vec(c1);
+      anzt_s_wnyt_group_kernel<<<tiles1, kSW_T, 0, stream()>>>(d_c1.as<SwnytCall>(), (int)c1.size());
+      LAKGB_CUDA(cudaGetLastError());
+      count_launch();
+    }
+    if (!c2.empty()) {
+      d_c2 = upload_vec(c2);
+      attyn_wtszn_group_kernel<<<tiles2, kWZ_T, 0, stream()>>>(d_c2.as<WtszCall>(), (int)c2.size());
+      LAKGB_CUDA(cudaGetLastError());
+      count_launch();
+    }
+    for (const DeferKind &k : t_kinds) k.enqueue();
+    if (profile_calls_on()) {
+      LAKGB_PROFILE_CALL("(kernel wait)");
+      LAKGB_CUDA(cudaStreamSynchronize(stream()));
+    }
+    LAKGB_PROFILE_CALL("(copy back + sync)");
+    for (auto &d : t_swnyt)
+      if (d.length)
+        LAKGB_CUDA(cudaMemcpyAsync(d.host_out, d.c.out, d.length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    for (auto &d : t_wtsz)
+      if (d.length)
+        LAKGB_CUDA(cudaMemcpyAsync(d.host_out, d.c.out, d.length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    for (auto &c : t_copies)
+      if (c.length)
+        LAKGB_CUDA(cudaMemcpyAsync(c.host, c.dev.p, c.length * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  }
+  t_copies.clear();
+  t_swnyt.clear();
+  t_wtsz.clear();
+  for (const DeferKind &k : t_kinds) k.clear();
+  t_kinds.clear();
 }
 
 extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *thread_in, int output_spacing_a,
@@ -311,9 +472,12 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
     set_error(4, "wrap_AtTYn____WtSZn_vv__run: L_handle smaller than the rows and columns it is indexed by");
     return (int)length;
   }
-  // Mirrored inputs (lmirror.cu) are read in place.
+  // Mirrored inputs (lmirror.cu) are read in place; inside a deferral scope
+  // the uploads are owned buffers and the kernel runs when the scope ends.
   Mirror *mLA = find_mirror(LA), *mLZ = find_mirror(LZ);
-  Stager st;
+  const bool defer = t_defer_depth > 0;
+  std::optional<Stager> st;
+  if (!defer) st.emplace();
   DBuf dA = mLA ? DBuf() : upload_L(LA, true);
   DBuf dZ = (mLZ || LZ == LA) ? DBuf() : upload_L(LZ, true);
   const double *pA = mLA ? mLA->d : dA.as<double>();
@@ -323,13 +487,25 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
   DBuf d_D = upload_vec(Dy), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
   DBuf d_out(length * sizeof(double));
   d_out.zero();
-  dim3 grid((npairs + 127) / 128, nS);
-  st.flush();
-  attyn_wtszn_kernel<<<grid, 128, 0, stream()>>>(pA, d_aa.as<unsigned long long>(), d_ay.as<unsigned long long>(),
-                                                 d_as.as<unsigned long long>(), pZ, d_zz.as<unsigned long long>(),
-                                                 d_zw.as<unsigned long long>(), d_zs.as<unsigned long long>(),
-                                                 d_D.as<double>(), npairs, ninner, nS, d_or.as<unsigned long long>(),
-                                                 d_so.as<unsigned long long>(), d_out.as<double>());
+  WtszCall c{};
+  c.AY = pA; c.ay_a = d_aa.as<unsigned long long>(); c.ay_y = d_ay.as<unsigned long long>();
+  c.ay_s = d_as.as<unsigned long long>();
+  c.ZW = pZ; c.zw_z = d_zz.as<unsigned long long>(); c.zw_w = d_zw.as<unsigned long long>();
+  c.zw_s = d_zs.as<unsigned long long>();
+  c.Dy = d_D.as<double>(); c.npairs = npairs; c.ninner = ninner; c.nS = nS;
+  c.out_r = d_or.as<unsigned long long>(); c.s_off = d_so.as<unsigned long long>(); c.out = d_out.as<double>();
+  if (defer) {
+    WtszDeferred d;
+    d.c = c;
+    d.host_out = out->lf;
+    d.length = length;
+    for (DBuf *b : {&dA, &dZ, &d_aa, &d_ay, &d_as, &d_zz, &d_zw, &d_zs, &d_D, &d_or, &d_so, &d_out})
+      d.keep.push_back(std::move(*b));
+    t_wtsz.push_back(std::move(d));
+    return (int)length;
+  }
+  st->flush();
+  attyn_wtszn_kernel<<<dim3((npairs + kWZ_T - 1) / kWZ_T, nS), kWZ_T, 0, stream()>>>(c);
   LAKGB_CUDA(cudaGetLastError());
   count_launch();
   copy_back(out->lf, d_out, length);

@@ -96,11 +96,23 @@ inline DBuf upload_vec(const std::vector<T> &v) {
 // this host thread is inside one, and a group of held-back calls that another
 // translation unit keeps -- `enqueue` launches them and their copies back to
 // the host on the library stream when the outermost scope ends, `clear`
-// releases them after the stream has drained.
+// (after the stream has drained) sets what they leave in host structs and
+// releases them.
 bool defer_active();
 void defer_register(void (*enqueue)(), void (*clear)());
 // A copy of `length` doubles of `dev` into `host`, made when the scope ends.
 void defer_copy(double *host, DBuf &&dev, unsigned long long length);
+// Small inputs of a held-back call: copied into this thread's page-locked
+// scope chunks (reused from scope to scope) and sent by defer_flush() with one
+// asynchronous copy per call; the device pointer stays valid until the
+// outermost scope ends.
+const void *defer_put(const void *h, size_t n);
+void defer_flush();
+template <class T>
+inline DBuf defer_upload(const std::vector<T> &v) {
+  const size_t n = v.size() * sizeof(T);
+  return DBuf::view(defer_put(v.data(), n), n);
+}
 
 // The call's device output into its host L_handle -- inside a deferral scope
 // when the scope ends (the device buffer is kept until then).

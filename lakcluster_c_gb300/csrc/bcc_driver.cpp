@@ -1071,6 +1071,7 @@ void singlestudy_ww(State &S) {  // bcc_singlestudy_ww (bcc_flattenloop.c:773-83
       }
     }
   }
+  S.defer_begin();
   for (auto &Ep : S.E) {
     Single *E = Ep.get();
     if (E->A_rbother && S.A_cbother) {
@@ -1080,6 +1081,7 @@ void singlestudy_ww(State &S) {  // bcc_singlestudy_ww (bcc_flattenloop.c:773-83
                  E->lf_An_a1d1->lf, &E->M_An->h.nrows, &one, &out, &b_mlt, 0);
     }
   }
+  S.defer_end();
   S.defer_begin();
   for (auto &Ep : S.E) {
     Single *E = Ep.get();
@@ -1112,6 +1114,7 @@ void doublestudy_ww(State &S) {  // bcc_doublestudy_ww (bcc_flattenloop.c:977-10
     if (E->A_rbother && S.A_cbother) a2d2_excerpt(S, E->M_At->p(), E->M_Tt->p(), E->lf_AtTn, E->lf_a2d2_AtTn);
   }
   int b_mlt = S.P.B_MLT;
+  S.defer_begin();
   for (auto &E : S.E) {
     if (E->Z_rbother && S.A_cbother) {
       M_handle *out = E->M_a2d2_ZtSn->p();
@@ -1124,6 +1127,7 @@ void doublestudy_ww(State &S) {  // bcc_doublestudy_ww (bcc_flattenloop.c:977-10
                  E->lf_a2d2_AtTn->lf, &E->M_At->h.nrows, &E->M_Tt->h.nrows, &out, &b_mlt, 0);
     }
   }
+  S.defer_end();
   S.defer_begin();  // the bin pairs' products, read from flattenloop on
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
@@ -1803,7 +1807,9 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
       }
     }
   g_clock.tick("lrup_QC_a1");
-  // a2
+  // a2: the quantisations of every bin pair, one joined group (their planes
+  // and scalars are read from a3 on)
+  S.defer_begin();
   for (int nb1 = 0; nb1 < S.nbins; ++nb1)
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) {
       Double *F = S.f(nb1, nb2);
@@ -1817,6 +1823,7 @@ void lrup_QC(State &S) {  // bcc_lrup_QC_YnWt_stage_a0..a3, b0..b2 (bcc_lrup.c:5
         if (nb1 <= nb2) xcalc_excerpt(S, F->M_knkt_trm, E1->M_kn, E2->M_kn, F->lf_knkt, F->M_knkt);
       }
     }
+  S.defer_end();
   g_clock.tick("lrup_QC_a2");
   // a3: independent bit-plane products of every bin pair, one joined group
   S.defer_begin();

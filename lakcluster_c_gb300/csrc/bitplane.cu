@@ -579,8 +579,9 @@ void bitplane_deferred_enqueue() {
         tiles += bitplane_tc_tiles(d.p, d.nT);
       }
     if (ps.empty()) continue;
-    t_bp_groups.push_back(upload_vec(ps));
-    t_bp_groups.push_back(upload_vec(tile0));
+    t_bp_groups.push_back(defer_upload(ps));
+    t_bp_groups.push_back(defer_upload(tile0));
+    defer_flush();
     launch_bitplane_tc_group(B, t_bp_groups[t_bp_groups.size() - 2].as<BitplaneParams>(),
                              t_bp_groups.back().as<int>(), (int)ps.size(), tiles, stream());
   }
@@ -666,11 +667,15 @@ extern "C" int wrap_At_T_YnWt_S_Zn_ww__run(int *tidx, void **vpra, pthread_t *th
   p.plane_bytes = (long long)M_YnWt->mc_length;
   p.Zt = (const uint8_t *)resident(M_Zt->wX, (size_t)M_Zt->rpop_b * M_Zt->mc_length);
   p.zt_row_bytes = (long long)M_Zt->mc_length;
-  DBuf mask = upload_bytes(M_At->mc_j, M_At->mc_length);
+  // a held-back call's small inputs go through the scope's page-locked chunks
+  auto up = [&](const auto &v) { return defer ? defer_upload(v) : upload_vec(v); };
+  DBuf mask = defer ? DBuf::view(defer_put(M_At->mc_j, M_At->mc_length), M_At->mc_length)
+                    : upload_bytes(M_At->mc_j, M_At->mc_length);
   p.mask = mask.as<uint8_t>(); p.P = P; p.npairs = npairs;
-  DBuf d_at = upload_vec(at_rowb), d_zt = upload_vec(zt_rowb), d_tt = upload_vec(tt_rowb), d_mw = upload_vec(mw_a);
-  DBuf d_vS = upload_vec(vS), d_aA = upload_vec(aA), d_aZ = upload_vec(aZ);
-  DBuf d_oo = upload_vec(out_off), d_to = upload_vec(t_off);
+  DBuf d_at = up(at_rowb), d_zt = up(zt_rowb), d_tt = up(tt_rowb), d_mw = up(mw_a);
+  DBuf d_vS = up(vS), d_aA = up(aA), d_aZ = up(aZ);
+  DBuf d_oo = up(out_off), d_to = up(t_off);
+  if (defer) defer_flush();
   p.at_rowb = d_at.as<uint32_t>(); p.zt_rowb = d_zt.as<uint32_t>(); p.tt_rowb = d_tt.as<uint32_t>();
   p.mw_a = d_mw.as<uint32_t>(); p.nW = nW; p.B = B; p.ncols_per = ncols_per;
   p.vS = d_vS.as<int8_t>(); p.aA = d_aA.as<double>(); p.aZ = d_aZ.as<double>();

@@ -185,24 +185,47 @@ void DBuf::zero() {
 // address must never be served from an old device copy.
 bool residency_enabled() { return t_scope_depth > 0 || g_residency; }
 
+// The cache entries of one host buffer (any size): the map is ordered by host
+// pointer first, so they form one range.  Caller holds g_mu.
+void erase_host_locked(const void *host) {
+  auto it = g_res.lower_bound(std::make_pair(host, (size_t)0));
+  while (it != g_res.end() && it->first.first == host) {
+    cudaFreeAsync(it->second.d, stream());
+    it = g_res.erase(it);
+  }
+}
+
 const void *resident(const void *host, size_t bytes) {
   if (bytes == 0) return nullptr;
   stream();  // create the stream before taking the lock
-  std::lock_guard<std::mutex> lk(g_mu);
-  auto key = std::make_pair(host, bytes);
-  auto it = g_res.find(key);
+  const auto key = std::make_pair(host, bytes);
   const bool on = residency_enabled();
-  if (on && it != g_res.end()) return it->second.d;
-  if (it != g_res.end()) {
-    cudaFreeAsync(it->second.d, stream());
-    g_res.erase(it);
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_res.find(key);
+    if (on && it != g_res.end()) return it->second.d;
+    if (it != g_res.end()) {
+      cudaFreeAsync(it->second.d, stream());
+      g_res.erase(it);
+    }
   }
   if (!on && t_active) return t_active->put_bytes(host, bytes);
+  // The copy is made without the lock, so other threads' lookups do not wait
+  // for it; it completes before other threads' streams may read it.
   void *d = nullptr;
   LAKGB_CUDA(cudaMallocAsync(&d, bytes, stream()));
   LAKGB_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, stream()));
-  // Complete before other threads' streams may read it.
   LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_res.find(key);
+  if (it != g_res.end()) {  // another thread cached the same buffer meanwhile
+    if (on) {
+      cudaFreeAsync(d, stream());
+      return it->second.d;
+    }
+    cudaFreeAsync(it->second.d, stream());
+    g_res.erase(it);
+  }
   g_res[key] = ResEntry{d, bytes};
   if (t_scope_depth > 0) t_scope_keys.push_back(key);
   return d;
@@ -211,14 +234,7 @@ const void *resident(const void *host, size_t bytes) {
 void resident_put(const void *host, size_t bytes, DBuf &&d) {
   stream();
   std::lock_guard<std::mutex> lk(g_mu);
-  for (auto it = g_res.begin(); it != g_res.end();) {
-    if (it->first.first == host) {
-      cudaFreeAsync(it->second.d, stream());
-      it = g_res.erase(it);
-    } else {
-      ++it;
-    }
-  }
+  erase_host_locked(host);
   if (!residency_enabled() || bytes == 0 || !d.p) return;  // d frees itself
   const auto key = std::make_pair(host, bytes);
   g_res[key] = ResEntry{d.p, bytes};
@@ -408,15 +424,8 @@ extern "C" void lakgb_residency_scope(int enter) {
 
 extern "C" void lakgb_forget_host_buffer(const void *host_ptr) {
   stream();
-  std::lock_guard<std::mutex> lk(g_mu);
-  for (auto it = g_res.begin(); it != g_res.end();) {
-    if (it->first.first == host_ptr) {
-      cudaFreeAsync(it->second.d, stream());
-      it = g_res.erase(it);
-    } else {
-      ++it;
-    }
-  }
+  std::lock_guard<std::mutex> lk(lakgb::g_mu);
+  lakgb::erase_host_locked(host_ptr);
 }
 
 extern "C" unsigned long long lakgb_kernel_launches(void) { return g_launches.load(); }

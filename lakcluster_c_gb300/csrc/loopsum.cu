@@ -175,6 +175,15 @@ thread_local std::vector<DeferKind> t_kinds;  // groups of other translation uni
 struct DeferCopy { double *host; DBuf dev; unsigned long long length; };
 thread_local std::vector<DeferCopy> t_copies;  // other calls' outputs
 
+// Page-locked host chunks and their device twins for held-back calls'
+// inputs: bump-allocated, 16-byte aligned; `sent` is how much has been
+// copied.  Arrays larger than a chunk get a chunk of their own.  Reset (not
+// freed) when the outermost scope ends.
+struct UpChunk { uint8_t *h = nullptr; uint8_t *d = nullptr; size_t cap = 0, used = 0, sent = 0; };
+constexpr size_t kUpChunk = 4u << 20;
+thread_local std::vector<UpChunk> t_up;
+thread_local size_t t_up_cur = 0;
+
 constexpr int kLd = kBlockWords + 1;
 constexpr int kTY_M = 64, kTY_N = 64, kTY_TM = 4, kTY_TN = 4, kTY_T = 256;
 
@@ -276,6 +285,32 @@ __global__ void __launch_bounds__(kTY_T, 2) attyn_kernel(AtTYnParams p) {
 
 bool defer_active() { return t_defer_depth > 0; }
 
+const void *defer_put(const void *h, size_t n) {
+  const size_t need = (n + 15) & ~(size_t)15;
+  while (t_up_cur < t_up.size() && t_up[t_up_cur].used + need > t_up[t_up_cur].cap) ++t_up_cur;
+  if (t_up_cur == t_up.size()) {
+    if (!t_up.empty()) defer_flush();  // the earlier chunks' pending bytes go first
+    UpChunk c;
+    c.cap = std::max(kUpChunk, need);
+    LAKGB_CUDA(cudaHostAlloc((void **)&c.h, c.cap, cudaHostAllocDefault));
+    LAKGB_CUDA(cudaMalloc((void **)&c.d, c.cap));
+    t_up.push_back(c);
+  }
+  UpChunk &c = t_up[t_up_cur];
+  if (n) memcpy(c.h + c.used, h, n);
+  const void *d = c.d + c.used;
+  c.used += need;
+  return d;
+}
+
+void defer_flush() {
+  for (UpChunk &c : t_up) {
+    if (c.used > c.sent)
+      LAKGB_CUDA(cudaMemcpyAsync(c.d + c.sent, c.h + c.sent, c.used - c.sent, cudaMemcpyHostToDevice, stream()));
+    c.sent = c.used;
+  }
+}
+
 void defer_copy(double *host, DBuf &&dev, unsigned long long length) {
   t_copies.push_back(DeferCopy{host, std::move(dev), length});
 }
@@ -340,8 +375,10 @@ extern "C" int wrap_AnZt_S_WnYt_vv__run(int *tidx, void **vpra, pthread_t *threa
   DBuf dY = (mY || lf_YnWt == lf_AnZt) ? DBuf() : upload_L(lf_YnWt, false);
   const double *pA = mA ? mA->d : dA.as<double>();
   const double *pY = mY ? mY->d : ((lf_YnWt == lf_AnZt) ? pA : dY.as<double>());
-  DBuf d_ar = upload_vec(a_r), d_yr = upload_vec(y_r), d_ac = upload_vec(a_c), d_yc = upload_vec(y_c);
-  DBuf d_vS = upload_vec(vS), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
+  auto up = [&](const auto &v) { return defer ? defer_upload(v) : upload_vec(v); };
+  DBuf d_ar = up(a_r), d_yr = up(y_r), d_ac = up(a_c), d_yc = up(y_c);
+  DBuf d_vS = up(vS), d_or = up(out_r), d_so = up(s_off);
+  if (defer) defer_flush();
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   SwnytCall c{};
@@ -393,13 +430,15 @@ extern "C" void lakgb_defer_end(void) {
   {
     DBuf d_c1, d_c2;
     if (!c1.empty()) {
-      d_c1 = upload_vec(c1);
+      d_c1 = defer_upload(c1);
+      defer_flush();
       anzt_s_wnyt_group_kernel<<<tiles1, kSW_T, 0, stream()>>>(d_c1.as<SwnytCall>(), (int)c1.size());
       LAKGB_CUDA(cudaGetLastError());
       count_launch();
     }
     if (!c2.empty()) {
-      d_c2 = upload_vec(c2);
+      d_c2 = defer_upload(c2);
+      defer_flush();
       attyn_wtszn_group_kernel<<<tiles2, kWZ_T, 0, stream()>>>(d_c2.as<WtszCall>(), (int)c2.size());
       LAKGB_CUDA(cudaGetLastError());
       count_launch();
@@ -422,6 +461,8 @@ extern "C" void lakgb_defer_end(void) {
     LAKGB_CUDA(cudaStreamSynchronize(stream()));
   }
   t_copies.clear();
+  for (UpChunk &c : t_up) c.used = c.sent = 0;  // the stream has drained: reuse the chunks
+  t_up_cur = 0;
   t_swnyt.clear();
   t_wtsz.clear();
   for (const DeferKind &k : t_kinds) k.clear();
@@ -482,9 +523,11 @@ extern "C" int wrap_AtTYn____WtSZn_vv__run(int *tidx, void **vpra, pthread_t *th
   DBuf dZ = (mLZ || LZ == LA) ? DBuf() : upload_L(LZ, true);
   const double *pA = mLA ? mLA->d : dA.as<double>();
   const double *pZ = mLZ ? mLZ->d : ((LZ == LA) ? pA : dZ.as<double>());
-  DBuf d_aa = upload_vec(ay_a), d_ay = upload_vec(ay_y), d_as = upload_vec(ay_s);
-  DBuf d_zz = upload_vec(zw_z), d_zw = upload_vec(zw_w), d_zs = upload_vec(zw_s);
-  DBuf d_D = upload_vec(Dy), d_or = upload_vec(out_r), d_so = upload_vec(s_off);
+  auto up = [&](const auto &v) { return defer ? defer_upload(v) : upload_vec(v); };
+  DBuf d_aa = up(ay_a), d_ay = up(ay_y), d_as = up(ay_s);
+  DBuf d_zz = up(zw_z), d_zw = up(zw_w), d_zs = up(zw_s);
+  DBuf d_D = up(Dy), d_or = up(out_r), d_so = up(s_off);
+  if (defer) defer_flush();
   DBuf d_out(length * sizeof(double));
   d_out.zero();
   WtszCall c{};

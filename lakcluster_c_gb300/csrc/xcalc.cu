@@ -54,6 +54,7 @@ struct XcalcParams {
   uint8_t *planes;
   unsigned long long lf_n, planes_n;  // elements of lf, bytes of planes (bounds checks)
   int *bad;                  // set when an index would leave its buffer (access skipped)
+  const double *dev_scalars; // a deferred call: device min, max, mlt (then min / mlt above are unused)
 };
 
 // The masked min / max compare order keys instead of doubles: GB300's FP64
@@ -141,6 +142,35 @@ __global__ void xcalc_minmax_kernel(const double *lf, const long long *rows_j, i
   }
 }
 
+// A deferred call's min / max partials reduced on the device (one warp), and
+// min, max and mlt formed from them with the host's operations (xcalc.c:34,
+// :130): out = {min, max, mlt}.
+__global__ void xcalc_scalars_from_partials_kernel(const double *pmin, const double *pmax, const int *pany,
+                                                   int blocks, double d_mlt, double *out) {
+  unsigned long long kmn = ~0ull, kmx = 0ull;
+  for (int i = threadIdx.x; i < blocks; i += 32)
+    if (pany[i]) {
+      const unsigned long long a = order_key(pmin[i]), b = order_key(pmax[i]);
+      kmn = a < kmn ? a : kmn;
+      kmx = b > kmx ? b : kmx;
+    }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(0xffffffffu, kmn, o), b = __shfl_xor_sync(0xffffffffu, kmx, o);
+    kmn = a < kmn ? a : kmn;
+    kmx = b > kmx ? b : kmx;
+  }
+  if (threadIdx.x == 0) {
+    double mn = 0.0, mx = 0.0;
+    if (kmn <= kmx) { mn = key_value(kmn); mx = key_value(kmx); }
+    if (mn >= mx) mx = __dadd_rn(mn, 1.0);
+    const double w = __dsub_rn(mx, mn);
+    const double lo = __dsub_rn(mn, __dmul_rn(0.0625, w)), hi = __dadd_rn(mx, __dmul_rn(0.0625, w));
+    out[0] = lo;
+    out[1] = hi;
+    out[2] = __ddiv_rn(d_mlt, __dsub_rn(hi, lo));
+  }
+}
+
 // Warp per (column, 128-row group): lane l quantises rows 128g + 32k + l,
 // k = 0..3 (four independent coalesced loads).  Per k, the 32 x 32 bit
 // matrix (row l = bits nb0 .. nb0+31 of lane l's value) is transposed in
@@ -166,7 +196,9 @@ __global__ void xcalc_planes_kernel(XcalcParams p) {
       atomicCAS(p.bad, 0, 1);
     } else if (ro >= 0) {
       const double x = p.lf[ro + co];
-      unsigned long long v = __double2ull_rz(__dmul_rn(p.mlt, __dsub_rn(x, p.min)));
+      const double pmin = p.dev_scalars ? p.dev_scalars[0] : p.min;
+      const double pmlt = p.dev_scalars ? p.dev_scalars[2] : p.mlt;
+      unsigned long long v = __double2ull_rz(__dmul_rn(pmlt, __dsub_rn(x, pmin)));
       if (v < 1ull) v = 1ull;
       if (v > p.dmax) v = p.dmax;
       cz[k] = v;
@@ -356,6 +388,51 @@ int *bad_flag() {
   }
   return d;
 }
+
+// Calls inside a deferral scope: their min, max and mlt stay on the device
+// (three doubles per call, in chunks of kSlots calls) until the scope ends;
+// then M_X's fields are set from them.
+constexpr int kSlots = 256;
+struct XcalcDeferred { M_handle *M_X; int slot; };
+thread_local std::vector<DBuf> t_xs_chunks;
+thread_local int t_xs_used = 0;
+thread_local std::vector<XcalcDeferred> t_xs;
+
+double *xcalc_slot(int &slot) {
+  if (t_xs_used == (int)t_xs_chunks.size() * kSlots) t_xs_chunks.emplace_back((size_t)kSlots * 3 * sizeof(double));
+  slot = t_xs_used++;
+  return t_xs_chunks[slot / kSlots].as<double>() + (size_t)(slot % kSlots) * 3;
+}
+
+void xcalc_deferred_enqueue() {}
+
+// After the scope's wait: the scalars into M_X (xcalc.c:240), the planes
+// kernels' bounds flag checked once.
+void xcalc_deferred_finish() {
+  std::vector<double> h((size_t)t_xs_used * 3);
+  for (size_t c = 0; c < t_xs_chunks.size(); ++c) {
+    const int n = std::min(kSlots, t_xs_used - (int)c * kSlots);
+    if (n > 0)
+      LAKGB_CUDA(cudaMemcpyAsync(h.data() + c * kSlots * 3, t_xs_chunks[c].p, (size_t)n * 3 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, stream()));
+  }
+  int hbad = 0;
+  LAKGB_CUDA(cudaMemcpyAsync(&hbad, bad_flag(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  LAKGB_CUDA(cudaStreamSynchronize(stream()));
+  for (const XcalcDeferred &d : t_xs) {
+    const double *v = h.data() + (size_t)d.slot * 3;
+    d.M_X->min_d = v[0]; d.M_X->max_d = v[1]; d.M_X->mlt_d = v[2];
+    if (!isfinite(d.M_X->mlt_d) || d.M_X->mlt_d <= 0) d.M_X->mlt_d = 1;
+  }
+  if (hbad) {
+    printf(" %% Warning! wrap_xcalc: a call skipped an out-of-range index (code %d)\n", hbad);
+    set_error(5, "wrap_xcalc: a call skipped an out-of-range index (code %d)", hbad);
+    LAKGB_CUDA(cudaMemsetAsync(bad_flag(), 0, sizeof(int), stream()));
+  }
+  t_xs.clear();
+  t_xs_chunks.clear();
+  t_xs_used = 0;
+}
 }  // namespace
 }  // namespace lakgb
 
@@ -418,6 +495,12 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
   // A mirrored matrix (lmirror.cu) is read in place.
   Mirror *mlf = (lf_YnWt && YnWt == lf_YnWt->lf) ? find_mirror(lf_YnWt) : nullptr;
   const double *plf = nullptr;
+  // Inside a deferral scope (and when no host copy of the planes is wanted)
+  // min, max and mlt stay on the device: the planes kernel reads them there
+  // and M_X's fields are set when the scope ends, so the call does not wait.
+  const bool deferred = defer_active() && !host_planes_wanted();
+  double *dev_scalars = nullptr;
+  int slot = -1;
   if (nr > 0 && nc > 0 && YnWt) {
     if (mlf && lf_elems <= mlf->n) {
       plf = mlf->d;
@@ -444,24 +527,32 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
                                                        d_max.as<double>(), d_any.as<int>());
     LAKGB_CUDA(cudaGetLastError());
     count_launch();
-    std::vector<double> hmin(blocks), hmax(blocks);
-    std::vector<int> hany(blocks);
-    int hbad = 0;  // an earlier call's planes kernel met an index outside its buffers
-    LAKGB_CUDA(cudaMemcpyAsync(&hbad, bad_flag(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
-    LAKGB_CUDA(cudaMemcpyAsync(hmin.data(), d_min.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
-    LAKGB_CUDA(cudaMemcpyAsync(hmax.data(), d_max.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
-    LAKGB_CUDA(cudaMemcpyAsync(hany.data(), d_any.p, blocks * sizeof(int), cudaMemcpyDeviceToHost, stream()));
-    LAKGB_CUDA(cudaStreamSynchronize(stream()));
-    if (hbad) {
-      printf(" %% Warning! wrap_xcalc: an earlier call skipped an out-of-range index (code %d)\n", hbad);
-      set_error(5, "wrap_xcalc: an earlier call skipped an out-of-range index (code %d)", hbad);
-      LAKGB_CUDA(cudaMemsetAsync(bad_flag(), 0, sizeof(int), stream()));
-    }
-    bool set = false;
-    for (int i = 0; i < blocks; ++i) {
-      if (!hany[i]) continue;
-      if (!set) { min_data = hmin[i]; max_data = hmax[i]; set = true; }
-      else { min_data = hmin[i] < min_data ? hmin[i] : min_data; max_data = hmax[i] > max_data ? hmax[i] : max_data; }
+    if (deferred) {
+      dev_scalars = xcalc_slot(slot);
+      xcalc_scalars_from_partials_kernel<<<1, 32, 0, stream()>>>(d_min.as<double>(), d_max.as<double>(),
+                                                                 d_any.as<int>(), blocks, (double)g_d_mlt, dev_scalars);
+      LAKGB_CUDA(cudaGetLastError());
+      count_launch();
+    } else {
+      std::vector<double> hmin(blocks), hmax(blocks);
+      std::vector<int> hany(blocks);
+      int hbad = 0;  // an earlier call's planes kernel met an index outside its buffers
+      LAKGB_CUDA(cudaMemcpyAsync(&hbad, bad_flag(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
+      LAKGB_CUDA(cudaMemcpyAsync(hmin.data(), d_min.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+      LAKGB_CUDA(cudaMemcpyAsync(hmax.data(), d_max.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+      LAKGB_CUDA(cudaMemcpyAsync(hany.data(), d_any.p, blocks * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+      LAKGB_CUDA(cudaStreamSynchronize(stream()));
+      if (hbad) {
+        printf(" %% Warning! wrap_xcalc: an earlier call skipped an out-of-range index (code %d)\n", hbad);
+        set_error(5, "wrap_xcalc: an earlier call skipped an out-of-range index (code %d)", hbad);
+        LAKGB_CUDA(cudaMemsetAsync(bad_flag(), 0, sizeof(int), stream()));
+      }
+      bool set = false;
+      for (int i = 0; i < blocks; ++i) {
+        if (!hany[i]) continue;
+        if (!set) { min_data = hmin[i]; max_data = hmax[i]; set = true; }
+        else { min_data = hmin[i] < min_data ? hmin[i] : min_data; max_data = hmax[i] > max_data ? hmax[i] : max_data; }
+      }
     }
   }
   if (min_data >= max_data) max_data = min_data + 1;
@@ -493,6 +584,7 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
       p.row_off = d_roff_all.as<long long>(); p.nrows_a = Yn_nrows;
       p.col_off = d_cols.as<long long>(); p.ncols_j = nc;
       p.min = min; p.mlt = mlt; p.dmax = (unsigned long long)(g_d_mlt - 1);
+      p.dev_scalars = dev_scalars;
       p.ncols_per = ncols_per; p.brows = brows; p.planes = planes.as<uint8_t>();
       p.lf_n = (plf == d_lf.p) ? (unsigned long long)lf_elems : (unsigned long long)mlf->n;
       p.planes_n = (unsigned long long)nbytes;
@@ -520,8 +612,14 @@ extern "C" void wrap_xcalc(int *tidx, void **vpra, pthread_t *thread_in, unsigne
   for (unsigned long i = 0; i < M_X->mc_length; ++i) { M_X->mc_b[i] = mr_b[i]; M_X->mc_j[i] = mr_j[i]; }
   M_X->cpop_b = rpop_b; M_X->cpop_j = rpop_j;
   M_X->wX = M_X->Ara;
-  M_X->ncols_per_z = ncols_per; M_X->max_d = max; M_X->min_d = min; M_X->mlt_d = mlt;
-  if (!isfinite(M_X->mlt_d) || M_X->mlt_d <= 0) M_X->mlt_d = 1;
+  M_X->ncols_per_z = ncols_per;
+  if (dev_scalars) {
+    t_xs.push_back(XcalcDeferred{M_X, slot});
+    defer_register(xcalc_deferred_enqueue, xcalc_deferred_finish);
+  } else {
+    M_X->max_d = max; M_X->min_d = min; M_X->mlt_d = mlt;
+    if (!isfinite(M_X->mlt_d) || M_X->mlt_d <= 0) M_X->mlt_d = 1;
+  }
   lakbcc::mhandle_mxget(M_X);
 }
 

@@ -127,3 +127,53 @@ def test_deferred_copies_of_other_entry_points(gpu_lib):
     w2 = kc.call_gram("oracle", False, abi.TYPE_pm, abi.SPACING_b, abi.SPACING_b, MA, MZ, A_ajdk, None, None)
     assert kc._take(o1, n1).tobytes() == w1.tobytes()
     assert kc._take(o2, n2).tobytes() == w2.tobytes()
+
+
+def test_deferred_xcalc(gpu_lib):
+    """wrap_xcalc inside a scope (device-only planes, residency on, as in a
+    solve): M_X's min, max and mlt are set when the scope ends and equal the
+    oracle's, and the planes it left on the device give the same An_ZtSn_ww
+    product as a call made outside a scope."""
+    from test_xcalc_gpu import _run
+    from test_zz_no_alloc import _bind, _case
+    _bind(gpu_lib)
+    lib = gpu_lib
+    rng = np.random.default_rng(31)
+    Yn, Wn, B = 300, 4, 32
+    d = _case(rng, Yn, Wn, 0)
+    want = _run("oracle", d, Yn, Wn, 0)
+    rows, mr_b, mr_j = kc.make_matrix_case(rng, 50, Yn, 0.9, 0.9)
+    An = kc.mhandle(rows, mr_b, mr_j, np.ones(Yn, np.uint8), np.ones(Yn, np.uint8))
+    ylen = abi.bsize(Yn)
+    lib.lakgb_set_residency(1)
+    lib.lakgb_device_only_planes(1)
+    try:
+        outs, scal = [], []
+        for deferred in (False, True):
+            MX = abi.MHandle(None, nrows=(B + 1) * Wn, ncols=Yn, wX=np.zeros(((B + 1) * Wn, ylen), np.uint8))
+            px = C.pointer(MX.s)
+            vpra = (C.c_void_p * 128)()
+            mr_jp, mr_bp = abi.pack_bits(d["mr_j"], ylen), abi.pack_bits(d["mr_b"], ylen)
+            wlen = abi.bsize(Wn)
+            mc_jp, mc_bp = abi.pack_bits(d["mc_j"], wlen), abi.pack_bits(d["mc_b"], wlen)
+            if deferred:
+                lib.lakgb_defer_begin()
+            lib.wrap_xcalc(C.byref(C.c_int(0)), C.cast(vpra, C.c_void_p), None, mr_jp.ctypes.data, mr_bp.ctypes.data,
+                           mc_jp.ctypes.data, mc_bp.ctypes.data, C.byref(d["L"]), d["lf"].ctypes.data,
+                           C.byref(C.c_int(Yn)), C.byref(C.c_int(Wn)), C.byref(px), C.byref(C.c_int(B)), 0)
+            if deferred:
+                lib.lakgb_defer_end()
+            scal.append((MX.s.min_d, MX.s.max_d, MX.s.mlt_d, MX.s.nrows, MX.s.ncols))
+            # one covariate row per retained W column (the planes' groups)
+            St = abi.MHandle(np.ones((MX.s.nrows // (B + 1), 16), np.uint8))
+            out = C.POINTER(L_handle)()
+            n = lib.wrap_An_ZtSn_ww__run(*kc._thread_args(), abi.SPACING_a, abi.SPACING_a, An.ptr, None, px, St.ptr,
+                                         C.byref(out))
+            outs.append(kc._take(out, n))
+        assert scal[0] == scal[1] == want[1]
+        assert outs[0].size > 0 and np.any(outs[0]) and outs[0].tobytes() == outs[1].tobytes()
+        buf = C.create_string_buffer(256)
+        assert lib.lakgb_last_error(buf, 256) == 0, buf.value
+    finally:
+        lib.lakgb_device_only_planes(0)
+        lib.lakgb_set_residency(0)

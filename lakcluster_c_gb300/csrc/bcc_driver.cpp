@@ -256,30 +256,31 @@ void get_xdrop(const Params &P, double lrij, double lcij, int *rdrop_p, int *cdr
 }
 
 // dQuickSort_xij, dir_c/Quicksort.c:83-141 (first-element pivot, recursion
-// limit), written with an explicit stack.
-int partition_xij(double *d, int *i_, int *ib, int *ij, int *nb, int *ga, int *gb, int l, int r) {
+// limit), written with an explicit stack.  The reference swaps the value and
+// its six index arrays together at every step; here the values are sorted
+// with one permutation array swapped alongside, and the index arrays are
+// permuted by it once at the end -- the same comparisons and the same swaps,
+// so the same order, equal values included.
+int partition_xij(double *d, int *perm, int l, int r) {
   const double pivot = d[l];
   int i = l, j = r + 1;
-  auto sw = [&](int a, int b) {
-    std::swap(d[a], d[b]);
-    if (i_) std::swap(i_[a], i_[b]);
-    if (ib) std::swap(ib[a], ib[b]);
-    if (ij) std::swap(ij[a], ij[b]);
-    if (nb) std::swap(nb[a], nb[b]);
-    if (ga) std::swap(ga[a], ga[b]);
-    if (gb) std::swap(gb[a], gb[b]);
-  };
   while (true) {
     do { i++; } while (i <= r && d[i] <= pivot);
     do { j--; } while (d[j] > pivot);
     if (i >= j) break;
-    sw(i, j);
+    std::swap(d[i], d[j]);
+    std::swap(perm[i], perm[j]);
   }
-  sw(l, j);
+  std::swap(d[l], d[j]);
+  std::swap(perm[l], perm[j]);
   return j;
 }
 
 void quicksort_xij(unsigned limit, double *d, int *i_, int *ib, int *ij, int *nb, int *ga, int *gb, int l, int r) {
+  if (l >= r) return;
+  std::vector<int> perm((size_t)r + 1);  // entries l .. r used
+  for (int k = l; k <= r; ++k) perm[k] = k;
+  int *pm = perm.data();
   struct Node { int l, r; unsigned nn; };
   std::vector<Node> st;
   st.push_back({l, r, 0});
@@ -287,12 +288,18 @@ void quicksort_xij(unsigned limit, double *d, int *i_, int *ib, int *ij, int *nb
     Node n = st.back();
     st.pop_back();
     if (n.l < n.r) {
-      int j = partition_xij(d, i_, ib, ij, nb, ga, gb, n.l, n.r);
+      int j = partition_xij(d, pm, n.l, n.r);
       if (n.nn < limit) {
         st.push_back({j + 1, n.r, n.nn + 1});
         st.push_back({n.l, j - 1, n.nn + 1});
       }
     }
+  }
+  std::vector<int> tmp((size_t)(r - l + 1));
+  for (int *a : {i_, ib, ij, nb, ga, gb}) {
+    if (!a) continue;
+    for (int k = l; k <= r; ++k) tmp[k - l] = a[pm[k]];
+    for (int k = l; k <= r; ++k) a[k] = tmp[k - l];
   }
 }
 

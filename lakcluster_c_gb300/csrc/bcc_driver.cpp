@@ -276,22 +276,71 @@ int partition_xij(double *d, int *perm, int l, int r) {
   return j;
 }
 
+// The permutation that sorts d[l .. r] ascending, when those values are all
+// distinct and none is NaN (false otherwise): an LSD radix sort, 11 bits a
+// pass, of order-preserving integer keys (a non-negative value's bits with
+// the sign bit set, a negative value's bits inverted).  Distinct values have
+// one ascending order, so any correct sort of them gives the quicksort's.
+bool sort_distinct(const double *d, int l, int r, int *pm) {
+  const int n = r - l + 1;
+  std::vector<uint64_t> key((size_t)n), key2((size_t)n);
+  std::vector<int> idx((size_t)n), idx2((size_t)n);
+  constexpr int kBits = 11, kPasses = 6, kBins = 1 << kBits;
+  std::vector<unsigned> hist((size_t)kPasses * kBins, 0);
+  for (int k = 0; k < n; ++k) {
+    const double v = d[l + k];
+    if (v != v) return false;
+    uint64_t u;
+    memcpy(&u, &v, 8);
+    u = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+    key[k] = u;
+    idx[k] = l + k;
+    for (int p = 0; p < kPasses; ++p) hist[(size_t)p * kBins + ((u >> (kBits * p)) & (kBins - 1))]++;
+  }
+  for (int p = 0; p < kPasses; ++p) {
+    unsigned *h = &hist[(size_t)p * kBins];
+    const uint64_t first = (key[0] >> (kBits * p)) & (kBins - 1);
+    if (h[first] == (unsigned)n) continue;  // every key has this digit
+    unsigned run = 0;
+    for (int b = 0; b < kBins; ++b) { const unsigned c = h[b]; h[b] = run; run += c; }
+    for (int k = 0; k < n; ++k) {
+      const unsigned o = h[(key[k] >> (kBits * p)) & (kBins - 1)]++;
+      key2[o] = key[k];
+      idx2[o] = idx[k];
+    }
+    key.swap(key2);
+    idx.swap(idx2);
+  }
+  for (int k = 1; k < n; ++k)
+    if (d[idx[k - 1]] == d[idx[k]]) return false;  // a tie (+0 and -0 included)
+  for (int k = 0; k < n; ++k) pm[l + k] = idx[k];
+  return true;
+}
+
 void quicksort_xij(unsigned limit, double *d, int *i_, int *ib, int *ij, int *nb, int *ga, int *gb, int l, int r) {
   if (l >= r) return;
   std::vector<int> perm((size_t)r + 1);  // entries l .. r used
-  for (int k = l; k <= r; ++k) perm[k] = k;
   int *pm = perm.data();
-  struct Node { int l, r; unsigned nn; };
-  std::vector<Node> st;
-  st.push_back({l, r, 0});
-  while (!st.empty()) {
-    Node n = st.back();
-    st.pop_back();
-    if (n.l < n.r) {
-      int j = partition_xij(d, pm, n.l, n.r);
-      if (n.nn < limit) {
-        st.push_back({j + 1, n.r, n.nn + 1});
-        st.push_back({n.l, j - 1, n.nn + 1});
+  // A subarray at depth nn holds at most n - nn values, so with n <= limit no
+  // call reaches the recursion limit and the quicksort sorts d completely.
+  if ((long)r - l + 1 <= (long)limit && sort_distinct(d, l, r, pm)) {
+    std::vector<double> v((size_t)(r - l + 1));
+    for (int k = l; k <= r; ++k) v[k - l] = d[pm[k]];
+    for (int k = l; k <= r; ++k) d[k] = v[k - l];
+  } else {
+    for (int k = l; k <= r; ++k) perm[k] = k;
+    struct Node { int l, r; unsigned nn; };
+    std::vector<Node> st;
+    st.push_back({l, r, 0});
+    while (!st.empty()) {
+      Node n = st.back();
+      st.pop_back();
+      if (n.l < n.r) {
+        int j = partition_xij(d, pm, n.l, n.r);
+        if (n.nn < limit) {
+          st.push_back({j + 1, n.r, n.nn + 1});
+          st.push_back({n.l, j - 1, n.nn + 1});
+        }
       }
     }
   }
@@ -2635,7 +2684,9 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     sumscores_ifT(S);
     if (S.P.Ireq > 0) sumscores_srt(S);
     sumscores_cmb(S);
+    g_clock.tick("sumscores (nrm, ifT, srt, cmb)");  // LAKBCC_PROFILE only
     sumscores_xij(S);
+    g_clock.tick("sumscores (xij)");
     sumscores_mxA(S);
     trace_stage(S, "sumscores");
     lrup_QR(S); trace_stage(S, "lrup_QR");
@@ -2643,6 +2694,7 @@ int solve(const Params &P, const Input &I, Output &O, std::string &err, const Ho
     if (qc_ynwt(S)) { lrup_QC(S); trace_stage(S, "lrup_QC"); }
     lrup_mxdup(S);
     M_mxset_all(S);
+    g_clock.tick("lrup_mxdup, M_mxset");
     // bcc_M_YnWt here requantises the updated Grams, but nothing on the
     // YnWt path reads those planes before they are rebuilt, so it is skipped.
     lf_AtTYn____WtSZn_all(S); trace_stage(S, "lf_AtTYn____WtSZn");
@@ -2782,11 +2834,14 @@ int dcc_solve(const Params &P, const Input &I, Output &O, std::string &err, cons
     sumscores_ifT(S);
     if (S.P.Ireq > 0) sumscores_srt(S);
     sumscores_cmb(S);
+    g_clock.tick("sumscores (nrm, ifT, srt, cmb)");  // LAKBCC_PROFILE only
     sumscores_xij(S);
+    g_clock.tick("sumscores (xij)");
     sumscores_mxA(S);
     trace_stage(S, "sumscores");
     lrup_mxdup(S);
     M_mxset_all(S);
+    g_clock.tick("lrup_mxdup, M_mxset");
     dcc_subscores(S);
     if (O.iterations > 10000000) { err = "iteration limit"; return 5; }
   }

@@ -65,14 +65,47 @@ static void mxget_excerpt(int n, const unsigned char *mb, const unsigned char *m
                           long long *pop_j, unsigned int *a_, unsigned int *b_, long length) {
   *pop_b = popcount_bytes(mb, length);
   *pop_j = popcount_bytes(mj, length);
-  int a = 0, b = 0, j = 0;
-  while (a < n) {
-    while (a < n && !bget_on(mb, a)) a++;
-    if (a < n && bget_on(mb, a) && bget_on(mj, a)) {
-      b_[j] = (unsigned)b; a_[j] = (unsigned)a;
-      j++; b++; a++;
-    } else if (a < n && bget_on(mb, a)) {
-      b++; a++;
+  // The reference walks the n bits one at a time: every bit on in mb takes
+  // the next b index, and those also on in mj are listed with their a and b
+  // indices.  Same lists here, 64 elements at a time (bit 7 of a byte is its
+  // first element, so a big-endian word holds element 64w + k at bit 63 - k):
+  // empty words are skipped, full words written as one run, and in the
+  // others only the listed bits are visited, their b index being b plus the
+  // mb bits before them.
+  if (n <= 0) return;
+  unsigned b = 0, j = 0;
+  const long nwords = (long)n / 64;
+  for (long w = 0; w < nwords; ++w) {
+    const uint64_t on_b = load_be64(mb + 8 * w);
+    if (!on_b) continue;
+    uint64_t on_j = on_b & load_be64(mj + 8 * w);
+    const unsigned a0 = (unsigned)(64 * w);
+    if (on_j == ~0ull) {
+      for (unsigned k = 0; k < 64; ++k) { a_[j + k] = a0 + k; b_[j + k] = b + k; }
+      j += 64; b += 64;
+      continue;
+    }
+    while (on_j) {
+      const int k = __builtin_clzll(on_j);
+      const uint64_t before = k ? on_b >> (64 - k) : 0;  // mb bits of elements 64w .. 64w + k - 1
+      a_[j] = a0 + (unsigned)k; b_[j] = b + (unsigned)__builtin_popcountll(before); ++j;
+      on_j &= ~(0x8000000000000000ull >> k);
+    }
+    b += (unsigned)__builtin_popcountll(on_b);
+  }
+  const long nbytes = ((long)n + 7) / 8;
+  for (long i = nwords * 8; i < nbytes; ++i) {
+    unsigned on_b = mb[i];
+    const long rest = (long)n - i * 8;
+    if (rest < 8) on_b &= (0xFFu << (8 - rest)) & 0xFFu;  // bits past n are not elements
+    if (!on_b) continue;
+    const unsigned on_j = on_b & mj[i];
+    while (on_b) {
+      const int k = __builtin_clz(on_b) - 24;  // position from the byte's first element
+      const unsigned bit = 0x80u >> k;
+      if (on_j & bit) { b_[j] = b; a_[j] = (unsigned)(i * 8 + k); ++j; }
+      ++b;
+      on_b &= ~bit;
     }
   }
 }

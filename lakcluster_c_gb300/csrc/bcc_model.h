@@ -36,8 +36,25 @@ inline void bset_off(unsigned char *b, long n) { b[n / 8] &= (unsigned char)~(1 
 
 inline unsigned popcount_bytes(const unsigned char *p, long n) {
   unsigned c = 0;
-  for (long i = 0; i < n; ++i) c += (unsigned)__builtin_popcount((unsigned)p[i]);
+  long i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w;
+    memcpy(&w, p + i, 8);
+    c += (unsigned)__builtin_popcountll(w);
+  }
+  for (; i < n; ++i) c += (unsigned)__builtin_popcount((unsigned)p[i]);
   return c;
+}
+
+// Eight mask bytes as one word whose bit 63 is the first byte's bit 7 (the
+// masks' first element), whatever the host's byte order.
+inline uint64_t load_be64(const unsigned char *p) {
+  uint64_t w;
+  memcpy(&w, p, 8);
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+  w = __builtin_bswap64(w);
+#endif
+  return w;
 }
 
 // Owning wrapper around an M_handle.  wX either points at another handle's

@@ -1387,23 +1387,47 @@ void flattenloop(State &S) {
 }
 
 // dra_plusdivequals_s___m_m (ra_stats.c:69-76)
+// f(r) for every r < n whose bit is on in m1 (and in m2 when given), in
+// ascending order, a mask byte at a time.
+template <typename F>
+inline void for_each_on(const unsigned char *m1, const unsigned char *m2, unsigned long long n, F f) {
+  const unsigned long long nbytes = (n + 7) / 8;
+  for (unsigned long long i = 0; i < nbytes; ++i) {
+    const unsigned v = m2 ? (unsigned)(m1[i] & m2[i]) : (unsigned)m1[i];
+    if (!v) continue;
+    const unsigned long long r0 = i * 8;
+    if (v == 0xFFu && r0 + 8 <= n) {
+      for (unsigned long long r = r0; r < r0 + 8; ++r) f(r);
+    } else {
+      for (unsigned k = 0; k < 8 && r0 + k < n; ++k)
+        if ((v >> (7 - k)) & 1u) f(r0 + k);
+    }
+  }
+}
+
+// Every element below is updated on its own, so the order of the visits
+// does not change the results.
 void plusdiv(const State &S, double *d1, unsigned long long nrows, unsigned long long ncols, const double *d2,
              double denominator, const unsigned char *bmr, const unsigned char *bmc) {
   double d_use = denominator;
   if (fabs(d_use) < S.P.tolerance) d_use = 1;
   for (unsigned long long c = 0; c < ncols; ++c)
-    if (bget_on(bmc, (long)c))
-      for (unsigned long long r = 0; r < nrows; ++r)
-        if (bget_on(bmr, (long)r)) d1[r + c * nrows] += d2[r + c * nrows] / d_use;
+    if (bget_on(bmc, (long)c)) {
+      double *o = d1 + c * nrows;
+      const double *in = d2 + c * nrows;
+      for_each_on(bmr, nullptr, nrows, [&](unsigned long long r) { o[r] += in[r] / d_use; });
+    }
 }
 
 // dra_plustimesequals_s___m_m (ra_stats.c:63-68)
 void plustimes(double *d1, unsigned long long nrows, unsigned long long ncols, const double *d2, double m,
                const unsigned char *bmr, const unsigned char *bmc) {
   for (unsigned long long c = 0; c < ncols; ++c)
-    if (bget_on(bmc, (long)c))
-      for (unsigned long long r = 0; r < nrows; ++r)
-        if (bget_on(bmr, (long)r)) d1[r + c * nrows] += m * d2[r + c * nrows];
+    if (bget_on(bmc, (long)c)) {
+      double *o = d1 + c * nrows;
+      const double *in = d2 + c * nrows;
+      for_each_on(bmr, nullptr, nrows, [&](unsigned long long r) { o[r] += m * in[r]; });
+    }
 }
 
 void dra_sumx0(double *d, unsigned long long stride, unsigned long long length) {
@@ -1589,23 +1613,23 @@ void sumscores_nrm(State &S) {  // bcc_sumscores_nrm (bcc_sumscores.c:550-779)
       Single *E = S.E[nb1].get();
       const unsigned long long AN = (unsigned long long)E->A_nrows;
       if (E->A_rbother && S.A_cbother && E->Z_rbother)
-        for (int ma = 0; ma < E->A_nrows; ++ma)
-          if (bget_on(E->A_bmr_b.data(), ma) && bget_on(E->A_bmr_j.data(), ma))
-            dra_sumx0(&E->QR_AnZtSZnAt_nrm[ma + ns_a * AN], AN * T, nb);
+        for_each_on(E->A_bmr_b.data(), E->A_bmr_j.data(), AN, [&](unsigned long long ma) {
+          dra_sumx0(&E->QR_AnZtSZnAt_nrm[ma + ns_a * AN], AN * T, nb);
+        });
       if (E->A_rbother && S.A_cbother)
-        for (int ma = 0; ma < E->A_nrows; ++ma)
-          if (bget_on(E->A_bmr_b.data(), ma) && bget_on(E->A_bmr_j.data(), ma))
-            dra_sumx0(&E->QR_AnAtTAnAt_nrm[ma + ns_a * AN], AN * T, nb);
+        for_each_on(E->A_bmr_b.data(), E->A_bmr_j.data(), AN, [&](unsigned long long ma) {
+          dra_sumx0(&E->QR_AnAtTAnAt_nrm[ma + ns_a * AN], AN * T, nb);
+        });
     }
     const unsigned long long AC = (unsigned long long)S.A_ncols;
     if (S.A_rpop_b_total && S.A_cbother && S.Z_rpop_b_total)
-      for (int na = 0; na < S.A_ncols; ++na)
-        if (bget_on(S.A_bmc_b.data(), na) && bget_on(S.A_bmc_j.data(), na))
-          dra_sumx0(&S.QC_AtTAnZtSZn_nrm[na + ns_a * AC], AC * T, (unsigned long long)nb * nb);
+      for_each_on(S.A_bmc_b.data(), S.A_bmc_j.data(), AC, [&](unsigned long long na) {
+        dra_sumx0(&S.QC_AtTAnZtSZn_nrm[na + ns_a * AC], AC * T, (unsigned long long)nb * nb);
+      });
     if (S.A_cbother && S.A_rpop_b_total)
-      for (int na = 0; na < S.A_ncols; ++na)
-        if (bget_on(S.A_bmc_b.data(), na) && bget_on(S.A_bmc_j.data(), na))
-          dra_sumx0(&S.QC_AtTAnAtTAn_nrm[na + ns_a * AC], AC * T, (unsigned long long)nb * nb);
+      for_each_on(S.A_bmc_b.data(), S.A_bmc_j.data(), AC, [&](unsigned long long na) {
+        dra_sumx0(&S.QC_AtTAnAtTAn_nrm[na + ns_a * AC], AC * T, (unsigned long long)nb * nb);
+      });
   }
 }
 

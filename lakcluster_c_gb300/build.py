@@ -24,7 +24,7 @@ CU_SOURCES = ["lakgb_runtime.cu", "gram.cu", "gram_tc.cu", "rowvec.cu", "abi_ker
               "bitplane_tc.cu", "loopsum.cu", "lmirror.cu",
               "vv_kernels.cu", "transpose.cu", "bed.cu", "condense.cu"]
 # Host-only translation units (the solve driver and its input reader).
-CPP_SOURCES = ["bcc_model.cpp", "bcc_driver.cpp", "bcc_io.cpp", "bcc_abi.cpp", "bcc_server.cpp"]
+CPP_SOURCES = ["bcc_model.cpp", "bcc_sort.cpp", "bcc_driver.cpp", "bcc_io.cpp", "bcc_abi.cpp", "bcc_server.cpp"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-pthread", "-I" + os.path.join(ROOT, "include")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <chrono>
 #include <memory>
+#include <thread>
 
 namespace lakbcc {
 
@@ -284,26 +285,52 @@ inline uint64_t transpose8(uint64_t x) {
   return x;
 }
 
+// Column blocks [k0, k1) of transpose_rows, in tiles of 64 x 64 bytes (512
+// rows x 512 columns) so that the rows read and the columns written stay in
+// cache while a tile is done.
+void transpose_tiles(const unsigned char *rows, unsigned char *t, int nrows, int ncols, long rb, long tb, int k0,
+                     int k1) {
+  const int rblocks = (nrows + 7) / 8;
+  for (int kb = k0; kb < k1; kb += 64)
+    for (int ib = 0; ib < rblocks; ib += 64) {
+      const int ke = std::min(k1, kb + 64), ie = std::min(rblocks, ib + 64);
+      for (int i = ib; i < ie; ++i)
+        for (int k = kb; k < ke; ++k) {
+          uint64_t x = 0;
+          for (int q = 0; q < 8; ++q) {
+            const int r = 8 * i + q;
+            const uint64_t byte = r < nrows ? rows[(size_t)r * rb + k] : 0;
+            x |= byte << (8 * (7 - q));
+          }
+          if (!x) continue;
+          x = transpose8(x);
+          for (int q = 0; q < 8; ++q) {
+            const int c = 8 * k + q;
+            if (c < ncols) t[(size_t)c * tb + i] = (unsigned char)(x >> (8 * (7 - q)));
+          }
+        }
+    }
+}
+
+// The bit transpose of a packed row-major matrix (8 x 8 blocks).  Matrices of
+// 64 MB or more are split over up to 8 host threads by column blocks (each
+// writes its own output rows).
 std::vector<unsigned char> transpose_rows(const std::vector<unsigned char> &rows, int nrows, int ncols) {
   const long rb = bsize(ncols), tb = bsize(nrows);
   std::vector<unsigned char> t((size_t)std::max(1, ncols) * (size_t)tb, 0);
-  const int rblocks = (nrows + 7) / 8, cblocks = (ncols + 7) / 8;
-  for (int i = 0; i < rblocks; ++i) {
-    for (int k = 0; k < cblocks; ++k) {
-      uint64_t x = 0;
-      for (int q = 0; q < 8; ++q) {
-        const int r = 8 * i + q;
-        const uint64_t byte = r < nrows ? rows[(size_t)r * rb + k] : 0;
-        x |= byte << (8 * (7 - q));
-      }
-      if (!x) continue;
-      x = transpose8(x);
-      for (int q = 0; q < 8; ++q) {
-        const int c = 8 * k + q;
-        if (c < ncols) t[(size_t)c * tb + i] = (unsigned char)(x >> (8 * (7 - q)));
-      }
-    }
+  const int cblocks = (ncols + 7) / 8;
+  const int nth = (size_t)nrows * (size_t)rb >= (size_t(64) << 20)
+                      ? (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency()))
+                      : 1;
+  if (nth <= 1) {
+    transpose_tiles(rows.data(), t.data(), nrows, ncols, rb, tb, 0, cblocks);
+    return t;
   }
+  const int per = ((cblocks + nth - 1) / nth + 63) / 64 * 64;
+  std::vector<std::thread> th;
+  for (int k0 = 0; k0 < cblocks; k0 += per)
+    th.emplace_back(transpose_tiles, rows.data(), t.data(), nrows, ncols, rb, tb, k0, std::min(cblocks, k0 + per));
+  for (auto &x : th) x.join();
   return t;
 }
 

@@ -1291,7 +1291,6 @@ void flattenloop(State &S) {
     for (int nb2 = 0; nb2 < S.nbins; ++nb2) flattenloop_pair(S, S.f(nb1, nb2));
 }
 
-// dra_plusdivequals_s___m_m (ra_stats.c:69-76)
 // f(r) for every r < n whose bit is on in m1 (and in m2 when given), in
 // ascending order, a mask byte at a time.
 template <typename F>
@@ -1310,8 +1309,9 @@ inline void for_each_on(const unsigned char *m1, const unsigned char *m2, unsign
   }
 }
 
-// Every element below is updated on its own, so the order of the visits
-// does not change the results.
+// dra_plusdivequals_s___m_m (ra_stats.c:69-76).  Every element here and in
+// plustimes is updated on its own, so the order of the visits does not
+// change the results.
 void plusdiv(const State &S, double *d1, unsigned long long nrows, unsigned long long ncols, const double *d2,
              double denominator, const unsigned char *bmr, const unsigned char *bmc) {
   double d_use = denominator;
